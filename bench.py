@@ -1,0 +1,334 @@
+"""Benchmark of the GMorpho hot path on GB300: variable-radius ball closing
+plus contour marching cubes (with normals and 20 bilateral iterations) of a
+1024^3 fine grid, in the reference's bit-exact two-level mode.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0.  ``value`` is whole-job Gvoxel/s with the inputs
+resident in HBM (device-timed with CUDA events); ``e2e`` is the same metric
+through the host-buffer C ABI call gm_update + gm_mesh_download (pinned host
+buffers, H2D of the grid and the radius field and D2H of the mesh inside the
+timed region).  Under torchrun every rank closes its own replica (weak
+scaling, no collective on the data path).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gvoxel/s closing+MC at 1024^3 (bit-exact)"
+UNIT = "Gvoxel/s"
+RES = 512                # base cells per axis -> 1024^3 fine voxels
+SEED = 3000              # seed = 1000 * config + instance
+BLOBS = 200
+BILATERAL = 20           # symmetric closing (GMorpho.cu:7808-7811)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_inputs(res, seed, device):
+    from broxy_gb300 import synth
+    X = synth.blob_grid(res, seed, count=BLOBS, device=device)
+    R = synth.radius_field(res, seed, base=2, span=30, device=device)
+    return X.contiguous(), R.contiguous()
+
+
+# Algorithmic bytes per fine voxel of each kernel (its compulsory input and
+# output streams in the layout it works on).
+KERNEL_BYTES_PER_VOXEL = {
+    "k_dil_pass_x": 1 / 8 + 1,            # packed grid in, u8 distance out
+    "k_axis_pass": 2 + 2,                 # u16 (or u8) field in, u16 out (full-resolution passes)
+    "k_final_z": 2 + 1 + 1 / 8,           # u16 in, radius in (dilation), packed bits out
+    "k_ero_pass_x": 1 / 8 + 1 + 2 + 1,    # contour bits + radius in, centre + lattice fields out
+}
+
+
+def run_ours(args, rank, world):
+    import torch
+    from broxy_gb300 import api
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ctx = api.Context(dev.index)
+    res = args.res
+    V = (2 * res) ** 3
+    X, R = make_inputs(res, SEED + rank * 0, dev)
+    desc = api.make_desc(res, cell_size=1.0 / res)
+    out = torch.empty_like(X)
+
+    def step():
+        ctx.close(desc, X, R, 0, api.L.GM_REF, api.L.GM_SE_SPHERE, out=out)
+        Vm, Nm, Tm = ctx.mesh(desc, out, BILATERAL)
+        return Vm.shape[0], Tm.shape[0]
+
+    for _ in range(args.warmup):
+        nv, nt = step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = ctx.kernel_launches
+    ctx.profile(True)
+    ctx.profile_reset()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(args.steps):
+            nv, nt = step()
+        e1.record(st)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    launches = ctx.kernel_launches - launches0
+    ms_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * V / (ms_max * 1e-3) / 1e9
+
+    # ---- e2e through the host-buffer C ABI (gm_update + gm_mesh_download)
+    hX = torch.empty(X.numel(), dtype=torch.uint8, pin_memory=True)
+    hR = torch.empty(R.numel(), dtype=torch.int8, pin_memory=True)
+    hX.copy_(X.cpu())
+    hR.copy_(R.cpu())
+    gs = 0.5  # global scale in world units: gates the morphology on (GMorpho.cu:7783)
+    ctx.update(desc, hX, hR, gs)
+    hV = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True)
+    hN = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True)
+    hT = torch.empty((nt, 3), dtype=torch.int32, pin_memory=True)
+    import ctypes as C
+
+    def e2e_step():
+        nv2, nt2 = ctx.update(desc, hX, hR, gs)
+        st_ = ctx.lib.gm_mesh_download(ctx.ctx, C.c_void_p(hV.data_ptr()), C.c_void_p(hN.data_ptr()),
+                                       C.c_void_p(hT.data_ptr()), api._stream())
+        api.L.check(ctx.ctx, st_)
+        return nv2, nt2
+
+    for _ in range(max(1, args.warmup - 1)):
+        e2e_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        nv2, nt2 = e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    assert (nv2, nt2) == (nv, nt)
+
+    # ---- roofline of the dominant kernel and of the morphology passes
+    hbm, peak_kind = peaks()
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else (None, None)
+    roof = None
+    if top[0] is not None:
+        name, rec = top
+        per_launch_ms = rec["ms"] / rec["launches"]
+        bpv = KERNEL_BYTES_PER_VOXEL.get(name)
+        if bpv is not None:
+            ach = bpv * V / (per_launch_ms * 1e-3) / 1e9
+            roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": None,
+                    "bytes_per_voxel": round(bpv, 4), "per_launch_ms": round(per_launch_ms, 4)}
+        else:
+            roof = {"kernel": name, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+                    "peak_kind": peak_kind, "traffic": None, "per_launch_ms": round(per_launch_ms, 4)}
+    morph_kernels = [k for k in prof if not k.startswith(("k_mc", "k_adj", "k_scan", "k_vertex", "k_bilateral"))]
+    morph_ms = sum(prof[k]["ms"] for k in morph_kernels) / args.steps
+    mesh_ms = sum(prof[k]["ms"] for k in prof if k not in morph_kernels) / args.steps
+    # survey per-pass algorithmic bytes: dilation V/8 + R + V/8, erosion V/8 + R + V/8
+    morph_bytes = 2 * (V / 8 + V + V / 8)
+    morph_gbs = morph_bytes / (morph_ms * 1e-3) / 1e9 if morph_ms > 0 else None
+
+    clocks = clk.summary()
+    result = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8/u16 (integer distance transforms), f32 mesh", "data": "synthetic",
+        "config": {"workload": "config 3: 1024^3 fine grid (res 512), 200-blob solid, variable radius "
+                               "r = 2 + floor(30 s(x)), GM_REF sphere closing + contour MC + 20 bilateral",
+                   "fine_voxels": V, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (1 GiB radius field + 2 GiB intermediate fields)",
+                   "mesh_vertices": nv, "mesh_triangles": nt},
+        "e2e": {"value": round(world * V / (e2e_ms * 1e-3) / 1e9, 3), "unit": UNIT, "ms_per_step": round(e2e_ms, 3),
+                "h2d_bytes_per_step": int(X.numel() + R.numel()),
+                "d2h_bytes_per_step": int(24 * nv + 12 * nt)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "morphology": {"ms": round(morph_ms, 3), "algorithmic_bytes": int(morph_bytes),
+                       "achieved_gbs": round(morph_gbs, 1) if morph_gbs else None,
+                       "frac_of_peak": round(morph_gbs / hbm, 4) if morph_gbs else None},
+        "mesh_ms": round(mesh_ms, 3),
+        "kernels": {k: {"launches": v["launches"], "ms_per_step": round(v["ms"] / args.steps, 4)}
+                    for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])},
+        "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(X, R, res, args.cpu_res)
+    ctx.close_ctx()
+    return result
+
+
+def cpu_crop(X, R, res, sub):
+    """Centre crop of `sub` base cells per axis of the device inputs."""
+    Xh = X.cpu().numpy().reshape(res, res, res)
+    Rh = R.cpu().numpy().reshape(2 * res, 2 * res, 2 * res)
+    o = (res - sub) // 2
+    Xc = np.ascontiguousarray(Xh[o:o + sub, o:o + sub, o:o + sub]).reshape(-1)
+    Rc = np.ascontiguousarray(Rh[2 * o:2 * (o + sub), 2 * o:2 * (o + sub), 2 * o:2 * (o + sub)]).reshape(-1)
+    return Xc, Rc
+
+
+def cpu_baseline(X, R, res, sub):
+    """The oracle's reference-algorithm closing + MC + normals on all host
+    cores, on a centre crop of the same inputs (bounded sample)."""
+    from oracle import oracle as O
+    Xc, Rc = cpu_crop(X, R, res, sub)
+    t0 = time.perf_counter()
+    _, _, Cc = O.close(Xc, sub, [sub] * 3, Rc, 0, 0)
+    Vc, Tc = O.mc(Cc, sub, np.zeros(3, np.float32), 1.0 / res)
+    O.normals(Vc, Tc, BILATERAL)
+    dt = time.perf_counter() - t0
+    vox = (2 * sub) ** 3
+    return {"value": round(vox / dt / 1e9, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "centre crop of %d^3 fine voxels of the same grid and radius field; oracle GM_REF closing "
+                      "(pyramid traversal, OpenMP) + contour MC + %d bilateral iterations; %.1f s" %
+                      (2 * sub, BILATERAL, dt)}
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's algorithm on the host cores (the oracle
+    port; the reference itself cannot be built here), same metric."""
+    if rank != 0:
+        return None
+    import torch
+    from broxy_gb300 import synth
+    res, sub = args.res, args.cpu_res
+    X = synth.blob_grid(res, SEED, count=BLOBS, device=None if not torch.cuda.is_available() else "cuda")
+    R = synth.radius_field(res, SEED, base=2, span=30,
+                           device=None if not torch.cuda.is_available() else "cuda")
+    import torch as _t
+    X = _t.as_tensor(X)
+    R = _t.as_tensor(R)
+    times = []
+    from oracle import oracle as O
+    Xc, Rc = cpu_crop(X, R, res, sub)
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, _, Cc = O.close(Xc, sub, [sub] * 3, Rc, 0, 0)
+        Vc, Tc = O.mc(Cc, sub, np.zeros(3, np.float32), 1.0 / res)
+        O.normals(Vc, Tc, BILATERAL)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    vox = (2 * sub) ** 3
+    val = vox / statistics.mean(times) / 1e9
+    return {"metric": METRIC, "value": round(val, 6), "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.mean(times), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int (CPU)",
+            "data": "synthetic",
+            "config": {"workload": "config 3 crop: %d^3 fine voxels of the 1024^3 grid, same radius field" % (2 * sub)},
+            "cpu_baseline": {"value": round(val, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": "centre crop of %d^3 fine voxels per step" % (2 * sub)},
+            "e2e": {"value": round(val, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--res", type=int, default=RES)
+    ap.add_argument("--cpu-res", type=int, default=64, help="base cells per axis of the CPU crop")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        r = run_reference(args, rank, world)
+    else:
+        r = run_ours(args, rank, world)
+    if rank == 0 and r is not None:
+        print(json.dumps(r))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+"""Functional Python API over the C ABI (include/gmorpho_gb300.h).
+
+Device buffers are torch CUDA tensors (torch is only the allocator and the
+stream provider here); every computation runs in libgmorpho_gb300.so.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class DevicePtrArray:
+    """Zero-copy view of a device buffer owned by the library
+    (__cuda_array_interface__), e.g. the mesh of a context."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (ptr or 0, True),
+                                         "version": 3, "strides": None}
+
+
+def make_desc(res, data_res=None, bbox_min=(0.0, 0.0, 0.0), cell_size=None):
+    d = L.GridDesc()
+    cs = cell_size if cell_size is not None else 1.0 / res
+    for a in range(3):
+        d.bbox_min[a] = bbox_min[a]
+        d.bbox_max[a] = bbox_min[a] + cs * res
+        d.data_res[a] = res if data_res is None else int(data_res[a])
+    d.res = res
+    d.cell_size = cs
+    return d
+
+
+def grid_attributes(points, base_res, margin):
+    P = np.ascontiguousarray(points, dtype=np.float32)
+    d = L.GridDesc()
+    st = L.load().gm_grid_attributes(P.ctypes.data_as(C.c_void_p), len(P), base_res, margin, C.byref(d))
+    L.check(None, st)
+    return d
+
+
+class Context:
+    """One device context (cached workspaces + last mesh)."""
+
+    def __init__(self, device=0):
+        import torch
+        torch.cuda.init()
+        self.lib = L.load()
+        self.ctx = C.c_void_p()
+        st = self.lib.gm_ctx_create(device, C.byref(self.ctx))
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_ctx_create(%d)" % device)
+        self.device = device
+
+    def close_ctx(self):
+        if self.ctx:
+            self.lib.gm_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close_ctx()
+        except Exception:
+            pass
+
+    @property
+    def kernel_launches(self):
+        return int(self.lib.gm_ctx_kernel_launches(self.ctx))
+
+    def _check(self, st):
+        L.check(self.ctx, st)
+
+    def profile(self, enable=True):
+        """Per-kernel CUDA-event timing of every launch on this context."""
+        self._check(self.lib.gm_ctx_profile(self.ctx, 1 if enable else 0))
+
+    def profile_reset(self):
+        self._check(self.lib.gm_ctx_profile_reset(self.ctx))
+
+    def profile_read(self):
+        import json
+        n = self.lib.gm_ctx_profile_read(self.ctx, None, 0)
+        buf = C.create_string_buffer(int(n))
+        self.lib.gm_ctx_profile_read(self.ctx, buf, n)
+        return json.loads(buf.value.decode())
+
+    # a5..a11
+    def close(self, desc, X, R=None, uniform_radius=4, mode=L.GM_REF, se=L.GM_SE_SPHERE, out=None, D=None, S=None):
+        import torch
+        if out is None:
+            out = torch.empty_like(X)
+        st = self.lib.gm_close(self.ctx, C.byref(desc), _ptr(X), _ptr(R), int(uniform_radius), mode, se, _ptr(out),
+                               _ptr(D), _ptr(S), _stream())
+        self._check(st)
+        return out
+
+    # a12..a16
+    def mesh(self, desc, Cg, bilateral_iters=20):
+        """Returns (V, N, T) as zero-copy device arrays owned by the context
+        (valid until the next mesh-producing call) and the counts."""
+        import torch
+        mv = L.MeshView()
+        st = self.lib.gm_mesh(self.ctx, C.byref(desc), _ptr(Cg), int(bilateral_iters), C.byref(mv), _stream())
+        self._check(st)
+        nv, nt = mv.num_vertices, mv.num_triangles
+        V = torch.as_tensor(DevicePtrArray(mv.vertices, (nv, 3), "<f4"), device="cuda")
+        N = torch.as_tensor(DevicePtrArray(mv.normals, (nv, 3), "<f4"), device="cuda")
+        T = torch.as_tensor(DevicePtrArray(mv.triangles, (nt, 3), "<u4"), device="cuda")
+        return V, N, T
+
+    def mesh_download(self, nv, nt):
+        V = np.empty((nv, 3), np.float32)
+        N = np.empty((nv, 3), np.float32)
+        T = np.empty((nt, 3), np.uint32)
+        st = self.lib.gm_mesh_download(self.ctx, V.ctypes.data_as(C.c_void_p), N.ctypes.data_as(C.c_void_p),
+                                       T.ctypes.data_as(C.c_void_p), _stream())
+        self._check(st)
+        return V, N, T
+
+    # a17
+    def update(self, desc, h_X, h_R=None, global_scale=0.0, asymmetric=False, bilateral=True, mode=L.GM_REF):
+        """GMorpho::Update from host buffers (numpy arrays or pinned tensors)."""
+        o = L.UpdateOpts(1 if asymmetric else 0, 1 if bilateral else 0, mode)
+        nv = C.c_int64(0)
+        nt = C.c_int64(0)
+        hx = C.c_void_p(h_X.data_ptr()) if hasattr(h_X, "data_ptr") else h_X.ctypes.data_as(C.c_void_p)
+        hr = None
+        if h_R is not None:
+            hr = C.c_void_p(h_R.data_ptr()) if hasattr(h_R, "data_ptr") else h_R.ctypes.data_as(C.c_void_p)
+        st = self.lib.gm_update(self.ctx, C.byref(desc), hx, hr, float(global_scale), C.byref(o), C.byref(nv),
+                                C.byref(nt), _stream())
+        self._check(st)
+        return nv.value, nt.value
+
+    # a4
+    def pyramid(self, desc, grid, R=None, uniform_radius=4):
+        import torch
+        n = self.lib.gm_pyramid_texels(desc.res)
+        out = torch.empty(n, dtype=torch.int64, device=grid.device)
+        st = self.lib.gm_pyramid_build(self.ctx, C.byref(desc), _ptr(grid), _ptr(R), int(uniform_radius), _ptr(out),
+                                       _stream())
+        self._check(st)
+        return out
+
+    # a3
+    def scale_fill(self, R, value):
+        self._check(self.lib.gm_scalefield_fill(self.ctx, _ptr(R), R.numel(), int(value), _stream()))
+
+    def scale_brush(self, R, fine_res, bbox_min, cell_size, position, scale, support, global_scale, mode):
+        bm = (C.c_float * 3)(*bbox_min)
+        pos = (C.c_float * 3)(*position)
+        self._check(self.lib.gm_scalefield_brush(self.ctx, _ptr(R), fine_res, bm, float(cell_size), pos, float(scale),
+                                                 float(support), float(global_scale), int(mode), _stream()))
+
+    # a2
+    def voxelize(self, desc, P, T, out=None):
+        import torch
+        if out is None:
+            out = torch.zeros(desc.res ** 3, dtype=torch.uint8, device=P.device)
+        st = self.lib.gm_voxelize(self.ctx, C.byref(desc), _ptr(P), P.shape[0], _ptr(T), T.shape[0], _ptr(out),
+                                  _stream())
+        self._check(st)
+        return out
+
+    def zwords_to_packed(self, res, zw, out):
+        self._check(self.lib.gm_layout_zwords_to_packed(self.ctx, res, _ptr(zw), _ptr(out), _stream()))
+        return out
+
+    def packed_to_zwords(self, res, grid, out):
+        self._check(self.lib.gm_layout_packed_to_zwords(self.ctx, res, _ptr(grid), _ptr(out), _stream()))
+        return out

@@ -1,0 +1,512 @@
+// capi.cu — the extern "C" boundary of libgmorpho_gb300 (gmorpho_gb300.h).
+//
+// Validates arguments, owns cached device workspaces per context, turns
+// CUDA errors into gm_status codes (never aborts), and counts the kernels it
+// launches.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/gmorpho_gb300.h"
+#include "gm_common.cuh"
+#include "gm_internal.h"
+
+namespace gm {
+
+cudaEvent_t KernelCounter::start(cudaStream_t st) {
+  cudaEvent_t e;
+  if (!pool.empty()) {
+    e = pool.back();
+    pool.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    return nullptr;
+  }
+  cudaEventRecord(e, st);
+  return e;
+}
+
+void KernelCounter::stop(const char* name, cudaStream_t st, cudaEvent_t a) {
+  launches++;
+  if (!profiling || a == nullptr) return;
+  cudaEvent_t b;
+  if (!pool.empty()) {
+    b = pool.back();
+    pool.pop_back();
+  } else if (cudaEventCreate(&b) != cudaSuccess) {
+    pool.push_back(a);
+    return;
+  }
+  cudaEventRecord(b, st);
+  pending.push_back(Pending{name, a, b});
+  if (pending.size() > 4096) flush();
+}
+
+void KernelCounter::flush() {
+  for (const Pending& p : pending) {
+    cudaEventSynchronize(p.b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    auto& t = totals[p.name];
+    t.first += 1;
+    t.second += ms;
+    pool.push_back(p.a);
+    pool.push_back(p.b);
+  }
+  pending.clear();
+}
+
+void KernelCounter::release() {
+  flush();
+  for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  pool.clear();
+}
+
+}  // namespace gm
+
+struct gm_ctx {
+  int device = 0;
+  int num_sms = 152;
+  std::string last_error;
+  gm::KernelCounter kc;
+  // closing workspace
+  uint8_t* ws = nullptr;
+  size_t ws_bytes = 0;
+  // gm_update staging
+  uint8_t* d_X = nullptr;
+  size_t X_bytes = 0;
+  int8_t* d_R = nullptr;
+  size_t R_bytes = 0;
+  uint8_t* d_C = nullptr;
+  size_t C_bytes = 0;
+  int* d_int = nullptr;
+  // voxelizer scratch
+  uint8_t* vox = nullptr;
+  size_t vox_bytes = 0;
+  // last mesh
+  gm::MeshBuffers mesh;
+  int64_t nv = 0, nt = 0;
+  bool has_mesh = false;
+};
+
+namespace {
+
+gm_status fail(gm_ctx* ctx, gm_status s, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return s;
+}
+
+gm_status cuda_fail(gm_ctx* ctx, cudaError_t e, const char* where) {
+  const gm_status s = e == cudaErrorMemoryAllocation ? GM_ERR_OUT_OF_MEMORY : GM_ERR_CUDA;
+  return fail(ctx, s, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define GM_CHECK_CUDA(ctx, expr, where)              \
+  do {                                               \
+    cudaError_t e_ = (expr);                         \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, where); \
+  } while (0)
+
+bool pow2(int v) { return v > 0 && (v & (v - 1)) == 0; }
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+gm_status check_desc(gm_ctx* ctx, const gm_grid_desc* d) {
+  if (!d) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "grid descriptor is NULL");
+  if (!pow2(d->res) || d->res < 16 || d->res > 1024)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "res must be a power of two in [16, 1024], got " + std::to_string(d->res));
+  for (int a = 0; a < 3; a++)
+    if (d->data_res[a] < 0 || d->data_res[a] > d->res)
+      return fail(ctx, GM_ERR_INVALID_ARGUMENT, "data_res must lie in [0, res]");
+  return GM_OK;
+}
+
+gm_status ensure(gm_ctx* ctx, void** p, size_t& have, size_t need, const char* what) {
+  if (have >= need && *p) return GM_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  have = 0;
+  cudaError_t e = cudaMalloc(p, need);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(ctx, e == cudaErrorMemoryAllocation ? GM_ERR_OUT_OF_MEMORY : GM_ERR_CUDA,
+                std::string("allocating ") + what + " (" + std::to_string(need) + " bytes): " + cudaGetErrorString(e));
+  }
+  have = need;
+  return GM_OK;
+}
+
+gm_status set_device(gm_ctx* ctx) {
+  GM_CHECK_CUDA(ctx, cudaSetDevice(ctx->device), "cudaSetDevice");
+  return GM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gm_status_string(gm_status s) {
+  switch (s) {
+    case GM_OK: return "ok";
+    case GM_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GM_ERR_CUDA: return "CUDA error";
+    case GM_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case GM_ERR_UNSUPPORTED: return "unsupported";
+    case GM_ERR_CAPACITY: return "capacity exceeded";
+    case GM_ERR_NOT_READY: return "not ready";
+  }
+  return "unknown status";
+}
+
+int gm_abi_version(void) { return GM_ABI_VERSION; }
+
+gm_status gm_ctx_create(int device, gm_ctx** out) {
+  if (!out) return GM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) { cudaGetLastError(); return GM_ERR_CUDA; }
+  if (device < 0 || device >= n) return GM_ERR_INVALID_ARGUMENT;
+  gm_ctx* c = new gm_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) { delete c; return GM_ERR_CUDA; }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaMalloc(&c->d_int, 16 * sizeof(int)) != cudaSuccess) { delete c; return GM_ERR_OUT_OF_MEMORY; }
+  *out = c;
+  return GM_OK;
+}
+
+gm_status gm_ctx_destroy(gm_ctx* ctx) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  cudaFree(ctx->ws);
+  cudaFree(ctx->d_X);
+  cudaFree(ctx->d_R);
+  cudaFree(ctx->d_C);
+  cudaFree(ctx->d_int);
+  cudaFree(ctx->vox);
+  gm::MeshBuffers& b = ctx->mesh;
+  cudaFree(b.V); cudaFree(b.N); cudaFree(b.N2); cudaFree(b.T); cudaFree(b.adj); cudaFree(b.rowptr);
+  cudaFree(b.cursor); cudaFree(b.cell_voff); cudaFree(b.brick_tot); cudaFree(b.fix);
+  ctx->kc.release();
+  delete ctx;
+  return GM_OK;
+}
+
+const char* gm_ctx_last_error(const gm_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "NULL context"; }
+
+long long gm_ctx_kernel_launches(const gm_ctx* ctx) { return ctx ? ctx->kc.launches : -1; }
+
+gm_status gm_ctx_profile(gm_ctx* ctx, int32_t enable) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  ctx->kc.flush();
+  ctx->kc.profiling = enable != 0;
+  return GM_OK;
+}
+
+gm_status gm_ctx_profile_reset(gm_ctx* ctx) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  ctx->kc.flush();
+  ctx->kc.totals.clear();
+  return GM_OK;
+}
+
+int64_t gm_ctx_profile_read(gm_ctx* ctx, char* buf, int64_t cap) {
+  if (!ctx) return -1;
+  ctx->kc.flush();
+  std::string js = "{";
+  bool first = true;
+  for (const auto& kv : ctx->kc.totals) {
+    char tmp[256];
+    snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f}", first ? "" : ", ", kv.first.c_str(),
+             kv.second.first, kv.second.second);
+    js += tmp;
+    first = false;
+  }
+  js += "}";
+  const int64_t need = (int64_t)js.size() + 1;
+  if (buf && cap >= need) memcpy(buf, js.c_str(), (size_t)need);
+  return need;
+}
+
+// ------------------------------------------------------------------ a2
+
+gm_status gm_grid_attributes(const float* P, int64_t nv, int32_t base_res, float margin, gm_grid_desc* out) {
+  if (!P || nv <= 0 || !out || !pow2(base_res) || base_res < 16 || base_res > 1024) return GM_ERR_INVALID_ARGUMENT;
+  float mn[3] = {P[0], P[1], P[2]}, mx[3] = {P[0], P[1], P[2]};
+  for (int64_t i = 0; i < nv; i++)
+    for (int a = 0; a < 3; a++) {
+      const float v = P[3 * i + a];
+      if (v < mn[a]) mn[a] = v;
+      if (v > mx[a]) mx[a] = v;
+    }
+  const float ext = std::fmax(std::fabs(mx[0] - mn[0]), std::fmax(std::fabs(mx[1] - mn[1]), std::fabs(mx[2] - mn[2])));
+  const float thickness = ext / (float)base_res;
+  const float off = 2.f * thickness + margin;
+  for (int a = 0; a < 3; a++) { mn[a] -= off; mx[a] += off; }
+  const float c = std::fmax(std::fabs(mx[0] - mn[0]), std::fmax(std::fabs(mx[1] - mn[1]), std::fabs(mx[2] - mn[2]))) /
+                  (float)base_res;
+  for (int a = 0; a < 3; a++) {
+    out->bbox_min[a] = mn[a];
+    out->bbox_max[a] = mx[a];
+    out->data_res[a] = (int32_t)std::ceil((mx[a] - mn[a]) / c);
+    if (out->data_res[a] > base_res) out->data_res[a] = base_res;
+  }
+  out->res = base_res;
+  out->cell_size = c;
+  return GM_OK;
+}
+
+gm_status gm_voxelize(gm_ctx* ctx, const gm_grid_desc* desc, const float* d_points, int64_t num_points,
+                      const uint32_t* d_triangles, int64_t num_triangles, uint8_t* d_grid, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_grid || (num_triangles > 0 && (!d_points || !d_triangles)) || num_points < 0 || num_triangles < 0)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_voxelize: NULL buffer or negative count");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  if ((s = ensure(ctx, (void**)&ctx->vox, ctx->vox_bytes, gm::voxelize_scratch_bytes(desc->res), "voxelizer scratch")) !=
+      GM_OK)
+    return s;
+  GM_CHECK_CUDA(ctx,
+                gm::launch_voxelize(d_points, num_points, d_triangles, num_triangles, desc->res, desc->bbox_min,
+                                    desc->cell_size, d_grid, ctx->vox, (cudaStream_t)stream, &ctx->kc),
+                "gm_voxelize");
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ a3
+
+__global__ void k_fill_i8(int8_t* p, int64_t n, int8_t v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+gm_status gm_scalefield_fill(gm_ctx* ctx, int8_t* d_scale, int64_t n, int32_t value, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!d_scale || n < 0) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_scalefield_fill: bad buffer");
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  // cudaMemset stores the low byte of the value (GMorpho/ScaleField.cu:143-146)
+  GM_CHECK_CUDA(ctx, cudaMemsetAsync(d_scale, value & 0xff, (size_t)n, (cudaStream_t)stream), "gm_scalefield_fill");
+  return GM_OK;
+}
+
+gm_status gm_scalefield_brush(gm_ctx* ctx, int8_t* d_scale, int32_t fine_res, const float* bbox_min, float cell_size,
+                              const float* position, float scale, float support, float global_scale,
+                              gm_brush_mode mode, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!d_scale || !bbox_min || !position || fine_res <= 0 || !(cell_size > 0))
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_scalefield_brush: bad argument");
+  if (mode != GM_BRUSH_MAX && mode != GM_BRUSH_MIN && mode != GM_BRUSH_ZERO)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_scalefield_brush: unknown mode");
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  GM_CHECK_CUDA(ctx,
+                gm::launch_scale_brush(d_scale, fine_res, bbox_min, cell_size, position, scale, support, global_scale,
+                                       (int)mode, (cudaStream_t)stream, &ctx->kc),
+                "gm_scalefield_brush");
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ a4
+
+int64_t gm_pyramid_texels(int32_t res) {
+  if (!pow2(res)) return -1;
+  return (int64_t)gm::pyramid_texels(res);
+}
+
+gm_status gm_pyramid_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_grid, const int8_t* d_scale,
+                           int32_t uniform_radius, uint64_t* d_pyramid, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_grid || !d_pyramid) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_pyramid_build: NULL buffer");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  GM_CHECK_CUDA(ctx, gm::launch_pyramid(d_grid, d_scale, uniform_radius, desc->res, d_pyramid, (cudaStream_t)stream,
+                                        &ctx->kc),
+                "gm_pyramid_build");
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ a5..a11
+
+static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
+                            int32_t uniform_radius, int mode, int se, uint8_t* d_closing, uint8_t* d_dilation,
+                            uint8_t* d_contour, cudaStream_t st) {
+  gm_status s;
+  const int res = desc->res;
+  const int64_t fine = (int64_t)8 * res * res * res;
+  int rmax;
+  if (d_scale) {
+    GM_CHECK_CUDA(ctx, gm::launch_rmax(d_scale, fine, ctx->d_int, ctx->num_sms, st, &ctx->kc), "radius bound");
+    int h = 0;
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_int, sizeof(int), cudaMemcpyDeviceToHost, st), "radius bound");
+    GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "radius bound");
+    rmax = h;
+  } else {
+    rmax = gm::clamp_radius(uniform_radius);
+  }
+  if ((s = ensure(ctx, (void**)&ctx->ws, ctx->ws_bytes, gm::close_workspace_bytes(res), "closing workspace")) != GM_OK)
+    return s;
+  gm::CloseArgs a;
+  a.res = res;
+  for (int i = 0; i < 3; i++) a.data_res[i] = desc->data_res[i];
+  a.X = d_input;
+  a.R = d_scale;
+  a.uniform_r = uniform_radius;
+  a.rmax = rmax;
+  a.mode = mode;
+  a.se = se;
+  a.C_out = d_closing;
+  a.D_out = d_dilation;
+  a.S_out = d_contour;
+  a.workspace = ctx->ws;
+  a.num_sms = ctx->num_sms;
+  GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close");
+  return GM_OK;
+}
+
+gm_status gm_close(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
+                   int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, uint8_t* d_dilation,
+                   uint8_t* d_contour, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_input || !d_closing) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close: NULL input or output");
+  if (!aligned16(d_input) || (d_scale && !aligned16(d_scale)))
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close: device buffers must be 16-byte aligned");
+  if (mode != GM_REF && mode != GM_EXACT) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close: unknown mode");
+  if (se != GM_SE_SPHERE && se != GM_SE_CUBE) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close: unknown se");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  return close_impl(ctx, desc, d_input, d_scale, uniform_radius, (int)mode, (int)se, d_closing, d_dilation, d_contour,
+                    (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------------ a12..a16
+
+static gm_status mesh_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closing, int iters,
+                           cudaStream_t st) {
+  gm::MeshArgs a;
+  a.res = desc->res;
+  a.C = d_closing;
+  for (int i = 0; i < 3; i++) a.bbox_min[i] = desc->bbox_min[i];
+  a.cell_size = desc->cell_size;
+  a.isovalue = 0.95f;  // GMorpho.cu:6922
+  a.bilateral_iters = iters;
+  a.num_sms = ctx->num_sms;
+  int64_t nv = 0, nt = 0;
+  ctx->has_mesh = false;
+  GM_CHECK_CUDA(ctx, gm::mesh_count(a, ctx->mesh, st, &ctx->kc, &nv, &nt), "gm_mesh (count)");
+  if (nv > 0xfffffff0LL || nt > 0x7ffffff0LL)
+    return fail(ctx, GM_ERR_CAPACITY, "gm_mesh: mesh exceeds 32-bit vertex/triangle indexing");
+  GM_CHECK_CUDA(ctx, gm::mesh_emit(a, ctx->mesh, nv, nt, st, &ctx->kc), "gm_mesh (emit)");
+  ctx->nv = nv;
+  ctx->nt = nt;
+  ctx->has_mesh = true;
+  return GM_OK;
+}
+
+gm_status gm_mesh(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closing, int32_t bilateral_iters,
+                  gm_mesh_view* out, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_closing || !out || bilateral_iters < 0)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh: NULL buffer or negative iteration count");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  if ((s = mesh_impl(ctx, desc, d_closing, bilateral_iters, (cudaStream_t)stream)) != GM_OK) return s;
+  out->vertices = ctx->mesh.V;
+  out->normals = ctx->mesh.N;
+  out->triangles = ctx->mesh.T;
+  out->num_vertices = ctx->nv;
+  out->num_triangles = ctx->nt;
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ a17
+
+gm_status gm_update(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_input, const int8_t* h_scale,
+                    float global_scale, const gm_update_opts* opts, int64_t* num_vertices, int64_t* num_triangles,
+                    void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!h_input) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_update: NULL input grid");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int res = desc->res;
+  const size_t cells = (size_t)res * res * res;
+  const int asym = opts ? opts->use_asymmetric_closing : 0;
+  const int bil = opts ? opts->bilateral_filtering : 1;
+  const int mode = opts ? opts->mode : GM_REF;
+  if ((s = ensure(ctx, (void**)&ctx->d_X, ctx->X_bytes, cells, "input grid")) != GM_OK) return s;
+  if ((s = ensure(ctx, (void**)&ctx->d_C, ctx->C_bytes, cells, "closing grid")) != GM_OK) return s;
+  GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_X, h_input, cells, cudaMemcpyHostToDevice, st), "gm_update H2D");
+  const int8_t* d_scale = nullptr;
+  if (h_scale) {
+    if ((s = ensure(ctx, (void**)&ctx->d_R, ctx->R_bytes, 8 * cells, "scale grid")) != GM_OK) return s;
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_R, h_scale, 8 * cells, cudaMemcpyHostToDevice, st), "gm_update H2D");
+    d_scale = ctx->d_R;
+  }
+  // uniform radius in fine voxels: floor(global_scale / (cell_size / 2))
+  // (GMorpho/ScaleField.cu:143-146 with cell_size_sf = cell_size / 2)
+  const float gate = std::floor(2.f * global_scale / desc->cell_size);
+  const int uniform = (int)std::floor(global_scale / (0.5f * desc->cell_size));
+  if (gate > 1.f) {
+    s = close_impl(ctx, desc, ctx->d_X, d_scale, uniform, mode, asym ? GM_SE_CUBE : GM_SE_SPHERE, ctx->d_C, nullptr,
+                   nullptr, st);
+    if (s != GM_OK) return s;
+  } else {
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_C, ctx->d_X, cells, cudaMemcpyDeviceToDevice, st), "gm_update copy");
+  }
+  const int iters = bil ? (asym ? 200 : 20) : 0;  // GMorpho.cu:7808-7811
+  if ((s = mesh_impl(ctx, desc, ctx->d_C, iters, st)) != GM_OK) return s;
+  if (num_vertices) *num_vertices = ctx->nv;
+  if (num_triangles) *num_triangles = ctx->nt;
+  return GM_OK;
+}
+
+gm_status gm_mesh_download(gm_ctx* ctx, float* h_V, float* h_N, uint32_t* h_T, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!ctx->has_mesh) return fail(ctx, GM_ERR_NOT_READY, "gm_mesh_download: no mesh on this context");
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (h_V && ctx->nv)
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(h_V, ctx->mesh.V, 12 * (size_t)ctx->nv, cudaMemcpyDeviceToHost, st), "D2H");
+  if (h_N && ctx->nv)
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(h_N, ctx->mesh.N, 12 * (size_t)ctx->nv, cudaMemcpyDeviceToHost, st), "D2H");
+  if (h_T && ctx->nt)
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(h_T, ctx->mesh.T, 12 * (size_t)ctx->nt, cudaMemcpyDeviceToHost, st), "D2H");
+  GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "gm_mesh_download");
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ layout
+
+gm_status gm_layout_zwords_to_packed(gm_ctx* ctx, int32_t res, const uint32_t* d_zwords, uint8_t* d_grid,
+                                     void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!pow2(res) || res < 16 || res > 1024 || !d_zwords || !d_grid)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_layout_zwords_to_packed: bad argument");
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  GM_CHECK_CUDA(ctx, gm::launch_layout(res, d_zwords, d_grid, 0, (cudaStream_t)stream, &ctx->kc), "layout");
+  return GM_OK;
+}
+
+gm_status gm_layout_packed_to_zwords(gm_ctx* ctx, int32_t res, const uint8_t* d_grid, uint32_t* d_zwords,
+                                     void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!pow2(res) || res < 16 || res > 1024 || !d_zwords || !d_grid)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_layout_packed_to_zwords: bad argument");
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  GM_CHECK_CUDA(ctx, gm::launch_layout(res, d_zwords, const_cast<uint8_t*>(d_grid), 1, (cudaStream_t)stream, &ctx->kc),
+                "layout");
+  return GM_OK;
+}
+
+}  // extern "C"

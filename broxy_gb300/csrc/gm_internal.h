@@ -1,0 +1,116 @@
+// gm_internal.h — launch interfaces shared by the .cu translation units of
+// libgmorpho_gb300 (not part of the public C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+namespace gm {
+
+// Counts the kernels this library launches (reported by the C ABI so that a
+// caller can see that the CUDA path ran) and, when profiling is on, times
+// every launch with a pair of CUDA events recorded on its own stream.
+struct KernelCounter {
+  long long launches = 0;
+  bool profiling = false;
+  struct Pending {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> pool;
+  std::map<std::string, std::pair<long long, double>> totals;  // name -> (launches, ms)
+
+  cudaEvent_t start(cudaStream_t st);
+  void stop(const char* name, cudaStream_t st, cudaEvent_t a);
+  void flush();    // waits for the pending events and accumulates
+  void release();  // destroys the event pool
+};
+
+#define GM_LAUNCH(kc, name, st, ...)                               \
+  do {                                                             \
+    cudaEvent_t gm_ev0_ = nullptr;                                 \
+    if ((kc) != nullptr && (kc)->profiling) gm_ev0_ = (kc)->start(st); \
+    __VA_ARGS__;                                                   \
+    if ((kc) != nullptr) (kc)->stop(name, st, gm_ev0_);            \
+  } while (0)
+
+struct CloseArgs {
+  int res;            // base resolution (power of two, >= 16)
+  int data_res[3];    // cells with data (GMorpho/Voxelizer.cu:453-454)
+  const uint8_t* X;   // input packed grid, res^3
+  const int8_t* R;    // fine radius grid (2res)^3, or nullptr for uniform_r
+  int uniform_r;      // radius when R == nullptr
+  int rmax;           // upper bound of the clamped radius over the grid
+  int mode;           // 0 = GM_REF, 1 = GM_EXACT
+  int se;             // 0 = sphere dilation, 1 = cube dilation
+  uint8_t* C_out;     // closing, res^3
+  uint8_t* D_out;     // optional dilation, res^3
+  uint8_t* S_out;     // optional dilation contour, res^3
+  uint8_t* workspace; // close_workspace_bytes(res)
+  int num_sms;
+};
+
+size_t close_workspace_bytes(int res);
+cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
+cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc);
+
+// ---------------------------------------------------------------- pyramid
+size_t pyramid_texels(int res);
+cudaError_t launch_pyramid(const uint8_t* grid, const int8_t* R, int uniform_r, int res, uint64_t* pyr,
+                           cudaStream_t st, KernelCounter* kc);
+
+// ---------------------------------------------------------------- mesh
+struct MeshArgs {
+  int res;
+  const uint8_t* C;     // closed grid
+  float bbox_min[3];
+  float cell_size;      // base cell size (fine = cell_size / 2)
+  float isovalue;       // 0.95 in the reference (GMorpho.cu:6922)
+  int bilateral_iters;  // 20 / 200 / 0
+  int num_sms;
+};
+
+// Device-side mesh buffers, grown on demand by the caller of launch_mesh.
+struct MeshBuffers {
+  float* V = nullptr;       // 3 * v_cap
+  float* N = nullptr;       // 3 * v_cap
+  float* N2 = nullptr;      // 3 * v_cap (bilateral ping-pong)
+  uint32_t* T = nullptr;    // 3 * t_cap
+  uint32_t* adj = nullptr;  // 3 * t_cap (vertex -> corner list)
+  uint32_t* rowptr = nullptr;  // v_cap + 1
+  uint32_t* cursor = nullptr;  // v_cap
+  int64_t v_cap = 0, t_cap = 0;
+  // per-cell / per-brick scratch
+  uint32_t* cell_voff = nullptr;  // res^3
+  uint32_t* brick_tot = nullptr;  // 3 * (bricks + 1)
+  uint32_t* fix = nullptr;        // case-91 fix list: 1 + 4 * fix_cap
+  int64_t cells_cap = 0, bricks_cap = 0;
+  int fix_cap = 0;
+};
+
+// Phase 1: counts (host-synchronous: returns the vertex/triangle totals).
+cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc, int64_t* nv,
+                       int64_t* nt);
+// Phase 2: emission into b (capacities must be >= counts).
+cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt, cudaStream_t st,
+                      KernelCounter* kc);
+
+// ---------------------------------------------------------------- scale field
+cudaError_t launch_scale_brush(int8_t* R, int n, const float* bbox_min, float cell_size, const float* pos,
+                               float scale, float support, float global_scale, int mode, cudaStream_t st,
+                               KernelCounter* kc);
+
+// ---------------------------------------------------------------- voxelizer
+cudaError_t launch_voxelize(const float* P, int64_t nv, const uint32_t* T, int64_t nf, int res,
+                            const float* bbox_min, float cell_size, uint8_t* grid, uint8_t* scratch_fine,
+                            cudaStream_t st, KernelCounter* kc);
+size_t voxelize_scratch_bytes(int res);
+// dir 0: z-words -> packed grid; dir 1: packed grid -> z-words
+cudaError_t launch_layout(int res, const uint32_t* zw, uint8_t* grid, int dir, cudaStream_t st, KernelCounter* kc);
+
+}  // namespace gm

@@ -1,0 +1,643 @@
+// mc.cu — contour marching cubes and mesh normals (reference rows a12..a16:
+// Grid::ComputeContourMCM, ComputeMCMData/CompactMCMData, SplatIndices/
+// BuildNeighbors, MarchingCubesMesher::createMesh3D, ComputeMeshNormals,
+// BilateralMeshFiltering; GMorpho/Grid.cu:1329-1462, 1873-1973,
+// GMorpho/GMorpho.cu:6109-6496, 6498-6620, 6814-7001,
+// GMorpho/MarchingCubesMesher.cu:1297-1618).
+//
+// Emission order equals the reference's: base cells in Morton order (the
+// reference sorts its contour list by 30-bit Morton code), eight sub-cubes
+// per cell in child order, non-empty cubes compacted, owned edges 0, 3, 8
+// numbered in that order.  Instead of a sort, cells are visited directly in
+// Morton order: a 16^3 brick of cells is one contiguous 4096-code Morton
+// range, so one block per brick with an in-block scan and a scan of the
+// brick totals gives every cell its output offsets.  Instead of the 4V-byte
+// splat map, a neighbour cube's vertex offset is its cell's offset (one u32
+// per cell) plus an in-cell prefix recomputed from the grid.
+#include "gm_common.cuh"
+#include "gm_internal.h"
+#include "mc_tables.inc"
+
+namespace gm {
+
+__constant__ uint64_t c_tri_packed[256] = GM_MC_TRI_PACKED_INIT;
+__constant__ uint8_t c_tri_count[256] = GM_MC_TRI_COUNT_INIT;
+__constant__ uint8_t c_tri_len[256] = GM_MC_TRI_LEN_INIT;
+
+// Edge mask of an MC cube value, derived from the corner order v0..v7 =
+// 000,100,110,010,001,101,111,011 and the edge list (0,1)(1,2)(2,3)(3,0)
+// (4,5)(5,6)(6,7)(7,4)(0,4)(1,5)(2,6)(3,7).
+__device__ __forceinline__ int edge_mask(int v) {
+  const int x = v ^ (v >> 1);
+  const int e3 = (v ^ (v >> 3)) & 1;
+  const int e7 = ((v >> 7) ^ (v >> 4)) & 1;
+  return (x & 7) | (e3 << 3) | (((x >> 4) & 7) << 4) | (e7 << 7) | (((v ^ (v >> 4)) & 0xF) << 8);
+}
+__device__ __forceinline__ int nv_owned(int em) { return (em & 1) + ((em >> 3) & 1) + ((em >> 8) & 1); }
+
+constexpr int kBrick = 16;               // cells per brick edge
+constexpr int kTileE = kBrick + 2;       // tile edge (halo 2 for neighbour cells)
+constexpr int kTileCells = kTileE * kTileE * kTileE;
+constexpr int kCellsPerBrick = kBrick * kBrick * kBrick;
+constexpr int kMcThreads = 256;
+constexpr int kCellsPerThread = kCellsPerBrick / kMcThreads;
+
+__device__ __forceinline__ void brick_origin(int b, int& ox, int& oy, int& oz) {
+  ox = (int)gather_bits3((uint32_t)b) * kBrick;
+  oy = (int)gather_bits3((uint32_t)b >> 1) * kBrick;
+  oz = (int)gather_bits3((uint32_t)b >> 2) * kBrick;
+}
+
+__device__ void load_tile(const uint8_t* __restrict__ C, int res, int ox, int oy, int oz, uint8_t* tile) {
+  for (int i = threadIdx.x; i < kTileCells; i += blockDim.x) {
+    const int lx = i % kTileE, ly = (i / kTileE) % kTileE, lz = i / (kTileE * kTileE);
+    const int x = ox + lx, y = oy + ly, z = oz + lz;
+    tile[i] = (x < res && y < res && z < res) ? C[cell_index(x, y, z, res)] : (uint8_t)0;
+  }
+}
+
+// The eight MC cube values of cell (local lx,ly,lz): cube k has its min
+// corner at fine voxel 2c + o_k; value bit j = occupancy of corner j
+// (ComputeMCMData, GMorpho.cu:6146-6232).
+__device__ __forceinline__ void cube_values(const uint8_t* tile, int lx, int ly, int lz, int vals[8]) {
+  uint32_t b27 = 0;
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const uint8_t cell = tile[(lx + (i >> 1)) + kTileE * (ly + (j >> 1)) + kTileE * kTileE * (lz + (k >> 1))];
+        const uint32_t bit = (cell >> ((i & 1) + 2 * (j & 1) + 4 * (k & 1))) & 1u;
+        b27 |= bit << (i + 3 * j + 9 * k);
+      }
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    const int ox = s & 1, oy = (s >> 1) & 1, oz = s >> 2;
+    const int b = ox + 3 * oy + 9 * oz;
+    // corners 000,100,110,010,001,101,111,011 -> offsets in the 27-cube
+    int v = 0;
+    v |= ((b27 >> (b + 0)) & 1) << 0;
+    v |= ((b27 >> (b + 1)) & 1) << 1;
+    v |= ((b27 >> (b + 4)) & 1) << 2;
+    v |= ((b27 >> (b + 3)) & 1) << 3;
+    v |= ((b27 >> (b + 9)) & 1) << 4;
+    v |= ((b27 >> (b + 10)) & 1) << 5;
+    v |= ((b27 >> (b + 13)) & 1) << 6;
+    v |= ((b27 >> (b + 12)) & 1) << 7;
+    vals[s] = v;
+  }
+}
+
+// mixed-cube mask of a cell; cells outside [1, res-2]^3 are never tagged
+// (TagVoxelsContourMCM, Grid.cu:1334-1340).
+__device__ __forceinline__ int mixed_mask(const int vals[8], int gx, int gy, int gz, int res) {
+  if (gx < 1 || gy < 1 || gz < 1 || gx > res - 2 || gy > res - 2 || gz > res - 2) return 0;
+  int m = 0;
+#pragma unroll
+  for (int s = 0; s < 8; s++) m |= (vals[s] != 0 && vals[s] != 255) ? (1 << s) : 0;
+  return m;
+}
+
+struct CellCounts {
+  uint32_t cubes, verts, tris, n91;
+};
+
+__device__ __forceinline__ CellCounts cell_counts(const int vals[8], int mask) {
+  CellCounts c{0, 0, 0, 0};
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    if (!((mask >> s) & 1)) continue;
+    c.cubes += 1;
+    c.verts += nv_owned(edge_mask(vals[s]));
+    c.tris += c_tri_count[vals[s]];
+    c.n91 += c_tri_len[vals[s]] > c_tri_count[vals[s]] ? 1 : 0;
+  }
+  return c;
+}
+
+__device__ __forceinline__ void local_coords(int l, int& lx, int& ly, int& lz) {
+  lx = (int)gather_bits3((uint32_t)l);
+  ly = (int)gather_bits3((uint32_t)l >> 1);
+  lz = (int)gather_bits3((uint32_t)l >> 2);
+}
+
+// block-wide exclusive scan of 4 counters (256 threads)
+__device__ __forceinline__ CellCounts block_exclusive_scan(CellCounts v, CellCounts& total) {
+  __shared__ uint32_t warp_tot[4][kMcThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t a[4] = {v.cubes, v.verts, v.tris, v.n91};
+  uint32_t inc[4];
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    uint32_t x = a[c];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    inc[c] = x;
+    if (lane == 31) warp_tot[c][wid] = x;
+  }
+  __syncthreads();
+  uint32_t wpre[4] = {0, 0, 0, 0}, tot[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int c = 0; c < 4; c++)
+    for (int w = 0; w < kMcThreads / 32; w++) {
+      if (w < wid) wpre[c] += warp_tot[c][w];
+      tot[c] += warp_tot[c][w];
+    }
+  __syncthreads();
+  total = CellCounts{tot[0], tot[1], tot[2], tot[3]};
+  return CellCounts{wpre[0] + inc[0] - a[0], wpre[1] + inc[1] - a[1], wpre[2] + inc[2] - a[2],
+                    wpre[3] + inc[3] - a[3]};
+}
+
+__global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, int res,
+                                                          uint32_t* __restrict__ brick_tot) {
+  __shared__ uint8_t tile[kTileCells];
+  int ox, oy, oz;
+  brick_origin(blockIdx.x, ox, oy, oz);
+  load_tile(C, res, ox, oy, oz, tile);
+  __syncthreads();
+  CellCounts acc{0, 0, 0, 0};
+  for (int i = 0; i < kCellsPerThread; i++) {
+    const int l = threadIdx.x * kCellsPerThread + i;
+    int lx, ly, lz;
+    local_coords(l, lx, ly, lz);
+    int vals[8];
+    cube_values(tile, lx, ly, lz, vals);
+    const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
+    if (!m) continue;
+    const CellCounts c = cell_counts(vals, m);
+    acc.cubes += c.cubes; acc.verts += c.verts; acc.tris += c.tris; acc.n91 += c.n91;
+  }
+  CellCounts tot;
+  block_exclusive_scan(acc, tot);
+  if (threadIdx.x == 0) {
+    brick_tot[4 * blockIdx.x + 0] = tot.cubes;
+    brick_tot[4 * blockIdx.x + 1] = tot.verts;
+    brick_tot[4 * blockIdx.x + 2] = tot.tris;
+    brick_tot[4 * blockIdx.x + 3] = tot.n91;
+  }
+}
+
+// exclusive scan of the brick totals, in place; totals at index nb.
+__global__ void __launch_bounds__(1024) k_scan_bricks(uint32_t* __restrict__ bt, int nb) {
+  __shared__ uint32_t part[4][1024];
+  const int t = threadIdx.x;
+  const int per = (nb + 1023) / 1024;
+  const int b0 = t * per, b1 = min(nb, b0 + per);
+  uint32_t s[4] = {0, 0, 0, 0};
+  for (int b = b0; b < b1; b++)
+    for (int c = 0; c < 4; c++) s[c] += bt[4 * b + c];
+  for (int c = 0; c < 4; c++) part[c][t] = s[c];
+  __syncthreads();
+  // Hillis-Steele over 1024 partial sums
+  for (int o = 1; o < 1024; o <<= 1) {
+    uint32_t v[4];
+    for (int c = 0; c < 4; c++) v[c] = t >= o ? part[c][t - o] : 0;
+    __syncthreads();
+    for (int c = 0; c < 4; c++) part[c][t] += v[c];
+    __syncthreads();
+  }
+  uint32_t run[4];
+  for (int c = 0; c < 4; c++) run[c] = part[c][t] - s[c];
+  for (int b = b0; b < b1; b++)
+    for (int c = 0; c < 4; c++) {
+      const uint32_t v = bt[4 * b + c];
+      bt[4 * b + c] = run[c];
+      run[c] += v;
+    }
+  if (t == 1023)
+    for (int c = 0; c < 4; c++) bt[4 * nb + c] = part[c][1023];
+}
+
+// Float expressions of findIntersection (MarchingCubesMesher.cu:98-100) with
+// the corner point minC + idx * cellSize (MarchingCubesMesher.cu:1329-1331),
+// evaluated with explicit rounding so that host and device agree bit for bit.
+__device__ __forceinline__ float lerp_coord(float p1, float p2, float v1, float v2, float iso) {
+  const float t = __fsub_rn(iso, v1);
+  return __fadd_rn(p1, __fdiv_rn(__fmul_rn(t, __fsub_rn(p2, p1)), __fsub_rn(v2, v1)));
+}
+
+__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, int res,
+                                                             const uint32_t* __restrict__ brick_off,
+                                                             uint32_t* __restrict__ cell_voff,
+                                                             float* __restrict__ V, float bx, float by, float bz,
+                                                             float cs, float iso) {
+  __shared__ uint8_t tile[kTileCells];
+  int ox, oy, oz;
+  brick_origin(blockIdx.x, ox, oy, oz);
+  load_tile(C, res, ox, oy, oz, tile);
+  __syncthreads();
+  CellCounts acc{0, 0, 0, 0};
+  for (int i = 0; i < kCellsPerThread; i++) {
+    const int l = threadIdx.x * kCellsPerThread + i;
+    int lx, ly, lz;
+    local_coords(l, lx, ly, lz);
+    int vals[8];
+    cube_values(tile, lx, ly, lz, vals);
+    const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
+    if (!m) continue;
+    const CellCounts c = cell_counts(vals, m);
+    acc.verts += c.verts;
+  }
+  CellCounts tot;
+  const CellCounts pre = block_exclusive_scan(acc, tot);
+  uint32_t vo = brick_off[4 * blockIdx.x + 1] + pre.verts;
+  for (int i = 0; i < kCellsPerThread; i++) {
+    const int l = threadIdx.x * kCellsPerThread + i;
+    int lx, ly, lz;
+    local_coords(l, lx, ly, lz);
+    int vals[8];
+    cube_values(tile, lx, ly, lz, vals);
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    const int m = mixed_mask(vals, gx, gy, gz, res);
+    if (!m) continue;
+    cell_voff[cell_index(gx, gy, gz, res)] = vo;
+    for (int s = 0; s < 8; s++) {
+      if (!((m >> s) & 1)) continue;
+      const int v = vals[s];
+      const int em = edge_mask(v);
+      const int fx = 2 * gx + (s & 1), fy = 2 * gy + ((s >> 1) & 1), fz = 2 * gz + (s >> 2);
+      const float px = __fmaf_rn((float)fx, cs, bx);
+      const float py = __fmaf_rn((float)fy, cs, by);
+      const float pz = __fmaf_rn((float)fz, cs, bz);
+      const float v0 = (v & 1) ? 1.f : 0.f, v1 = (v & 2) ? 1.f : 0.f, v3 = (v & 8) ? 1.f : 0.f,
+                  v4 = (v & 16) ? 1.f : 0.f;
+      if (em & 1) {  // edge 0: point -> point + (cs,0,0)
+        float* o = V + 3 * (size_t)vo;
+        o[0] = lerp_coord(px, __fadd_rn(px, cs), v0, v1, iso);
+        o[1] = lerp_coord(py, py, v0, v1, iso);
+        o[2] = lerp_coord(pz, pz, v0, v1, iso);
+        vo++;
+      }
+      if (em & 8) {  // edge 3: point + (0,cs,0) -> point
+        const float p1y = __fadd_rn(py, cs);
+        float* o = V + 3 * (size_t)vo;
+        o[0] = lerp_coord(px, px, v3, v0, iso);
+        o[1] = lerp_coord(p1y, py, v3, v0, iso);
+        o[2] = lerp_coord(pz, pz, v3, v0, iso);
+        vo++;
+      }
+      if (em & 256) {  // edge 8: point -> point + (0,0,cs)
+        float* o = V + 3 * (size_t)vo;
+        o[0] = lerp_coord(px, px, v0, v4, iso);
+        o[1] = lerp_coord(py, py, v0, v4, iso);
+        o[2] = lerp_coord(pz, __fadd_rn(pz, cs), v0, v4, iso);
+        vo++;
+      }
+    }
+  }
+}
+
+// vertex offset of the cube at fine min corner (fx,fy,fz) and its edge
+// mask, or -1 when the cube is not in the compacted list.  The cell must lie
+// in the block tile (local coordinates 0..16).
+__device__ __forceinline__ long long cube_voff(const uint8_t* tile, const uint32_t* __restrict__ cell_voff,
+                                               int res, int ox, int oy, int oz, int fx, int fy, int fz, int& em) {
+  const int gx = fx >> 1, gy = fy >> 1, gz = fz >> 1;
+  const int k = (fx & 1) | ((fy & 1) << 1) | ((fz & 1) << 2);
+  int vals[8];
+  cube_values(tile, gx - ox, gy - oy, gz - oz, vals);
+  const int m = mixed_mask(vals, gx, gy, gz, res);
+  if (!((m >> k) & 1)) { em = 0; return -1; }
+  uint32_t off = cell_voff[cell_index(gx, gy, gz, res)];
+  for (int s = 0; s < k; s++)
+    if ((m >> s) & 1) off += nv_owned(edge_mask(vals[s]));
+  em = edge_mask(vals[k]);
+  return (long long)off;
+}
+
+__global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __restrict__ C, int res,
+                                                              const uint32_t* __restrict__ brick_off,
+                                                              const uint32_t* __restrict__ cell_voff,
+                                                              uint32_t* __restrict__ T, uint32_t nt_total,
+                                                              uint32_t* __restrict__ fix, int fix_cap) {
+  __shared__ uint8_t tile[kTileCells];
+  int ox, oy, oz;
+  brick_origin(blockIdx.x, ox, oy, oz);
+  load_tile(C, res, ox, oy, oz, tile);
+  __syncthreads();
+  CellCounts acc{0, 0, 0, 0};
+  for (int i = 0; i < kCellsPerThread; i++) {
+    const int l = threadIdx.x * kCellsPerThread + i;
+    int lx, ly, lz;
+    local_coords(l, lx, ly, lz);
+    int vals[8];
+    cube_values(tile, lx, ly, lz, vals);
+    const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
+    if (!m) continue;
+    acc.tris += cell_counts(vals, m).tris;
+  }
+  CellCounts tot;
+  const CellCounts pre = block_exclusive_scan(acc, tot);
+  uint32_t to = brick_off[4 * blockIdx.x + 2] + pre.tris;
+  for (int i = 0; i < kCellsPerThread; i++) {
+    const int l = threadIdx.x * kCellsPerThread + i;
+    int lx, ly, lz;
+    local_coords(l, lx, ly, lz);
+    int vals[8];
+    cube_values(tile, lx, ly, lz, vals);
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    const int m = mixed_mask(vals, gx, gy, gz, res);
+    if (!m) continue;
+    uint32_t vo = cell_voff[cell_index(gx, gy, gz, res)];
+    for (int s = 0; s < 8; s++) {
+      if (!((m >> s) & 1)) continue;
+      const int v = vals[s];
+      const int em = edge_mask(v);
+      const int fx = 2 * gx + (s & 1), fy = 2 * gy + ((s >> 1) & 1), fz = 2 * gz + (s >> 2);
+      uint32_t vert[12];
+#pragma unroll
+      for (int e = 0; e < 12; e++) vert[e] = 0;
+      {
+        uint32_t ind = 0;
+        if (em & 1) vert[0] = vo + ind++;
+        if (em & 8) vert[3] = vo + ind++;
+        if (em & 256) vert[8] = vo + ind++;
+        vo += ind;
+      }
+      // neighbour cubes +x, +x+y, +y, +z, +x+z, +y+z (BuildNeighbors order,
+      // GMorpho.cu:6480-6487) and the edges they own
+      // (MarchingCubesMesher.cu:1392-1456)
+      int e1, e2, e3, e4, e5, e7;
+      const long long id1 = (em & (2 | 512)) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx + 1, fy, fz, e1) : -1;
+      const long long id2 = (em & 1024) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx + 1, fy + 1, fz, e2) : -1;
+      const long long id3 = (em & (4 | 2048)) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx, fy + 1, fz, e3) : -1;
+      const long long id4 = (em & (16 | 128)) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx, fy, fz + 1, e4) : -1;
+      const long long id5 = (em & 32) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx + 1, fy, fz + 1, e5) : -1;
+      const long long id7 = (em & 64) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx, fy + 1, fz + 1, e7) : -1;
+      if ((em & 2) && id1 >= 0) vert[1] = (uint32_t)id1 + (e1 & 1);
+      if (em & 4) vert[2] = id3 >= 0 ? (uint32_t)id3 : 0u;
+      if (em & 16) vert[4] = id4 >= 0 ? (uint32_t)id4 : 0u;
+      if ((em & 32) && id5 >= 0) vert[5] = (uint32_t)id5 + (e5 & 1);
+      if (em & 64) vert[6] = id7 >= 0 ? (uint32_t)id7 : 0u;
+      if ((em & 128) && id4 >= 0) vert[7] = (uint32_t)id4 + (e4 & 1);
+      if (em & 512) vert[9] = id1 >= 0 ? (uint32_t)id1 + (e1 & 1) + ((e1 >> 3) & 1) : 0u;
+      if (em & 1024) vert[10] = id2 >= 0 ? (uint32_t)id2 + (e2 & 1) + ((e2 >> 3) & 1) : 0u;
+      if (em & 2048) vert[11] = id3 >= 0 ? (uint32_t)id3 + (e3 & 1) + ((e3 >> 3) & 1) : 0u;
+      // reversed winding (MarchingCubesMesher.cu:1487-1497)
+      const uint64_t tl = c_tri_packed[v];
+      const int cnt = c_tri_count[v];
+      for (int t = 0; t < cnt; t++) {
+        uint32_t* o = T + 3 * (size_t)(to + t);
+        o[0] = vert[(tl >> (4 * (3 * t + 2))) & 0xf];
+        o[1] = vert[(tl >> (4 * (3 * t + 1))) & 0xf];
+        o[2] = vert[(tl >> (4 * (3 * t))) & 0xf];
+      }
+      if (c_tri_len[v] > cnt) {
+        // Case 91: the reference writes one more triangle than its slot
+        // count; it lands on the next slot (the next cube's first triangle)
+        // and, written later, wins; past the end it is dropped.
+        const uint32_t slot = to + cnt;
+        if (slot < nt_total) {
+          const int idx = (int)atomicAdd(fix, 1u);
+          if (idx < fix_cap) {
+            uint32_t* f = fix + 1 + 4 * idx;
+            f[0] = slot;
+            f[1] = vert[(tl >> (4 * (3 * cnt + 2))) & 0xf];
+            f[2] = vert[(tl >> (4 * (3 * cnt + 1))) & 0xf];
+            f[3] = vert[(tl >> (4 * (3 * cnt))) & 0xf];
+          }
+        }
+      }
+      to += cnt;
+    }
+  }
+}
+
+__global__ void k_mc_fix91(const uint32_t* __restrict__ fix, int fix_cap, uint32_t* __restrict__ T) {
+  const int n = min((int)fix[0], fix_cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t* f = fix + 1 + 4 * i;
+    uint32_t* o = T + 3 * (size_t)f[0];
+    o[0] = f[1]; o[1] = f[2]; o[2] = f[3];
+  }
+}
+
+// ------------------------------------------------------------------ normals
+
+__global__ void k_adj_count(const uint32_t* __restrict__ T, int64_t nt, uint32_t* __restrict__ cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nt; i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(cnt + T[i], 1u);
+}
+
+// exclusive scan of n u32 (single block, chunked) -> out[0..n]
+__global__ void __launch_bounds__(1024) k_scan_u32(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                    int64_t n) {
+  __shared__ uint32_t part[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (n + 1023) / 1024;
+  const int64_t b0 = t * per, b1 = min(n, b0 + per);
+  uint32_t s = 0;
+  for (int64_t b = b0; b < b1; b++) s += in[b];
+  part[t] = s;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const uint32_t v = t >= o ? part[t - o] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - s;
+  for (int64_t b = b0; b < b1; b++) {
+    const uint32_t v = in[b];
+    out[b] = run;
+    run += v;
+  }
+  if (t == 1023) out[n] = part[1023];
+}
+
+__global__ void k_adj_fill(const uint32_t* __restrict__ T, int64_t nt, const uint32_t* __restrict__ rowptr,
+                           uint32_t* __restrict__ cursor, uint32_t* __restrict__ adj) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nt; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = T[i];
+    const uint32_t slot = atomicAdd(cursor + v, 1u);
+    adj[rowptr[v] + slot] = (uint32_t)i;  // corner id = 3 t + role
+  }
+}
+
+__global__ void k_adj_sort(const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj, int64_t nv) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t b = rowptr[v], e = rowptr[v + 1];
+    for (uint32_t i = b + 1; i < e; i++) {
+      const uint32_t key = adj[i];
+      uint32_t j = i;
+      while (j > b && adj[j - 1] > key) { adj[j] = adj[j - 1]; j--; }
+      adj[j] = key;
+    }
+  }
+}
+
+__device__ __forceinline__ float3 ld3(const float* p, uint32_t i) {
+  return make_float3(p[3 * (size_t)i], p[3 * (size_t)i + 1], p[3 * (size_t)i + 2]);
+}
+
+__device__ __forceinline__ float3 normalize3(float3 n) {
+  const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(n.x, n.x), __fmul_rn(n.y, n.y)), __fmul_rn(n.z, n.z)));
+  return make_float3(__fdiv_rn(n.x, l), __fdiv_rn(n.y, l), __fdiv_rn(n.z, l));
+}
+
+// Area-weighted normals (ComputeMeshNormals, GMorpho.cu:6498-6524) summed per
+// vertex in triangle order, then normalised (GMorpho.cu:6526-6537).
+__global__ void k_vertex_normals(const float* __restrict__ V, const uint32_t* __restrict__ T,
+                                 const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
+                                 float* __restrict__ N) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
+      const uint32_t t = adj[i] / 3;
+      const float3 p0 = ld3(V, T[3 * (size_t)t]), p1 = ld3(V, T[3 * (size_t)t + 1]), p2 = ld3(V, T[3 * (size_t)t + 2]);
+      const float3 a = make_float3(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
+      const float3 b = make_float3(__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z));
+      const float nx = __fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y));
+      const float ny = __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z));
+      const float nz = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
+      acc = make_float3(__fadd_rn(acc.x, nx), __fadd_rn(acc.y, ny), __fadd_rn(acc.z, nz));
+    }
+    const float3 n = normalize3(acc);
+    N[3 * v] = n.x; N[3 * v + 1] = n.y; N[3 * v + 2] = n.z;
+  }
+}
+
+__device__ __forceinline__ float dist2(float3 a, float3 b) {
+  const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// One bilateral normal iteration (BilateralMeshFiltering{,Normalize},
+// GMorpho.cu:6539-6620): each incident triangle adds w1 n_b + w2 n_c,
+// accumulated per vertex in triangle order.
+__global__ void k_bilateral(const float* __restrict__ V, const float* __restrict__ Nin,
+                            const uint32_t* __restrict__ T, const uint32_t* __restrict__ rowptr,
+                            const uint32_t* __restrict__ adj, int64_t nv, float sp2, float sn2,
+                            float* __restrict__ Nout) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    const float3 pa = ld3(V, (uint32_t)v), na = ld3(Nin, (uint32_t)v);
+    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
+      const uint32_t corner = adj[i];
+      const uint32_t t = corner / 3, role = corner - 3 * t;
+      const uint32_t ib = T[3 * (size_t)t + (role == 0 ? 1 : 0)];
+      const uint32_t ic = T[3 * (size_t)t + (role == 2 ? 1 : 2)];
+      const float3 pb = ld3(V, ib), pc = ld3(V, ic), nb = ld3(Nin, ib), nc = ld3(Nin, ic);
+      const float w1 = expf(-__fadd_rn(__fdiv_rn(dist2(pa, pb), sp2), __fdiv_rn(dist2(na, nb), sn2)));
+      const float w2 = expf(-__fadd_rn(__fdiv_rn(dist2(pa, pc), sp2), __fdiv_rn(dist2(na, nc), sn2)));
+      acc.x = __fadd_rn(acc.x, __fadd_rn(__fmul_rn(w1, nb.x), __fmul_rn(w2, nc.x)));
+      acc.y = __fadd_rn(acc.y, __fadd_rn(__fmul_rn(w1, nb.y), __fmul_rn(w2, nc.y)));
+      acc.z = __fadd_rn(acc.z, __fadd_rn(__fmul_rn(w1, nb.z), __fmul_rn(w2, nc.z)));
+    }
+    const float3 n = normalize3(acc);
+    Nout[3 * v] = n.x; Nout[3 * v + 1] = n.y; Nout[3 * v + 2] = n.z;
+  }
+}
+
+// ------------------------------------------------------------------ host
+
+static int gs_blocks(int64_t n, int threads, int sms) {
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)(sms > 0 ? sms : 152) * 16;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc, int64_t* nv,
+                       int64_t* nt) {
+  const int res = a.res;
+  const int64_t cells = (int64_t)res * res * res;
+  const int nb = (int)(cells / kCellsPerBrick);
+  cudaError_t e;
+  if (nb + 1 > b.bricks_cap) {
+    if (b.brick_tot) cudaFree(b.brick_tot);
+    b.brick_tot = nullptr;
+    e = cudaMalloc(&b.brick_tot, sizeof(uint32_t) * 4 * (size_t)(nb + 1));
+    if (e != cudaSuccess) return e;
+    b.bricks_cap = nb + 1;
+  }
+  if (cells > b.cells_cap) {
+    if (b.cell_voff) cudaFree(b.cell_voff);
+    b.cell_voff = nullptr;
+    e = cudaMalloc(&b.cell_voff, sizeof(uint32_t) * (size_t)cells);
+    if (e != cudaSuccess) return e;
+    b.cells_cap = cells;
+  }
+  GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, res, b.brick_tot));
+  GM_LAUNCH(kc, "k_scan_bricks", st, k_scan_bricks<<<1, 1024, 0, st>>>(b.brick_tot, nb));
+  uint32_t tot[4];
+  e = cudaMemcpyAsync(tot, b.brick_tot + 4 * (size_t)nb, sizeof(tot), cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  *nv = tot[1];
+  *nt = tot[2];
+  const int need_fix = (int)tot[3];
+  if (need_fix + 1 > b.fix_cap || b.fix == nullptr) {
+    if (b.fix) cudaFree(b.fix);
+    b.fix = nullptr;
+    const int c = need_fix + 64;
+    e = cudaMalloc(&b.fix, sizeof(uint32_t) * (1 + 4 * (size_t)c));
+    if (e != cudaSuccess) return e;
+    b.fix_cap = c;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt, cudaStream_t st,
+                      KernelCounter* kc) {
+  const int res = a.res;
+  const int nb = (int)((int64_t)res * res * res / kCellsPerBrick);
+  cudaError_t e;
+  // per-vertex buffers share one capacity, per-triangle buffers another
+  if (b.v_cap < nv || b.V == nullptr) {
+    cudaFree(b.V); cudaFree(b.N); cudaFree(b.N2); cudaFree(b.rowptr); cudaFree(b.cursor);
+    b.V = b.N = b.N2 = nullptr;
+    b.rowptr = b.cursor = nullptr;
+    b.v_cap = 0;
+    const int64_t c = nv + nv / 4 + 1024;
+    if ((e = cudaMalloc(&b.V, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.N, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.N2, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.rowptr, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.cursor, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
+    b.v_cap = c;
+  }
+  if (b.t_cap < nt || b.T == nullptr) {
+    cudaFree(b.T); cudaFree(b.adj);
+    b.T = b.adj = nullptr;
+    b.t_cap = 0;
+    const int64_t c = nt + nt / 4 + 1024;
+    if ((e = cudaMalloc(&b.T, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.adj, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
+    b.t_cap = c;
+  }
+  const float cs = 0.5f * a.cell_size;  // exact: scaling by a power of two
+  cudaMemsetAsync(b.fix, 0, sizeof(uint32_t), st);
+  GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, res, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],
+                                           a.bbox_min[2], cs, a.isovalue));
+  GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, 0, st>>>(a.C, res, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
+                                            b.fix_cap));
+  GM_LAUNCH(kc, "k_mc_fix91", st, k_mc_fix91<<<1, 256, 0, st>>>(b.fix, b.fix_cap, b.T));
+  if (nv == 0 || nt == 0) return cudaGetLastError();
+  // normals
+  const int sms = a.num_sms;
+  cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
+  GM_LAUNCH(kc, "k_adj_count", st, k_adj_count<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.cursor));
+  GM_LAUNCH(kc, "k_scan_u32", st, k_scan_u32<<<1, 1024, 0, st>>>(b.cursor, b.rowptr, nv));
+  cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
+  GM_LAUNCH(kc, "k_adj_fill", st, k_adj_fill<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.rowptr, b.cursor, b.adj));
+  GM_LAUNCH(kc, "k_adj_sort", st, k_adj_sort<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.rowptr, b.adj, nv));
+  GM_LAUNCH(kc, "k_vertex_normals", st, k_vertex_normals<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, b.N));
+  float* nin = b.N;
+  float* nout = b.N2;
+  for (int it = 0; it < a.bilateral_iters; it++) {
+    const float sn = it < 2 ? 1e10f : 0.2f;  // GMorpho.cu:6959-6969
+    GM_LAUNCH(kc, "k_bilateral", st, k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, nin, b.T, b.rowptr, b.adj, nv, 1.f, sn * sn, nout));
+    float* t = nin; nin = nout; nout = t;
+  }
+  if (nin != b.N) cudaMemcpyAsync(b.N, nin, sizeof(float) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, st);
+  return cudaGetLastError();
+}
+
+}  // namespace gm

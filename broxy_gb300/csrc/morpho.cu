@@ -1,0 +1,635 @@
+// morpho.cu — variable-radius ball/cube closing on GB300 (reference rows
+// a5..a11: GMorpho::DilateBySphereMipmap / DilateByCubeMipmap /
+// ErodeBySphereMipmap, GMorpho/GMorpho.cu:3231-3314, 3538-3596, 6627-6702).
+//
+// The reference answers every dilation/erosion predicate by a per-thread
+// stack traversal of a texture pyramid.  Here the same predicates are
+// computed as separable min-plus distance transforms over fine-voxel
+// fields, one axis per pass, each pass a tiled, coalesced, HBM-streaming
+// kernel:
+//
+//   dilation (query radius r(p), GMorpho.cu:2858-2867):
+//       D(p) = min_q sum_a d_a(q - p)^2 < (r(p) + 1)^2   (sphere)
+//       D(p) = max_a-combined L-inf lattice distance <= r(p)   (cube)
+//     with d(delta) the distance from lattice point p to the box of voxel q.
+//   erosion (source radius r(q), GMorpho.cu:4403-4411, 5283-5349):
+//       E(s) = min_q [K - 4 (r(q)-1)^2 + sum_a e_a^2] < K,  q in contour S,
+//     in half-voxel units (e = box distance from point s to voxel q),
+//     K = 4 (rmax - 1)^2, at voxel centres (fine pass) and at the lattice
+//     points 2c+1 (base pass).
+//
+// The two-level structure of the reference (base pass on whole cells,
+// refinement of contour cells only) is then applied exactly by the select
+// kernels, which reproduces the reference grids bit for bit (GM_REF), or
+// skipped (GM_EXACT).
+#include "gm_common.cuh"
+#include "gm_internal.h"
+
+namespace gm {
+
+// ---------------------------------------------------------------------
+// pass X of the dilation: 1-D lattice distance to the nearest occupied
+// voxel along each fine row, from the packed byte grid.
+// ---------------------------------------------------------------------
+
+// One block per packed byte-row (cy, cz), i.e. the four fine rows
+// y = 2cy + j, z = 2cz + i.  Shared: 4 rows of N bits (occupied voxels),
+// then the corner sets L = bits | bits << 1 (the lattice points that bound
+// an occupied voxel), then the nearest set bit of L for every x.
+__global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ X, uint8_t* __restrict__ A,
+                                                    int res, int dcap) {
+  extern __shared__ uint32_t sm_words[];
+  const int N = 2 * res, W = N >> 5;
+  const int cy = blockIdx.x, cz = blockIdx.y;
+  uint32_t* bits = sm_words;      // [4][W]
+  uint32_t* corner = sm_words + 4 * W;  // [4][W]
+  const uint8_t* row = X + (int64_t)res * cy + (int64_t)res * res * cz;
+  // word w of a fine row covers bytes 16w .. 16w+15 of the byte row
+  for (int w = threadIdx.x; w < W; w += blockDim.x) {
+    const uint4 q = *reinterpret_cast<const uint4*>(row + 16 * w);
+    const uint32_t by[4] = {q.x, q.y, q.z, q.w};
+    uint32_t o[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int b = 0; b < 16; b++) {
+      const uint32_t v = (by[b >> 2] >> (8 * (b & 3))) & 0xffu;
+#pragma unroll
+      for (int r = 0; r < 4; r++) o[r] |= ((v >> (2 * r)) & 3u) << (2 * b);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) bits[r * W + w] = o[r];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 4 * W; i += blockDim.x) {
+    const int r = i / W, w = i - r * W;
+    const uint32_t b = bits[i];
+    const uint32_t carry = w > 0 ? bits[r * W + w - 1] >> 31 : 0u;
+    corner[i] = b | (b << 1) | carry;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 4 * N; i += blockDim.x) {
+    const int r = i / N, p = i - r * N;
+    const uint32_t* L = corner + r * W;
+    const int w = p >> 5, b = p & 31;
+    int dr = dcap, dl = dcap;
+    uint32_t m = L[w] >> b;
+    if (m) {
+      dr = __ffs(m) - 1;
+    } else {
+      int acc = 32 - b;
+      for (int k = w + 1; k < W && acc < dcap; k++) {
+        const uint32_t v = L[k];
+        if (v) { acc += __ffs(v) - 1; dr = acc; break; }
+        acc += 32;
+      }
+    }
+    m = L[w] << (31 - b);
+    if (m) {
+      dl = __clz(m);
+    } else {
+      int acc = b + 1;
+      for (int k = w - 1; k >= 0 && acc < dcap; k--) {
+        const uint32_t v = L[k];
+        if (v) { acc += __clz(v); dl = acc; break; }
+        acc += 32;
+      }
+    }
+    int d = dr < dl ? dr : dl;
+    if (d > dcap) d = dcap;
+    const int y = 2 * cy + (r & 1), z = 2 * cz + (r >> 1);
+    A[fine_index(p, y, z, N)] = (uint8_t)d;
+  }
+}
+
+// ---------------------------------------------------------------------
+// pass X of the erosion: sites are the contour voxels of one fine row;
+// outputs the half-voxel-unit partial sums at every voxel centre (HC) and
+// at the odd lattice points x = 2c+1 (HL).
+// ---------------------------------------------------------------------
+
+__global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ S, const int8_t* __restrict__ R,
+                                                    int uniform_r, int res, int halo, uint32_t K,
+                                                    uint16_t* __restrict__ HC, uint16_t* __restrict__ HL) {
+  extern __shared__ uint32_t sm_words[];
+  const int N = 2 * res, W = N >> 5;
+  const int cy = blockIdx.x, cz = blockIdx.y;
+  uint32_t* bits = sm_words;  // [4][W]
+  uint8_t* rad = reinterpret_cast<uint8_t*>(sm_words + 4 * W);  // [4][N] clamped radii
+  const uint8_t* row = S + (int64_t)res * cy + (int64_t)res * res * cz;
+  __shared__ int any_site;
+  if (threadIdx.x == 0) any_site = 0;
+  __syncthreads();
+  for (int w = threadIdx.x; w < W; w += blockDim.x) {
+    const uint4 q = *reinterpret_cast<const uint4*>(row + 16 * w);
+    const uint32_t by[4] = {q.x, q.y, q.z, q.w};
+    uint32_t o[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int b = 0; b < 16; b++) {
+      const uint32_t v = (by[b >> 2] >> (8 * (b & 3))) & 0xffu;
+#pragma unroll
+      for (int r = 0; r < 4; r++) o[r] |= ((v >> (2 * r)) & 3u) << (2 * b);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) bits[r * W + w] = o[r];
+    if (o[0] | o[1] | o[2] | o[3]) any_site = 1;
+  }
+  __syncthreads();
+  const bool empty = any_site == 0;
+  if (!empty && R != nullptr) {
+    // clamped radii of the four fine rows (only read where a site sits)
+    for (int i = threadIdx.x; i < 4 * (N >> 4); i += blockDim.x) {
+      const int r = i / (N >> 4), seg = i - r * (N >> 4);
+      const int y = 2 * cy + (r & 1), z = 2 * cz + (r >> 1);
+      const uint4 v = *reinterpret_cast<const uint4*>(R + fine_index(16 * seg, y, z, N));
+      const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+      uint32_t* dst = reinterpret_cast<uint32_t*>(rad + r * N + 16 * seg);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        uint32_t o = 0;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const int s = (int)(int8_t)((w4[j] >> (8 * b)) & 0xff);
+          o |= (uint32_t)clamp_radius(s) << (8 * b);
+        }
+        dst[j] = o;
+      }
+    }
+    __syncthreads();
+  }
+  const int ru = clamp_radius(uniform_r);
+  const int total = 4 * N + 4 * res;
+  for (int i = threadIdx.x; i < total; i += blockDim.x) {
+    int r, p;
+    bool center;
+    if (i < 4 * N) { r = i / N; p = i - r * N; center = true; }
+    else { const int j = i - 4 * N; r = j / res; p = 2 * (j - r * res) + 1; center = false; }
+    uint32_t best = K;
+    if (!empty) {
+      const uint32_t* L = bits + r * W;
+      int lo = p - halo, hi = p + halo;
+      if (lo < 0) lo = 0;
+      if (hi > N - 1) hi = N - 1;
+      for (int w = lo >> 5; w <= (hi >> 5); w++) {
+        uint32_t m = L[w];
+        if (!m) continue;
+        const int base = w << 5;
+        if (base < lo) m &= 0xffffffffu << (lo - base);
+        if (base + 31 > hi) m &= 0xffffffffu >> (base + 31 - hi);
+        while (m) {
+          const int q = base + __ffs(m) - 1;
+          m &= m - 1;
+          const int rq = R != nullptr ? (int)rad[r * N + q] : ru;
+          const uint32_t u = K - 4u * (uint32_t)((rq - 1) * (rq - 1));
+          const int e = center ? center_dist2(q - p) : 2 * lattice_dist(q - p);
+          const uint32_t v = u + (uint32_t)(e * e);
+          best = v < best ? v : best;
+        }
+      }
+    }
+    const int y = 2 * cy + (r & 1), z = 2 * cz + (r >> 1);
+    if (center) HC[fine_index(p, y, z, N)] = (uint16_t)best;
+    else HL[(int64_t)(p >> 1) + (int64_t)res * y + (int64_t)res * N * z] = (uint16_t)best;
+  }
+}
+
+// ---------------------------------------------------------------------
+// generic axis pass (y or z): out(o) = min over delta of
+//     in(pos(o) + delta) (+) g(delta)
+// ---------------------------------------------------------------------
+
+enum Kern { KERN_LAT = 0, KERN_LAT2 = 1, KERN_CEN2 = 2, KERN_CUBE = 3 };
+
+template <int G>
+__device__ __forceinline__ uint32_t kern_g(int delta) {
+  if (G == KERN_LAT) { const int d = lattice_dist(delta); return (uint32_t)(d * d); }
+  if (G == KERN_LAT2) { const int d = 2 * lattice_dist(delta); return (uint32_t)(d * d); }
+  if (G == KERN_CEN2) { const int d = center_dist2(delta); return (uint32_t)(d * d); }
+  return (uint32_t)lattice_dist(delta);  // KERN_CUBE
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t combine(uint32_t v, uint32_t g) {
+  if (G == KERN_CUBE) return v > g ? v : g;
+  return v + g;
+}
+
+// Minimum over a window of the tile column `col` (stride 32 between
+// consecutive positions) around index sp, scanning outward and stopping as
+// soon as the kernel alone reaches the best value (inputs are >= 0).
+template <int G>
+__device__ __forceinline__ uint32_t column_min(const uint16_t* col, int sp, int span, int halo) {
+  uint32_t best = combine<G>(col[sp * 32], kern_g<G>(0));
+  for (int k = 1; k <= halo; k++) {
+    const uint32_t gp = kern_g<G>(k), gm_ = kern_g<G>(-k);
+    if ((gp < gm_ ? gp : gm_) >= best) break;
+    if (sp + k < span) { const uint32_t v = combine<G>(col[(sp + k) * 32], gp); best = v < best ? v : best; }
+    if (sp - k >= 0) { const uint32_t v = combine<G>(col[(sp - k) * 32], gm_); best = v < best ? v : best; }
+  }
+  return best;
+}
+
+constexpr int kTileOut = 64;  // outputs per block along the pass axis
+constexpr int kRows = 8;      // blockDim.y
+
+// Input element conversion: u8 fields hold 1-D distances d (pass X of the
+// dilation) and enter the sphere kernel squared.
+template <int G, typename TIn>
+__device__ __forceinline__ uint16_t load_in(const TIn* p, uint32_t cap) {
+  const uint32_t v = (uint32_t)*p;
+  if (sizeof(TIn) == 1 && G != KERN_CUBE) { const uint32_t s = v * v; return (uint16_t)(s < cap ? s : cap); }
+  return (uint16_t)(v < cap ? v : cap);
+}
+
+// in/out fields are x-fastest with dims (nx, ny, nz).  axis = 1 (y) or 2
+// (z).  sub: output only the odd input positions 2o+1 along the axis.
+template <int G, typename TIn>
+__global__ void __launch_bounds__(256) k_axis_pass(const TIn* __restrict__ in, uint16_t* __restrict__ out,
+                                                   int nx, int ny, int nz, int axis, int sub, int halo,
+                                                   uint32_t cap) {
+  extern __shared__ uint16_t tile[];  // [span][32]
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x = blockIdx.x * 32 + tx;
+  const int na = axis == 1 ? ny : nz;
+  const int nout = sub ? na / 2 : na;
+  const int third = blockIdx.z;  // z for axis y, y for axis z
+  const int64_t sa = axis == 1 ? (int64_t)nx : (int64_t)nx * ny;
+  const int64_t s3 = axis == 1 ? (int64_t)nx * ny : (int64_t)nx;
+  const int o0 = blockIdx.y * kTileOut;
+  const int p_first = sub ? 2 * o0 + 1 : o0;
+  const int o_last = min(o0 + kTileOut, nout) - 1;
+  const int p_last = sub ? 2 * o_last + 1 : o_last;
+  const int lo = p_first - halo;
+  const int span = p_last + halo - lo + 1;
+  for (int s = ty; s < span; s += kRows) {
+    const int a = lo + s;
+    uint16_t v = (uint16_t)cap;
+    if (x < nx && a >= 0 && a < na) v = load_in<G, TIn>(in + x + sa * a + s3 * third, cap);
+    tile[s * 32 + tx] = v;
+  }
+  __syncthreads();
+  if (x >= nx) return;
+  // output dims: same as input except the pass axis (nout)
+  const int64_t osa = sa;
+  const int64_t os3 = axis == 1 ? (int64_t)nx * nout : (int64_t)nx;
+  for (int o = o0 + ty; o <= o_last; o += kRows) {
+    const int p = sub ? 2 * o + 1 : o;
+    const uint32_t best = column_min<G>(tile + tx, p - lo, span, halo);
+    out[x + osa * o + os3 * third] = (uint16_t)(best < cap ? best : cap);
+  }
+}
+
+// ---------------------------------------------------------------------
+// final z pass at full resolution, fused with the per-voxel threshold and
+// the packing of 2x2x2 bits into reference bytes.
+//   FIN_DIL: bit = sum < (r(p)+1)^2 (sphere) / sum <= r(p) (cube)
+//   FIN_ERO: bit = sum < K (eroded)
+// block (32, 8): tx = x, ty & 1 = y parity, ty >> 1 = group of 16 z.
+// ---------------------------------------------------------------------
+
+enum Fin { FIN_DIL = 0, FIN_ERO = 1 };
+
+template <int G, int F>
+__global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in, uint8_t* __restrict__ out_cells,
+                                                 const int8_t* __restrict__ R, int uniform_r, int res, int halo,
+                                                 uint32_t cap) {
+  extern __shared__ uint16_t tile2[];  // [2][span][32]
+  const int N = 2 * res;
+  const int tx = threadIdx.x, yp = threadIdx.y & 1, zg = threadIdx.y >> 1;
+  const int x = blockIdx.x * 32 + tx;
+  const int y = 2 * blockIdx.z + yp;
+  const int z0 = blockIdx.y * kTileOut;
+  const int z_last = min(z0 + kTileOut, N) - 1;
+  const int lo = z0 - halo;
+  const int span = z_last + halo - lo + 1;
+  uint16_t* tile = tile2 + yp * span * 32;
+  for (int s = zg; s < span; s += 4) {
+    const int a = lo + s;
+    uint16_t v = (uint16_t)cap;
+    if (x < N && a >= 0 && a < N) {
+      const uint32_t t = in[fine_index(x, y, a, N)];
+      v = (uint16_t)(t < cap ? t : cap);
+    }
+    tile[s * 32 + tx] = v;
+  }
+  __syncthreads();
+  __shared__ uint8_t ybits[8][32][2];  // [z pair][lane][y parity] hmm: per group
+  // each thread: 16 consecutive z = z0 + 16 zg + j
+  uint32_t bits = 0;
+  const int ru = clamp_radius(uniform_r);
+  if (x < N) {
+#pragma unroll 1
+    for (int j = 0; j < 16; j++) {
+      const int z = z0 + 16 * zg + j;
+      if (z > z_last) break;
+      const uint32_t v = column_min<G>(tile + tx, z - lo, span, halo);
+      bool b;
+      if (F == FIN_DIL) {
+        const int r = R != nullptr ? clamp_radius(R[fine_index(x, y, z, N)]) : ru;
+        if (G == KERN_CUBE) b = v <= (uint32_t)r;
+        else b = v < (uint32_t)((r + 1) * (r + 1));
+      } else {
+        b = v < cap;
+      }
+      bits |= (uint32_t)b << j;
+    }
+  }
+  // pack: for z pair q (0..7), this voxel contributes bit (xb + 2 yb) for the
+  // lower z and (xb + 2 yb + 4) for the upper z.
+  const int xb = x & 1;
+  uint32_t packed = 0;  // byte q in bits 8q..8q+7, q = 0..3 (first 8 z) / second word
+  uint32_t packed_hi = 0;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const uint32_t lo_b = (bits >> (2 * q)) & 1u, hi_b = (bits >> (2 * q + 1)) & 1u;
+    const uint32_t byte = (lo_b << (xb + 2 * yp)) | (hi_b << (xb + 2 * yp + 4));
+    if (q < 4) packed |= byte << (8 * q);
+    else packed_hi |= byte << (8 * (q - 4));
+  }
+  packed |= __shfl_xor_sync(0xffffffffu, packed, 1);
+  packed_hi |= __shfl_xor_sync(0xffffffffu, packed_hi, 1);
+  __shared__ uint32_t ex[2][4][32][2];
+  ex[yp][zg][tx][0] = packed;
+  ex[yp][zg][tx][1] = packed_hi;
+  __syncthreads();
+  (void)ybits;
+  if (yp == 0 && (tx & 1) == 0 && x < N) {
+    const uint32_t w0 = packed | ex[1][zg][tx][0];
+    const uint32_t w1 = packed_hi | ex[1][zg][tx][1];
+    const int cx = x >> 1, cyy = y >> 1;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int zc = (z0 + 16 * zg) / 2 + q;
+      if (2 * zc > z_last) break;
+      const uint32_t byte = q < 4 ? (w0 >> (8 * q)) & 0xffu : (w1 >> (8 * (q - 4))) & 0xffu;
+      out_cells[cell_index(cx, cyy, zc, res)] = (uint8_t)byte;
+    }
+  }
+}
+
+// final z pass of the base erosion: lattice points 2c+1 only; one flag byte
+// per base cell (1 = the cell centre is eroded).
+__global__ void __launch_bounds__(256) k_final_z_base(const uint16_t* __restrict__ in, uint8_t* __restrict__ flags,
+                                                      int res, int halo, uint32_t cap) {
+  extern __shared__ uint16_t tile[];
+  const int N = 2 * res;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x = blockIdx.x * 32 + tx;  // cx
+  const int cyy = blockIdx.z;
+  const int o0 = blockIdx.y * kTileOut;
+  const int o_last = min(o0 + kTileOut, res) - 1;
+  const int lo = 2 * o0 + 1 - halo;
+  const int span = 2 * o_last + 1 + halo - lo + 1;
+  for (int s = ty; s < span; s += kRows) {
+    const int a = lo + s;
+    uint16_t v = (uint16_t)cap;
+    if (x < res && a >= 0 && a < N) {
+      const uint32_t t = in[(int64_t)x + (int64_t)res * cyy + (int64_t)res * res * a];
+      v = (uint16_t)(t < cap ? t : cap);
+    }
+    tile[s * 32 + tx] = v;
+  }
+  __syncthreads();
+  if (x >= res) return;
+  for (int o = o0 + ty; o <= o_last; o += kRows) {
+    const uint32_t v = column_min<KERN_LAT2>(tile + tx, 2 * o + 1 - lo, span, halo);
+    flags[cell_index(x, cyy, o, res)] = v < cap ? 1 : 0;
+  }
+}
+
+// ---------------------------------------------------------------------
+// cell-level kernels
+// ---------------------------------------------------------------------
+
+__device__ __forceinline__ bool in_box(int x, int y, int z, const int* dr) {
+  return x < dr[0] && y < dr[1] && z < dr[2];
+}
+
+struct DataRes { int v[3]; };
+
+// GM_REF dilation select: base pass (cells inside data_res that are not
+// full take 0xff when their child-0 corner is dilated, GMorpho.cu:2848-2927)
+// then the tight contour (forward 2x2x2 block mixes full and non-full,
+// Grid.cu:1589-1607) takes the fine per-voxel byte (GMorpho.cu:2930-3056).
+__device__ __forceinline__ uint8_t base_dil(const uint8_t* X, const uint8_t* Df, int64_t c, bool inside) {
+  const uint8_t x = X[c];
+  return (inside && x != 0xff && (Df[c] & 1)) ? (uint8_t)0xff : x;
+}
+
+__global__ void k_dil_select(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
+                             uint8_t* __restrict__ D, int res, DataRes dr) {
+  const int64_t total = (int64_t)res * res * res;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(c % res), y = (int)((c / res) % res), z = (int)(c / ((int64_t)res * res));
+    const uint8_t d0 = base_dil(X, Df, c, in_box(x, y, z, dr.v));
+    bool tag = false;
+    if (x <= res - 2 && y <= res - 2 && z <= res - 2) {
+      int full = d0 == 0xff;
+#pragma unroll
+      for (int k = 1; k < 8; k++) {
+        const int xx = x + (k & 1), yy = y + ((k >> 1) & 1), zz = z + (k >> 2);
+        full += base_dil(X, Df, cell_index(xx, yy, zz, res), in_box(xx, yy, zz, dr.v)) == 0xff;
+      }
+      tag = full != 0 && full != 8;
+    }
+    D[c] = tag ? Df[c] : d0;
+  }
+}
+
+// Contour of the dilation: fine voxels outside D that are 6-adjacent to D.
+// GM_REF: only for cells in [1, res-2]^3 whose byte is not 0xff
+// (TagVoxelsContourByErosion, Grid.cu:1230-1327); GM_EXACT: whole grid.
+__device__ __forceinline__ uint8_t adj6(uint8_t v, uint8_t xm, uint8_t xp, uint8_t ym, uint8_t yp, uint8_t zm,
+                                        uint8_t zp) {
+  uint32_t t = ((v & 0xAAu) >> 1) | ((xp & 0x55u) << 1);
+  t |= ((v & 0x55u) << 1) | ((xm & 0xAAu) >> 1);
+  t |= ((v & 0xCCu) >> 2) | ((yp & 0x33u) << 2);
+  t |= ((v & 0x33u) << 2) | ((ym & 0xCCu) >> 2);
+  t |= ((v & 0xF0u) >> 4) | ((zp & 0x0Fu) << 4);
+  t |= ((v & 0x0Fu) << 4) | ((zm & 0xF0u) >> 4);
+  return (uint8_t)t;
+}
+
+__global__ void k_contour(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, int res, int exact) {
+  const int64_t total = (int64_t)res * res * res;
+  const int64_t s1 = res, s2 = (int64_t)res * res;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(c % res), y = (int)((c / res) % res), z = (int)(c / s2);
+    const uint8_t v = D[c];
+    uint8_t out = 0;
+    if (exact) {
+      const uint8_t xm = x > 0 ? D[c - 1] : 0, xp = x < res - 1 ? D[c + 1] : 0;
+      const uint8_t ym = y > 0 ? D[c - s1] : 0, yp = y < res - 1 ? D[c + s1] : 0;
+      const uint8_t zm = z > 0 ? D[c - s2] : 0, zp = z < res - 1 ? D[c + s2] : 0;
+      out = adj6(v, xm, xp, ym, yp, zm, zp) & (uint8_t)~v;
+    } else if (x >= 1 && y >= 1 && z >= 1 && x <= res - 2 && y <= res - 2 && z <= res - 2 && v != 0xff) {
+      out = adj6(v, D[c - 1], D[c + 1], D[c - s1], D[c + s1], D[c - s2], D[c + s2]) & (uint8_t)~v;
+    }
+    S[c] = out;
+  }
+}
+
+// GM_REF erosion select: base pass (cells inside data_res with D != 0 and
+// X != 0xff are cleared when the centre 2c+1 is eroded, GMorpho.cu:4360-4370,
+// 4644-4646), then cells whose byte differs from a 6-neighbour
+// (Grid.cu:1499-1570) take 0xff & ~eroded (GMorpho.cu:5353-5360).
+__device__ __forceinline__ uint8_t base_ero(const uint8_t* X, const uint8_t* D, const uint8_t* Eb, int64_t c,
+                                            bool inside) {
+  const uint8_t d = D[c];
+  return (inside && d != 0 && X[c] != 0xff && Eb[c]) ? (uint8_t)0 : d;
+}
+
+__global__ void k_ero_select(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
+                             const uint8_t* __restrict__ Eb, const uint8_t* __restrict__ Ef,
+                             uint8_t* __restrict__ C, int res, DataRes dr, int exact) {
+  const int64_t total = (int64_t)res * res * res;
+  const int64_t s1 = res, s2 = (int64_t)res * res;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+    if (exact) { C[c] = D[c] & (uint8_t)~Ef[c]; continue; }
+    const int x = (int)(c % res), y = (int)((c / res) % res), z = (int)(c / s2);
+    const uint8_t c0 = base_ero(X, D, Eb, c, in_box(x, y, z, dr.v));
+    bool tag = false;
+    if (x >= 1 && y >= 1 && z >= 1 && x <= res - 2 && y <= res - 2 && z <= res - 2) {
+      tag = base_ero(X, D, Eb, c - 1, in_box(x - 1, y, z, dr.v)) != c0 ||
+            base_ero(X, D, Eb, c + 1, in_box(x + 1, y, z, dr.v)) != c0 ||
+            base_ero(X, D, Eb, c - s1, in_box(x, y - 1, z, dr.v)) != c0 ||
+            base_ero(X, D, Eb, c + s1, in_box(x, y + 1, z, dr.v)) != c0 ||
+            base_ero(X, D, Eb, c - s2, in_box(x, y, z - 1, dr.v)) != c0 ||
+            base_ero(X, D, Eb, c + s2, in_box(x, y, z + 1, dr.v)) != c0;
+    }
+    C[c] = tag ? (uint8_t)(0xff & ~Ef[c]) : c0;
+  }
+}
+
+// max clamped radius over the fine radius grid
+__global__ void k_rmax(const int8_t* __restrict__ R, int64_t n, int* __restrict__ out) {
+  int m = 2;
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * 16; i < n;
+       i += (int64_t)gridDim.x * blockDim.x * 16) {
+    const uint4 v = *reinterpret_cast<const uint4*>(R + i);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      const int s = (int)(int8_t)((w[j >> 2] >> (8 * (j & 3))) & 0xff);
+      const int r = clamp_radius(s);
+      m = r > m ? r : m;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) { const int t = __shfl_xor_sync(0xffffffffu, m, o); m = t > m ? t : m; }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// ---------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------
+
+static inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+static int grid_stride_blocks(int64_t n, int threads, int sms) {
+  int64_t b = (n + threads - 1) / threads;
+  const int64_t cap = (int64_t)sms * 32;
+  return (int)(b < cap ? b : cap);
+}
+
+size_t close_workspace_bytes(int res) {
+  const size_t N = 2 * (size_t)res, V = N * N * N, cells = (size_t)res * res * res;
+  // buf16 x2, buf8, HL1, HL2, Df, Eb, Ef, S, D + slack for alignment
+  return 2 * V * 2 + V + (size_t)res * N * N * 2 + (size_t)res * res * N * 2 + 5 * cells + 16 * 256;
+}
+
+static inline uint8_t* carve(uint8_t*& p, size_t bytes) {
+  uint8_t* r = p;
+  p += (bytes + 255) & ~(size_t)255;
+  return r;
+}
+
+cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc) {
+  const int res = a.res, N = 2 * res;
+  const size_t V = (size_t)N * N * N, cells = (size_t)res * res * res;
+  uint8_t* p = a.workspace;
+  uint16_t* buf16a = reinterpret_cast<uint16_t*>(carve(p, V * 2));
+  uint16_t* buf16b = reinterpret_cast<uint16_t*>(carve(p, V * 2));
+  uint8_t* buf8 = carve(p, V);
+  uint16_t* HL1 = reinterpret_cast<uint16_t*>(carve(p, (size_t)res * N * N * 2));
+  uint16_t* HL2 = reinterpret_cast<uint16_t*>(carve(p, (size_t)res * res * N * 2));
+  uint8_t* Df = carve(p, cells);
+  uint8_t* Eb = carve(p, cells);
+  uint8_t* Ef = carve(p, cells);
+  uint8_t* S = carve(p, cells);
+  uint8_t* D = a.D_out != nullptr ? a.D_out : carve(p, cells);
+  int sms = a.num_sms > 0 ? a.num_sms : 152;
+  const int rmax = a.rmax;
+  DataRes dr{{a.data_res[0], a.data_res[1], a.data_res[2]}};
+  const bool exact = a.mode == 1;
+
+  // ---- dilation ----
+  const int dil_r = rmax + 1;  // "Safety Measure" radius + 1 (GMorpho.cu:2864)
+  const int dcap = (a.se == 1 ? rmax + 2 : dil_r + 1) < 255 ? (a.se == 1 ? rmax + 2 : dil_r + 1) : 255;
+  const uint32_t dil_cap = a.se == 1 ? (uint32_t)(rmax + 1) : (uint32_t)(dil_r * dil_r);
+  const int dil_halo = dil_r + 1;
+  {
+    const int W = N >> 5;
+    GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x<<<dim3(res, res), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, res, dcap));
+    const int span = kTileOut + 2 * dil_halo;
+    dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
+    if (a.se == 1)
+      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CUBE, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(buf8, buf16a, N, N, N, 1, 0,
+                                                                              dil_halo, dil_cap));
+    else
+      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(buf8, buf16a, N, N, N, 1, 0,
+                                                                             dil_halo, dil_cap));
+    dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
+    uint8_t* dst = exact ? D : Df;
+    if (a.se == 1)
+      GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CUBE, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(buf16a, dst, a.R, a.uniform_r, res,
+                                                                               dil_halo, dil_cap));
+    else
+      GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(buf16a, dst, a.R, a.uniform_r, res,
+                                                                              dil_halo, dil_cap));
+    if (!exact) {
+      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(a.X, Df, D, res, dr));
+    }
+  }
+  // ---- contour ----
+  GM_LAUNCH(kc, "k_contour", st, k_contour<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(D, S, res, exact ? 1 : 0));
+  // ---- erosion ----
+  {
+    const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
+    const int ehalo = rmax + 1;
+    const int W = N >> 5;
+    const size_t smem = 4 * W * sizeof(uint32_t) + (a.R != nullptr ? 4 * (size_t)N : 0);
+    GM_LAUNCH(kc, "k_ero_pass_x", st, k_ero_pass_x<<<dim3(res, res), 256, smem, st>>>(S, a.R, a.uniform_r, res, ehalo, K, buf16a, HL1));
+    const int span = kTileOut + 2 * ehalo;
+    // centres: y pass then fused final z pass
+    dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
+    GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CEN2, uint16_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(buf16a, buf16b, N, N, N, 1, 0,
+                                                                             ehalo, K));
+    dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
+    GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CEN2, FIN_ERO><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(buf16b, Ef, nullptr, 0, res, ehalo,
+                                                                              K));
+    if (!exact) {
+      // lattice points 2c+1: y pass (sub) then final z pass (sub)
+      const int span_s = 2 * kTileOut + 2 * ehalo;
+      dim3 gy(cdiv(res, 32), cdiv(res, kTileOut), N);
+      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT2, uint16_t><<<gy, dim3(32, kRows), span_s * 32 * 2, st>>>(HL1, HL2, res, N, N, 1, 1,
+                                                                                  ehalo, K));
+      dim3 gzb(cdiv(res, 32), cdiv(res, kTileOut), res);
+      GM_LAUNCH(kc, "k_final_z_base", st, k_final_z_base<<<gzb, dim3(32, kRows), span_s * 32 * 2, st>>>(HL2, Eb, res, ehalo, K));
+    }
+    GM_LAUNCH(kc, "k_ero_select", st, k_ero_select<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(a.X, D, Eb, Ef, a.C_out, res, dr,
+                                                                    exact ? 1 : 0));
+  }
+  if (a.S_out) {
+    cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc) {
+  cudaMemsetAsync(d_out, 0, sizeof(int), st);
+  const int64_t vec = n / 16;
+  int blocks = grid_stride_blocks(vec, 256, sms);
+  if (blocks < 1) blocks = 1;
+  GM_LAUNCH(kc, "k_rmax", st, k_rmax<<<blocks, 256, 0, st>>>(R, n, d_out));
+  return cudaGetLastError();
+}
+
+}  // namespace gm

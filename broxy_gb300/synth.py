@@ -1,0 +1,199 @@
+"""Seeded synthetic inputs for the GMorpho workloads.
+
+No dataset ships with the reference; these generators stand in for its
+inputs with the shapes, sizes and value distributions named by the
+benchmark configurations:
+
+  * union of 64 level-3 icospheres (the reference's own sphere.off is a
+    642-vertex / 1280-face level-3 icosphere), centres U[0.2,0.8]^3,
+    radii U[0.03,0.12];
+  * sum of isotropic Gaussian blobs (sigma U[0.01,0.05], weights
+    U[0.5,1.5], centres U[0.2,0.8]^3) classified at level 0.5;
+  * a variable radius field r = 2 + floor(30 s(x)), s a normalised sum of
+    16 Gaussian RBFs clamped to [0,1], evaluated in double on the host side
+    of the generator and stored as int8 per fine voxel.
+
+Seeds follow seed = 1000 * config + instance.
+"""
+import numpy as np
+
+
+def icosphere(level=3):
+    """Subdivided icosahedron on the unit sphere (level 3: 642 v, 1280 f)."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = list(f)
+    for _ in range(level):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts, dtype=np.float64), np.array(faces, dtype=np.uint32)
+
+
+def spheres_mesh(seed=1000, count=64, level=3):
+    """Concatenated icospheres (the configuration-1 input mesh)."""
+    rng = np.random.default_rng(seed)
+    V0, F0 = icosphere(level)
+    centres = rng.uniform(0.2, 0.8, size=(count, 3))
+    radii = rng.uniform(0.03, 0.12, size=count)
+    Vs, Fs = [], []
+    for i in range(count):
+        Vs.append(V0 * radii[i] + centres[i])
+        Fs.append(F0 + i * len(V0))
+    return np.concatenate(Vs).astype(np.float32), np.concatenate(Fs).astype(np.uint32)
+
+
+def blob_params(seed, count=200):
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(0.2, 0.8, size=(count, 3))
+    sigmas = rng.uniform(0.01, 0.05, size=count)
+    weights = rng.uniform(0.5, 1.5, size=count)
+    return centres, sigmas, weights
+
+
+def radius_params(seed, count=16):
+    rng = np.random.default_rng(seed + 7)
+    centres = rng.uniform(0.0, 1.0, size=(count, 3))
+    widths = rng.uniform(0.05, 0.25, size=count)
+    amps = rng.uniform(0.5, 1.0, size=count)
+    return centres, widths, amps
+
+
+def _axis(n, lo=0.0, hi=1.0):
+    return lo + (np.arange(n, dtype=np.float64) + 0.5) * (hi - lo) / n
+
+
+def blob_grid(res, seed, count=200, level=0.5, device=None):
+    """Packed grid (uint8 res^3) of the blob solid {f >= level} sampled at the
+    fine voxel centres of the unit cube.  With ``device`` (a torch device) the
+    field is evaluated with torch on that device in float64 slabs."""
+    N = 2 * res
+    centres, sigmas, weights = blob_params(seed, count)
+    if device is None:
+        x = _axis(N)
+        occ = np.zeros((N, N, N), dtype=bool)  # [z, y, x]
+        for z0 in range(0, N, 16):
+            zs = x[z0:z0 + 16]
+            f = np.zeros((len(zs), N, N))
+            for c, s, w in zip(centres, sigmas, weights):
+                gx = np.exp(-(x - c[0]) ** 2 / (2 * s * s))
+                gy = np.exp(-(x - c[1]) ** 2 / (2 * s * s))
+                gz = np.exp(-(zs - c[2]) ** 2 / (2 * s * s))
+                f += w * gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+            occ[z0:z0 + 16] = f >= level
+        return pack_dense(occ)
+    import torch
+    x = torch.as_tensor(_axis(N), device=device)
+    occ = torch.zeros((N, N, N), dtype=torch.bool, device=device)
+    c = torch.as_tensor(centres, device=device)
+    s = torch.as_tensor(sigmas, device=device)
+    w = torch.as_tensor(weights, device=device)
+    gx = torch.exp(-(x[None, :] - c[:, 0:1]) ** 2 / (2 * s[:, None] ** 2)) * w[:, None]  # [count, N]
+    gy = torch.exp(-(x[None, :] - c[:, 1:2]) ** 2 / (2 * s[:, None] ** 2))
+    gz = torch.exp(-(x[None, :] - c[:, 2:3]) ** 2 / (2 * s[:, None] ** 2))
+    for z0 in range(0, N, 8):
+        f = torch.einsum("kz,ky,kx->zyx", gz[:, z0:z0 + 8], gy, gx)
+        occ[z0:z0 + 8] = f >= level
+    return pack_dense_torch(occ)
+
+
+def radius_field(res, seed, base=2, span=30, count=16, device=None):
+    """int8 fine radius grid r = base + floor(span * clamp(s, 0, 1))."""
+    N = 2 * res
+    centres, widths, amps = radius_params(seed, count)
+    if device is None:
+        x = _axis(N)
+        out = np.empty((N, N, N), dtype=np.int8)
+        for z0 in range(0, N, 16):
+            zs = x[z0:z0 + 16]
+            f = np.zeros((len(zs), N, N))
+            for c, s, a in zip(centres, widths, amps):
+                f += a * np.exp(-(zs - c[2])[:, None, None] ** 2 / (2 * s * s)) * \
+                    np.exp(-(x - c[1])[None, :, None] ** 2 / (2 * s * s)) * \
+                    np.exp(-(x - c[0])[None, None, :] ** 2 / (2 * s * s))
+            out[z0:z0 + 16] = base + np.floor(span * np.clip(f, 0.0, 1.0)).astype(np.int8)
+        return out.reshape(-1)
+    import torch
+    x = torch.as_tensor(_axis(N), device=device)
+    c = torch.as_tensor(centres, device=device)
+    s = torch.as_tensor(widths, device=device)
+    a = torch.as_tensor(amps, device=device)
+    gx = torch.exp(-(x[None, :] - c[:, 0:1]) ** 2 / (2 * s[:, None] ** 2)) * a[:, None]
+    gy = torch.exp(-(x[None, :] - c[:, 1:2]) ** 2 / (2 * s[:, None] ** 2))
+    gz = torch.exp(-(x[None, :] - c[:, 2:3]) ** 2 / (2 * s[:, None] ** 2))
+    out = torch.empty((N, N, N), dtype=torch.int8, device=device)
+    for z0 in range(0, N, 8):
+        f = torch.einsum("kz,ky,kx->zyx", gz[:, z0:z0 + 8], gy, gx)
+        out[z0:z0 + 8] = (base + torch.floor(span * f.clamp(0.0, 1.0))).to(torch.int8)
+    return out.reshape(-1)
+
+
+def pack_dense(occ):
+    """Dense bool [z, y, x] (edge N) -> packed grid uint8[res^3] (x-fastest)."""
+    N = occ.shape[0]
+    res = N // 2
+    o = occ.reshape(res, 2, res, 2, res, 2)  # z, zb, y, yb, x, xb
+    out = np.zeros((res, res, res), dtype=np.uint8)
+    for zb in range(2):
+        for yb in range(2):
+            for xb in range(2):
+                out |= (o[:, zb, :, yb, :, xb].astype(np.uint8) << (xb + 2 * yb + 4 * zb))
+    return out.reshape(-1)
+
+
+def unpack_dense(grid, res):
+    g = np.asarray(grid, dtype=np.uint8).reshape(res, res, res)
+    occ = np.zeros((res, 2, res, 2, res, 2), dtype=bool)
+    for zb in range(2):
+        for yb in range(2):
+            for xb in range(2):
+                occ[:, zb, :, yb, :, xb] = (g >> (xb + 2 * yb + 4 * zb)) & 1
+    return occ.reshape(2 * res, 2 * res, 2 * res)
+
+
+def pack_dense_torch(occ):
+    import torch
+    N = occ.shape[0]
+    res = N // 2
+    o = occ.reshape(res, 2, res, 2, res, 2).to(torch.uint8)
+    out = torch.zeros((res, res, res), dtype=torch.uint8, device=occ.device)
+    for zb in range(2):
+        for yb in range(2):
+            for xb in range(2):
+                out |= o[:, zb, :, yb, :, xb] << (xb + 2 * yb + 4 * zb)
+    return out.reshape(-1)
+
+
+def random_grid(res, seed, density=0.5, blobs=6):
+    """Small random test grid: a few random spheres plus sparse noise."""
+    rng = np.random.default_rng(seed)
+    N = 2 * res
+    z, y, x = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    occ = np.zeros((N, N, N), dtype=bool)
+    for _ in range(blobs):
+        c = rng.uniform(0.25 * N, 0.75 * N, size=3)
+        r = rng.uniform(0.05 * N, 0.18 * N)
+        occ |= (x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2 <= r * r
+    noise = rng.random((N, N, N)) < 0.002 * density
+    inner = np.zeros_like(occ)
+    m = N // 5
+    inner[m:N - m, m:N - m, m:N - m] = True
+    occ |= noise & inner
+    return pack_dense(occ)

@@ -1,0 +1,169 @@
+/*
+ * gmorpho_gb300.h — C ABI of libgmorpho_gb300, the GB300-native GMorpho.
+ *
+ * Drop-in boundary for the reference library's hot path
+ *   GMorpho::Load -> Voxelizer, ScaleField, GMorpho::Update
+ *   (dilation, erosion, marching cubes, normals), Grid pyramids, BVH.
+ * Each entry point names the reference interface it replaces
+ * (superboubek/Broxy, GMorpho/...).
+ *
+ * Conventions
+ *   - plain pointers and sizes; d_* are device pointers, h_* host pointers;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream);
+ *   - every call returns a gm_status and never aborts; a message for the
+ *     last failure is available from gm_ctx_last_error();
+ *   - grids use the reference's packed layout: uint8[res^3], byte
+ *     cx + res*cy + res*res*cz holds fine voxels 2c + (i,j,k) at bit
+ *     i + 2j + 4k; fine fields (radius grid) are x-fastest with edge 2*res;
+ *   - device buffers passed in must be 16-byte aligned;
+ *   - res is a power of two in [16, 1024] (fine edge 32 .. 2048).
+ */
+#ifndef GMORPHO_GB300_H
+#define GMORPHO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GM_ABI_VERSION 1
+
+typedef enum {
+  GM_OK = 0,
+  GM_ERR_INVALID_ARGUMENT = 1,
+  GM_ERR_CUDA = 2,
+  GM_ERR_OUT_OF_MEMORY = 3,
+  GM_ERR_UNSUPPORTED = 4,
+  GM_ERR_CAPACITY = 5,
+  GM_ERR_NOT_READY = 6
+} gm_status;
+
+/* GM_REF reproduces the reference's two-level closing bit for bit;
+ * GM_EXACT applies the fine predicates at every voxel (pure ball closing). */
+typedef enum { GM_REF = 0, GM_EXACT = 1 } gm_mode;
+/* dilation structuring element; the erosion is always by sphere
+ * (GMorpho/GMorpho.cu:7784-7790). */
+typedef enum { GM_SE_SPHERE = 0, GM_SE_CUBE = 1 } gm_se;
+/* ScaleField brush modes (GMorpho/ScaleField.h:33, EditMode). */
+typedef enum { GM_BRUSH_MAX = 1, GM_BRUSH_MIN = 2, GM_BRUSH_ZERO = 3 } gm_brush_mode;
+
+typedef struct gm_ctx gm_ctx;
+
+/* Grid attributes (GMorpho/Grid.h:40-58 GridGPU: bbox, res, data_res,
+ * cell_size). */
+typedef struct {
+  float bbox_min[3];
+  float bbox_max[3];
+  int32_t res;
+  int32_t data_res[3];
+  float cell_size;
+} gm_grid_desc;
+
+/* A mesh resident on the device, owned by the context and valid until the
+ * next call that produces a mesh on the same context. */
+typedef struct {
+  const float* vertices;      /* 3 * num_vertices */
+  const float* normals;       /* 3 * num_vertices */
+  const uint32_t* triangles;  /* 3 * num_triangles */
+  int64_t num_vertices;
+  int64_t num_triangles;
+} gm_mesh_view;
+
+/* Options of gm_update (GMorpho::set_* setters, GMorpho/GMorpho.h:67-72). */
+typedef struct {
+  int32_t use_asymmetric_closing; /* 1: cube dilation + 200 bilateral iterations */
+  int32_t bilateral_filtering;    /* 0: plain normals */
+  int32_t mode;                   /* gm_mode */
+} gm_update_opts;
+
+/* ---------------------------------------------------------------- misc */
+const char* gm_status_string(gm_status s);
+int gm_abi_version(void);
+
+/* Context: device selection, cached workspaces and the last mesh.  Replaces
+ * the global GMorpho / Grid / MarchingCubesMesher state of the reference
+ * (GMorpho/GMorpho.h:48-170, BroxyViewer.cpp:42-45). */
+gm_status gm_ctx_create(int device, gm_ctx** out);
+gm_status gm_ctx_destroy(gm_ctx* ctx);
+const char* gm_ctx_last_error(const gm_ctx* ctx);
+/* number of this library's kernels launched on the context so far */
+long long gm_ctx_kernel_launches(const gm_ctx* ctx);
+/* Per-kernel timing (the reference prints GET_TIME spans around each
+ * kernel, GMorpho/timing.h:28): when enabled, every launch is bracketed by
+ * CUDA events on its own stream.  gm_ctx_profile_read writes a JSON object
+ * {kernel: {"launches": n, "ms": total}} into buf and returns the bytes
+ * needed (including the terminating zero). */
+gm_status gm_ctx_profile(gm_ctx* ctx, int32_t enable);
+gm_status gm_ctx_profile_reset(gm_ctx* ctx);
+int64_t gm_ctx_profile_read(gm_ctx* ctx, char* buf, int64_t cap);
+
+/* ---------------------------------------------------------------- a2 */
+/* Voxelizer::ComputeGridAttributes (GMorpho/Voxelizer.cu:431-455): bbox of
+ * the points grown by 2*maxExtent/base_res + margin, cubic res = base_res. */
+gm_status gm_grid_attributes(const float* h_points, int64_t num_points, int32_t base_res, float margin,
+                             gm_grid_desc* out);
+/* Voxelizer::VoxelizeConservative (GMorpho/Voxelizer.cu:724-796): parity
+ * solid fill plus conservative surface voxels, into a zeroed packed grid. */
+gm_status gm_voxelize(gm_ctx* ctx, const gm_grid_desc* desc, const float* d_points, int64_t num_points,
+                      const uint32_t* d_triangles, int64_t num_triangles, uint8_t* d_grid, void* stream);
+
+/* ---------------------------------------------------------------- a3 */
+/* ScaleField::UpdateGridGlobalScale (GMorpho/ScaleField.cu:143-146). */
+gm_status gm_scalefield_fill(gm_ctx* ctx, int8_t* d_scale, int64_t num_voxels, int32_t value, void* stream);
+/* ScaleField::UpdateGrid / UpdateScaleGrid (GMorpho/ScaleField.cu:81-202),
+ * one brush point; cell_size is the fine (scale-field) cell size. */
+gm_status gm_scalefield_brush(gm_ctx* ctx, int8_t* d_scale, int32_t fine_res, const float* bbox_min,
+                              float cell_size, const float* position, float scale, float support,
+                              float global_scale, gm_brush_mode mode, void* stream);
+
+/* ---------------------------------------------------------------- a4 */
+/* Grid::BuildTexMipmaps(const ScaleField&) (GMorpho/Grid.cu:1000-1154): the
+ * OR / max-radius texel pyramid, levels 0..log2(res) concatenated. */
+int64_t gm_pyramid_texels(int32_t res);
+gm_status gm_pyramid_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_grid, const int8_t* d_scale,
+                           int32_t uniform_radius, uint64_t* d_pyramid, void* stream);
+
+/* ---------------------------------------------------------------- a5..a11 */
+/* GMorpho::DilateBySphereMipmap / DilateByCubeMipmap + ErodeBySphereMipmap
+ * (GMorpho/GMorpho.cu:3231-3314, 3538-3596, 6627-6702) on device buffers.
+ * d_scale = NULL uses uniform_radius everywhere; radii are clamped to
+ * [2,127] (GMorpho/Grid.cu:990-991).  d_dilation / d_contour may be NULL. */
+gm_status gm_close(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
+                   int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, uint8_t* d_dilation,
+                   uint8_t* d_contour, void* stream);
+
+/* ---------------------------------------------------------------- a12..a16 */
+/* GMorpho::ExtractClosingMesh (GMorpho/GMorpho.cu:6814-7001): contour
+ * marching cubes at isovalue 0.95 in the reference's emission order, then
+ * normals and `bilateral_iters` bilateral normal iterations. */
+gm_status gm_mesh(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closing, int32_t bilateral_iters,
+                  gm_mesh_view* out, void* stream);
+
+/* ---------------------------------------------------------------- a17 */
+/* GMorpho::Update(Mesh&, const ScaleField&, const FrameField&)
+ * (GMorpho/GMorpho.cu:7775-7817) from host buffers: copies the input grid
+ * (and the scale grid when h_scale != NULL) to the device, closes (skipped
+ * when floor(2*global_scale/cell_size) <= 1, GMorpho.cu:7783), meshes, and
+ * leaves the mesh on the context; fetch it with gm_mesh_download. */
+gm_status gm_update(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_input, const int8_t* h_scale,
+                    float global_scale, const gm_update_opts* opts, int64_t* num_vertices,
+                    int64_t* num_triangles, void* stream);
+/* Copy the context's last mesh to host buffers (GMorpho.cu:6992-7000);
+ * any pointer may be NULL to skip that array. */
+gm_status gm_mesh_download(gm_ctx* ctx, float* h_vertices, float* h_normals, uint32_t* h_triangles, void* stream);
+
+/* ---------------------------------------------------------------- layout */
+/* Voxelizer::ConvertBucketToPacketGrid (GMorpho/Voxelizer.cu:798-849):
+ * z-words (uint32 of 32 consecutive z voxels, x-fastest over (N, N, N/32))
+ * to the packed byte grid, and back. */
+gm_status gm_layout_zwords_to_packed(gm_ctx* ctx, int32_t res, const uint32_t* d_zwords, uint8_t* d_grid,
+                                     void* stream);
+gm_status gm_layout_packed_to_zwords(gm_ctx* ctx, int32_t res, const uint8_t* d_grid, uint32_t* d_zwords,
+                                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GMORPHO_GB300_H */
