@@ -24,7 +24,7 @@ class DevicePtrArray:
     (__cuda_array_interface__), e.g. the mesh of a context."""
 
     def __init__(self, ptr, shape, typestr):
-        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (ptr or 0, True),
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (ptr or 0, False),
                                          "version": 3, "strides": None}
 
 
