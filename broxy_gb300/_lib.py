@@ -56,6 +56,7 @@ PROTOTYPES = {
     "gm_pyramid_texels": (C.c_int64, [C.c_int32]),
     "gm_pyramid_build": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int32, _P, _P]),
     "gm_close": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int32, C.c_int, C.c_int, _P, _P, _P, _P]),
+    "gm_close_noalloc": (C.c_int, [C.POINTER(GridDesc), _P, _P, C.c_int32, C.c_int, C.c_int, _P, _P, _P, _P]),
     "gm_mesh": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.c_int32, C.POINTER(MeshView), _P]),
     "gm_update": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_float, C.POINTER(UpdateOpts),
                             C.POINTER(C.c_int64), C.POINTER(C.c_int64), _P]),

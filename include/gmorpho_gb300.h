@@ -134,6 +134,22 @@ gm_status gm_close(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input
                    int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, uint8_t* d_dilation,
                    uint8_t* d_contour, void* stream);
 
+/* The closing of gm_close for callers that cannot call cudaMalloc (a host
+ * application that owns the device memory budget and forbids library
+ * allocations, or a latency-bound loop that cannot take cudaMalloc's
+ * implicit synchronisation).  No counterpart in the reference library.
+ * Allocates nothing: its scratch is a fixed 16 MiB array held by the library
+ * on every GPU that loads it (until exit), so res <= 64 (128^3 fine voxels);
+ * larger grids return GM_ERR_CAPACITY.  Inputs and outputs are the caller's,
+ * as for gm_close, on the current device.  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (other streams, other threads) race on it.  No context,
+ * no kernel counter, no error message beyond the status. */
+gm_status gm_close_noalloc(const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
+                           int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing,
+                           uint8_t* d_dilation, uint8_t* d_contour, void* stream);
+
 /* ---------------------------------------------------------------- a12..a16 */
 /* GMorpho::ExtractClosingMesh (GMorpho/GMorpho.cu:6814-7001): contour
  * marching cubes at isovalue 0.95 in the reference's emission order, then
