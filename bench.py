@@ -101,9 +101,15 @@ def make_inputs(res, seed, device):
 # output streams in the layout it works on).
 KERNEL_BYTES_PER_VOXEL = {
     "k_dil_pass_x": 1 / 8 + 1,            # packed grid in, u8 distance out
-    "k_axis_pass": 2 + 2,                 # u16 (or u8) field in, u16 out (full-resolution passes)
-    "k_final_z": 2 + 1 + 1 / 8,           # u16 in, radius in (dilation), packed bits out
+    "k_pass_dil_y": 1 + 2,                # u8 distances in, u16 partial sums out
+    "k_pass_dil_z": 2 + 1 + 1 / 8,        # u16 in, radius in, packed dilation bits out
+    "k_pass_ero_y": 2 + 2,                # u16 in, u16 out (voxel centres)
+    "k_pass_ero_z": 2 + 1 / 8,            # u16 in, packed eroded bits out
+    "k_pass_erob_y": 1 + 0.5,             # lattice points 2c+1: (res, N, N) u16 in, (res, res, N) out
+    "k_pass_erob_z": 0.5 + 1 / 8,         # (res, res, N) u16 in, one flag per cell out
     "k_ero_pass_x": 1 / 8 + 1 + 2 + 1,    # contour bits + radius in, centre + lattice fields out
+    "k_axis_pass": 2 + 2,                 # general-radius fallback passes
+    "k_final_z": 2 + 1 + 1 / 8,
 }
 
 
@@ -153,6 +159,17 @@ def run_ours(args, rank, world):
     value = world * V / (ms_max * 1e-3) / 1e9
 
     # ---- e2e through the host-buffer C ABI (gm_update + gm_mesh_download)
+    if args.no_e2e:
+        e2e_ms, nv2, nt2 = float("nan"), nv, nt
+    else:
+        e2e_ms, nv2, nt2 = run_e2e(args, ctx, desc, X, R, nv, nt, world, dev)
+    assert (nv2, nt2) == (nv, nt)
+    return finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value)
+
+
+def run_e2e(args, ctx, desc, X, R, nv, nt, world, dev):
+    import torch
+    from broxy_gb300 import api
     hX = torch.empty(X.numel(), dtype=torch.uint8, pin_memory=True)
     hR = torch.empty(R.numel(), dtype=torch.int8, pin_memory=True)
     hX.copy_(X.cpu())
@@ -185,8 +202,10 @@ def run_ours(args, rank, world):
         t = torch.tensor([e2e_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    assert (nv2, nt2) == (nv, nt)
+    return e2e_ms, nv2, nt2
 
+
+def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value):
     # ---- roofline of the dominant kernel and of the morphology passes
     hbm, peak_kind = peaks()
     top = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else (None, None)
@@ -311,6 +330,7 @@ def main():
     ap.add_argument("--res", type=int, default=RES)
     ap.add_argument("--cpu-res", type=int, default=64, help="base cells per axis of the CPU crop")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -292,21 +292,36 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
   }
 }
 
-// vertex offset of the cube at fine min corner (fx,fy,fz) and its edge
-// mask, or -1 when the cube is not in the compacted list.  The cell must lie
-// in the block tile (local coordinates 0..16).
-__device__ __forceinline__ long long cube_voff(const uint8_t* tile, const uint32_t* __restrict__ cell_voff,
-                                               int res, int ox, int oy, int oz, int fx, int fy, int fz, int& em) {
-  const int gx = fx >> 1, gy = fy >> 1, gz = fz >> 1;
-  const int k = (fx & 1) | ((fy & 1) << 1) | ((fz & 1) << 2);
+// Per-cell summary used for neighbour lookups: bits 0..7 = mixed cubes,
+// bits 8+k / 16+k / 24+k = cube k owns a vertex on edge 0 / 3 / 8.
+__device__ __forceinline__ uint32_t cell_info(const uint8_t* tile, int lx, int ly, int lz, int gx, int gy, int gz,
+                                              int res) {
   int vals[8];
-  cube_values(tile, gx - ox, gy - oy, gz - oz, vals);
+  cube_values(tile, lx, ly, lz, vals);
   const int m = mixed_mask(vals, gx, gy, gz, res);
-  if (!((m >> k) & 1)) { em = 0; return -1; }
-  uint32_t off = cell_voff[cell_index(gx, gy, gz, res)];
-  for (int s = 0; s < k; s++)
-    if ((m >> s) & 1) off += nv_owned(edge_mask(vals[s]));
-  em = edge_mask(vals[k]);
+  uint32_t info = (uint32_t)m;
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    if (!((m >> s) & 1)) continue;
+    const int em = edge_mask(vals[s]);
+    info |= (uint32_t)(em & 1) << (8 + s);
+    info |= (uint32_t)((em >> 3) & 1) << (16 + s);
+    info |= (uint32_t)((em >> 8) & 1) << (24 + s);
+  }
+  return info;
+}
+
+constexpr int kInfoE = kBrick + 1;  // cells 0..16 of the brick (own + one neighbour layer)
+
+// Vertex offset of cube k of the cell whose summary is `info` (absent: -1),
+// with its edge-0 / edge-3 ownership.
+__device__ __forceinline__ long long cube_voff(uint32_t info, uint32_t cell_off, int k, int& e0, int& e3) {
+  if (!((info >> k) & 1)) { e0 = e3 = 0; return -1; }
+  const uint32_t below = info & ((1u << k) - 1u);
+  const uint32_t off = cell_off + __popc((info >> 8) & below) + __popc((info >> 16) & below) +
+                       __popc((info >> 24) & below);
+  e0 = (info >> (8 + k)) & 1;
+  e3 = (info >> (16 + k)) & 1;
   return (long long)off;
 }
 
@@ -316,20 +331,25 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
                                                               uint32_t* __restrict__ T, uint32_t nt_total,
                                                               uint32_t* __restrict__ fix, int fix_cap) {
   __shared__ uint8_t tile[kTileCells];
+  __shared__ uint32_t info[kInfoE * kInfoE * kInfoE];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
   load_tile(C, res, ox, oy, oz, tile);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) {
+    const int lx = i % kInfoE, ly = (i / kInfoE) % kInfoE, lz = i / (kInfoE * kInfoE);
+    info[i] = cell_info(tile, lx, ly, lz, ox + lx, oy + ly, oz + lz, res);
+  }
   __syncthreads();
   CellCounts acc{0, 0, 0, 0};
   for (int i = 0; i < kCellsPerThread; i++) {
     const int l = threadIdx.x * kCellsPerThread + i;
     int lx, ly, lz;
     local_coords(l, lx, ly, lz);
+    if (!(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
-    if (!m) continue;
-    acc.tris += cell_counts(vals, m).tris;
+    acc.tris += cell_counts(vals, (int)(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu)).tris;
   }
   CellCounts tot;
   const CellCounts pre = block_exclusive_scan(acc, tot);
@@ -338,11 +358,12 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
     const int l = threadIdx.x * kCellsPerThread + i;
     int lx, ly, lz;
     local_coords(l, lx, ly, lz);
+    const uint32_t myinfo = info[lx + kInfoE * (ly + kInfoE * lz)];
+    const int m = (int)(myinfo & 0xffu);
+    if (!m) continue;
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    const int m = mixed_mask(vals, gx, gy, gz, res);
-    if (!m) continue;
     uint32_t vo = cell_voff[cell_index(gx, gy, gz, res)];
     for (int s = 0; s < 8; s++) {
       if (!((m >> s) & 1)) continue;
@@ -362,22 +383,42 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
       // neighbour cubes +x, +x+y, +y, +z, +x+z, +y+z (BuildNeighbors order,
       // GMorpho.cu:6480-6487) and the edges they own
       // (MarchingCubesMesher.cu:1392-1456)
-      int e1, e2, e3, e4, e5, e7;
-      const long long id1 = (em & (2 | 512)) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx + 1, fy, fz, e1) : -1;
-      const long long id2 = (em & 1024) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx + 1, fy + 1, fz, e2) : -1;
-      const long long id3 = (em & (4 | 2048)) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx, fy + 1, fz, e3) : -1;
-      const long long id4 = (em & (16 | 128)) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx, fy, fz + 1, e4) : -1;
-      const long long id5 = (em & 32) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx + 1, fy, fz + 1, e5) : -1;
-      const long long id7 = (em & 64) ? cube_voff(tile, cell_voff, res, ox, oy, oz, fx, fy + 1, fz + 1, e7) : -1;
-      if ((em & 2) && id1 >= 0) vert[1] = (uint32_t)id1 + (e1 & 1);
-      if (em & 4) vert[2] = id3 >= 0 ? (uint32_t)id3 : 0u;
-      if (em & 16) vert[4] = id4 >= 0 ? (uint32_t)id4 : 0u;
-      if ((em & 32) && id5 >= 0) vert[5] = (uint32_t)id5 + (e5 & 1);
-      if (em & 64) vert[6] = id7 >= 0 ? (uint32_t)id7 : 0u;
-      if ((em & 128) && id4 >= 0) vert[7] = (uint32_t)id4 + (e4 & 1);
-      if (em & 512) vert[9] = id1 >= 0 ? (uint32_t)id1 + (e1 & 1) + ((e1 >> 3) & 1) : 0u;
-      if (em & 1024) vert[10] = id2 >= 0 ? (uint32_t)id2 + (e2 & 1) + ((e2 >> 3) & 1) : 0u;
-      if (em & 2048) vert[11] = id3 >= 0 ? (uint32_t)id3 + (e3 & 1) + ((e3 >> 3) & 1) : 0u;
+      auto nb = [&](int dx, int dy, int dz, int& e0, int& e3) -> long long {
+        const int nfx = fx + dx, nfy = fy + dy, nfz = fz + dz;
+        const int cx = (nfx >> 1) - ox, cy = (nfy >> 1) - oy, cz = (nfz >> 1) - oz;
+        const uint32_t ninfo = info[cx + kInfoE * (cy + kInfoE * cz)];
+        const int k = (nfx & 1) | ((nfy & 1) << 1) | ((nfz & 1) << 2);
+        if (!((ninfo >> k) & 1)) { e0 = e3 = 0; return -1; }
+        return cube_voff(ninfo, cell_voff[cell_index(nfx >> 1, nfy >> 1, nfz >> 1, res)], k, e0, e3);
+      };
+      int a0 = 0, a3 = 0;
+      if (em & (2 | 512)) {
+        const long long id1 = nb(1, 0, 0, a0, a3);
+        if ((em & 2) && id1 >= 0) vert[1] = (uint32_t)id1 + a0;
+        if (em & 512) vert[9] = id1 >= 0 ? (uint32_t)id1 + a0 + a3 : 0u;
+      }
+      if (em & 1024) {
+        const long long id2 = nb(1, 1, 0, a0, a3);
+        vert[10] = id2 >= 0 ? (uint32_t)id2 + a0 + a3 : 0u;
+      }
+      if (em & (4 | 2048)) {
+        const long long id3 = nb(0, 1, 0, a0, a3);
+        if (em & 4) vert[2] = id3 >= 0 ? (uint32_t)id3 : 0u;
+        if (em & 2048) vert[11] = id3 >= 0 ? (uint32_t)id3 + a0 + a3 : 0u;
+      }
+      if (em & (16 | 128)) {
+        const long long id4 = nb(0, 0, 1, a0, a3);
+        if (em & 16) vert[4] = id4 >= 0 ? (uint32_t)id4 : 0u;
+        if ((em & 128) && id4 >= 0) vert[7] = (uint32_t)id4 + a0;
+      }
+      if (em & 32) {
+        const long long id5 = nb(1, 0, 1, a0, a3);
+        if (id5 >= 0) vert[5] = (uint32_t)id5 + a0;
+      }
+      if (em & 64) {
+        const long long id7 = nb(0, 1, 1, a0, a3);
+        vert[6] = id7 >= 0 ? (uint32_t)id7 : 0u;
+      }
       // reversed winding (MarchingCubesMesher.cu:1487-1497)
       const uint64_t tl = c_tri_packed[v];
       const int cnt = c_tri_count[v];
@@ -424,30 +465,79 @@ __global__ void k_adj_count(const uint32_t* __restrict__ T, int64_t nt, uint32_t
     atomicAdd(cnt + T[i], 1u);
 }
 
-// exclusive scan of n u32 (single block, chunked) -> out[0..n]
-__global__ void __launch_bounds__(1024) k_scan_u32(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
-                                                    int64_t n) {
+// Exclusive scan of n u32 into out[0..n] in three kernels: per-block sums of
+// 2048-element chunks, a scan of the block sums, then per-chunk scans.
+constexpr int kScanChunk = 2048;
+
+__global__ void __launch_bounds__(256) k_scan_sums(const uint32_t* __restrict__ in, int64_t n,
+                                                    uint32_t* __restrict__ sums) {
+  __shared__ uint32_t ws[8];
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk;
+  uint32_t s = 0;
+  for (int i = threadIdx.x; i < kScanChunk; i += 256)
+    if (base + i < n) s += in[base + i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; w++) t += ws[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_scan_small(uint32_t* __restrict__ v, int n) {
   __shared__ uint32_t part[1024];
   const int t = threadIdx.x;
-  const int64_t per = (n + 1023) / 1024;
-  const int64_t b0 = t * per, b1 = min(n, b0 + per);
+  const int per = (n + 1023) / 1024;
+  const int b0 = t * per, b1 = min(n, b0 + per);
   uint32_t s = 0;
-  for (int64_t b = b0; b < b1; b++) s += in[b];
+  for (int b = b0; b < b1; b++) s += v[b];
   part[t] = s;
   __syncthreads();
   for (int o = 1; o < 1024; o <<= 1) {
-    const uint32_t v = t >= o ? part[t - o] : 0;
+    const uint32_t x = t >= o ? part[t - o] : 0;
     __syncthreads();
-    part[t] += v;
+    part[t] += x;
     __syncthreads();
   }
   uint32_t run = part[t] - s;
-  for (int64_t b = b0; b < b1; b++) {
-    const uint32_t v = in[b];
-    out[b] = run;
-    run += v;
+  for (int b = b0; b < b1; b++) {
+    const uint32_t x = v[b];
+    v[b] = run;
+    run += x;
   }
-  if (t == 1023) out[n] = part[1023];
+  if (t == 1023) v[n] = part[1023];
+}
+
+__global__ void __launch_bounds__(256) k_scan_apply(const uint32_t* __restrict__ in, int64_t n,
+                                                     const uint32_t* __restrict__ sums, uint32_t* __restrict__ out) {
+  __shared__ uint32_t wtot[8];
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * 8;
+  uint32_t v[8], s = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    v[j] = base + j < n ? in[base + j] : 0u;
+    s += v[j];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
+  }
+  if (lane == 31) wtot[wid] = x;
+  __syncthreads();
+  uint32_t wpre = 0;
+  for (int w = 0; w < wid; w++) wpre += wtot[w];
+  uint32_t run = sums[blockIdx.x] + wpre + x - s;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    if (base + j < n) out[base + j] = run;
+    run += v[j];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 255) out[n] = sums[gridDim.x];
 }
 
 __global__ void k_adj_fill(const uint32_t* __restrict__ T, int64_t nt, const uint32_t* __restrict__ rowptr,
@@ -624,7 +714,14 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   const int sms = a.num_sms;
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
   GM_LAUNCH(kc, "k_adj_count", st, k_adj_count<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.cursor));
-  GM_LAUNCH(kc, "k_scan_u32", st, k_scan_u32<<<1, 1024, 0, st>>>(b.cursor, b.rowptr, nv));
+  {
+    const int nchunks = (int)((nv + kScanChunk - 1) / kScanChunk);
+    // chunk sums go to the per-cell offsets buffer, unused once triangles are out
+    uint32_t* sums = b.cell_voff;
+    GM_LAUNCH(kc, "k_scan_sums", st, k_scan_sums<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums));
+    GM_LAUNCH(kc, "k_scan_small", st, k_scan_small<<<1, 1024, 0, st>>>(sums, nchunks));
+    GM_LAUNCH(kc, "k_scan_apply", st, k_scan_apply<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums, b.rowptr));
+  }
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
   GM_LAUNCH(kc, "k_adj_fill", st, k_adj_fill<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.rowptr, b.cursor, b.adj));
   GM_LAUNCH(kc, "k_adj_sort", st, k_adj_sort<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.rowptr, b.adj, nv));

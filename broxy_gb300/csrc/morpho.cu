@@ -396,6 +396,213 @@ __global__ void __launch_bounds__(256) k_final_z_base(const uint16_t* __restrict
 }
 
 // ---------------------------------------------------------------------
+// packed 16-bit min-plus pass (y or z) with DPX add-min
+//
+// Each thread owns two adjacent x columns (one u32 = two u16 lanes) and 16
+// consecutive outputs along the pass axis, so one __viaddmin_u16x2 updates
+// two outputs per tap.  A block is 64 columns x 64 outputs x 2 "third"
+// coordinates (256 threads); the input tile with its halo sits in shared
+// memory.  Taps are visited outward (|delta| = 0, 1, 2, ...); a warp stops
+// as soon as the kernel alone exceeds every output it holds.  A tile with
+// no finite input is written directly.  Requires cap <= 32767 so that
+// value + kernel never wraps in 16 bits.
+//   FIN 0: write the u16 field;  FIN 1: dilation threshold + packed bytes;
+//   FIN 2: erosion threshold (centres) + packed bytes;
+//   FIN 3: erosion threshold at lattice points 2c+1, one flag per cell.
+// ---------------------------------------------------------------------
+
+constexpr int kDpxCols = 64;   // x columns per block
+constexpr int kDpxOut = 64;    // outputs per block along the axis (4 warps x 16)
+constexpr int kDpxPer = 16;    // outputs per thread
+
+template <int G>
+__device__ __forceinline__ uint32_t gpair(int delta, uint32_t cap) {
+  uint32_t g = kern_g<G>(delta);
+  g = g < cap ? g : cap;
+  return g | (g << 16);
+}
+
+template <int G>
+__device__ __forceinline__ uint32_t step_min(uint32_t row, uint32_t g, uint32_t best) {
+  if (G == KERN_CUBE) return __vminu2(__vmaxu2(row, g), best);
+  return __viaddmin_u16x2(row, g, best);
+}
+
+template <int G, typename TIn>
+__device__ __forceinline__ uint32_t load_pair(const TIn* p, uint32_t cap) {
+  uint32_t a, b;
+  if (sizeof(TIn) == 1) {
+    const uint16_t v = *reinterpret_cast<const uint16_t*>(p);
+    a = v & 0xffu;
+    b = v >> 8;
+    if (G != KERN_CUBE) { a = a * a; b = b * b; }
+  } else {
+    const uint32_t v = *reinterpret_cast<const uint32_t*>(p);
+    a = v & 0xffffu;
+    b = v >> 16;
+  }
+  a = a < cap ? a : cap;
+  b = b < cap ? b : cap;
+  return a | (b << 16);
+}
+
+size_t dpx_smem_bytes(int sub, int halo) {
+  const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
+  return (size_t)2 * span * 32 * sizeof(uint32_t);
+}
+
+template <int G, typename TIn, int FIN>
+__global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
+                                                  uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
+                                                  int sub, int halo, uint32_t cap, const int8_t* __restrict__ R,
+                                                  int uniform_r, int res) {
+  extern __shared__ uint32_t tileu[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int tpar = w >> 2, grp = w & 3;
+  const int x = blockIdx.x * kDpxCols + 2 * lane;
+  const int na = axis == 1 ? ny : nz;
+  const int n3 = axis == 1 ? nz : ny;
+  const int nout = sub ? na / 2 : na;
+  const int third = 2 * blockIdx.z + tpar;
+  const int64_t sa = axis == 1 ? (int64_t)nx : (int64_t)nx * ny;
+  const int64_t s3 = axis == 1 ? (int64_t)nx * ny : (int64_t)nx;
+  const int o0 = blockIdx.y * kDpxOut;
+  const int step = sub ? 2 : 1;
+  const int lo = (sub ? 2 * o0 + 1 : o0) - halo;
+  const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
+  const uint32_t capp = cap | (cap << 16);
+  uint32_t* tile = tileu + tpar * span * 32;
+  const bool colok = x < nx && third < n3;
+  int finite = 0;
+  for (int s = grp; s < span; s += 4) {
+    const int a = lo + s;
+    uint32_t v = capp;
+    if (colok && a >= 0 && a < na) v = load_pair<G, TIn>(in + x + sa * a + s3 * third, cap);
+    tile[s * 32 + lane] = v;
+    finite |= v != capp;
+  }
+  finite = __syncthreads_or(finite);
+  const int obase = o0 + grp * kDpxPer;
+  const int sp0 = (sub ? 2 * obase + 1 : obase) - lo;
+  uint32_t best[kDpxPer];
+  if (finite) {
+    const uint32_t g0 = gpair<G>(0, cap);
+#pragma unroll
+    for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tile[(sp0 + step * j) * 32 + lane], g0, capp);
+    for (int k = 1; k <= halo; k++) {
+      const uint32_t gp = gpair<G>(k, cap), gm_ = gpair<G>(-k, cap);
+#pragma unroll
+      for (int j = 0; j < kDpxPer; j++) {
+        const int sp = sp0 + step * j;
+        best[j] = step_min<G>(tile[(sp + k) * 32 + lane], gp, best[j]);
+        best[j] = step_min<G>(tile[(sp - k) * 32 + lane], gm_, best[j]);
+      }
+      if ((k & 1) == 0) {
+        uint32_t m = best[0];
+#pragma unroll
+        for (int j = 1; j < kDpxPer; j++) m = __vmaxu2(m, best[j]);
+        const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
+        const uint32_t np = kern_g<G>(k + 1), nm = kern_g<G>(-(k + 1));
+        const uint32_t nxt = np < nm ? np : nm;
+        if (__all_sync(0xffffffffu, nxt >= mx)) break;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kDpxPer; j++) best[j] = capp;
+  }
+  if (FIN == 0) {
+    if (!colok) return;
+    const int64_t osa = axis == 1 ? (int64_t)nx : (int64_t)nx * ny;
+    const int64_t os3 = axis == 1 ? (int64_t)nx * nout : (int64_t)nx;
+#pragma unroll
+    for (int j = 0; j < kDpxPer; j++) {
+      const int o = obase + j;
+      if (o < nout) *reinterpret_cast<uint32_t*>(out16 + x + osa * o + os3 * third) = best[j];
+    }
+  } else if (FIN == 3) {
+    if (!colok) return;
+    // x is a cell index here; outputs are cells (x, third, o)
+#pragma unroll
+    for (int j = 0; j < kDpxPer; j++) {
+      const int o = obase + j;
+      if (o >= nout) continue;
+      const uint32_t v = best[j];
+      uint8_t* dst = out8 + cell_index(x, third, o, res);
+      dst[0] = (v & 0xffffu) < cap ? 1 : 0;
+      dst[1] = (v >> 16) < cap ? 1 : 0;
+    }
+  } else {
+    // threshold then pack 2 (x) x 2 (y = third pair) x 2 (z) bits per byte
+    __shared__ uint32_t xch[4][32][2];
+    const int N = 2 * res;
+    const int ru = clamp_radius(uniform_r);
+    uint32_t bytes[2] = {0u, 0u};  // 8 z pairs: bytes q = 0..7
+#pragma unroll
+    for (int j = 0; j < kDpxPer; j++) {
+      const int z = obase + j;
+      const uint32_t v = best[j];
+      uint32_t blo, bhi;
+      if (FIN == 1) {
+        int rlo = ru, rhi = ru;
+        if (R != nullptr && colok && z < N) {
+          const uint16_t rr = *reinterpret_cast<const uint16_t*>(R + fine_index(x, third, z, N));
+          rlo = clamp_radius((int)(int8_t)(rr & 0xff));
+          rhi = clamp_radius((int)(int8_t)(rr >> 8));
+        }
+        if (G == KERN_CUBE) {
+          blo = (v & 0xffffu) <= (uint32_t)rlo;
+          bhi = (v >> 16) <= (uint32_t)rhi;
+        } else {
+          blo = (v & 0xffffu) < (uint32_t)((rlo + 1) * (rlo + 1));
+          bhi = (v >> 16) < (uint32_t)((rhi + 1) * (rhi + 1));
+        }
+      } else {
+        blo = (v & 0xffffu) < cap;
+        bhi = (v >> 16) < cap;
+      }
+      const int q = j >> 1, zb = j & 1;
+      const uint32_t bits = (blo << (2 * tpar + 4 * zb)) | (bhi << (1 + 2 * tpar + 4 * zb));
+      bytes[q >> 2] |= bits << (8 * (q & 3));
+    }
+    if (tpar == 1) {
+      xch[grp][lane][0] = bytes[0];
+      xch[grp][lane][1] = bytes[1];
+    }
+    __syncthreads();
+    if (tpar == 0 && colok) {
+      bytes[0] |= xch[grp][lane][0];
+      bytes[1] |= xch[grp][lane][1];
+      const int cx = x >> 1, cy = third >> 1;
+#pragma unroll
+      for (int q = 0; q < kDpxPer / 2; q++) {
+        const int cz = obase / 2 + q;
+        if (2 * cz < N) out8[cell_index(cx, cy, cz, res)] = (uint8_t)((bytes[q >> 2] >> (8 * (q & 3))) & 0xffu);
+      }
+    }
+  }
+}
+
+template <int G, typename TIn, int FIN>
+static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
+                       int halo, uint32_t cap, const int8_t* R, int uniform_r, int res, cudaStream_t st,
+                       KernelCounter* kc, const char* name) {
+  const size_t smem = dpx_smem_bytes(sub, halo);
+  static size_t configured = 0;
+  if (smem > 48 * 1024 && smem > configured) {
+    cudaFuncSetAttribute(k_pass_dpx<G, TIn, FIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  const int na = axis == 1 ? ny : nz;
+  const int n3 = axis == 1 ? nz : ny;
+  const int nout = sub ? na / 2 : na;
+  dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, (n3 + 1) / 2);
+  GM_LAUNCH(kc, name, st,
+            k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
+                                                          uniform_r, res));
+}
+
+// ---------------------------------------------------------------------
 // cell-level kernels
 // ---------------------------------------------------------------------
 
@@ -568,22 +775,36 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   {
     const int W = N >> 5;
     GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x<<<dim3(res, res), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, res, dcap));
-    const int span = kTileOut + 2 * dil_halo;
-    dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
-    if (a.se == 1)
-      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CUBE, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(buf8, buf16a, N, N, N, 1, 0,
-                                                                              dil_halo, dil_cap));
-    else
-      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(buf8, buf16a, N, N, N, 1, 0,
-                                                                             dil_halo, dil_cap));
-    dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
     uint8_t* dst = exact ? D : Df;
-    if (a.se == 1)
-      GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CUBE, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(buf16a, dst, a.R, a.uniform_r, res,
-                                                                               dil_halo, dil_cap));
-    else
-      GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(buf16a, dst, a.R, a.uniform_r, res,
-                                                                              dil_halo, dil_cap));
+    if (dil_cap <= 32767) {
+      if (a.se == 1) {
+        launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, nullptr, 0, res, st,
+                                          kc, "k_pass_dil_y");
+        launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, N, N, N, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r,
+                                           res, st, kc, "k_pass_dil_z");
+      } else {
+        launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, nullptr, 0, res, st,
+                                         kc, "k_pass_dil_y");
+        launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, N, N, N, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r, res,
+                                          st, kc, "k_pass_dil_z");
+      }
+    } else {
+      const int span = kTileOut + 2 * dil_halo;
+      dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
+      if (a.se == 1)
+        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CUBE, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(
+                                             buf8, buf16a, N, N, N, 1, 0, dil_halo, dil_cap));
+      else
+        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(
+                                             buf8, buf16a, N, N, N, 1, 0, dil_halo, dil_cap));
+      dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
+      if (a.se == 1)
+        GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CUBE, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
+                                           buf16a, dst, a.R, a.uniform_r, res, dil_halo, dil_cap));
+      else
+        GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
+                                           buf16a, dst, a.R, a.uniform_r, res, dil_halo, dil_cap));
+    }
     if (!exact) {
       GM_LAUNCH(kc, "k_dil_select", st, k_dil_select<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(a.X, Df, D, res, dr));
     }
@@ -597,22 +818,34 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     const int W = N >> 5;
     const size_t smem = 4 * W * sizeof(uint32_t) + (a.R != nullptr ? 4 * (size_t)N : 0);
     GM_LAUNCH(kc, "k_ero_pass_x", st, k_ero_pass_x<<<dim3(res, res), 256, smem, st>>>(S, a.R, a.uniform_r, res, ehalo, K, buf16a, HL1));
-    const int span = kTileOut + 2 * ehalo;
-    // centres: y pass then fused final z pass
-    dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
-    GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CEN2, uint16_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(buf16a, buf16b, N, N, N, 1, 0,
-                                                                             ehalo, K));
-    dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
-    GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CEN2, FIN_ERO><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(buf16b, Ef, nullptr, 0, res, ehalo,
-                                                                              K));
-    if (!exact) {
-      // lattice points 2c+1: y pass (sub) then final z pass (sub)
-      const int span_s = 2 * kTileOut + 2 * ehalo;
-      dim3 gy(cdiv(res, 32), cdiv(res, kTileOut), N);
-      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT2, uint16_t><<<gy, dim3(32, kRows), span_s * 32 * 2, st>>>(HL1, HL2, res, N, N, 1, 1,
-                                                                                  ehalo, K));
-      dim3 gzb(cdiv(res, 32), cdiv(res, kTileOut), res);
-      GM_LAUNCH(kc, "k_final_z_base", st, k_final_z_base<<<gzb, dim3(32, kRows), span_s * 32 * 2, st>>>(HL2, Eb, res, ehalo, K));
+    if (K <= 32767) {
+      launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, N, N, N, 1, 0, ehalo, K, nullptr, 0, res, st, kc,
+                                         "k_pass_ero_y");
+      launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, N, N, N, 2, 0, ehalo, K, nullptr, 0, res, st, kc,
+                                         "k_pass_ero_z");
+      if (!exact) {
+        launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, res, N, N, 1, 1, ehalo, K, nullptr, 0, res, st, kc,
+                                           "k_pass_erob_y");
+        launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, res, res, N, 2, 1, ehalo, K, nullptr, 0, res, st, kc,
+                                           "k_pass_erob_z");
+      }
+    } else {
+      const int span = kTileOut + 2 * ehalo;
+      dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
+      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CEN2, uint16_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(
+                                           buf16a, buf16b, N, N, N, 1, 0, ehalo, K));
+      dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
+      GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CEN2, FIN_ERO><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
+                                         buf16b, Ef, nullptr, 0, res, ehalo, K));
+      if (!exact) {
+        const int span_s = 2 * kTileOut + 2 * ehalo;
+        dim3 gy(cdiv(res, 32), cdiv(res, kTileOut), N);
+        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT2, uint16_t><<<gy, dim3(32, kRows), span_s * 32 * 2, st>>>(
+                                             HL1, HL2, res, N, N, 1, 1, ehalo, K));
+        dim3 gzb(cdiv(res, 32), cdiv(res, kTileOut), res);
+        GM_LAUNCH(kc, "k_final_z_base", st, k_final_z_base<<<gzb, dim3(32, kRows), span_s * 32 * 2, st>>>(
+                                                HL2, Eb, res, ehalo, K));
+      }
     }
     GM_LAUNCH(kc, "k_ero_select", st, k_ero_select<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(a.X, D, Eb, Ef, a.C_out, res, dr,
                                                                     exact ? 1 : 0));
