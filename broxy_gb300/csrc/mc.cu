@@ -56,6 +56,25 @@ __device__ void load_tile(const uint8_t* __restrict__ C, int res, int ox, int oy
   }
 }
 
+// Loads the tile and tells (block-uniformly) whether it can hold a mixed
+// cube: a tile whose bytes are all 0x00 or all 0xff has none.
+__device__ bool load_tile_mixed(const uint8_t* __restrict__ C, int res, int ox, int oy, int oz, uint8_t* tile) {
+  int seen0 = 0, seen1 = 0, part = 0;
+  for (int i = threadIdx.x; i < kTileCells; i += blockDim.x) {
+    const int lx = i % kTileE, ly = (i / kTileE) % kTileE, lz = i / (kTileE * kTileE);
+    const int x = ox + lx, y = oy + ly, z = oz + lz;
+    const uint8_t v = (x < res && y < res && z < res) ? C[cell_index(x, y, z, res)] : (uint8_t)0;
+    tile[i] = v;
+    seen0 |= v == 0x00;
+    seen1 |= v == 0xff;
+    part |= v != 0x00 && v != 0xff;
+  }
+  const int mixed = __syncthreads_or(part | (seen0 & seen1));
+  if (mixed) return true;
+  // a block may have seen only zeros while another saw only full bytes
+  return __syncthreads_or(seen0) && __syncthreads_or(seen1);
+}
+
 // The eight MC cube values of cell (local lx,ly,lz): cube k has its min
 // corner at fine voxel 2c + o_k; value bit j = occupancy of corner j
 // (ComputeMCMData, GMorpho.cu:6146-6232).
@@ -158,8 +177,10 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restri
   __shared__ uint8_t tile[kTileCells];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  load_tile(C, res, ox, oy, oz, tile);
-  __syncthreads();
+  if (!load_tile_mixed(C, res, ox, oy, oz, tile)) {
+    if (threadIdx.x < 4) brick_tot[4 * blockIdx.x + threadIdx.x] = 0;
+    return;
+  }
   CellCounts acc{0, 0, 0, 0};
   for (int i = 0; i < kCellsPerThread; i++) {
     const int l = threadIdx.x * kCellsPerThread + i;
@@ -229,8 +250,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
   __shared__ uint8_t tile[kTileCells];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  load_tile(C, res, ox, oy, oz, tile);
-  __syncthreads();
+  if (!load_tile_mixed(C, res, ox, oy, oz, tile)) return;
   CellCounts acc{0, 0, 0, 0};
   for (int i = 0; i < kCellsPerThread; i++) {
     const int l = threadIdx.x * kCellsPerThread + i;
@@ -334,8 +354,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
   __shared__ uint32_t info[kInfoE * kInfoE * kInfoE];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  load_tile(C, res, ox, oy, oz, tile);
-  __syncthreads();
+  if (!load_tile_mixed(C, res, ox, oy, oz, tile)) return;
   for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) {
     const int lx = i % kInfoE, ly = (i / kInfoE) % kInfoE, lz = i / (kInfoE * kInfoE);
     info[i] = cell_info(tile, lx, ly, lz, ox + lx, oy + ly, oz + lz, res);

@@ -706,6 +706,152 @@ __global__ void k_ero_select(const uint8_t* __restrict__ X, const uint8_t* __res
   }
 }
 
+// ---------------------------------------------------------------------
+// the same cell-level kernels, four consecutive cells (one u32) per thread
+// block (64, 4): x quads along threadIdx.x, y along threadIdx.y, z = blockIdx.z
+// ---------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t ld4(const uint8_t* g, int x4, int y, int z, int res) {
+  return *reinterpret_cast<const uint32_t*>(g + cell_index(x4, y, z, res));
+}
+__device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
+
+__global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
+                                                     uint8_t* __restrict__ D, int res, DataRes dr) {
+  const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
+  const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
+  if (x4 >= res || y >= res) return;
+  // full flags of the base-pass byte for x in [x4, x4+4], (y, y+1) x (z, z+1)
+  uint32_t full[2][2];
+  uint32_t center = 0, dfc = 0;
+#pragma unroll
+  for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++) {
+      const int yy = y + dy, zz = z + dz;
+      uint32_t f = 0;
+      if (yy < res && zz < res) {
+        const uint32_t xw = ld4(X, x4, yy, zz, res), dw = ld4(Df, x4, yy, zz, res);
+        const bool iyz = yy < dr.v[1] && zz < dr.v[2];
+#pragma unroll
+        for (int i = 0; i < 5; i++) {
+          const int xx = x4 + i;
+          if (xx >= res) break;
+          const uint32_t xb = i < 4 ? byte_of(xw, i) : X[cell_index(xx, yy, zz, res)];
+          const uint32_t db = i < 4 ? byte_of(dw, i) : Df[cell_index(xx, yy, zz, res)];
+          const bool inside = iyz && xx < dr.v[0];
+          const uint32_t d0 = (inside && xb != 0xffu && (db & 1u)) ? 0xffu : xb;
+          f |= (uint32_t)(d0 == 0xffu) << i;
+          if (dz == 0 && dy == 0 && i < 4) { center |= d0 << (8 * i); }
+        }
+        if (dz == 0 && dy == 0) dfc = dw;
+      }
+      full[dz][dy] = f;
+    }
+  uint32_t out = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int x = x4 + i;
+    bool tag = false;
+    if (x <= res - 2 && y <= res - 2 && z <= res - 2) {
+      const uint32_t m = 3u << i;
+      const int n = __popc(full[0][0] & m) + __popc(full[0][1] & m) + __popc(full[1][0] & m) + __popc(full[1][1] & m);
+      tag = n != 0 && n != 8;
+    }
+    out |= (tag ? byte_of(dfc, i) : byte_of(center, i)) << (8 * i);
+  }
+  *reinterpret_cast<uint32_t*>(D + cell_index(x4, y, z, res)) = out;
+}
+
+__global__ void __launch_bounds__(256) k_contour4(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, int res,
+                                                  int exact) {
+  const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
+  const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
+  if (x4 >= res || y >= res) return;
+  const uint32_t v4 = ld4(D, x4, y, z, res);
+  const uint32_t xm = x4 > 0 ? D[cell_index(x4 - 1, y, z, res)] : 0u;
+  const uint32_t xp = x4 + 4 < res ? D[cell_index(x4 + 4, y, z, res)] : 0u;
+  const uint32_t ym4 = y > 0 ? ld4(D, x4, y - 1, z, res) : 0u, yp4 = y < res - 1 ? ld4(D, x4, y + 1, z, res) : 0u;
+  const uint32_t zm4 = z > 0 ? ld4(D, x4, y, z - 1, res) : 0u, zp4 = z < res - 1 ? ld4(D, x4, y, z + 1, res) : 0u;
+  uint32_t out = 0;
+  const bool yz_in = y >= 1 && z >= 1 && y <= res - 2 && z <= res - 2;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int x = x4 + i;
+    const uint32_t v = byte_of(v4, i);
+    const uint32_t l = i == 0 ? xm : byte_of(v4, i - 1), r = i == 3 ? xp : byte_of(v4, i + 1);
+    uint32_t o = 0;
+    if (exact || (yz_in && x >= 1 && x <= res - 2 && v != 0xffu))
+      o = adj6((uint8_t)v, (uint8_t)l, (uint8_t)r, (uint8_t)byte_of(ym4, i), (uint8_t)byte_of(yp4, i),
+               (uint8_t)byte_of(zm4, i), (uint8_t)byte_of(zp4, i)) & ~v & 0xffu;
+    out |= o << (8 * i);
+  }
+  *reinterpret_cast<uint32_t*>(S + cell_index(x4, y, z, res)) = out;
+}
+
+__device__ __forceinline__ uint32_t c0_of(uint32_t x, uint32_t d, uint32_t eb, bool inside) {
+  return (inside && d != 0u && x != 0xffu && eb) ? 0u : d;
+}
+
+__global__ void __launch_bounds__(256) k_ero_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
+                                                     const uint8_t* __restrict__ Eb, const uint8_t* __restrict__ Ef,
+                                                     uint8_t* __restrict__ C, int res, DataRes dr, int exact) {
+  const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
+  const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
+  if (x4 >= res || y >= res) return;
+  const uint32_t d4 = ld4(D, x4, y, z, res), ef4 = ld4(Ef, x4, y, z, res);
+  if (exact) {
+    *reinterpret_cast<uint32_t*>(C + cell_index(x4, y, z, res)) = d4 & ~ef4;
+    return;
+  }
+  const uint32_t x4v = ld4(X, x4, y, z, res), eb4 = ld4(Eb, x4, y, z, res);
+  const bool iyz = y < dr.v[1] && z < dr.v[2];
+  // C0 along the row at x4-1 .. x4+4
+  uint32_t row[6];
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    const int xx = x4 - 1 + i;
+    if (xx < 0 || xx >= res) { row[i] = 0u; continue; }
+    uint32_t xb, db, eb;
+    if (i >= 1 && i <= 4) { xb = byte_of(x4v, i - 1); db = byte_of(d4, i - 1); eb = byte_of(eb4, i - 1); }
+    else { const int64_t c = cell_index(xx, y, z, res); xb = X[c]; db = D[c]; eb = Eb[c]; }
+    row[i] = c0_of(xb, db, eb, iyz && xx < dr.v[0]);
+  }
+  // C0 of the four y/z neighbour rows
+  uint32_t nb[4] = {0u, 0u, 0u, 0u};
+  const int ny[4] = {y - 1, y + 1, y, y};
+  const int nz[4] = {z, z, z - 1, z + 1};
+  const bool interior_yz = y >= 1 && z >= 1 && y <= res - 2 && z <= res - 2;
+  if (interior_yz) {
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      const uint32_t xw = ld4(X, x4, ny[n], nz[n], res), dw = ld4(D, x4, ny[n], nz[n], res),
+                     ew = ld4(Eb, x4, ny[n], nz[n], res);
+      const bool in_yz = ny[n] < dr.v[1] && nz[n] < dr.v[2];
+      uint32_t w = 0;
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+        w |= c0_of(byte_of(xw, i), byte_of(dw, i), byte_of(ew, i), in_yz && x4 + i < dr.v[0]) << (8 * i);
+      nb[n] = w;
+    }
+  }
+  uint32_t out = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const int x = x4 + i;
+    const uint32_t c0 = row[i + 1];
+    bool tag = false;
+    if (interior_yz && x >= 1 && x <= res - 2) {
+      tag = row[i] != c0 || row[i + 2] != c0 || byte_of(nb[0], i) != c0 || byte_of(nb[1], i) != c0 ||
+            byte_of(nb[2], i) != c0 || byte_of(nb[3], i) != c0;
+    }
+    out |= (tag ? (0xffu & ~byte_of(ef4, i)) : c0) << (8 * i);
+  }
+  *reinterpret_cast<uint32_t*>(C + cell_index(x4, y, z, res)) = out;
+}
+
+static dim3 quad_grid(int res) { return dim3((res / 4 + 63) / 64, (res + 3) / 4, res); }
+
 // max clamped radius over the fine radius grid
 __global__ void k_rmax(const int8_t* __restrict__ R, int64_t n, int* __restrict__ out) {
   int m = 2;
@@ -762,7 +908,6 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   uint8_t* Ef = carve(p, cells);
   uint8_t* S = carve(p, cells);
   uint8_t* D = a.D_out != nullptr ? a.D_out : carve(p, cells);
-  int sms = a.num_sms > 0 ? a.num_sms : 152;
   const int rmax = a.rmax;
   DataRes dr{{a.data_res[0], a.data_res[1], a.data_res[2]}};
   const bool exact = a.mode == 1;
@@ -806,11 +951,11 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                            buf16a, dst, a.R, a.uniform_r, res, dil_halo, dil_cap));
     }
     if (!exact) {
-      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(a.X, Df, D, res, dr));
+      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(res), dim3(64, 4), 0, st>>>(a.X, Df, D, res, dr));
     }
   }
   // ---- contour ----
-  GM_LAUNCH(kc, "k_contour", st, k_contour<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(D, S, res, exact ? 1 : 0));
+  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(res), dim3(64, 4), 0, st>>>(D, S, res, exact ? 1 : 0));
   // ---- erosion ----
   {
     const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
@@ -847,8 +992,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                                 HL2, Eb, res, ehalo, K));
       }
     }
-    GM_LAUNCH(kc, "k_ero_select", st, k_ero_select<<<grid_stride_blocks(cells, 256, sms), 256, 0, st>>>(a.X, D, Eb, Ef, a.C_out, res, dr,
-                                                                    exact ? 1 : 0));
+    GM_LAUNCH(kc, "k_ero_select", st, k_ero_select4<<<quad_grid(res), dim3(64, 4), 0, st>>>(a.X, D, Eb, Ef, a.C_out, res, dr,
+                                                                                         exact ? 1 : 0));
   }
   if (a.S_out) {
     cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
