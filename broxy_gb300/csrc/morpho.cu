@@ -41,9 +41,10 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
   extern __shared__ uint32_t sm_words[];
   const int N = 2 * res, W = N >> 5;
   const int cy = blockIdx.x, cz = blockIdx.y;
-  uint32_t* bits = sm_words;      // [4][W]
+  uint32_t* bits = sm_words;            // [4][W]
   uint32_t* corner = sm_words + 4 * W;  // [4][W]
   const uint8_t* row = X + (int64_t)res * cy + (int64_t)res * res * cz;
+  int any = 0, all = 1;
   // word w of a fine row covers bytes 16w .. 16w+15 of the byte row
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
     const uint4 q = *reinterpret_cast<const uint4*>(row + 16 * w);
@@ -57,8 +58,20 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
     }
 #pragma unroll
     for (int r = 0; r < 4; r++) bits[r * W + w] = o[r];
+    any |= (q.x | q.y | q.z | q.w) != 0u;
+    all &= (q.x & q.y & q.z & q.w) == 0xffffffffu;
   }
-  __syncthreads();
+  any = __syncthreads_or(any);
+  all = __syncthreads_and(all);
+  if (!any || all) {
+    // empty rows: nothing within reach; full rows: every corner is a site
+    const uint32_t v = !any ? (uint32_t)dcap * 0x01010101u : 0u;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {  // 4 rows x N/4 words
+      const int r = i / (N >> 2), p4 = 4 * (i - r * (N >> 2));
+      *reinterpret_cast<uint32_t*>(A + fine_index(p4, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)) = v;
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < 4 * W; i += blockDim.x) {
     const int r = i / W, w = i - r * W;
     const uint32_t b = bits[i];
@@ -66,37 +79,42 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
     corner[i] = b | (b << 1) | carry;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < 4 * N; i += blockDim.x) {
-    const int r = i / N, p = i - r * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const int r = i / (N >> 2), p4 = 4 * (i - r * (N >> 2));
     const uint32_t* L = corner + r * W;
-    const int w = p >> 5, b = p & 31;
-    int dr = dcap, dl = dcap;
-    uint32_t m = L[w] >> b;
-    if (m) {
-      dr = __ffs(m) - 1;
-    } else {
-      int acc = 32 - b;
-      for (int k = w + 1; k < W && acc < dcap; k++) {
-        const uint32_t v = L[k];
-        if (v) { acc += __ffs(v) - 1; dr = acc; break; }
-        acc += 32;
+    uint32_t packed = 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int p = p4 + j;
+      const int w = p >> 5, b = p & 31;
+      int dr = dcap, dl = dcap;
+      uint32_t m = L[w] >> b;
+      if (m) {
+        dr = __ffs(m) - 1;
+      } else {
+        int acc = 32 - b;
+        for (int k = w + 1; k < W && acc < dcap; k++) {
+          const uint32_t v = L[k];
+          if (v) { acc += __ffs(v) - 1; dr = acc; break; }
+          acc += 32;
+        }
       }
-    }
-    m = L[w] << (31 - b);
-    if (m) {
-      dl = __clz(m);
-    } else {
-      int acc = b + 1;
-      for (int k = w - 1; k >= 0 && acc < dcap; k--) {
-        const uint32_t v = L[k];
-        if (v) { acc += __clz(v); dl = acc; break; }
-        acc += 32;
+      m = L[w] << (31 - b);
+      if (m) {
+        dl = __clz(m);
+      } else {
+        int acc = b + 1;
+        for (int k = w - 1; k >= 0 && acc < dcap; k--) {
+          const uint32_t v = L[k];
+          if (v) { acc += __clz(v); dl = acc; break; }
+          acc += 32;
+        }
       }
+      int d = dr < dl ? dr : dl;
+      if (d > dcap) d = dcap;
+      packed |= (uint32_t)d << (8 * j);
     }
-    int d = dr < dl ? dr : dl;
-    if (d > dcap) d = dcap;
-    const int y = 2 * cy + (r & 1), z = 2 * cz + (r >> 1);
-    A[fine_index(p, y, z, N)] = (uint8_t)d;
+    *reinterpret_cast<uint32_t*>(A + fine_index(p4, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)) = packed;
   }
 }
 
@@ -106,18 +124,25 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
 // at the odd lattice points x = 2c+1 (HL).
 // ---------------------------------------------------------------------
 
+// Sites are sparse (the contour shell), so each site splats its
+// contribution u(q) + e(q - p)^2 to the outputs within reach with shared
+// atomicMin, instead of every output scanning the window.
 __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ S, const int8_t* __restrict__ R,
                                                     int uniform_r, int res, int halo, uint32_t K,
                                                     uint16_t* __restrict__ HC, uint16_t* __restrict__ HL) {
   extern __shared__ uint32_t sm_words[];
   const int N = 2 * res, W = N >> 5;
   const int cy = blockIdx.x, cz = blockIdx.y;
-  uint32_t* bits = sm_words;  // [4][W]
-  uint8_t* rad = reinterpret_cast<uint8_t*>(sm_words + 4 * W);  // [4][N] clamped radii
+  uint32_t* bits = sm_words;              // [4][W]
+  uint32_t* hc = sm_words + 4 * W;        // [4][N] centre outputs
+  uint32_t* hl = hc + 4 * N;              // [4][res] lattice outputs (x = 2c+1)
+  uint32_t* site_pos = hl + 4 * res;      // compacted sites: (row << 16) | x
+  uint32_t* site_u = site_pos + 4 * N;    // their offsets K - 4 (r-1)^2
+  __shared__ int nsites;
   const uint8_t* row = S + (int64_t)res * cy + (int64_t)res * res * cz;
-  __shared__ int any_site;
-  if (threadIdx.x == 0) any_site = 0;
+  if (threadIdx.x == 0) nsites = 0;
   __syncthreads();
+  int any = 0;
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
     const uint4 q = *reinterpret_cast<const uint4*>(row + 16 * w);
     const uint32_t by[4] = {q.x, q.y, q.z, q.w};
@@ -130,64 +155,63 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
     }
 #pragma unroll
     for (int r = 0; r < 4; r++) bits[r * W + w] = o[r];
-    if (o[0] | o[1] | o[2] | o[3]) any_site = 1;
+    any |= (q.x | q.y | q.z | q.w) != 0u;
   }
-  __syncthreads();
-  const bool empty = any_site == 0;
-  if (!empty && R != nullptr) {
-    // clamped radii of the four fine rows (only read where a site sits)
-    for (int i = threadIdx.x; i < 4 * (N >> 4); i += blockDim.x) {
-      const int r = i / (N >> 4), seg = i - r * (N >> 4);
-      const int y = 2 * cy + (r & 1), z = 2 * cz + (r >> 1);
-      const uint4 v = *reinterpret_cast<const uint4*>(R + fine_index(16 * seg, y, z, N));
-      const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-      uint32_t* dst = reinterpret_cast<uint32_t*>(rad + r * N + 16 * seg);
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        uint32_t o = 0;
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-          const int s = (int)(int8_t)((w4[j] >> (8 * b)) & 0xff);
-          o |= (uint32_t)clamp_radius(s) << (8 * b);
-        }
-        dst[j] = o;
+  any = __syncthreads_or(any);
+  const int ru = clamp_radius(uniform_r);
+  if (any) {
+    for (int i = threadIdx.x; i < 4 * N; i += blockDim.x) hc[i] = K;
+    for (int i = threadIdx.x; i < 4 * res; i += blockDim.x) hl[i] = K;
+    // compact the sites with their offsets
+    for (int i = threadIdx.x; i < 4 * W; i += blockDim.x) {
+      uint32_t m = bits[i];
+      if (!m) continue;
+      const int r = i / W, w = i - r * W;
+      const int base = atomicAdd(&nsites, __popc(m));
+      int k = 0;
+      while (m) {
+        const int x = (w << 5) + __ffs(m) - 1;
+        m &= m - 1;
+        int rq = ru;
+        if (R != nullptr)
+          rq = clamp_radius(R[fine_index(x, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)]);
+        site_pos[base + k] = ((uint32_t)r << 16) | (uint32_t)x;
+        site_u[base + k] = K - 4u * (uint32_t)((rq - 1) * (rq - 1));
+        k++;
+      }
+    }
+    __syncthreads();
+    const int ns = nsites;
+    const int taps = 2 * halo + 1;
+    for (int i = threadIdx.x; i < ns * taps; i += blockDim.x) {
+      const int sidx = i / taps, dq = i - sidx * taps - halo;
+      const uint32_t sp = site_pos[sidx];
+      const int r = (int)(sp >> 16), q = (int)(sp & 0xffffu);
+      const uint32_t u = site_u[sidx];
+      const int p = q - dq;  // output position, delta = q - p = dq
+      if (p < 0 || p >= N) continue;
+      const int ec = center_dist2(dq);
+      const uint32_t vc = u + (uint32_t)(ec * ec);
+      if (vc < K) atomicMin(&hc[r * N + p], vc);
+      if (p & 1) {
+        const int el = 2 * lattice_dist(dq);
+        const uint32_t vl = u + (uint32_t)(el * el);
+        if (vl < K) atomicMin(&hl[r * res + (p >> 1)], vl);
       }
     }
     __syncthreads();
   }
-  const int ru = clamp_radius(uniform_r);
-  const int total = 4 * N + 4 * res;
-  for (int i = threadIdx.x; i < total; i += blockDim.x) {
-    int r, p;
-    bool center;
-    if (i < 4 * N) { r = i / N; p = i - r * N; center = true; }
-    else { const int j = i - 4 * N; r = j / res; p = 2 * (j - r * res) + 1; center = false; }
-    uint32_t best = K;
-    if (!empty) {
-      const uint32_t* L = bits + r * W;
-      int lo = p - halo, hi = p + halo;
-      if (lo < 0) lo = 0;
-      if (hi > N - 1) hi = N - 1;
-      for (int w = lo >> 5; w <= (hi >> 5); w++) {
-        uint32_t m = L[w];
-        if (!m) continue;
-        const int base = w << 5;
-        if (base < lo) m &= 0xffffffffu << (lo - base);
-        if (base + 31 > hi) m &= 0xffffffffu >> (base + 31 - hi);
-        while (m) {
-          const int q = base + __ffs(m) - 1;
-          m &= m - 1;
-          const int rq = R != nullptr ? (int)rad[r * N + q] : ru;
-          const uint32_t u = K - 4u * (uint32_t)((rq - 1) * (rq - 1));
-          const int e = center ? center_dist2(q - p) : 2 * lattice_dist(q - p);
-          const uint32_t v = u + (uint32_t)(e * e);
-          best = v < best ? v : best;
-        }
-      }
-    }
-    const int y = 2 * cy + (r & 1), z = 2 * cz + (r >> 1);
-    if (center) HC[fine_index(p, y, z, N)] = (uint16_t)best;
-    else HL[(int64_t)(p >> 1) + (int64_t)res * y + (int64_t)res * N * z] = (uint16_t)best;
+  // write out (u16 pairs)
+  for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) {
+    const int r = i / (N >> 1), p2 = 2 * (i - r * (N >> 1));
+    const uint32_t v = any ? (hc[r * N + p2] | (hc[r * N + p2 + 1] << 16)) : (K | (K << 16));
+    *reinterpret_cast<uint32_t*>(HC + fine_index(p2, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)) = v;
+  }
+  for (int i = threadIdx.x; i < 2 * res; i += blockDim.x) {
+    const int r = i / (res >> 1), c2 = 2 * (i - r * (res >> 1));
+    const uint32_t v = any ? (hl[r * res + c2] | (hl[r * res + c2 + 1] << 16)) : (K | (K << 16));
+    *reinterpret_cast<uint32_t*>(HL + (int64_t)c2 + (int64_t)res * (2 * cy + (r & 1)) +
+                                 (int64_t)res * N * (2 * cz + (r >> 1))) = v;
   }
 }
 
@@ -961,7 +985,13 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
     const int ehalo = rmax + 1;
     const int W = N >> 5;
-    const size_t smem = 4 * W * sizeof(uint32_t) + (a.R != nullptr ? 4 * (size_t)N : 0);
+    // bits, centre and lattice accumulators, compacted sites
+    const size_t smem = sizeof(uint32_t) * (4 * (size_t)W + 4 * (size_t)N + 4 * (size_t)res + 8 * (size_t)N);
+    static size_t ero_x_configured = 0;
+    if (smem > 48 * 1024 && smem > ero_x_configured) {
+      cudaFuncSetAttribute(k_ero_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      ero_x_configured = smem;
+    }
     GM_LAUNCH(kc, "k_ero_pass_x", st, k_ero_pass_x<<<dim3(res, res), 256, smem, st>>>(S, a.R, a.uniform_r, res, ehalo, K, buf16a, HL1));
     if (K <= 32767) {
       launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, N, N, N, 1, 0, ehalo, K, nullptr, 0, res, st, kc,
