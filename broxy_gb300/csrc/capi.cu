@@ -188,7 +188,8 @@ gm_status gm_ctx_destroy(gm_ctx* ctx) {
   cudaFree(ctx->d_int);
   cudaFree(ctx->vox);
   gm::MeshBuffers& b = ctx->mesh;
-  cudaFree(b.V); cudaFree(b.N); cudaFree(b.N2); cudaFree(b.T); cudaFree(b.adj); cudaFree(b.rowptr);
+  cudaFree(b.V); cudaFree(b.N); cudaFree(b.N4a); cudaFree(b.N4b); cudaFree(b.T); cudaFree(b.adj);
+  cudaFree(b.nbr); cudaFree(b.wpos); cudaFree(b.rowptr);
   cudaFree(b.cursor); cudaFree(b.cell_voff); cudaFree(b.brick_tot); cudaFree(b.fix);
   ctx->kc.release();
   delete ctx;

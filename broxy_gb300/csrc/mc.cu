@@ -108,6 +108,19 @@ __device__ __forceinline__ void cube_values(const uint8_t* tile, int lx, int ly,
   }
 }
 
+// True when the 2x2x2 block of cells c .. c+1 is all empty or all full: then
+// none of the eight sub-cubes of c is mixed (cheap test before cube_values).
+__device__ __forceinline__ bool cell_uniform(const uint8_t* tile, int lx, int ly, int lz) {
+  uint32_t o = 0, a = 0xffu;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const uint32_t v = tile[(lx + (k & 1)) + kTileE * (ly + ((k >> 1) & 1)) + kTileE * kTileE * (lz + (k >> 2))];
+    o |= v;
+    a &= v;
+  }
+  return o == 0u || a == 0xffu;
+}
+
 // mixed-cube mask of a cell; cells outside [1, res-2]^3 are never tagged
 // (TagVoxelsContourMCM, Grid.cu:1334-1340).
 __device__ __forceinline__ int mixed_mask(const int vals[8], int gx, int gy, int gz, int res) {
@@ -186,6 +199,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restri
     const int l = threadIdx.x * kCellsPerThread + i;
     int lx, ly, lz;
     local_coords(l, lx, ly, lz);
+    if (cell_uniform(tile, lx, ly, lz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
     const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
@@ -256,6 +270,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
     const int l = threadIdx.x * kCellsPerThread + i;
     int lx, ly, lz;
     local_coords(l, lx, ly, lz);
+    if (cell_uniform(tile, lx, ly, lz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
     const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
@@ -270,6 +285,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
     const int l = threadIdx.x * kCellsPerThread + i;
     int lx, ly, lz;
     local_coords(l, lx, ly, lz);
+    if (cell_uniform(tile, lx, ly, lz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
     const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
@@ -316,6 +332,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
 // bits 8+k / 16+k / 24+k = cube k owns a vertex on edge 0 / 3 / 8.
 __device__ __forceinline__ uint32_t cell_info(const uint8_t* tile, int lx, int ly, int lz, int gx, int gy, int gz,
                                               int res) {
+  if (cell_uniform(tile, lx, ly, lz)) return 0u;
   int vals[8];
   cube_values(tile, lx, ly, lz, vals);
   const int m = mixed_mask(vals, gx, gy, gz, res);
@@ -593,7 +610,7 @@ __device__ __forceinline__ float3 normalize3(float3 n) {
 // vertex in triangle order, then normalised (GMorpho.cu:6526-6537).
 __global__ void k_vertex_normals(const float* __restrict__ V, const uint32_t* __restrict__ T,
                                  const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
-                                 float* __restrict__ N) {
+                                 float4* __restrict__ N4, float* __restrict__ N3) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
     float3 acc = make_float3(0.f, 0.f, 0.f);
     for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
@@ -607,7 +624,8 @@ __global__ void k_vertex_normals(const float* __restrict__ V, const uint32_t* __
       acc = make_float3(__fadd_rn(acc.x, nx), __fadd_rn(acc.y, ny), __fadd_rn(acc.z, nz));
     }
     const float3 n = normalize3(acc);
-    N[3 * v] = n.x; N[3 * v + 1] = n.y; N[3 * v + 2] = n.z;
+    N4[v] = make_float4(n.x, n.y, n.z, 0.f);
+    if (N3) { N3[3 * v] = n.x; N3[3 * v + 1] = n.y; N3[3 * v + 2] = n.z; }
   }
 }
 
@@ -616,30 +634,52 @@ __device__ __forceinline__ float dist2(float3 a, float3 b) {
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-// One bilateral normal iteration (BilateralMeshFiltering{,Normalize},
-// GMorpho.cu:6539-6620): each incident triangle adds w1 n_b + w2 n_c,
-// accumulated per vertex in triangle order.
-__global__ void k_bilateral(const float* __restrict__ V, const float* __restrict__ Nin,
-                            const uint32_t* __restrict__ T, const uint32_t* __restrict__ rowptr,
-                            const uint32_t* __restrict__ adj, int64_t nv, float sp2, float sn2,
-                            float* __restrict__ Nout) {
+// Per corner (vertex a of triangle t): the other two vertices b, c in the
+// reference's order and the iteration-invariant position terms
+// |pa - pb|^2 / sigma_p^2 (GMorpho.cu:6561-6569).
+__global__ void k_adj_prep(const float* __restrict__ V, const uint32_t* __restrict__ T,
+                           const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
+                           float sp2, uint2* __restrict__ nbr, float2* __restrict__ wpos) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
-    float3 acc = make_float3(0.f, 0.f, 0.f);
-    const float3 pa = ld3(V, (uint32_t)v), na = ld3(Nin, (uint32_t)v);
+    const float3 pa = ld3(V, (uint32_t)v);
     for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
       const uint32_t corner = adj[i];
       const uint32_t t = corner / 3, role = corner - 3 * t;
       const uint32_t ib = T[3 * (size_t)t + (role == 0 ? 1 : 0)];
       const uint32_t ic = T[3 * (size_t)t + (role == 2 ? 1 : 2)];
-      const float3 pb = ld3(V, ib), pc = ld3(V, ic), nb = ld3(Nin, ib), nc = ld3(Nin, ic);
-      const float w1 = expf(-__fadd_rn(__fdiv_rn(dist2(pa, pb), sp2), __fdiv_rn(dist2(na, nb), sn2)));
-      const float w2 = expf(-__fadd_rn(__fdiv_rn(dist2(pa, pc), sp2), __fdiv_rn(dist2(na, nc), sn2)));
+      nbr[i] = make_uint2(ib, ic);
+      wpos[i] = make_float2(__fdiv_rn(dist2(pa, ld3(V, ib)), sp2), __fdiv_rn(dist2(pa, ld3(V, ic)), sp2));
+    }
+  }
+}
+
+__device__ __forceinline__ float dist2n(float4 a, float4 b) {
+  const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// One bilateral normal iteration (BilateralMeshFiltering{,Normalize},
+// GMorpho.cu:6539-6620): each incident triangle adds w1 n_b + w2 n_c,
+// accumulated per vertex in triangle order.
+__global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __restrict__ rowptr,
+                            const uint2* __restrict__ nbr, const float2* __restrict__ wpos, int64_t nv, float sn2,
+                            float4* __restrict__ Nout, float* __restrict__ N3) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    const float4 na = Nin[v];
+    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
+      const uint2 bc = nbr[i];
+      const float2 wp = wpos[i];
+      const float4 nb = Nin[bc.x], nc = Nin[bc.y];
+      const float w1 = expf(-__fadd_rn(wp.x, __fdiv_rn(dist2n(na, nb), sn2)));
+      const float w2 = expf(-__fadd_rn(wp.y, __fdiv_rn(dist2n(na, nc), sn2)));
       acc.x = __fadd_rn(acc.x, __fadd_rn(__fmul_rn(w1, nb.x), __fmul_rn(w2, nc.x)));
       acc.y = __fadd_rn(acc.y, __fadd_rn(__fmul_rn(w1, nb.y), __fmul_rn(w2, nc.y)));
       acc.z = __fadd_rn(acc.z, __fadd_rn(__fmul_rn(w1, nb.z), __fmul_rn(w2, nc.z)));
     }
     const float3 n = normalize3(acc);
-    Nout[3 * v] = n.x; Nout[3 * v + 1] = n.y; Nout[3 * v + 2] = n.z;
+    Nout[v] = make_float4(n.x, n.y, n.z, 0.f);
+    if (N3) { N3[3 * v] = n.x; N3[3 * v + 1] = n.y; N3[3 * v + 2] = n.z; }
   }
 }
 
@@ -700,25 +740,31 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   cudaError_t e;
   // per-vertex buffers share one capacity, per-triangle buffers another
   if (b.v_cap < nv || b.V == nullptr) {
-    cudaFree(b.V); cudaFree(b.N); cudaFree(b.N2); cudaFree(b.rowptr); cudaFree(b.cursor);
-    b.V = b.N = b.N2 = nullptr;
+    cudaFree(b.V); cudaFree(b.N); cudaFree(b.N4a); cudaFree(b.N4b); cudaFree(b.rowptr); cudaFree(b.cursor);
+    b.V = b.N = nullptr;
+    b.N4a = b.N4b = nullptr;
     b.rowptr = b.cursor = nullptr;
     b.v_cap = 0;
     const int64_t c = nv + nv / 4 + 1024;
     if ((e = cudaMalloc(&b.V, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.N, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.N2, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.N4a, sizeof(float4) * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.N4b, sizeof(float4) * (size_t)c)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.rowptr, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.cursor, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
     b.v_cap = c;
   }
   if (b.t_cap < nt || b.T == nullptr) {
-    cudaFree(b.T); cudaFree(b.adj);
+    cudaFree(b.T); cudaFree(b.adj); cudaFree(b.nbr); cudaFree(b.wpos);
     b.T = b.adj = nullptr;
+    b.nbr = nullptr;
+    b.wpos = nullptr;
     b.t_cap = 0;
     const int64_t c = nt + nt / 4 + 1024;
     if ((e = cudaMalloc(&b.T, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.adj, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.nbr, sizeof(uint2) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.wpos, sizeof(float2) * 3 * (size_t)c)) != cudaSuccess) return e;
     b.t_cap = c;
   }
   const float cs = 0.5f * a.cell_size;  // exact: scaling by a power of two
@@ -744,15 +790,23 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
   GM_LAUNCH(kc, "k_adj_fill", st, k_adj_fill<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.rowptr, b.cursor, b.adj));
   GM_LAUNCH(kc, "k_adj_sort", st, k_adj_sort<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.rowptr, b.adj, nv));
-  GM_LAUNCH(kc, "k_vertex_normals", st, k_vertex_normals<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, b.N));
-  float* nin = b.N;
-  float* nout = b.N2;
-  for (int it = 0; it < a.bilateral_iters; it++) {
-    const float sn = it < 2 ? 1e10f : 0.2f;  // GMorpho.cu:6959-6969
-    GM_LAUNCH(kc, "k_bilateral", st, k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, nin, b.T, b.rowptr, b.adj, nv, 1.f, sn * sn, nout));
-    float* t = nin; nin = nout; nout = t;
+  const int iters = a.bilateral_iters;
+  GM_LAUNCH(kc, "k_vertex_normals", st,
+            k_vertex_normals<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, b.N4a,
+                                                                      iters == 0 ? b.N : nullptr));
+  if (iters > 0) {
+    GM_LAUNCH(kc, "k_adj_prep", st,
+              k_adj_prep<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, 1.f, b.nbr, b.wpos));
   }
-  if (nin != b.N) cudaMemcpyAsync(b.N, nin, sizeof(float) * 3 * (size_t)nv, cudaMemcpyDeviceToDevice, st);
+  float4* nin = b.N4a;
+  float4* nout = b.N4b;
+  for (int it = 0; it < iters; it++) {
+    const float sn = it < 2 ? 1e10f : 0.2f;  // GMorpho.cu:6959-6969
+    GM_LAUNCH(kc, "k_bilateral", st,
+              k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.rowptr, b.nbr, b.wpos, nv, sn * sn, nout,
+                                                                   it == iters - 1 ? b.N : nullptr));
+    float4* t = nin; nin = nout; nout = t;
+  }
   return cudaGetLastError();
 }
 

@@ -509,7 +509,49 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
   const int obase = o0 + grp * kDpxPer;
   const int sp0 = (sub ? 2 * obase + 1 : obase) - lo;
   uint32_t best[kDpxPer];
-  if (finite) {
+  if (finite && step == 1) {
+    // Register sliding windows: wp[(j + k) % 16] holds tile row sp0 + j + k
+    // and wm[(j - k) mod 16] holds row sp0 + j - k, so that after tap k only
+    // one new row per side is loaded (into the slot its leaving row frees).
+    const uint32_t* tcol = tile + lane;
+    uint32_t wp[kDpxPer], wm[kDpxPer];
+#pragma unroll
+    for (int j = 0; j < kDpxPer; j++) {
+      wp[j] = tcol[(sp0 + j + (j < 1 ? kDpxPer : 0)) * 32];
+      wm[j] = tcol[(sp0 + (j < kDpxPer - 1 ? j : -1)) * 32];
+    }
+    const uint32_t g0 = gpair<G>(0, cap);
+#pragma unroll
+    for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tcol[(sp0 + j) * 32], g0, capp);
+    for (int kb = 0; kb <= halo; kb += kDpxPer) {
+#pragma unroll
+      for (int u = 0; u < kDpxPer; u++) {
+        const int k = kb + u;
+        if (k == 0) continue;
+        if (k > halo) goto dpx_done;
+        const uint32_t gp = gpair<G>(k, cap), gm_ = gpair<G>(-k, cap);
+#pragma unroll
+        for (int j = 0; j < kDpxPer; j++) {
+          best[j] = step_min<G>(wp[(j + u) % kDpxPer], gp, best[j]);
+          best[j] = step_min<G>(wm[(j - u + kDpxPer) % kDpxPer], gm_, best[j]);
+        }
+        // rows sp0 + k + 16 and sp0 - k - 1 enter; the slots of rows
+        // sp0 + k and sp0 + 15 - k are free now (k <= halo keeps both in the tile)
+        wp[u] = tcol[(sp0 + k + kDpxPer) * 32];
+        wm[(kDpxPer - 1 - u) % kDpxPer] = tcol[(sp0 - k - 1) * 32];
+        if (u & 1) {
+          uint32_t m = best[0];
+#pragma unroll
+          for (int j = 1; j < kDpxPer; j++) m = __vmaxu2(m, best[j]);
+          const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
+          const uint32_t np = kern_g<G>(k + 1), nm = kern_g<G>(-(k + 1));
+          const uint32_t nxt = np < nm ? np : nm;
+          if (__all_sync(0xffffffffu, nxt >= mx)) goto dpx_done;
+        }
+      }
+    }
+  dpx_done:;
+  } else if (finite) {
     const uint32_t g0 = gpair<G>(0, cap);
 #pragma unroll
     for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tile[(sp0 + step * j) * 32 + lane], g0, capp);
