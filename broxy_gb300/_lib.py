@@ -57,10 +57,16 @@ PROTOTYPES = {
     "gm_pyramid_build": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int32, _P, _P]),
     "gm_close": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int32, C.c_int, C.c_int, _P, _P, _P, _P]),
     "gm_close_noalloc": (C.c_int, [C.POINTER(GridDesc), _P, _P, C.c_int32, C.c_int, C.c_int, _P, _P, _P, _P]),
+    "gm_contour": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int, _P]),
     "gm_mesh": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.c_int32, C.POINTER(MeshView), _P]),
     "gm_update": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_float, C.POINTER(UpdateOpts),
                             C.POINTER(C.c_int64), C.POINTER(C.c_int64), _P]),
     "gm_mesh_download": (C.c_int, [_P, _P, _P, _P, _P]),
+    "gm_bvh_build": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.POINTER(_P), C.POINTER(C.c_int64), _P]),
+    "gm_bvh_destroy": (C.c_int, [_P]),
+    "gm_bvh_query": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, _P, _P]),
+    "gm_bvh_leaves": (C.c_int, [_P, _P, _P, _P]),
+    "gm_erode_bvh": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int32, _P, _P]),
     "gm_layout_zwords_to_packed": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "gm_layout_packed_to_zwords": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
 }

@@ -103,6 +103,13 @@ class Context:
         self._check(st)
         return out
 
+    # a8
+    def contour(self, desc, grid, mode=L.GM_REF, inplace=False):
+        import torch
+        out = grid if inplace else torch.empty_like(grid)
+        self._check(self.lib.gm_contour(self.ctx, C.byref(desc), _ptr(grid), _ptr(out), mode, _stream()))
+        return out
+
     # a12..a16
     def mesh(self, desc, Cg, bilateral_iters=20):
         """Returns (V, N, T) as zero-copy device arrays owned by the context
@@ -171,6 +178,21 @@ class Context:
         self._check(st)
         return out
 
+    # a18
+    def bvh_build(self, desc, sites):
+        h = C.c_void_p()
+        n = C.c_int64(0)
+        self._check(self.lib.gm_bvh_build(self.ctx, C.byref(desc), _ptr(sites), C.byref(h), C.byref(n), _stream()))
+        return BVH(self, h, n.value)
+
+    def erode_bvh(self, desc, X, D, radius, out=None):
+        import torch
+        if out is None:
+            out = torch.empty_like(D)
+        self._check(self.lib.gm_erode_bvh(self.ctx, C.byref(desc), _ptr(X), _ptr(D), int(radius), _ptr(out),
+                                          _stream()))
+        return out
+
     def zwords_to_packed(self, res, zw, out):
         self._check(self.lib.gm_layout_zwords_to_packed(self.ctx, res, _ptr(zw), _ptr(out), _stream()))
         return out
@@ -178,3 +200,34 @@ class Context:
     def packed_to_zwords(self, res, grid, out):
         self._check(self.lib.gm_layout_packed_to_zwords(self.ctx, res, _ptr(grid), _ptr(out), _stream()))
         return out
+
+
+class BVH:
+    """Handle of a device BVH (gm_bvh_*)."""
+
+    def __init__(self, ctx, handle, n):
+        self.ctx, self.handle, self.n = ctx, handle, n
+
+    def query(self, points2, radius):
+        import torch
+        hits = torch.empty(points2.shape[0], dtype=torch.uint8, device=points2.device)
+        self.ctx._check(self.ctx.lib.gm_bvh_query(self.ctx.ctx, self.handle, _ptr(points2), points2.shape[0],
+                                                  int(radius), _ptr(hits), _stream()))
+        return hits
+
+    def leaves(self):
+        import torch
+        keys = torch.empty(max(self.n, 1), dtype=torch.int64, device="cuda")
+        self.ctx._check(self.ctx.lib.gm_bvh_leaves(self.ctx.ctx, self.handle, _ptr(keys), _stream()))
+        return keys[:self.n]
+
+    def destroy(self):
+        if self.handle:
+            self.ctx.lib.gm_bvh_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

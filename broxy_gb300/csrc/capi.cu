@@ -385,6 +385,27 @@ gm_status gm_close(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input
                     (cudaStream_t)stream);
 }
 
+gm_status gm_contour(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_grid, uint8_t* d_out, gm_mode mode,
+                     void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_grid || !d_out || !aligned16(d_grid) || !aligned16(d_out))
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_contour: NULL or misaligned buffer");
+  if (mode != GM_REF && mode != GM_EXACT) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_contour: unknown mode");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t cells = (size_t)desc->res * desc->res * desc->res;
+  uint8_t* dst = d_out;
+  if (d_out == d_grid) {  // the tagger reads neighbours: write to scratch, then copy back
+    if ((s = ensure(ctx, (void**)&ctx->vox, ctx->vox_bytes, cells, "contour scratch")) != GM_OK) return s;
+    dst = ctx->vox;
+  }
+  GM_CHECK_CUDA(ctx, gm::launch_contour(d_grid, dst, desc->res, mode == GM_EXACT ? 1 : 0, st, &ctx->kc), "gm_contour");
+  if (dst != d_out) GM_CHECK_CUDA(ctx, cudaMemcpyAsync(d_out, dst, cells, cudaMemcpyDeviceToDevice, st), "gm_contour");
+  return GM_OK;
+}
+
 // ------------------------------------------------------------------ a12..a16
 
 static gm_status mesh_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closing, int iters,
@@ -482,6 +503,104 @@ gm_status gm_mesh_download(gm_ctx* ctx, float* h_V, float* h_N, uint32_t* h_T, v
   if (h_T && ctx->nt)
     GM_CHECK_CUDA(ctx, cudaMemcpyAsync(h_T, ctx->mesh.T, 12 * (size_t)ctx->nt, cudaMemcpyDeviceToHost, st), "D2H");
   GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "gm_mesh_download");
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ a18
+
+struct gm_bvh {
+  void* dev = nullptr;
+  int64_t n = 0;
+  int device = 0;
+};
+
+static gm_status bvh_build_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_sites, gm_bvh** out,
+                                cudaStream_t st) {
+  const int res = desc->res;
+  const size_t nb = (size_t)res * res * res / 4096;
+  gm_status s;
+  if ((s = ensure(ctx, (void**)&ctx->vox, ctx->vox_bytes, sizeof(uint32_t) * (nb + 1), "bvh scratch")) != GM_OK)
+    return s;
+  void* h = nullptr;
+  int n = 0;
+  GM_CHECK_CUDA(ctx, gm::bvh_build(d_sites, res, &h, reinterpret_cast<uint32_t*>(ctx->vox), &n, st, &ctx->kc),
+                "gm_bvh_build");
+  gm_bvh* b = new gm_bvh();
+  b->dev = h;
+  b->n = n;
+  b->device = ctx->device;
+  *out = b;
+  return GM_OK;
+}
+
+gm_status gm_bvh_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_sites, gm_bvh** out,
+                       int64_t* num_leaves, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_sites || !out) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_bvh_build: NULL argument");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  if ((s = bvh_build_impl(ctx, desc, d_sites, out, (cudaStream_t)stream)) != GM_OK) return s;
+  if (num_leaves) *num_leaves = (*out)->n;
+  return GM_OK;
+}
+
+gm_status gm_bvh_destroy(gm_bvh* bvh) {
+  if (!bvh) return GM_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(bvh->device);
+  gm::bvh_free(bvh->dev);
+  delete bvh;
+  return GM_OK;
+}
+
+gm_status gm_bvh_query(gm_ctx* ctx, const gm_bvh* bvh, const int32_t* d_points2, int64_t n, int32_t radius,
+                       uint8_t* d_hits, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!bvh || (n > 0 && (!d_points2 || !d_hits)) || n < 0 || radius < 0)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_bvh_query: bad argument");
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  GM_CHECK_CUDA(ctx, gm::bvh_query(bvh->dev, d_points2, n, radius, d_hits, (cudaStream_t)stream, &ctx->kc),
+                "gm_bvh_query");
+  return GM_OK;
+}
+
+gm_status gm_bvh_leaves(gm_ctx* ctx, const gm_bvh* bvh, uint64_t* d_keys, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!bvh || !d_keys) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_bvh_leaves: NULL argument");
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  GM_CHECK_CUDA(ctx, gm::bvh_keys(bvh->dev, d_keys, (cudaStream_t)stream), "gm_bvh_leaves");
+  return GM_OK;
+}
+
+gm_status gm_erode_bvh(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const uint8_t* d_dilation,
+                       int32_t radius, uint8_t* d_closing, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_input || !d_dilation || !d_closing || !aligned16(d_dilation) || radius < 0)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_erode_bvh: bad argument");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t cells = (size_t)desc->res * desc->res * desc->res;
+  // contour of the dilation into the closing workspace, then its BVH
+  if ((s = ensure(ctx, (void**)&ctx->ws, ctx->ws_bytes, gm::close_workspace_bytes(desc->res), "workspace")) != GM_OK)
+    return s;
+  uint8_t* S = ctx->ws;
+  GM_CHECK_CUDA(ctx, gm::launch_contour(d_dilation, S, desc->res, 0, st, &ctx->kc), "gm_erode_bvh contour");
+  gm_bvh* b = nullptr;
+  if ((s = bvh_build_impl(ctx, desc, S, &b, st)) != GM_OK) return s;
+  int* d_over = ctx->d_int + 1;
+  const cudaError_t e = gm::bvh_erode(b->dev, d_input, d_dilation, desc->res, desc->data_res, radius, d_closing,
+                                      d_over, st, &ctx->kc);
+  int over = 0;
+  cudaMemcpyAsync(&over, d_over, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  gm_bvh_destroy(b);
+  (void)cells;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "gm_erode_bvh");
+  if (over) return fail(ctx, GM_ERR_CAPACITY, "gm_erode_bvh: traversal stack overflow");
   return GM_OK;
 }
 

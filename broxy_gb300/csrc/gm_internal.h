@@ -57,6 +57,7 @@ struct CloseArgs {
 
 size_t close_workspace_bytes(int res);
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
+cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc);
 
 // ---------------------------------------------------------------- pyramid
@@ -116,5 +117,16 @@ cudaError_t launch_voxelize(const float* P, int64_t nv, const uint32_t* T, int64
 size_t voxelize_scratch_bytes(int res);
 // dir 0: z-words -> packed grid; dir 1: packed grid -> z-words
 cudaError_t launch_layout(int res, const uint32_t* zw, uint8_t* grid, int dir, cudaStream_t st, KernelCounter* kc);
+
+// ---------------------------------------------------------------- BVH
+cudaError_t bvh_build(const uint8_t* grid, int res, void** handle, uint32_t* scratch_bricks, int* n_out,
+                      cudaStream_t st, KernelCounter* kc);
+void bvh_free(void* handle);
+cudaError_t bvh_query(const void* handle, const int32_t* q2, int64_t nq, int radius, uint8_t* out, cudaStream_t st,
+                      KernelCounter* kc);
+cudaError_t bvh_erode(const void* handle, const uint8_t* X, const uint8_t* D, int res, const int* data_res,
+                      int radius, uint8_t* C, int* d_overflow, cudaStream_t st, KernelCounter* kc);
+int bvh_size(const void* handle);
+cudaError_t bvh_keys(const void* handle, uint64_t* out, cudaStream_t st);
 
 }  // namespace gm

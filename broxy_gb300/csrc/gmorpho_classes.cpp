@@ -1,0 +1,381 @@
+// gmorpho_classes.cpp — the reference's C++ classes (namespace
+// MorphoGraphics: GMorpho, Grid, ScaleField, Voxelizer, Mesh; global
+// MarchingCubesMesher) implemented over the C ABI of libgmorpho_gb300.
+//
+// Error behaviour follows the reference: failures throw the class's
+// Exception (GMorpho/GMorpho.cu:50-56) carrying the library message.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+
+#include "../../include/gmorpho/GMorpho.h"
+#include "../../include/gmorpho/MarchingCubesMesher.h"
+#include "../../include/gmorpho_gb300.h"
+
+namespace {
+
+// One context per device for the classes that have none of their own.
+gm_ctx* shared_ctx() {
+  static std::mutex mu;
+  static gm_ctx* ctxs[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (dev < 0 || dev >= 64) return nullptr;
+  if (!ctxs[dev] && gm_ctx_create(dev, &ctxs[dev]) != GM_OK) ctxs[dev] = nullptr;
+  return ctxs[dev];
+}
+
+std::string message(gm_ctx* ctx, int status, const char* what) {
+  std::string m = std::string(what) + ": " + gm_status_string((gm_status)status);
+  if (ctx && gm_ctx_last_error(ctx)[0]) m += std::string(" (") + gm_ctx_last_error(ctx) + ")";
+  return m;
+}
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw MorphoGraphics::Grid::Exception(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+namespace MorphoGraphics {
+
+// ------------------------------------------------------------------ Mesh
+
+bool Mesh::loadOFF(const std::string& path) {
+  std::ifstream in(path);
+  if (!in) return false;
+  std::string head;
+  in >> head;
+  if (head != "OFF") return false;
+  size_t nv = 0, nf = 0, ne = 0;
+  in >> nv >> nf >> ne;
+  P_.resize(nv);
+  for (size_t i = 0; i < nv; i++) in >> P_[i][0] >> P_[i][1] >> P_[i][2];
+  T_.clear();
+  for (size_t i = 0; i < nf; i++) {
+    unsigned int n, a, b, c;
+    in >> n >> a >> b >> c;
+    T_.push_back(Vec3ui(a, b, c));
+    for (unsigned int k = 3; k < n; k++) {  // fan-triangulate polygons
+      unsigned int d;
+      in >> d;
+      T_.push_back(Vec3ui(a, c, d));
+      c = d;
+    }
+  }
+  N_.clear();
+  return (bool)in || in.eof();
+}
+
+bool Mesh::storeOFF(const std::string& path) const {
+  std::ofstream out(path);
+  if (!out) return false;
+  out << "OFF\n" << P_.size() << " " << T_.size() << " 0\n";
+  for (const Vec3f& p : P_) out << p[0] << " " << p[1] << " " << p[2] << "\n";
+  for (const Vec3ui& t : T_) out << "3 " << t[0] << " " << t[1] << " " << t[2] << "\n";
+  return (bool)out;
+}
+
+// ------------------------------------------------------------------ Grid
+
+Grid::Grid() {}
+Grid::~Grid() { Free(); }
+
+void Grid::Free() {
+  if (voxels_) cudaFree(voxels_);
+  if (pyramid_) cudaFree(pyramid_);
+  voxels_ = nullptr;
+  pyramid_ = nullptr;
+}
+
+void Grid::Init(const Vec3f& bmin, const Vec3f& bmax, const Vec3ui& res, const Vec3ui& data_res, float cell_size) {
+  if (res[0] != res[1] || res[0] != res[2]) throw Exception("grids are cubic");
+  const size_t n = (size_t)res[0] * res[1] * res[2];
+  if (voxels_ && res[0] == res_[0]) {
+    // keep the allocation
+  } else {
+    Free();
+    cuda_check(cudaMalloc(&voxels_, n), "Grid::Init");
+  }
+  bbox_min_ = bmin;
+  bbox_max_ = bmax;
+  res_ = res;
+  data_res_ = data_res;
+  cell_size_ = cell_size;
+}
+
+GridGPU Grid::grid_gpu() const {
+  GridGPU g;
+  for (int a = 0; a < 3; a++) {
+    g.bbox_min[a] = bbox_min_[a];
+    g.bbox_max[a] = bbox_max_[a];
+    g.res[a] = res_[a];
+    g.data_res[a] = data_res_[a];
+  }
+  g.cell_size = cell_size_;
+  g.voxels = voxels_;
+  g.pyramid = pyramid_;
+  int l = 0;
+  while ((1u << l) < res_[0]) l++;
+  g.max_mipmap_level = l + 1;
+  return g;
+}
+
+void Grid::SetGridValue(unsigned char value) {
+  cuda_check(cudaMemset(voxels_, value, (size_t)res_[0] * res_[1] * res_[2]), "Grid::SetGridValue");
+}
+
+void Grid::CopyVoxelsFrom(const Grid& grid) {
+  const size_t n = (size_t)res_[0] * res_[1] * res_[2];
+  const size_t m = (size_t)grid.res_[0] * grid.res_[1] * grid.res_[2];
+  if (n != m) throw Exception("impossible copy : size don't match");
+  cuda_check(cudaMemcpy(voxels_, grid.voxels_, n, cudaMemcpyDeviceToDevice), "Grid::CopyVoxelsFrom");
+}
+
+static gm_grid_desc desc_of(const Grid& g) {
+  gm_grid_desc d;
+  for (int a = 0; a < 3; a++) {
+    d.bbox_min[a] = g.bbox_min()[a];
+    d.bbox_max[a] = g.bbox_max()[a];
+    d.data_res[a] = (int32_t)g.data_res()[a];
+  }
+  d.res = (int32_t)g.res()[0];
+  d.cell_size = g.cell_size();
+  return d;
+}
+
+void Grid::BuildTexMipmaps(const ScaleField& sf) {
+  gm_ctx* ctx = shared_ctx();
+  if (!pyramid_) cuda_check(cudaMalloc(&pyramid_, 8 * (size_t)gm_pyramid_texels((int32_t)res_[0])), "pyramid");
+  gm_grid_desc d = desc_of(*this);
+  const int s = gm_pyramid_build(ctx, &d, voxels_, reinterpret_cast<const int8_t*>(sf.scale_grid()),
+                                 (int32_t)std::floor(sf.global_scale() / sf.cell_size()),
+                                 reinterpret_cast<uint64_t*>(pyramid_), nullptr);
+  if (s != GM_OK) throw Exception(message(ctx, s, "Grid::BuildTexMipmaps"));
+}
+
+void Grid::BuildTexMipmaps(float se_size) {
+  gm_ctx* ctx = shared_ctx();
+  if (!pyramid_) cuda_check(cudaMalloc(&pyramid_, 8 * (size_t)gm_pyramid_texels((int32_t)res_[0])), "pyramid");
+  gm_grid_desc d = desc_of(*this);
+  const int s = gm_pyramid_build(ctx, &d, voxels_, nullptr, (int32_t)std::floor(2.f * se_size / cell_size_),
+                                 reinterpret_cast<uint64_t*>(pyramid_), nullptr);
+  if (s != GM_OK) throw Exception(message(ctx, s, "Grid::BuildTexMipmaps"));
+}
+
+void Grid::TransformToContour() {
+  gm_ctx* ctx = shared_ctx();
+  gm_grid_desc d = desc_of(*this);
+  const int s = gm_contour(ctx, &d, voxels_, voxels_, GM_REF, nullptr);
+  if (s != GM_OK) throw Exception(message(ctx, s, "Grid::TransformToContour"));
+}
+
+// ------------------------------------------------------------------ ScaleField
+
+ScaleField::~ScaleField() {
+  if (scale_grid_) cudaFree(scale_grid_);
+}
+
+void ScaleField::Init(const Vec3f& bbox_min, const Vec3f& bbox_max, const Vec3ui& res, float cell_size) {
+  bbox_min_ = bbox_min;
+  bbox_max_ = bbox_max;
+  res_ = res;
+  cell_size_ = cell_size;
+  const size_t n = (size_t)res[0] * res[1] * res[2];
+  if (!scale_grid_) cuda_check(cudaMalloc(&scale_grid_, n), "ScaleField::Init");
+  cuda_check(cudaMemset(scale_grid_, 0, n), "ScaleField::Init");
+}
+
+void ScaleField::GetScaleGridCPU(char** out) {
+  const size_t n = (size_t)res_[0] * res_[1] * res_[2];
+  *out = new char[n];
+  cuda_check(cudaMemcpy(*out, scale_grid_, n, cudaMemcpyDeviceToHost), "ScaleField::GetScaleGridCPU");
+}
+
+void ScaleField::UpdateGridGlobalScale() {
+  gm_ctx* ctx = shared_ctx();
+  const size_t n = (size_t)res_[0] * res_[1] * res_[2];
+  const int s = gm_scalefield_fill(ctx, reinterpret_cast<int8_t*>(scale_grid_), (int64_t)n,
+                                   (int32_t)std::floor(global_scale_ / cell_size_), nullptr);
+  if (s != GM_OK) throw Exception(message(ctx, s, "ScaleField::UpdateGridGlobalScale"));
+}
+
+void ScaleField::UpdateGrid() {
+  if (points_.empty()) return;
+  gm_ctx* ctx = shared_ctx();
+  const ScalePoint& p = points_.back();  // the reference applies the last point only
+  const float bmin[3] = {bbox_min_[0], bbox_min_[1], bbox_min_[2]};
+  const float pos[3] = {p.position()[0], p.position()[1], p.position()[2]};
+  const gm_brush_mode mode = p.edit_mode() == MIN_BRUSH ? GM_BRUSH_MIN
+                             : p.edit_mode() == ZERO_BRUSH ? GM_BRUSH_ZERO
+                                                           : GM_BRUSH_MAX;
+  if (p.edit_mode() == NO_EDITION) return;
+  const int s = gm_scalefield_brush(ctx, reinterpret_cast<int8_t*>(scale_grid_), (int32_t)res_[0], bmin, cell_size_,
+                                    pos, p.scale(), p.support(), global_scale_, mode, nullptr);
+  if (s != GM_OK) throw Exception(message(ctx, s, "ScaleField::UpdateGrid"));
+}
+
+// ------------------------------------------------------------------ Voxelizer
+
+Voxelizer::~Voxelizer() {}
+
+void Voxelizer::Load(const float* P, const float* N, int nv, const unsigned int* T, int nf) {
+  (void)N;
+  P_.assign(P, P + 3 * (size_t)nv);
+  T_.assign(T, T + 3 * (size_t)nf);
+}
+
+void Voxelizer::VoxelizeConservative(int base_res, float margin) {
+  gm_grid_desc d;
+  int s = gm_grid_attributes(P_.data(), (int64_t)(P_.size() / 3), base_res, margin, &d);
+  if (s != GM_OK) throw Grid::Exception("Voxelizer: bad mesh or resolution");
+  grid_.Init(Vec3f(d.bbox_min[0], d.bbox_min[1], d.bbox_min[2]), Vec3f(d.bbox_max[0], d.bbox_max[1], d.bbox_max[2]),
+             Vec3ui(d.res, d.res, d.res), Vec3ui(d.data_res[0], d.data_res[1], d.data_res[2]), d.cell_size);
+  grid_.SetGridValue(0);
+  float* dP = nullptr;
+  unsigned int* dT = nullptr;
+  cuda_check(cudaMalloc(&dP, sizeof(float) * P_.size()), "Voxelizer");
+  cuda_check(cudaMalloc(&dT, sizeof(unsigned int) * (T_.size() + 1)), "Voxelizer");
+  cudaMemcpy(dP, P_.data(), sizeof(float) * P_.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(dT, T_.data(), sizeof(unsigned int) * T_.size(), cudaMemcpyHostToDevice);
+  gm_ctx* ctx = shared_ctx();
+  s = gm_voxelize(ctx, &d, dP, (int64_t)(P_.size() / 3), dT, (int64_t)(T_.size() / 3), grid_.grid_gpu().voxels,
+                  nullptr);
+  cudaDeviceSynchronize();
+  cudaFree(dP);
+  cudaFree(dT);
+  if (s != GM_OK) throw Grid::Exception(message(ctx, s, "Voxelizer::VoxelizeConservative"));
+}
+
+// ------------------------------------------------------------------ GMorpho
+
+GMorpho::GMorpho() {}
+GMorpho::~GMorpho() {
+  if (ctx_) gm_ctx_destroy(ctx_);
+}
+
+void GMorpho::check(int status, const char* what) {
+  if (status != GM_OK) throw Exception(message(ctx_, status, what));
+}
+
+void GMorpho::Load(const float* P, const float* N, int nv, const unsigned int* T, int nf, int base_res,
+                   float se_size) {
+  se_size_ = se_size;
+  const float margin = se_size_ + 2.f / (2 * (float)base_res);  // GMorpho.cu:7735
+  voxelizer_.Load(P, N, nv, T, nf);
+  voxelizer_.VoxelizeConservative(base_res, margin);
+  const Grid& g = voxelizer_.grid();
+  input_grid_.Init(g.bbox_min(), g.bbox_max(), g.res(), g.data_res(), g.cell_size());
+  input_grid_.CopyVoxelsFrom(g);
+  dilation_grid_.Init(g.bbox_min(), g.bbox_max(), g.res(), g.data_res(), g.cell_size());
+  dilation_grid_.CopyVoxelsFrom(input_grid_);
+  closing_grid_.Init(g.bbox_min(), g.bbox_max(), g.res(), g.data_res(), g.cell_size());
+  closing_grid_.CopyVoxelsFrom(dilation_grid_);
+  if (!ctx_) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    check(gm_ctx_create(dev, &ctx_), "gm_ctx_create");
+  }
+}
+
+void GMorpho::close(const ScaleField* sf, int uniform_radius, int se) {
+  if (!ctx_) throw Exception("Load must come first");
+  gm_grid_desc d = desc_of(input_grid_);
+  check(gm_close(ctx_, &d, input_grid_.grid_gpu().voxels,
+                 sf ? reinterpret_cast<const int8_t*>(sf->scale_grid()) : nullptr, uniform_radius, (gm_mode)mode_,
+                 (gm_se)se, closing_grid_.grid_gpu().voxels, dilation_grid_.grid_gpu().voxels, nullptr, nullptr),
+        "gm_close");
+}
+
+void GMorpho::Update(Mesh& mesh, const ScaleField& sf, const FrameField&) {
+  if (use_frame_field_) throw Exception("unsupported: frame-field (rotated cube) dilation");
+  // gate of GMorpho.cu:7783: morphology only when floor(2 gs / cell) > 1
+  if (std::floor(2.f * sf.global_scale() / cell_size()) > 1.f)
+    close(&sf, 0, use_asymmetric_closing_ ? GM_SE_CUBE : GM_SE_SPHERE);
+  else
+    closing_grid_.CopyVoxelsFrom(input_grid_);
+  ExtractClosingMesh(mesh, use_asymmetric_closing_ ? 200 : 20);
+}
+
+void GMorpho::DilateBySphereMipmap(const ScaleField& sf) { close(&sf, 0, GM_SE_SPHERE); }
+void GMorpho::DilateByCubeMipmap(const ScaleField& sf) { close(&sf, 0, GM_SE_CUBE); }
+// The closing runs both halves in one call; the erosion of the last
+// dilation is already in closing_grid().
+void GMorpho::ErodeBySphereMipmap(const ScaleField&) {}
+
+void GMorpho::Update(Mesh& mesh, float se_size) {
+  se_size_ = se_size;
+  close(nullptr, (int)std::floor(2.f * se_size / cell_size()), GM_SE_CUBE);  // GMorpho.cu:7819-7845
+  ExtractClosingMesh(mesh, 20);
+}
+
+void GMorpho::DilateByCubeMipmap(float se_size) { close(nullptr, (int)std::floor(2.f * se_size / cell_size()), GM_SE_CUBE); }
+void GMorpho::DilateBySphereMipmap(float se_size) {
+  close(nullptr, (int)std::floor(2.f * se_size / cell_size()), GM_SE_SPHERE);
+}
+void GMorpho::ErodeBySphereMipmap(float) {}
+
+void GMorpho::ExtractClosingMesh() { ExtractClosingMesh(morpho_mesh_, 20); }
+
+void GMorpho::ExtractClosingMesh(Mesh& mesh, int iters) {
+  gm_grid_desc d = desc_of(closing_grid_);
+  gm_mesh_view mv;
+  check(gm_mesh(ctx_, &d, closing_grid_.grid_gpu().voxels, bilateral_filtering_ ? iters : 0, &mv, nullptr), "gm_mesh");
+  mesh.P().resize((size_t)mv.num_vertices);
+  mesh.N().resize((size_t)mv.num_vertices);
+  mesh.T().resize((size_t)mv.num_triangles);
+  check(gm_mesh_download(ctx_, mv.num_vertices ? &mesh.P()[0][0] : nullptr,
+                         mv.num_vertices ? &mesh.N()[0][0] : nullptr, mv.num_triangles ? &mesh.T()[0][0] : nullptr,
+                         nullptr),
+        "gm_mesh_download");
+  if (&mesh != &morpho_mesh_) morpho_mesh_ = mesh;
+}
+
+}  // namespace MorphoGraphics
+
+// ------------------------------------------------------------------ MarchingCubesMesher
+
+MarchingCubesMesher::MarchingCubesMesher(Grid* grid) : grid_(grid) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (gm_ctx_create(dev, &ctx_) != GM_OK) ctx_ = nullptr;
+}
+
+MarchingCubesMesher::~MarchingCubesMesher() {
+  if (ctx_) gm_ctx_destroy(ctx_);
+}
+
+void MarchingCubesMesher::createMesh3D(const unsigned char* d_voxels, int iters) {
+  if (!ctx_) throw MorphoGraphics::Grid::Exception("MarchingCubesMesher: no context");
+  gm_grid_desc d;
+  const int res = (int)grid_->getNbCellsX() / 2;
+  for (int a = 0; a < 3; a++) {
+    d.bbox_min[a] = grid_->getOrigin()[a];
+    d.bbox_max[a] = grid_->getOrigin()[a] + 2.f * grid_->getCellSizeX() * res;
+    d.data_res[a] = res;
+  }
+  d.res = res;
+  d.cell_size = 2.f * grid_->getCellSizeX();
+  gm_mesh_view mv;
+  const int s = gm_mesh(ctx_, &d, d_voxels, iters, &mv, nullptr);
+  if (s != GM_OK) throw MorphoGraphics::Grid::Exception(message(ctx_, s, "MarchingCubesMesher::createMesh3D"));
+  V_ = mv.vertices;
+  N_ = mv.normals;
+  T_ = mv.triangles;
+  nv_ = (unsigned int)mv.num_vertices;
+  nt_ = (unsigned int)mv.num_triangles;
+}
+
+void MarchingCubesMesher::getDeviceMesh(const float** V, const float** N, unsigned int* VSize,
+                                        const unsigned int** T, unsigned int* TSize) const {
+  *V = V_;
+  *N = N_;
+  *VSize = nv_;
+  *T = T_;
+  *TSize = nt_;
+}

@@ -1073,6 +1073,11 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   return cudaGetLastError();
 }
 
+cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc) {
+  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(res), dim3(64, 4), 0, st>>>(D, S, res, exact));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc) {
   cudaMemsetAsync(d_out, 0, sizeof(int), st);
   const int64_t vec = n / 16;

@@ -150,6 +150,13 @@ gm_status gm_close_noalloc(const gm_grid_desc* desc, const uint8_t* d_input, con
                            int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing,
                            uint8_t* d_dilation, uint8_t* d_contour, void* stream);
 
+/* Grid::TransformToContour (GMorpho/Grid.cu:2381-2408, 1230-1327): fine
+ * voxels outside the grid's set that are 6-adjacent to it; GM_REF keeps the
+ * reference's restriction to cells in [1, res-2]^3 whose byte is not 0xff,
+ * GM_EXACT covers the whole grid.  d_out may equal d_grid. */
+gm_status gm_contour(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_grid, uint8_t* d_out, gm_mode mode,
+                     void* stream);
+
 /* ---------------------------------------------------------------- a12..a16 */
 /* GMorpho::ExtractClosingMesh (GMorpho/GMorpho.cu:6814-7001): contour
  * marching cubes at isovalue 0.95 in the reference's emission order, then
@@ -169,6 +176,29 @@ gm_status gm_update(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_inpu
 /* Copy the context's last mesh to host buffers (GMorpho.cu:6992-7000);
  * any pointer may be NULL to skip that array. */
 gm_status gm_mesh_download(gm_ctx* ctx, float* h_vertices, float* h_normals, uint32_t* h_triangles, void* stream);
+
+/* ---------------------------------------------------------------- a18 */
+/* BVH over the set fine voxels of a packed grid (BVH::BuildFromSEList,
+ * GMorpho/BVH.cu:661-739): Morton-ordered leaves, radix tree, bottom-up
+ * integer boxes.  The handle owns device memory until gm_bvh_destroy. */
+typedef struct gm_bvh gm_bvh;
+gm_status gm_bvh_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_sites, gm_bvh** out,
+                       int64_t* num_leaves, void* stream);
+gm_status gm_bvh_destroy(gm_bvh* bvh);
+/* For each query point (3 int32 per point, in half-voxel units: the centre
+ * of fine voxel p is 2p+1), hit = 1 when a leaf voxel centre is at distance
+ * < radius (fine voxels) — the leaf test of ErodeBySphereDynamicStack
+ * (GMorpho/GMorpho.cu:8957-9060), exact. */
+gm_status gm_bvh_query(gm_ctx* ctx, const gm_bvh* bvh, const int32_t* d_points2, int64_t num_points,
+                       int32_t radius, uint8_t* d_hits, void* stream);
+/* The leaves' 64-bit Morton keys (x in bit 0), ascending. */
+gm_status gm_bvh_leaves(gm_ctx* ctx, const gm_bvh* bvh, uint64_t* d_keys, void* stream);
+/* GMorpho::ErodeByBVH (GMorpho/GMorpho.cu:9308-9401): builds the BVH of the
+ * dilation's contour (TransformToContour) and removes every voxel of D, in
+ * cells with D != 0 and X != 0xff inside data_res, whose centre is within
+ * distance < radius of a contour voxel centre. */
+gm_status gm_erode_bvh(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const uint8_t* d_dilation,
+                       int32_t radius, uint8_t* d_closing, void* stream);
 
 /* ---------------------------------------------------------------- layout */
 /* Voxelizer::ConvertBucketToPacketGrid (GMorpho/Voxelizer.cu:798-849):

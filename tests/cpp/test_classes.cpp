@@ -1,0 +1,65 @@
+// Exercises the reference-style C++ classes over libgmorpho_gb300, the way
+// the reference viewer drives them (BroxyViewer.cpp:108-232): load a mesh,
+// set a global scale, Update, brush the scale field, Update again.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "gmorpho/GMorpho.h"
+
+using namespace MorphoGraphics;
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    fprintf(stderr, "usage: %s in.off out.off\n", argv[0]);
+    return 2;
+  }
+  Mesh input;
+  if (!input.loadOFF(argv[1])) {
+    fprintf(stderr, "cannot read %s\n", argv[1]);
+    return 2;
+  }
+  std::vector<float> P, N;
+  std::vector<unsigned int> T;
+  for (auto& p : input.P()) { P.push_back(p[0]); P.push_back(p[1]); P.push_back(p[2]); N.insert(N.end(), 3, 0.f); }
+  for (auto& t : input.T()) { T.push_back(t[0]); T.push_back(t[1]); T.push_back(t[2]); }
+  try {
+    GMorpho gm;
+    gm.Load(P.data(), N.data(), (int)input.P().size(), T.data(), (int)input.T().size(), 64, 0.3f);
+    ScaleField sf;
+    const unsigned int fr = 2 * gm.res()[0];
+    sf.set_global_scale(0.05f);
+    sf.Init(gm.bbox_min(), gm.bbox_max(), Vec3ui(fr, fr, fr), 0.5f * gm.cell_size());
+    sf.UpdateGridGlobalScale();
+    FrameField ff;
+    Mesh out;
+    gm.Update(out, sf, ff);
+    const size_t t1 = out.T().size();
+    // brush a bigger radius at the first vertex (BroxyViewer.cpp:667-672)
+    sf.AddPoint(input.P()[0], 0.15f, 0.3f);
+    sf.UpdateGrid();
+    gm.Update(out, sf, ff);
+    const size_t t2 = out.T().size();
+    gm.set_use_asymmetric_closing(true);
+    Mesh asym;
+    gm.Update(asym, sf, ff);
+    if (!out.storeOFF(argv[2])) return 3;
+    printf("%zu %zu %zu %zu\n", out.P().size(), t1, t2, asym.T().size());
+    for (auto& n : out.N())
+      if (!(std::fabs(n[0] * n[0] + n[1] * n[1] + n[2] * n[2] - 1.f) < 1e-3f)) return 4;
+    gm.set_use_frame_field(true);
+    try {
+      gm.Update(out, sf, ff);
+      return 5;
+    } catch (const GMorpho::Exception&) {
+    }
+  } catch (const GMorpho::Exception& e) {
+    fprintf(stderr, "%s\n", e.msg().c_str());
+    return 1;
+  } catch (const Grid::Exception& e) {
+    fprintf(stderr, "%s\n", e.msg().c_str());
+    return 1;
+  }
+  return 0;
+}
