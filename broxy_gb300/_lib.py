@@ -32,6 +32,27 @@ class MeshView(C.Structure):
                 ("num_vertices", C.c_int64), ("num_triangles", C.c_int64)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("desc", GridDesc), ("d_input", C.c_void_p), ("d_scale", C.c_void_p), ("uniform_radius", C.c_int32),
+                ("d_closing", C.c_void_p)]
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("max_crop_res", C.c_int32), ("rmax", C.c_int32), ("mode", C.c_int32),
+                ("bilateral_iters", C.c_int32)]
+
+
+class Edit(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("scale", C.c_float), ("support", C.c_float),
+                ("global_scale", C.c_float), ("mode", C.c_int32)]
+
+
+class EditResult(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("status", C.c_int32), ("latency_ms", C.c_float), ("device_ms", C.c_float),
+                ("dirty_lo", C.c_int32 * 3), ("dirty_hi", C.c_int32 * 3), ("patch", MeshView),
+                ("patch_keep", C.c_void_p)]
+
+
 class UpdateOpts(C.Structure):
     _fields_ = [("use_asymmetric_closing", C.c_int32), ("bilateral_filtering", C.c_int32), ("mode", C.c_int32)]
 
@@ -62,6 +83,16 @@ PROTOTYPES = {
     "gm_update": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_float, C.POINTER(UpdateOpts),
                             C.POINTER(C.c_int64), C.POINTER(C.c_int64), _P]),
     "gm_mesh_download": (C.c_int, [_P, _P, _P, _P, _P]),
+    "gm_batch_close_mesh": (C.c_int, [_P, C.c_int32, C.POINTER(BatchItem), C.c_int, C.c_int, C.c_int32, C.c_int32,
+                                       C.POINTER(MeshView), _P]),
+    "gm_batch_lanes": (C.c_int32, [_P]),
+    "gm_server_create": (C.c_int, [C.POINTER(GridDesc), _P, _P, C.POINTER(ServerOpts), C.POINTER(_P)]),
+    "gm_server_destroy": (C.c_int, [_P]),
+    "gm_server_submit": (C.c_int, [_P, C.POINTER(Edit), C.POINTER(C.c_uint64)]),
+    "gm_server_poll": (C.c_int, [_P, C.POINTER(EditResult), C.c_int32, C.POINTER(C.c_int32)]),
+    "gm_server_pending": (C.c_int32, [_P]),
+    "gm_server_closing": (C.c_void_p, [_P]),
+    "gm_server_kernel_launches": (C.c_longlong, [_P]),
     "gm_bvh_build": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.POINTER(_P), C.POINTER(C.c_int64), _P]),
     "gm_bvh_destroy": (C.c_int, [_P]),
     "gm_bvh_query": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, _P, _P]),

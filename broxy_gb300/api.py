@@ -178,6 +178,35 @@ class Context:
         self._check(st)
         return out
 
+    # batched closing + meshing of uneven grids
+    def batch_close_mesh(self, items, mode=L.GM_REF, se=L.GM_SE_SPHERE, bilateral_iters=20, lanes=0, mesh=True):
+        """items: list of (desc, X, R or None, uniform_radius, out).  Returns a
+        list of (V, N, T) zero-copy device arrays (or None when mesh=False)."""
+        import torch
+        n = len(items)
+        arr = (L.BatchItem * n)()
+        for i, (desc, X, R, r, out) in enumerate(items):
+            arr[i].desc = desc
+            arr[i].d_input = X.data_ptr()
+            arr[i].d_scale = R.data_ptr() if R is not None else None
+            arr[i].uniform_radius = int(r)
+            arr[i].d_closing = out.data_ptr()
+        views = (L.MeshView * n)() if mesh else None
+        self._check(self.lib.gm_batch_close_mesh(self.ctx, n, arr, mode, se, int(bilateral_iters), int(lanes),
+                                                 views, _stream()))
+        if not mesh:
+            return None
+        res = []
+        for v in views:
+            res.append((torch.as_tensor(DevicePtrArray(v.vertices, (v.num_vertices, 3), "<f4"), device="cuda"),
+                        torch.as_tensor(DevicePtrArray(v.normals, (v.num_vertices, 3), "<f4"), device="cuda"),
+                        torch.as_tensor(DevicePtrArray(v.triangles, (v.num_triangles, 3), "<u4"), device="cuda")))
+        return res
+
+    @property
+    def batch_lanes(self):
+        return int(self.lib.gm_batch_lanes(self.ctx))
+
     # a18
     def bvh_build(self, desc, sites):
         h = C.c_void_p()

@@ -1,0 +1,327 @@
+// batch.cu — many independent closings + meshes in one call (the batched
+// form of GMorpho::Update for a set of uneven grids).
+//
+// Instances are spread over L "lanes" (CUDA streams, each with its own
+// workspace), largest first onto the least-loaded lane, so that the small
+// kernels of small grids run side by side instead of one grid at a time.
+// The closing phase of a uniform-radius batch is captured once into a CUDA
+// graph (fork/join over the lane streams) and replayed while the batch
+// signature (pointers, sizes, radii, mode) does not change.  Meshing runs on
+// the same lanes with a single host synchronisation for all the vertex and
+// triangle counts.  The lane count is chosen by a small autotuner (timed
+// candidates 1, 2, 4, 8, 16 on the first call of a signature).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "../../include/gmorpho_gb300.h"
+#include "gm_common.cuh"
+#include "gm_internal.h"
+
+namespace gm {
+
+struct BatchLane {
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  uint8_t* ws = nullptr;
+  size_t ws_bytes = 0;
+};
+
+struct BatchState {
+  std::vector<BatchLane> lanes;
+  std::vector<MeshBuffers> meshes;
+  std::vector<int64_t> nv, nt;
+  uint32_t* h_tot = nullptr;  // pinned, 4 per instance
+  int h_tot_cap = 0;
+  int* d_rmax = nullptr;      // one int per instance
+  int* h_rmax = nullptr;      // pinned
+  int rmax_cap = 0;
+  cudaEvent_t fork = nullptr;
+  cudaStream_t cap_st = nullptr;  // capture / replay stream (the caller's may be the legacy stream)
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  uint64_t graph_sig = 0;
+  long long graph_kernels = 0;
+  std::map<uint64_t, int> tuned;
+};
+
+void batch_release(void* p) {
+  BatchState* b = static_cast<BatchState*>(p);
+  if (!b) return;
+  for (BatchLane& l : b->lanes) {
+    if (l.st) cudaStreamDestroy(l.st);
+    if (l.done) cudaEventDestroy(l.done);
+    cudaFree(l.ws);
+  }
+  for (MeshBuffers& m : b->meshes) m.release();
+  if (b->h_tot) cudaFreeHost(b->h_tot);
+  if (b->h_rmax) cudaFreeHost(b->h_rmax);
+  cudaFree(b->d_rmax);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->cap_st) cudaStreamDestroy(b->cap_st);
+  if (b->ev_in) cudaEventDestroy(b->ev_in);
+  if (b->ev_out) cudaEventDestroy(b->ev_out);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  delete b;
+}
+
+static uint64_t mix(uint64_t h, uint64_t v) {
+  h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+  return h;
+}
+
+static uint64_t signature(int n, const gm_batch_item* it, int mode, int se, int lanes) {
+  uint64_t h = mix(0, (uint64_t)n);
+  h = mix(h, (uint64_t)mode);
+  h = mix(h, (uint64_t)se);
+  h = mix(h, (uint64_t)lanes);
+  for (int i = 0; i < n; i++) {
+    h = mix(h, (uint64_t)it[i].desc.res);
+    for (int a = 0; a < 3; a++) h = mix(h, (uint64_t)it[i].desc.data_res[a]);
+    h = mix(h, (uint64_t)(uintptr_t)it[i].d_input);
+    h = mix(h, (uint64_t)(uintptr_t)it[i].d_scale);
+    h = mix(h, (uint64_t)(uintptr_t)it[i].d_closing);
+    h = mix(h, (uint64_t)it[i].uniform_radius);
+  }
+  return h;
+}
+
+static cudaError_t ensure_lanes(BatchState* b, int L) {
+  while ((int)b->lanes.size() < L) {
+    BatchLane l;
+    cudaError_t e = cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
+    b->lanes.push_back(l);
+  }
+  cudaError_t e = cudaSuccess;
+  if (!b->fork && (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+  if (!b->cap_st && (e = cudaStreamCreateWithFlags(&b->cap_st, cudaStreamNonBlocking)) != cudaSuccess) return e;
+  if (!b->ev_in && (e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming)) != cudaSuccess) return e;
+  if (!b->ev_out && (e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming)) != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+// largest grids first onto the least-loaded lane
+static std::vector<int> assign(int n, const gm_batch_item* it, int L) {
+  std::vector<int> order(n), lane(n, 0);
+  for (int i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return it[a].desc.res > it[b].desc.res; });
+  std::vector<double> load(L, 0.0);
+  for (int i : order) {
+    int best = 0;
+    for (int l = 1; l < L; l++)
+      if (load[l] < load[best]) best = l;
+    lane[i] = best;
+    load[best] += (double)it[i].desc.res * it[i].desc.res * it[i].desc.res;
+  }
+  return lane;
+}
+
+// The closing phase: fork from `st`, every lane runs its instances, join.
+static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* it, const int* rmax, int mode, int se,
+                                    int L, const std::vector<int>& lane, int sms, cudaStream_t st,
+                                    KernelCounter* kc) {
+  cudaError_t e = cudaEventRecord(b->fork, st);
+  if (e != cudaSuccess) return e;
+  for (int l = 0; l < L; l++)
+    if ((e = cudaStreamWaitEvent(b->lanes[l].st, b->fork, 0)) != cudaSuccess) return e;
+  for (int i = 0; i < n; i++) {
+    BatchLane& ln = b->lanes[lane[i]];
+    CloseArgs a;
+    a.res = it[i].desc.res;
+    for (int k = 0; k < 3; k++) a.data_res[k] = it[i].desc.data_res[k];
+    a.X = it[i].d_input;
+    a.R = it[i].d_scale;
+    a.uniform_r = it[i].uniform_radius;
+    a.rmax = rmax[i];
+    a.mode = mode;
+    a.se = se;
+    a.C_out = it[i].d_closing;
+    a.D_out = nullptr;
+    a.S_out = nullptr;
+    a.workspace = ln.ws;
+    a.num_sms = sms;
+    if ((e = launch_close(a, ln.st, kc)) != cudaSuccess) return e;
+  }
+  for (int l = 0; l < L; l++) {
+    if ((e = cudaEventRecord(b->lanes[l].done, b->lanes[l].st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, b->lanes[l].done, 0)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, int se, int bilateral, int lanes_req,
+                      gm_mesh_view* meshes, int sms, cudaStream_t st, KernelCounter* kc) {
+  if (!*state) *state = new BatchState();
+  BatchState* b = static_cast<BatchState*>(*state);
+  cudaError_t e;
+  // radius bounds: uniform radii are known; radius fields are reduced on
+  // the device in one round trip for the whole batch
+  std::vector<int> rmax(n);
+  bool all_uniform = true;
+  for (int i = 0; i < n; i++) {
+    rmax[i] = clamp_radius(it[i].uniform_radius);
+    if (it[i].d_scale) all_uniform = false;
+  }
+  if (!all_uniform) {
+    if (b->rmax_cap < n) {
+      cudaFree(b->d_rmax);
+      if (b->h_rmax) cudaFreeHost(b->h_rmax);
+      b->d_rmax = nullptr;
+      b->h_rmax = nullptr;
+      if ((e = cudaMalloc(&b->d_rmax, sizeof(int) * n)) != cudaSuccess) return e;
+      if ((e = cudaMallocHost(&b->h_rmax, sizeof(int) * n)) != cudaSuccess) return e;
+      b->rmax_cap = n;
+    }
+    for (int i = 0; i < n; i++)
+      if (it[i].d_scale) {
+        if ((e = launch_rmax(it[i].d_scale, (int64_t)8 * it[i].desc.res * it[i].desc.res * it[i].desc.res,
+                             b->d_rmax + i, sms, st, kc)) != cudaSuccess)
+          return e;
+        if ((e = cudaMemcpyAsync(b->h_rmax + i, b->d_rmax + i, sizeof(int), cudaMemcpyDeviceToHost, st)) !=
+            cudaSuccess)
+          return e;
+      }
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+    for (int i = 0; i < n; i++)
+      if (it[i].d_scale) rmax[i] = b->h_rmax[i];
+  }
+  // lane count: requested, tuned for this signature, or tuned now
+  int L = lanes_req;
+  const uint64_t tune_sig = signature(n, it, mode, se, 0);
+  if (L <= 0) {
+    auto f = b->tuned.find(tune_sig);
+    if (f != b->tuned.end()) L = f->second;
+  }
+  const bool tune = L <= 0;
+  const int cands[5] = {1, 2, 4, 8, 16};
+  const int maxL = tune ? 16 : std::max(1, std::min(L, 64));
+  if ((e = ensure_lanes(b, maxL)) != cudaSuccess) return e;
+  // per-lane workspaces sized for the largest grid of the batch
+  int maxres = 16;
+  for (int i = 0; i < n; i++) maxres = std::max(maxres, (int)it[i].desc.res);
+  const size_t wsb = close_workspace_bytes(maxres);
+  for (int l = 0; l < maxL; l++)
+    if (b->lanes[l].ws_bytes < wsb) {
+      cudaFree(b->lanes[l].ws);
+      b->lanes[l].ws = nullptr;
+      b->lanes[l].ws_bytes = 0;
+      if ((e = cudaMalloc(&b->lanes[l].ws, wsb)) != cudaSuccess) return e;
+      b->lanes[l].ws_bytes = wsb;
+    }
+  if (tune) {
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    float best_ms = 1e30f;
+    int best = 1;
+    for (int c : cands) {
+      const std::vector<int> lane = assign(n, it, c);
+      // one untimed pass (first-touch, function attributes), one timed
+      for (int rep = 0; rep < 2; rep++) {
+        cudaEventRecord(t0, st);
+        if ((e = enqueue_closings(b, n, it, rmax.data(), mode, se, c, lane, sms, st, nullptr)) != cudaSuccess) {
+          cudaEventDestroy(t0);
+          cudaEventDestroy(t1);
+          return e;
+        }
+        cudaEventRecord(t1, st);
+      }
+      cudaEventSynchronize(t1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, t0, t1);
+      if (ms < best_ms) { best_ms = ms; best = c; }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    L = best;
+    b->tuned[tune_sig] = L;
+  }
+  const std::vector<int> lane = assign(n, it, L);
+  // closing phase: replay the captured graph when the batch is unchanged
+  const uint64_t sig = signature(n, it, mode, se, L);
+  const bool graphable = all_uniform && !(kc && kc->profiling);
+  if (graphable) {
+    if (!b->graph || b->graph_sig != sig) {
+      if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      KernelCounter cap;  // counts the kernels the graph holds
+      if ((e = cudaStreamBeginCapture(b->cap_st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+      const cudaError_t ec = enqueue_closings(b, n, it, rmax.data(), mode, se, L, lane, sms, b->cap_st, &cap);
+      e = cudaStreamEndCapture(b->cap_st, &g);
+      if (ec != cudaSuccess) return ec;
+      if (e != cudaSuccess) return e;
+      e = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return e;
+      b->graph_sig = sig;
+      b->graph_kernels = cap.launches;
+    }
+    if ((e = cudaEventRecord(b->ev_in, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(b->cap_st, b->ev_in, 0)) != cudaSuccess) return e;
+    if ((e = cudaGraphLaunch(b->graph, b->cap_st)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(b->ev_out, b->cap_st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, b->ev_out, 0)) != cudaSuccess) return e;
+    if (kc) kc->launches += b->graph_kernels;
+  } else {
+    if ((e = enqueue_closings(b, n, it, rmax.data(), mode, se, L, lane, sms, st, kc)) != cudaSuccess) return e;
+  }
+  if (!meshes) return cudaGetLastError();
+  // meshing: counts on the lanes, one synchronisation, emission on the lanes
+  if ((int)b->meshes.size() < n) b->meshes.resize(n);
+  b->nv.assign(n, 0);
+  b->nt.assign(n, 0);
+  if (b->h_tot_cap < n) {
+    if (b->h_tot) cudaFreeHost(b->h_tot);
+    b->h_tot = nullptr;
+    if ((e = cudaMallocHost(&b->h_tot, sizeof(uint32_t) * 4 * n)) != cudaSuccess) return e;
+    b->h_tot_cap = n;
+  }
+  if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return e;
+  for (int l = 0; l < L; l++) cudaStreamWaitEvent(b->lanes[l].st, b->fork, 0);
+  std::vector<MeshArgs> ma(n);
+  for (int i = 0; i < n; i++) {
+    MeshArgs& a = ma[i];
+    a.res = it[i].desc.res;
+    a.C = it[i].d_closing;
+    for (int k = 0; k < 3; k++) a.bbox_min[k] = it[i].desc.bbox_min[k];
+    a.cell_size = it[i].desc.cell_size;
+    a.isovalue = 0.95f;
+    a.bilateral_iters = bilateral;
+    a.num_sms = sms;
+    if ((e = mesh_count_launch(a, b->meshes[i], b->lanes[lane[i]].st, kc, b->h_tot + 4 * i)) != cudaSuccess) return e;
+  }
+  for (int l = 0; l < L; l++)
+    if ((e = cudaStreamSynchronize(b->lanes[l].st)) != cudaSuccess) return e;
+  for (int i = 0; i < n; i++) {
+    if ((e = mesh_count_finish(b->meshes[i], b->h_tot + 4 * i, &b->nv[i], &b->nt[i])) != cudaSuccess) return e;
+    if (b->nv[i] > 0xfffffff0LL || b->nt[i] > 0x7ffffff0LL) return cudaErrorInvalidValue;
+    if ((e = mesh_emit(ma[i], b->meshes[i], b->nv[i], b->nt[i], b->lanes[lane[i]].st, kc)) != cudaSuccess) return e;
+    meshes[i].vertices = b->meshes[i].V;
+    meshes[i].normals = b->meshes[i].N;
+    meshes[i].triangles = b->meshes[i].T;
+    meshes[i].num_vertices = b->nv[i];
+    meshes[i].num_triangles = b->nt[i];
+  }
+  for (int l = 0; l < L; l++) {
+    cudaEventRecord(b->lanes[l].done, b->lanes[l].st);
+    cudaStreamWaitEvent(st, b->lanes[l].done, 0);
+  }
+  return cudaGetLastError();
+}
+
+int batch_lanes_tuned(void* state) {
+  BatchState* b = static_cast<BatchState*>(state);
+  if (!b || b->tuned.empty()) return 0;
+  return b->tuned.rbegin()->second;
+}
+
+}  // namespace gm

@@ -86,6 +86,8 @@ struct gm_ctx {
   // voxelizer scratch
   uint8_t* vox = nullptr;
   size_t vox_bytes = 0;
+  // batched closing + meshing state (lanes, per-instance meshes, graph)
+  void* batch = nullptr;
   // last mesh
   gm::MeshBuffers mesh;
   int64_t nv = 0, nt = 0;
@@ -187,10 +189,8 @@ gm_status gm_ctx_destroy(gm_ctx* ctx) {
   cudaFree(ctx->d_C);
   cudaFree(ctx->d_int);
   cudaFree(ctx->vox);
-  gm::MeshBuffers& b = ctx->mesh;
-  cudaFree(b.V); cudaFree(b.N); cudaFree(b.N4a); cudaFree(b.N4b); cudaFree(b.T); cudaFree(b.adj);
-  cudaFree(b.nbr); cudaFree(b.wpos); cudaFree(b.rowptr);
-  cudaFree(b.cursor); cudaFree(b.cell_voff); cudaFree(b.brick_tot); cudaFree(b.fix);
+  ctx->mesh.release();
+  gm::batch_release(ctx->batch);
   ctx->kc.release();
   delete ctx;
   return GM_OK;
@@ -505,6 +505,35 @@ gm_status gm_mesh_download(gm_ctx* ctx, float* h_V, float* h_N, uint32_t* h_T, v
   GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "gm_mesh_download");
   return GM_OK;
 }
+
+// ------------------------------------------------------------------ batch
+
+gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items, gm_mode mode, gm_se se,
+                              int32_t bilateral_iters, int32_t lanes, gm_mesh_view* meshes, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (n < 0 || (n > 0 && !items) || bilateral_iters < 0 || lanes < 0 || lanes > 64)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: bad argument");
+  if (mode != GM_REF && mode != GM_EXACT) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: mode");
+  if (se != GM_SE_SPHERE && se != GM_SE_CUBE) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: se");
+  for (int i = 0; i < n; i++) {
+    gm_status s = check_desc(ctx, &items[i].desc);
+    if (s != GM_OK) return s;
+    if (!items[i].d_input || !items[i].d_closing || !aligned16(items[i].d_input) ||
+        (items[i].d_scale && !aligned16(items[i].d_scale)))
+      return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: item " + std::to_string(i));
+  }
+  if (n == 0) return GM_OK;
+  gm_status s = set_device(ctx);
+  if (s != GM_OK) return s;
+  ctx->has_mesh = false;
+  GM_CHECK_CUDA(ctx,
+                gm::batch_run(&ctx->batch, n, items, (int)mode, (int)se, bilateral_iters, lanes, meshes, ctx->num_sms,
+                              (cudaStream_t)stream, &ctx->kc),
+                "gm_batch_close_mesh");
+  return GM_OK;
+}
+
+int32_t gm_batch_lanes(gm_ctx* ctx) { return ctx ? gm::batch_lanes_tuned(ctx->batch) : 0; }
 
 // ------------------------------------------------------------------ a18
 

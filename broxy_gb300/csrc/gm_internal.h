@@ -9,6 +9,8 @@
 #include <string>
 #include <vector>
 
+#include "../../include/gmorpho_gb300.h"
+
 namespace gm {
 
 // Counts the kernels this library launches (reported by the C ABI so that a
@@ -78,6 +80,7 @@ struct MeshArgs {
 
 // Device-side mesh buffers, grown on demand by the caller of launch_mesh.
 struct MeshBuffers {
+  void release();
   float* V = nullptr;       // 3 * v_cap
   float* N = nullptr;       // 3 * v_cap
   float* N2 = nullptr;      // unused (kept for ABI-stable layout of the struct)
@@ -101,6 +104,12 @@ struct MeshBuffers {
 // Phase 1: counts (host-synchronous: returns the vertex/triangle totals).
 cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc, int64_t* nv,
                        int64_t* nt);
+// Split form of mesh_count for callers that overlap several meshes: launch
+// the counting and an async copy of the 4 totals into h_tot4, then (after
+// the stream is synchronised) size the buffers from them.
+cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
+                              uint32_t* h_tot4);
+cudaError_t mesh_count_finish(MeshBuffers& b, const uint32_t* tot, int64_t* nv, int64_t* nt);
 // Phase 2: emission into b (capacities must be >= counts).
 cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt, cudaStream_t st,
                       KernelCounter* kc);
@@ -117,6 +126,12 @@ cudaError_t launch_voxelize(const float* P, int64_t nv, const uint32_t* T, int64
 size_t voxelize_scratch_bytes(int res);
 // dir 0: z-words -> packed grid; dir 1: packed grid -> z-words
 cudaError_t launch_layout(int res, const uint32_t* zw, uint8_t* grid, int dir, cudaStream_t st, KernelCounter* kc);
+
+// ---------------------------------------------------------------- batch
+void batch_release(void* state);
+cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, int se, int bilateral, int lanes_req,
+                      gm_mesh_view* meshes, int sms, cudaStream_t st, KernelCounter* kc);
+int batch_lanes_tuned(void* state);
 
 // ---------------------------------------------------------------- BVH
 cudaError_t bvh_build(const uint8_t* grid, int res, void** handle, uint32_t* scratch_bricks, int* n_out,

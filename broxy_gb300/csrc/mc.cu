@@ -692,8 +692,15 @@ static int gs_blocks(int64_t n, int threads, int sms) {
   return (int)(b < 1 ? 1 : b);
 }
 
-cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc, int64_t* nv,
-                       int64_t* nt) {
+void MeshBuffers::release() {
+  cudaFree(V); cudaFree(N); cudaFree(N2); cudaFree(N4a); cudaFree(N4b); cudaFree(T); cudaFree(adj);
+  cudaFree(nbr); cudaFree(wpos); cudaFree(rowptr); cudaFree(cursor); cudaFree(cell_voff); cudaFree(brick_tot);
+  cudaFree(fix);
+  *this = MeshBuffers();
+}
+
+cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
+                              uint32_t* h_tot4) {
   const int res = a.res;
   const int64_t cells = (int64_t)res * res * res;
   const int nb = (int)(cells / kCellsPerBrick);
@@ -714,11 +721,10 @@ cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, Kerne
   }
   GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, res, b.brick_tot));
   GM_LAUNCH(kc, "k_scan_bricks", st, k_scan_bricks<<<1, 1024, 0, st>>>(b.brick_tot, nb));
-  uint32_t tot[4];
-  e = cudaMemcpyAsync(tot, b.brick_tot + 4 * (size_t)nb, sizeof(tot), cudaMemcpyDeviceToHost, st);
-  if (e != cudaSuccess) return e;
-  e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(h_tot4, b.brick_tot + 4 * (size_t)nb, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+}
+
+cudaError_t mesh_count_finish(MeshBuffers& b, const uint32_t* tot, int64_t* nv, int64_t* nt) {
   *nv = tot[1];
   *nt = tot[2];
   const int need_fix = (int)tot[3];
@@ -726,10 +732,22 @@ cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, Kerne
     if (b.fix) cudaFree(b.fix);
     b.fix = nullptr;
     const int c = need_fix + 64;
-    e = cudaMalloc(&b.fix, sizeof(uint32_t) * (1 + 4 * (size_t)c));
+    cudaError_t e = cudaMalloc(&b.fix, sizeof(uint32_t) * (1 + 4 * (size_t)c));
     if (e != cudaSuccess) return e;
     b.fix_cap = c;
   }
+  return cudaSuccess;
+}
+
+cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc, int64_t* nv,
+                       int64_t* nt) {
+  uint32_t tot[4];
+  cudaError_t e = mesh_count_launch(a, b, st, kc, tot);
+  if (e != cudaSuccess) return e;
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  e = mesh_count_finish(b, tot, nv, nt);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

@@ -197,3 +197,60 @@ def random_grid(res, seed, density=0.5, blobs=6):
     inner[m:N - m, m:N - m, m:N - m] = True
     occ |= noise & inner
     return pack_dense(occ)
+
+
+def batch_instances(seed=4000, count=64, lo=64, hi=512, device=None):
+    """The batching workload: `count` grids whose fine edge E is drawn
+    log-uniform in [lo, hi] and padded to a multiple of 32, each embedded in
+    the next power-of-two cube (data_res = E/2 cells), holding a blob solid
+    scaled to its E-box, with its own uniform radius U{1..24}.  Returns a
+    list of dicts (res, data_res, X, radius, edge)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        E = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        E = int(np.ceil(E / 32.0) * 32)
+        N = 1
+        while N < E:
+            N *= 2
+        res = N // 2
+        radius = int(rng.integers(1, 25))
+        blobs = int(max(6, min(200, 200 * (E / 512.0) ** 2)))
+        X = _blob_box(res, E, seed * 100 + i, blobs, device)
+        out.append(dict(res=res, data_res=[E // 2] * 3, X=X, radius=radius, edge=E))
+    return out
+
+
+def _blob_box(res, E, seed, count, device):
+    """Blob solid with centres in [0.2, 0.8] of an E-voxel box at the grid
+    origin, classified at the fine voxel centres of the res-cell grid."""
+    N = 2 * res
+    centres, sigmas, weights = blob_params(seed, count)
+    scale = E / float(N)
+    centres = centres * scale
+    sigmas = sigmas * scale * 1.5
+    if device is None:
+        x = _axis(N)
+        occ = np.zeros((N, N, N), dtype=bool)
+        for z0 in range(0, N, 16):
+            zs = x[z0:z0 + 16]
+            f = np.zeros((len(zs), N, N))
+            for c, s, w in zip(centres, sigmas, weights):
+                f += w * np.exp(-(zs - c[2])[:, None, None] ** 2 / (2 * s * s)) * \
+                    np.exp(-(x - c[1])[None, :, None] ** 2 / (2 * s * s)) * \
+                    np.exp(-(x - c[0])[None, None, :] ** 2 / (2 * s * s))
+            occ[z0:z0 + 16] = f >= 0.5
+        return pack_dense(occ)
+    import torch
+    x = torch.as_tensor(_axis(N), device=device)
+    c = torch.as_tensor(centres, device=device)
+    s = torch.as_tensor(sigmas, device=device)
+    w = torch.as_tensor(weights, device=device)
+    gx = torch.exp(-(x[None, :] - c[:, 0:1]) ** 2 / (2 * s[:, None] ** 2)) * w[:, None]
+    gy = torch.exp(-(x[None, :] - c[:, 1:2]) ** 2 / (2 * s[:, None] ** 2))
+    gz = torch.exp(-(x[None, :] - c[:, 2:3]) ** 2 / (2 * s[:, None] ** 2))
+    occ = torch.zeros((N, N, N), dtype=torch.bool, device=device)
+    for z0 in range(0, N, 16):
+        f = torch.einsum("kz,ky,kx->zyx", gz[:, z0:z0 + 16], gy, gx)
+        occ[z0:z0 + 16] = f >= 0.5
+    return pack_dense_torch(occ)

@@ -177,6 +177,82 @@ gm_status gm_update(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_inpu
  * any pointer may be NULL to skip that array. */
 gm_status gm_mesh_download(gm_ctx* ctx, float* h_vertices, float* h_normals, uint32_t* h_triangles, void* stream);
 
+/* ---------------------------------------------------------------- batch */
+/* One instance of a batched closing: its own grid, radius and output. */
+typedef struct {
+  gm_grid_desc desc;
+  const uint8_t* d_input;
+  const int8_t* d_scale;   /* NULL: uniform_radius */
+  int32_t uniform_radius;
+  uint8_t* d_closing;      /* output, desc.res^3 bytes */
+} gm_batch_item;
+
+/* Batched form of GMorpho::Update for n independent grids of uneven sizes
+ * (no reference counterpart: the reference closes one grid per call).
+ * Instances run concurrently on `lanes` internal streams (0 = autotuned on
+ * the first call of a batch and cached); a uniform-radius batch replays its
+ * closing phase as one CUDA graph while the batch is unchanged.  When
+ * meshes != NULL every closing is meshed (bilateral_iters iterations) and
+ * meshes[i] views device buffers owned by the context until the next batch.
+ * Results equal n separate gm_close + gm_mesh calls bit for bit. */
+gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items, gm_mode mode, gm_se se,
+                              int32_t bilateral_iters, int32_t lanes, gm_mesh_view* meshes, void* stream);
+/* Lane count the autotuner chose for the last tuned batch (0: none yet). */
+int32_t gm_batch_lanes(gm_ctx* ctx);
+
+/* ---------------------------------------------------------------- serving */
+/* Resident-grid edit server (no reference counterpart: the reference
+ * re-closes and re-meshes the whole grid after each brush event,
+ * BroxyViewer.cpp:667-672).  An edit is one ScaleField brush point
+ * (ScaleField::UpdateGrid, GMorpho/ScaleField.cu:81-141) applied to the
+ * resident radius field, followed by an exact LOCAL re-closing of the
+ * region it can change and a re-mesh of that region.  Edits are admitted as
+ * slots free up (continuous batching); edits whose regions overlap an edit
+ * still on the GPU wait for it, disjoint edits run concurrently.  The
+ * server uses the current device; all calls come from one host thread. */
+typedef struct gm_server gm_server;
+
+typedef struct {
+  int32_t slots;            /* concurrent edits (1..16) */
+  int32_t max_crop_res;     /* largest local re-closing, base cells per axis (power of two) */
+  int32_t rmax;             /* radius bound (fine voxels) for edits and field */
+  int32_t mode;             /* gm_mode of the closing */
+  int32_t bilateral_iters;  /* normal filtering of the re-meshed patches */
+} gm_server_opts;
+
+typedef struct {
+  float center[3];     /* brush position (world) */
+  float scale;         /* ScalePoint::scale (world): target radius * fine cell, and the brush core */
+  float support;       /* ScalePoint::support (world) */
+  float global_scale;  /* ScaleField::global_scale, used by GM_BRUSH_ZERO */
+  int32_t mode;        /* gm_brush_mode */
+} gm_edit;
+
+typedef struct {
+  uint64_t ticket;
+  int32_t status;          /* GM_OK, GM_ERR_CAPACITY (crop or radius bound), GM_ERR_CUDA */
+  float latency_ms;        /* submit -> result, host clock */
+  float device_ms;         /* GPU time of the edit */
+  int32_t dirty_lo[3];     /* fine-voxel box whose closing was recomputed */
+  int32_t dirty_hi[3];
+  gm_mesh_view patch;      /* mesh of the re-closed crop (device, valid until its slot is reused) */
+  const uint8_t* patch_keep; /* per triangle: 1 when it lies in the dirty box */
+} gm_edit_result;
+
+/* d_input and d_scale stay owned by the caller and must outlive the server;
+ * the server edits d_scale in place and keeps its own closed grid. */
+gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int8_t* d_scale,
+                           const gm_server_opts* opts, gm_server** out);
+gm_status gm_server_destroy(gm_server* srv);
+gm_status gm_server_submit(gm_server* srv, const gm_edit* edit, uint64_t* ticket);
+/* Advances dispatch and returns up to cap finished edits. */
+gm_status gm_server_poll(gm_server* srv, gm_edit_result* results, int32_t cap, int32_t* count);
+/* Edits queued or on the GPU. */
+int32_t gm_server_pending(gm_server* srv);
+/* The resident closed grid (device, res^3 bytes). */
+const uint8_t* gm_server_closing(gm_server* srv);
+long long gm_server_kernel_launches(gm_server* srv);
+
 /* ---------------------------------------------------------------- a18 */
 /* BVH over the set fine voxels of a packed grid (BVH::BuildFromSEList,
  * GMorpho/BVH.cu:661-739): Morton-ordered leaves, radix tree, bottom-up
