@@ -10,6 +10,11 @@ through the host-buffer C ABI call gm_update + gm_mesh_download (pinned host
 buffers, H2D of the grid and the radius field and D2H of the mesh inside the
 timed region).  Under torchrun every rank closes its own replica (weak
 scaling, no collective on the data path).
+
+Two more objects ride on rank 0's line: ``batch`` (64 uneven grids, edges
+log-uniform in [64, 512], own radius U{1..24}: one batched call against 64
+plain calls) and ``serving`` (resident 2048^3 grid, Poisson 200/s brush
+edits: edits/s and p50/p99 latency).
 """
 import argparse
 import json
@@ -225,7 +230,7 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
     morph_kernels = [k for k in prof if not k.startswith(("k_mc", "k_adj", "k_scan", "k_vertex", "k_bilateral"))]
     morph_ms = sum(prof[k]["ms"] for k in morph_kernels) / args.steps
     mesh_ms = sum(prof[k]["ms"] for k in prof if k not in morph_kernels) / args.steps
-    # survey per-pass algorithmic bytes: dilation V/8 + R + V/8, erosion V/8 + R + V/8
+    # per-pass algorithmic bytes: dilation V/8 + R + V/8, erosion V/8 + R + V/8
     morph_bytes = 2 * (V / 8 + V + V / 8)
     morph_gbs = morph_bytes / (morph_ms * 1e-3) / 1e9 if morph_ms > 0 else None
 
@@ -234,7 +239,7 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8/u16 (integer distance transforms), f32 mesh", "data": "synthetic",
-        "config": {"workload": "config 3: 1024^3 fine grid (res 512), 200-blob solid, variable radius "
+        "config": {"workload": "1024^3 fine grid (res 512), 200-blob solid, variable radius "
                                "r = 2 + floor(30 s(x)), GM_REF sphere closing + contour MC + 20 bilateral",
                    "fine_voxels": V, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (1 GiB radius field + 2 GiB intermediate fields)",
@@ -254,8 +259,126 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
     }
     if rank == 0 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(X, R, res, args.cpu_res)
+    if rank == 0 and not args.no_batch:
+        try:
+            result["batch"] = run_batch(args, ctx)
+        except Exception as exc:  # reported, never hides the headline line
+            result["batch"] = {"error": repr(exc)[:300]}
+    if rank == 0 and not args.no_serve:
+        import torch
+        torch.cuda.empty_cache()
+        try:
+            result["serving"] = run_serve(args)
+        except Exception as exc:
+            result["serving"] = {"error": repr(exc)[:300]}
     ctx.close_ctx()
     return result
+
+
+def run_batch(args, ctx):
+    """Batching workload: 64 uneven grids (fine edge log-uniform in [64, 512],
+    padded to 32, embedded in the next power-of-two cube), own uniform radius
+    U{1..24}: 64 plain gm_close + gm_mesh calls against one batched call."""
+    import torch
+    from broxy_gb300 import api, synth
+    inst = synth.batch_instances(seed=4000, count=64, device="cuda")
+    items = []
+    for it in inst:
+        d = api.make_desc(it["res"], it["data_res"], cell_size=1.0 / it["res"])
+        items.append((d, it["X"].contiguous(), None, it["radius"], torch.empty_like(it["X"])))
+
+    def plain():
+        tris = 0
+        for d, X, R, r, out in items:
+            ctx.close(d, X, R, r, api.L.GM_REF, api.L.GM_SE_SPHERE, out=out)
+            _, _, T = ctx.mesh(d, out, BILATERAL)
+            tris += T.shape[0]
+        return tris
+
+    def batched():
+        ms = ctx.batch_close_mesh(items, bilateral_iters=BILATERAL, lanes=0)
+        return sum(m[2].shape[0] for m in ms)
+
+    def timed(fn, reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            v = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3 / reps, v
+
+    timed(plain, 1)
+    timed(batched, 1)  # first call: autotunes the lane count and captures the graph
+    plain_ms, t_plain = timed(plain, 3)
+    batch_ms, t_batch = timed(batched, 3)
+    assert t_plain == t_batch
+    vox = sum((2 * it["res"]) ** 3 for it in inst)
+    edges = [it["edge"] for it in inst]
+    return {"instances": len(inst), "plain_ms": round(plain_ms, 3), "batched_ms": round(batch_ms, 3),
+            "speedup": round(plain_ms / batch_ms, 3), "lanes": ctx.batch_lanes,
+            "edge_min": min(edges), "edge_max": max(edges), "fine_voxels": int(vox), "triangles": int(t_batch),
+            "radius": "U{1..24}", "closing": "GM_REF sphere, 20 bilateral iterations",
+            "batched_gvoxel_s": round(vox / (batch_ms * 1e-3) / 1e9, 3)}
+
+
+def run_serve(args):
+    """Serving workload: resident 2048^3 grid with base radius 8, Poisson
+    (200/s) brush edits, brush reach U[16,256] fine voxels, new local radius
+    U[1,32]; exact local re-closing + re-mesh of the dirty region."""
+    import torch
+    from broxy_gb300 import api, synth
+    res = args.serve_res
+    dev = torch.device("cuda")
+    X = synth.blob_grid(res, 5000, count=BLOBS, device=dev).contiguous()
+    R = torch.full(((2 * res) ** 3,), 8, dtype=torch.int8, device=dev)
+    desc = api.make_desc(res, cell_size=1.0 / res)
+    t0 = time.perf_counter()
+    srv = api.Server(desc, X, R, slots=args.serve_slots, max_crop_res=min(res, 512), rmax=32, mode=api.L.GM_REF,
+                     bilateral_iters=0)
+    init_ms = (time.perf_counter() - t0) * 1e3
+    rng = np.random.default_rng(5001)
+    n = args.serve_edits
+    arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=n))
+    cs = 0.5 / res
+    edits = []
+    for i in range(n):
+        c = rng.uniform(0.2, 0.8, size=3)
+        reach = float(rng.uniform(16, 256))
+        r_new = int(rng.integers(1, 33))
+        core = min(r_new, reach - 1)
+        scale = r_new * cs
+        support = (core + (reach - core) * np.sqrt(1 - np.sqrt(0.5))) * cs
+        mode = api.L.GM_BRUSH_MAX if r_new >= 8 else api.L.GM_BRUSH_MIN
+        edits.append((c, scale, support, mode))
+    # warm-up edit (first-touch of the slots)
+    srv.submit(edits[0][0], edits[0][1], edits[0][2], 0.0, edits[0][3])
+    srv.drain()
+    launches0 = srv.kernel_launches
+    results = []
+    start = time.perf_counter()
+    i = 0
+    while i < n or srv.pending > 0:
+        now = time.perf_counter() - start
+        while i < n and arrivals[i] <= now:
+            c, scale, support, mode = edits[i]
+            srv.submit(c, scale, support, 0.0, mode)
+            i += 1
+        results += srv.poll()
+    results += srv.poll()
+    wall = time.perf_counter() - start
+    ok = [r for r in results if r["status"] == 0]
+    lat = np.array([r["latency_ms"] for r in ok])
+    dev_ms = np.array([r["device_ms"] for r in ok])
+    out = {"grid": "%d^3 fine" % (2 * res), "edits": n, "completed": len(ok), "rejected": len(results) - len(ok),
+           "arrival_rate_per_s": 200, "edits_per_s": round(len(ok) / wall, 2),
+           "latency_p50_ms": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
+           "latency_p99_ms": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
+           "device_p50_ms": round(float(np.percentile(dev_ms, 50)), 3) if len(lat) else None,
+           "device_p99_ms": round(float(np.percentile(dev_ms, 99)), 3) if len(lat) else None,
+           "slots": args.serve_slots, "initial_closing_ms": round(init_ms, 1),
+           "gpu_launches": srv.kernel_launches - launches0, "target_p99_ms": 16.0}
+    srv.destroy()
+    return out
 
 
 def cpu_crop(X, R, res, sub):
@@ -315,7 +438,7 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.mean(times), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int (CPU)",
             "data": "synthetic",
-            "config": {"workload": "config 3 crop: %d^3 fine voxels of the 1024^3 grid, same radius field" % (2 * sub)},
+            "config": {"workload": "crop: %d^3 fine voxels of the 1024^3 grid, same radius field" % (2 * sub)},
             "cpu_baseline": {"value": round(val, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                              "sample": "centre crop of %d^3 fine voxels per step" % (2 * sub)},
             "e2e": {"value": round(val, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -331,6 +454,11 @@ def main():
     ap.add_argument("--cpu-res", type=int, default=64, help="base cells per axis of the CPU crop")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-grid batching comparison")
+    ap.add_argument("--no-serve", action="store_true", help="skip the edit-server measurement")
+    ap.add_argument("--serve-res", type=int, default=1024, help="base cells of the resident grid (1024 = 2048^3)")
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-edits", type=int, default=200)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

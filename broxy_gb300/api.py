@@ -260,3 +260,70 @@ class BVH:
             self.destroy()
         except Exception:
             pass
+
+
+class Server:
+    """Resident-grid edit server (gm_server_*): brush edits with exact local
+    re-closing and re-meshing, continuous batching over `slots`."""
+
+    def __init__(self, desc, X, R, slots=4, max_crop_res=256, rmax=32, mode=L.GM_REF, bilateral_iters=0):
+        self.lib = L.load()
+        self.desc, self.X, self.R = desc, X, R  # keep the device buffers alive
+        opts = L.ServerOpts(slots, max_crop_res, rmax, mode, bilateral_iters)
+        self.h = C.c_void_p()
+        st = self.lib.gm_server_create(C.byref(desc), _ptr(X), _ptr(R), C.byref(opts), C.byref(self.h))
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_create")
+
+    def submit(self, center, scale, support, global_scale=0.0, mode=L.GM_BRUSH_MAX):
+        e = L.Edit((C.c_float * 3)(*center), float(scale), float(support), float(global_scale), int(mode))
+        t = C.c_uint64(0)
+        st = self.lib.gm_server_submit(self.h, C.byref(e), C.byref(t))
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_submit")
+        return t.value
+
+    def poll(self, cap=256):
+        arr = (L.EditResult * cap)()
+        n = C.c_int32(0)
+        st = self.lib.gm_server_poll(self.h, arr, cap, C.byref(n))
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_poll")
+        out = []
+        for r in arr[:n.value]:
+            out.append(dict(ticket=r.ticket, status=r.status, latency_ms=r.latency_ms, device_ms=r.device_ms,
+                            dirty_lo=tuple(r.dirty_lo), dirty_hi=tuple(r.dirty_hi),
+                            patch_vertices=r.patch.num_vertices, patch_triangles=r.patch.num_triangles,
+                            patch=r.patch, patch_keep=r.patch_keep))
+        return out
+
+    @property
+    def pending(self):
+        return int(self.lib.gm_server_pending(self.h))
+
+    def drain(self):
+        out = []
+        while self.pending > 0:
+            out += self.poll()
+        out += self.poll()
+        return out
+
+    def closing(self):
+        import torch
+        p = self.lib.gm_server_closing(self.h)
+        return torch.as_tensor(DevicePtrArray(p, (self.desc.res ** 3,), "|u1"), device="cuda")
+
+    @property
+    def kernel_launches(self):
+        return int(self.lib.gm_server_kernel_launches(self.h))
+
+    def destroy(self):
+        if self.h:
+            self.lib.gm_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
