@@ -369,12 +369,15 @@ def run_serve(args):
     ok = [r for r in results if r["status"] == 0]
     lat = np.array([r["latency_ms"] for r in ok])
     dev_ms = np.array([r["device_ms"] for r in ok])
+    crops = np.array([r["crop_res"] for r in ok])
     out = {"grid": "%d^3 fine" % (2 * res), "edits": n, "completed": len(ok), "rejected": len(results) - len(ok),
            "arrival_rate_per_s": 200, "edits_per_s": round(len(ok) / wall, 2),
            "latency_p50_ms": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
            "latency_p99_ms": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
            "device_p50_ms": round(float(np.percentile(dev_ms, 50)), 3) if len(lat) else None,
            "device_p99_ms": round(float(np.percentile(dev_ms, 99)), 3) if len(lat) else None,
+           "crop_res_p50": int(np.percentile(crops, 50)) if len(ok) else None,
+           "crop_res_max": int(crops.max()) if len(ok) else None,
            "slots": args.serve_slots, "initial_closing_ms": round(init_ms, 1),
            "gpu_launches": srv.kernel_launches - launches0, "target_p99_ms": 16.0}
     srv.destroy()

@@ -49,8 +49,8 @@ class Edit(C.Structure):
 
 class EditResult(C.Structure):
     _fields_ = [("ticket", C.c_uint64), ("status", C.c_int32), ("latency_ms", C.c_float), ("device_ms", C.c_float),
-                ("dirty_lo", C.c_int32 * 3), ("dirty_hi", C.c_int32 * 3), ("patch", MeshView),
-                ("patch_keep", C.c_void_p)]
+                ("dirty_lo", C.c_int32 * 3), ("dirty_hi", C.c_int32 * 3), ("crop_res", C.c_int32),
+                ("patch", MeshView)]
 
 
 class UpdateOpts(C.Structure):
@@ -93,6 +93,8 @@ PROTOTYPES = {
     "gm_server_pending": (C.c_int32, [_P]),
     "gm_server_closing": (C.c_void_p, [_P]),
     "gm_server_kernel_launches": (C.c_longlong, [_P]),
+    "gm_server_profile": (C.c_int, [_P, C.c_int32]),
+    "gm_server_profile_read": (C.c_int64, [_P, C.c_char_p, C.c_int64]),
     "gm_bvh_build": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.POINTER(_P), C.POINTER(C.c_int64), _P]),
     "gm_bvh_destroy": (C.c_int, [_P]),
     "gm_bvh_query": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int32, _P, _P]),

@@ -267,6 +267,8 @@ class Server:
     re-closing and re-meshing, continuous batching over `slots`."""
 
     def __init__(self, desc, X, R, slots=4, max_crop_res=256, rmax=32, mode=L.GM_REF, bilateral_iters=0):
+        """max_crop_res: largest crop edge in cells (a multiple of 32, or
+        desc.res); an edit needing more is answered with GM_ERR_CAPACITY."""
         self.lib = L.load()
         self.desc, self.X, self.R = desc, X, R  # keep the device buffers alive
         opts = L.ServerOpts(slots, max_crop_res, rmax, mode, bilateral_iters)
@@ -292,9 +294,9 @@ class Server:
         out = []
         for r in arr[:n.value]:
             out.append(dict(ticket=r.ticket, status=r.status, latency_ms=r.latency_ms, device_ms=r.device_ms,
-                            dirty_lo=tuple(r.dirty_lo), dirty_hi=tuple(r.dirty_hi),
+                            dirty_lo=tuple(r.dirty_lo), dirty_hi=tuple(r.dirty_hi), crop_res=r.crop_res,
                             patch_vertices=r.patch.num_vertices, patch_triangles=r.patch.num_triangles,
-                            patch=r.patch, patch_keep=r.patch_keep))
+                            patch=r.patch))
         return out
 
     @property
@@ -316,6 +318,18 @@ class Server:
     @property
     def kernel_launches(self):
         return int(self.lib.gm_server_kernel_launches(self.h))
+
+    def profile(self, enable=True):
+        st = self.lib.gm_server_profile(self.h, 1 if enable else 0)
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_profile")
+
+    def profile_read(self):
+        import json
+        need = self.lib.gm_server_profile_read(self.h, None, 0)
+        buf = C.create_string_buffer(int(need))
+        self.lib.gm_server_profile_read(self.h, buf, need)
+        return json.loads(buf.value.decode())
 
     def destroy(self):
         if self.h:

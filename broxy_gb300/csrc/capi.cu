@@ -59,6 +59,23 @@ void KernelCounter::flush() {
   pending.clear();
 }
 
+int64_t profile_json(KernelCounter& kc, char* buf, int64_t cap) {
+  kc.flush();
+  std::string js = "{";
+  bool first = true;
+  for (const auto& kv : kc.totals) {
+    char tmp[256];
+    snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f}", first ? "" : ", ", kv.first.c_str(),
+             kv.second.first, kv.second.second);
+    js += tmp;
+    first = false;
+  }
+  js += "}";
+  const int64_t need = (int64_t)js.size() + 1;
+  if (buf && cap >= need) memcpy(buf, js.c_str(), (size_t)need);
+  return need;
+}
+
 void KernelCounter::release() {
   flush();
   for (cudaEvent_t e : pool) cudaEventDestroy(e);
@@ -216,20 +233,7 @@ gm_status gm_ctx_profile_reset(gm_ctx* ctx) {
 
 int64_t gm_ctx_profile_read(gm_ctx* ctx, char* buf, int64_t cap) {
   if (!ctx) return -1;
-  ctx->kc.flush();
-  std::string js = "{";
-  bool first = true;
-  for (const auto& kv : ctx->kc.totals) {
-    char tmp[256];
-    snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f}", first ? "" : ", ", kv.first.c_str(),
-             kv.second.first, kv.second.second);
-    js += tmp;
-    first = false;
-  }
-  js += "}";
-  const int64_t need = (int64_t)js.size() + 1;
-  if (buf && cap >= need) memcpy(buf, js.c_str(), (size_t)need);
-  return need;
+  return gm::profile_json(ctx->kc, buf, cap);
 }
 
 // ------------------------------------------------------------------ a2

@@ -33,6 +33,10 @@ struct KernelCounter {
   void release();  // destroys the event pool
 };
 
+// JSON {"name": {"launches": n, "ms": t}, ...} of the counter's totals;
+// returns the bytes needed (with the terminating zero), copies when cap allows
+int64_t profile_json(KernelCounter& kc, char* buf, int64_t cap);
+
 #define GM_LAUNCH(kc, name, st, ...)                               \
   do {                                                             \
     cudaEvent_t gm_ev0_ = nullptr;                                 \
@@ -76,6 +80,17 @@ struct MeshArgs {
   float isovalue;       // 0.95 in the reference (GMorpho.cu:6922)
   int bilateral_iters;  // 20 / 200 / 0
   int num_sms;
+  // Crop window (edit server).  gres == 0: the whole grid.  Otherwise the
+  // grid is a crop whose cell (0,0,0) is global cell `off`, cubes are tagged
+  // only in local cells [tag_lo, tag_hi) (and by the global border rule of
+  // gres), triangles come from local cells [emit_lo, emit_hi) only, and
+  // vertex positions use global fine coordinates with bbox_min the global
+  // grid's.
+  int gres = 0;
+  int off[3] = {0, 0, 0};
+  int tag_lo[3] = {0, 0, 0}, tag_hi[3] = {0, 0, 0};
+  int emit_lo[3] = {0, 0, 0}, emit_hi[3] = {0, 0, 0};
+  int zero_isolated = 0;  // (0,0,0) normal for vertices no triangle uses
 };
 
 // Device-side mesh buffers, grown on demand by the caller of launch_mesh.

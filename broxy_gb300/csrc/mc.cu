@@ -121,10 +121,39 @@ __device__ __forceinline__ bool cell_uniform(const uint8_t* tile, int lx, int ly
   return o == 0u || a == 0xffu;
 }
 
-// mixed-cube mask of a cell; cells outside [1, res-2]^3 are never tagged
-// (TagVoxelsContourMCM, Grid.cu:1334-1340).
-__device__ __forceinline__ int mixed_mask(const int vals[8], int gx, int gy, int gz, int res) {
-  if (gx < 1 || gy < 1 || gz < 1 || gx > res - 2 || gy > res - 2 || gz > res - 2) return 0;
+// Tagging / emission window of one meshing run.  A whole grid is its own
+// window: off = 0, gres = res, tag and emit boxes = [0, res).  The edit
+// server meshes the dirty box of a crop: the crop's cells sit at global
+// cells off + local, the border rule uses the global resolution, cubes are
+// tagged (own vertices) in the dirty box plus one cell on the + side (the
+// neighbour cubes whose edges the box's triangles use), and triangles come
+// from the dirty box only.
+struct McWin {
+  int off[3];
+  int gres;
+  int tlo[3], thi[3];  // local cells whose cubes may be tagged, [lo, hi)
+  int elo[3], ehi[3];  // local cells whose cubes emit triangles, [lo, hi)
+};
+
+// cells outside [1, gres-2]^3 are never tagged (TagVoxelsContourMCM,
+// Grid.cu:1334-1340)
+__device__ __forceinline__ bool win_tag(const McWin& w, int x, int y, int z) {
+  const int gx = x + w.off[0], gy = y + w.off[1], gz = z + w.off[2];
+  return gx >= 1 && gy >= 1 && gz >= 1 && gx <= w.gres - 2 && gy <= w.gres - 2 && gz <= w.gres - 2 &&
+         x >= w.tlo[0] && y >= w.tlo[1] && z >= w.tlo[2] && x < w.thi[0] && y < w.thi[1] && z < w.thi[2];
+}
+__device__ __forceinline__ bool win_emit(const McWin& w, int x, int y, int z) {
+  return x >= w.elo[0] && y >= w.elo[1] && z >= w.elo[2] && x < w.ehi[0] && y < w.ehi[1] && z < w.ehi[2];
+}
+// block-uniform: does the 16^3 brick at (ox, oy, oz) meet the tag box?
+__device__ __forceinline__ bool brick_live(const McWin& w, int ox, int oy, int oz) {
+  return ox < w.thi[0] && oy < w.thi[1] && oz < w.thi[2] && ox + kBrick > w.tlo[0] && oy + kBrick > w.tlo[1] &&
+         oz + kBrick > w.tlo[2];
+}
+
+// mixed-cube mask of a cell (0 when the cell is not tagged)
+__device__ __forceinline__ int mixed_mask(const int vals[8], bool tagged) {
+  if (!tagged) return 0;
   int m = 0;
 #pragma unroll
   for (int s = 0; s < 8; s++) m |= (vals[s] != 0 && vals[s] != 255) ? (1 << s) : 0;
@@ -185,12 +214,12 @@ __device__ __forceinline__ CellCounts block_exclusive_scan(CellCounts v, CellCou
                     wpre[3] + inc[3] - a[3]};
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, int res,
+__global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, int res, McWin w,
                                                           uint32_t* __restrict__ brick_tot) {
   __shared__ uint8_t tile[kTileCells];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  if (!load_tile_mixed(C, res, ox, oy, oz, tile)) {
+  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, res, ox, oy, oz, tile)) {
     if (threadIdx.x < 4) brick_tot[4 * blockIdx.x + threadIdx.x] = 0;
     return;
   }
@@ -202,10 +231,11 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restri
     if (cell_uniform(tile, lx, ly, lz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
+    const int m = mixed_mask(vals, win_tag(w, ox + lx, oy + ly, oz + lz));
     if (!m) continue;
     const CellCounts c = cell_counts(vals, m);
-    acc.cubes += c.cubes; acc.verts += c.verts; acc.tris += c.tris; acc.n91 += c.n91;
+    acc.cubes += c.cubes; acc.verts += c.verts;
+    if (win_emit(w, ox + lx, oy + ly, oz + lz)) { acc.tris += c.tris; acc.n91 += c.n91; }
   }
   CellCounts tot;
   block_exclusive_scan(acc, tot);
@@ -256,7 +286,7 @@ __device__ __forceinline__ float lerp_coord(float p1, float p2, float v1, float 
   return __fadd_rn(p1, __fdiv_rn(__fmul_rn(t, __fsub_rn(p2, p1)), __fsub_rn(v2, v1)));
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, int res,
+__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, int res, McWin w,
                                                              const uint32_t* __restrict__ brick_off,
                                                              uint32_t* __restrict__ cell_voff,
                                                              float* __restrict__ V, float bx, float by, float bz,
@@ -264,7 +294,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
   __shared__ uint8_t tile[kTileCells];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  if (!load_tile_mixed(C, res, ox, oy, oz, tile)) return;
+  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, res, ox, oy, oz, tile)) return;
   CellCounts acc{0, 0, 0, 0};
   for (int i = 0; i < kCellsPerThread; i++) {
     const int l = threadIdx.x * kCellsPerThread + i;
@@ -273,7 +303,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
     if (cell_uniform(tile, lx, ly, lz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, ox + lx, oy + ly, oz + lz, res);
+    const int m = mixed_mask(vals, win_tag(w, ox + lx, oy + ly, oz + lz));
     if (!m) continue;
     const CellCounts c = cell_counts(vals, m);
     acc.verts += c.verts;
@@ -289,14 +319,17 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
     const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    const int m = mixed_mask(vals, gx, gy, gz, res);
+    const int m = mixed_mask(vals, win_tag(w, gx, gy, gz));
     if (!m) continue;
     cell_voff[cell_index(gx, gy, gz, res)] = vo;
     for (int s = 0; s < 8; s++) {
       if (!((m >> s) & 1)) continue;
       const int v = vals[s];
       const int em = edge_mask(v);
-      const int fx = 2 * gx + (s & 1), fy = 2 * gy + ((s >> 1) & 1), fz = 2 * gz + (s >> 2);
+      // corner point from GLOBAL fine coordinates, so that a crop's vertices
+      // are bit-identical to the whole grid's
+      const int fx = 2 * (gx + w.off[0]) + (s & 1), fy = 2 * (gy + w.off[1]) + ((s >> 1) & 1),
+                fz = 2 * (gz + w.off[2]) + (s >> 2);
       const float px = __fmaf_rn((float)fx, cs, bx);
       const float py = __fmaf_rn((float)fy, cs, by);
       const float pz = __fmaf_rn((float)fz, cs, bz);
@@ -330,12 +363,11 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
 
 // Per-cell summary used for neighbour lookups: bits 0..7 = mixed cubes,
 // bits 8+k / 16+k / 24+k = cube k owns a vertex on edge 0 / 3 / 8.
-__device__ __forceinline__ uint32_t cell_info(const uint8_t* tile, int lx, int ly, int lz, int gx, int gy, int gz,
-                                              int res) {
-  if (cell_uniform(tile, lx, ly, lz)) return 0u;
+__device__ __forceinline__ uint32_t cell_info(const uint8_t* tile, int lx, int ly, int lz, bool tagged) {
+  if (!tagged || cell_uniform(tile, lx, ly, lz)) return 0u;
   int vals[8];
   cube_values(tile, lx, ly, lz, vals);
-  const int m = mixed_mask(vals, gx, gy, gz, res);
+  const int m = mixed_mask(vals, true);
   uint32_t info = (uint32_t)m;
 #pragma unroll
   for (int s = 0; s < 8; s++) {
@@ -362,7 +394,7 @@ __device__ __forceinline__ long long cube_voff(uint32_t info, uint32_t cell_off,
   return (long long)off;
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __restrict__ C, int res,
+__global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __restrict__ C, int res, McWin w,
                                                               const uint32_t* __restrict__ brick_off,
                                                               const uint32_t* __restrict__ cell_voff,
                                                               uint32_t* __restrict__ T, uint32_t nt_total,
@@ -371,10 +403,10 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
   __shared__ uint32_t info[kInfoE * kInfoE * kInfoE];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  if (!load_tile_mixed(C, res, ox, oy, oz, tile)) return;
+  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, res, ox, oy, oz, tile)) return;
   for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) {
     const int lx = i % kInfoE, ly = (i / kInfoE) % kInfoE, lz = i / (kInfoE * kInfoE);
-    info[i] = cell_info(tile, lx, ly, lz, ox + lx, oy + ly, oz + lz, res);
+    info[i] = cell_info(tile, lx, ly, lz, win_tag(w, ox + lx, oy + ly, oz + lz));
   }
   __syncthreads();
   CellCounts acc{0, 0, 0, 0};
@@ -383,6 +415,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
     int lx, ly, lz;
     local_coords(l, lx, ly, lz);
     if (!(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu)) continue;
+    if (!win_emit(w, ox + lx, oy + ly, oz + lz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
     acc.tris += cell_counts(vals, (int)(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu)).tris;
@@ -398,6 +431,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
     const int m = (int)(myinfo & 0xffu);
     if (!m) continue;
     const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    if (!win_emit(w, gx, gy, gz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
     uint32_t vo = cell_voff[cell_index(gx, gy, gz, res)];
@@ -405,7 +439,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
       if (!((m >> s) & 1)) continue;
       const int v = vals[s];
       const int em = edge_mask(v);
-      const int fx = 2 * gx + (s & 1), fy = 2 * gy + ((s >> 1) & 1), fz = 2 * gz + (s >> 2);
+      const int fx = 2 * gx + (s & 1), fy = 2 * gy + ((s >> 1) & 1), fz = 2 * gz + (s >> 2);  // local
       uint32_t vert[12];
 #pragma unroll
       for (int e = 0; e < 12; e++) vert[e] = 0;
@@ -496,9 +530,72 @@ __global__ void k_mc_fix91(const uint32_t* __restrict__ fix, int fix_cap, uint32
 
 // ------------------------------------------------------------------ normals
 
+// Vertex -> corner lists.  Corners of a vertex are listed in corner order
+// (the reference's per-vertex accumulation order).  Vertex 0 is special: the
+// reference's triangles take index 0 for an edge whose owning cube is not
+// tagged (cubes of border cells), so on grids whose surface reaches the
+// border vertex 0 collects an unbounded number of corners.  Its row is
+// built by an order-preserving compaction over all corners (linear), the
+// other rows (at most 20 corners each) by atomics and an in-row sort.
 __global__ void k_adj_count(const uint32_t* __restrict__ T, int64_t nt, uint32_t* __restrict__ cnt) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nt; i += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(cnt + T[i], 1u);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nt; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = T[i];
+    if (v != 0u) atomicAdd(cnt + v, 1u);
+  }
+}
+
+constexpr int kRow0Chunk = 2048;  // corners per block (256 threads x 8)
+
+// corners of vertex 0 per chunk of kRow0Chunk corners
+__global__ void __launch_bounds__(256) k_row0_count(const uint32_t* __restrict__ T, int64_t n,
+                                                     uint32_t* __restrict__ counts) {
+  __shared__ uint32_t ws[8];
+  const int64_t base = (int64_t)blockIdx.x * kRow0Chunk;
+  uint32_t c = 0;
+  for (int i = threadIdx.x; i < kRow0Chunk; i += 256)
+    if (base + i < n) c += T[base + i] == 0u;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; w++) t += ws[w];
+    counts[blockIdx.x] = t;
+  }
+}
+
+// the count of vertex 0 (total of the scanned chunk counts) into cnt[0]
+__global__ void k_row0_total(const uint32_t* __restrict__ offs, int nchunks, uint32_t* __restrict__ cnt) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cnt[0] = offs[nchunks];
+}
+
+// row 0 in corner order: chunk offset + rank inside the chunk
+__global__ void __launch_bounds__(256) k_row0_fill(const uint32_t* __restrict__ T, int64_t n,
+                                                    const uint32_t* __restrict__ offs,
+                                                    const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj) {
+  __shared__ uint32_t wtot[8];
+  const int64_t base = (int64_t)blockIdx.x * kRow0Chunk + (int64_t)threadIdx.x * 8;
+  uint32_t f = 0, s = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const bool z = base + j < n && T[base + j] == 0u;
+    f |= (z ? 1u : 0u) << j;
+    s += z ? 1u : 0u;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
+  }
+  if (lane == 31) wtot[wid] = x;
+  __syncthreads();
+  uint32_t pos = rowptr[0] + offs[blockIdx.x] + x - s;
+  for (int w = 0; w < wid; w++) pos += wtot[w];
+#pragma unroll
+  for (int j = 0; j < 8; j++)
+    if ((f >> j) & 1u) adj[pos++] = (uint32_t)(base + j);
 }
 
 // Exclusive scan of n u32 into out[0..n] in three kernels: per-block sums of
@@ -580,13 +677,14 @@ __global__ void k_adj_fill(const uint32_t* __restrict__ T, int64_t nt, const uin
                            uint32_t* __restrict__ cursor, uint32_t* __restrict__ adj) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * nt; i += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t v = T[i];
+    if (v == 0u) continue;  // row 0: k_row0_fill
     const uint32_t slot = atomicAdd(cursor + v, 1u);
     adj[rowptr[v] + slot] = (uint32_t)i;  // corner id = 3 t + role
   }
 }
 
 __global__ void k_adj_sort(const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj, int64_t nv) {
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t v = 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t b = rowptr[v], e = rowptr[v + 1];
     for (uint32_t i = b + 1; i < e; i++) {
       const uint32_t key = adj[i];
@@ -610,8 +708,13 @@ __device__ __forceinline__ float3 normalize3(float3 n) {
 // vertex in triangle order, then normalised (GMorpho.cu:6526-6537).
 __global__ void k_vertex_normals(const float* __restrict__ V, const uint32_t* __restrict__ T,
                                  const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
-                                 float4* __restrict__ N4, float* __restrict__ N3) {
+                                 int zero_isolated, float4* __restrict__ N4, float* __restrict__ N3) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    if (zero_isolated && rowptr[v] == rowptr[v + 1]) {
+      N4[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
+      continue;
+    }
     float3 acc = make_float3(0.f, 0.f, 0.f);
     for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
       const uint32_t t = adj[i] / 3;
@@ -663,8 +766,13 @@ __device__ __forceinline__ float dist2n(float4 a, float4 b) {
 // accumulated per vertex in triangle order.
 __global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __restrict__ rowptr,
                             const uint2* __restrict__ nbr, const float2* __restrict__ wpos, int64_t nv, float sn2,
-                            float4* __restrict__ Nout, float* __restrict__ N3) {
+                            int zero_isolated, float4* __restrict__ Nout, float* __restrict__ N3) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    if (zero_isolated && rowptr[v] == rowptr[v + 1]) {
+      Nout[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
+      continue;
+    }
     float3 acc = make_float3(0.f, 0.f, 0.f);
     const float4 na = Nin[v];
     for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
@@ -699,11 +807,35 @@ void MeshBuffers::release() {
   *this = MeshBuffers();
 }
 
+// Bricks are visited in Morton order over the smallest power-of-two cube of
+// bricks covering the grid; bricks outside the grid or the tag box return
+// at once.
+static int brick_count(int res) {
+  int p = kBrick;
+  while (p < res) p *= 2;
+  const int e = p / kBrick;
+  return e * e * e;
+}
+
+static McWin window_of(const MeshArgs& a) {
+  McWin w;
+  const bool crop = a.gres > 0;
+  w.gres = crop ? a.gres : a.res;
+  for (int k = 0; k < 3; k++) {
+    w.off[k] = crop ? a.off[k] : 0;
+    w.tlo[k] = crop ? a.tag_lo[k] : 0;
+    w.thi[k] = crop ? a.tag_hi[k] : a.res;
+    w.elo[k] = crop ? a.emit_lo[k] : 0;
+    w.ehi[k] = crop ? a.emit_hi[k] : a.res;
+  }
+  return w;
+}
+
 cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
                               uint32_t* h_tot4) {
   const int res = a.res;
   const int64_t cells = (int64_t)res * res * res;
-  const int nb = (int)(cells / kCellsPerBrick);
+  const int nb = brick_count(res);
   cudaError_t e;
   if (nb + 1 > b.bricks_cap) {
     if (b.brick_tot) cudaFree(b.brick_tot);
@@ -719,7 +851,7 @@ cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st
     if (e != cudaSuccess) return e;
     b.cells_cap = cells;
   }
-  GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, res, b.brick_tot));
+  GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, res, window_of(a), b.brick_tot));
   GM_LAUNCH(kc, "k_scan_bricks", st, k_scan_bricks<<<1, 1024, 0, st>>>(b.brick_tot, nb));
   return cudaMemcpyAsync(h_tot4, b.brick_tot + 4 * (size_t)nb, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
 }
@@ -754,7 +886,8 @@ cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, Kerne
 cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt, cudaStream_t st,
                       KernelCounter* kc) {
   const int res = a.res;
-  const int nb = (int)((int64_t)res * res * res / kCellsPerBrick);
+  const int nb = brick_count(res);
+  const McWin w = window_of(a);
   cudaError_t e;
   // per-vertex buffers share one capacity, per-triangle buffers another
   if (b.v_cap < nv || b.V == nullptr) {
@@ -787,30 +920,37 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   }
   const float cs = 0.5f * a.cell_size;  // exact: scaling by a power of two
   cudaMemsetAsync(b.fix, 0, sizeof(uint32_t), st);
-  GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, res, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],
+  GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, res, w, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],
                                            a.bbox_min[2], cs, a.isovalue));
-  GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, 0, st>>>(a.C, res, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
+  GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, 0, st>>>(a.C, res, w, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
                                             b.fix_cap));
   GM_LAUNCH(kc, "k_mc_fix91", st, k_mc_fix91<<<1, 256, 0, st>>>(b.fix, b.fix_cap, b.T));
   if (nv == 0 || nt == 0) return cudaGetLastError();
   // normals
   const int sms = a.num_sms;
+  const int nchunks = (int)((nv + kScanChunk - 1) / kScanChunk);
+  const int nchunks0 = (int)((3 * nt + kRow0Chunk - 1) / kRow0Chunk);
+  // chunk sums (rows, then row 0) go to the per-cell offsets buffer, unused
+  // once the triangles are out
+  if ((int64_t)nchunks + nchunks0 + 2 > b.cells_cap) return cudaErrorInvalidValue;
+  uint32_t* sums = b.cell_voff;
+  uint32_t* offs0 = b.cell_voff + nchunks + 1;
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
   GM_LAUNCH(kc, "k_adj_count", st, k_adj_count<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.cursor));
-  {
-    const int nchunks = (int)((nv + kScanChunk - 1) / kScanChunk);
-    // chunk sums go to the per-cell offsets buffer, unused once triangles are out
-    uint32_t* sums = b.cell_voff;
-    GM_LAUNCH(kc, "k_scan_sums", st, k_scan_sums<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums));
-    GM_LAUNCH(kc, "k_scan_small", st, k_scan_small<<<1, 1024, 0, st>>>(sums, nchunks));
-    GM_LAUNCH(kc, "k_scan_apply", st, k_scan_apply<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums, b.rowptr));
-  }
+  GM_LAUNCH(kc, "k_row0_count", st, k_row0_count<<<nchunks0, 256, 0, st>>>(b.T, 3 * nt, offs0));
+  GM_LAUNCH(kc, "k_scan_small", st, k_scan_small<<<1, 1024, 0, st>>>(offs0, nchunks0));
+  GM_LAUNCH(kc, "k_row0_total", st, k_row0_total<<<1, 32, 0, st>>>(offs0, nchunks0, b.cursor));
+  GM_LAUNCH(kc, "k_scan_sums", st, k_scan_sums<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums));
+  GM_LAUNCH(kc, "k_scan_small", st, k_scan_small<<<1, 1024, 0, st>>>(sums, nchunks));
+  GM_LAUNCH(kc, "k_scan_apply", st, k_scan_apply<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums, b.rowptr));
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
   GM_LAUNCH(kc, "k_adj_fill", st, k_adj_fill<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.rowptr, b.cursor, b.adj));
+  GM_LAUNCH(kc, "k_row0_fill", st, k_row0_fill<<<nchunks0, 256, 0, st>>>(b.T, 3 * nt, offs0, b.rowptr, b.adj));
   GM_LAUNCH(kc, "k_adj_sort", st, k_adj_sort<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.rowptr, b.adj, nv));
   const int iters = a.bilateral_iters;
+  const int zi = a.zero_isolated;
   GM_LAUNCH(kc, "k_vertex_normals", st,
-            k_vertex_normals<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, b.N4a,
+            k_vertex_normals<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, zi, b.N4a,
                                                                       iters == 0 ? b.N : nullptr));
   if (iters > 0) {
     GM_LAUNCH(kc, "k_adj_prep", st,
@@ -821,7 +961,7 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   for (int it = 0; it < iters; it++) {
     const float sn = it < 2 ? 1e10f : 0.2f;  // GMorpho.cu:6959-6969
     GM_LAUNCH(kc, "k_bilateral", st,
-              k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.rowptr, b.nbr, b.wpos, nv, sn * sn, nout,
+              k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.rowptr, b.nbr, b.wpos, nv, sn * sn, zi, nout,
                                                                    it == iters - 1 ? b.N : nullptr));
     float4* t = nin; nin = nout; nout = t;
   }

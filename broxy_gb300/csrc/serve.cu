@@ -6,13 +6,14 @@
 // (BroxyViewer.cpp:667-672).
 //
 // Exactness of the local re-closing.  The closing at a fine voxel depends on
-// the input grid and radii within (rmax+1) (dilation reach) + (rmax-1)
-// (erosion reach) fine voxels plus a few cells of contour tagging.  An edit
-// that changes radii inside box B can therefore only change the closing
-// inside A = B grown by M, and the closing on A is computed exactly from a
-// crop holding A grown by M again, M = 2 rmax + 8 fine voxels (cell
-// aligned).  Crops touching the grid border are aligned to it, so the
-// border rules of the reference ([1, res-2] cells, data_res) act the same.
+// the input grid and the radii within a bounded reach (dilation r+1, erosion
+// r-1, a few cells of block, contour and refinement rules), so an edit can
+// change it only in a box around its brush, and a crop holding that box
+// with a margin is exact on it.  plan_edit derives both margins from a host
+// map of the largest radius per 8-cell brick, so that they follow the radii
+// around each edit rather than the server's global bound.  Crops touching
+// the grid border are aligned to it, so the border rules of the reference
+// ([1, res-2] cells, data_res) act the same.
 //
 // Continuous batching: each slot owns a stream, crop buffers and a mesh
 // buffer.  Queued edits are dispatched in arrival order as slots free up; an
@@ -31,51 +32,43 @@
 
 namespace gm {
 
-// crop of the packed grid (cells) and of the radius field (fine voxels);
-// outside the source grid: empty cells, radius 0
-__global__ void k_crop(const uint8_t* __restrict__ X, const int8_t* __restrict__ R, int res, int cx0, int cy0,
-                       int cz0, int cres, uint8_t* __restrict__ Xc, int8_t* __restrict__ Rc) {
-  const int64_t cells = (int64_t)cres * cres * cres;
-  const int N = 2 * res, cN = 2 * cres;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cells; i += (int64_t)gridDim.x * blockDim.x) {
-    const int x = (int)(i % cres), y = (int)((i / cres) % cres), z = (int)(i / ((int64_t)cres * cres));
-    const int gx = cx0 + x, gy = cy0 + y, gz = cz0 + z;
-    const bool in = gx >= 0 && gy >= 0 && gz >= 0 && gx < res && gy < res && gz < res;
-    Xc[i] = in ? X[cell_index(gx, gy, gz, res)] : (uint8_t)0;
-    for (int k = 0; k < 8; k++) {
-      const int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
-      Rc[fine_index(fx, fy, fz, cN)] = in ? R[fine_index(2 * gx + (k & 1), 2 * gy + ((k >> 1) & 1), 2 * gz + (k >> 2), N)]
-                                          : (int8_t)0;
-    }
-  }
+// Copy of the box [s, s + e) of a cubic byte volume of edge sn into the box
+// [d, d + e) of a cubic volume of edge dn (the crops of the packed grid and
+// of the radius field, and the write-back of the dirty box).  One block per
+// row; the boxes lie inside both volumes by construction.
+__global__ void k_box_copy(const uint8_t* __restrict__ src, int sn, int sx, int sy, int sz, uint8_t* __restrict__ dst,
+                           int dn, int dx, int dy, int dz, int ex) {
+  const int y = blockIdx.x, z = blockIdx.y;
+  const uint8_t* s = src + cell_index(sx, sy + y, sz + z, sn);
+  uint8_t* d = dst + cell_index(dx, dy + y, dz + z, dn);
+  for (int x = threadIdx.x; x < ex; x += blockDim.x) d[x] = s[x];
 }
 
-// write the crop's closing back on the dirty box of cells [lo, hi)
-__global__ void k_writeback(const uint8_t* __restrict__ Cc, int cres, int cx0, int cy0, int cz0, uint8_t* __restrict__ C,
-                            int res, int lx, int ly, int lz, int hx, int hy, int hz) {
-  const int wx = hx - lx, wy = hy - ly, wz = hz - lz;
-  const int64_t total = (int64_t)wx * wy * wz;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int x = lx + (int)(i % wx), y = ly + (int)((i / wx) % wy), z = lz + (int)(i / ((int64_t)wx * wy));
-    C[cell_index(x, y, z, res)] = Cc[cell_index(x - cx0, y - cy0, z - cz0, cres)];
+// Largest radius of each 8-cell brick (16^3 fine voxels) of the radius
+// field: one block per brick, one 16-byte row segment per thread.
+constexpr int kRBrick = 8;  // cells per radius-map brick edge
+__global__ void __launch_bounds__(256) k_brick_rmax(const int8_t* __restrict__ R, int n, int nb,
+                                                     uint8_t* __restrict__ out) {
+  const int b = blockIdx.x;
+  const int bx = b % nb, by = (b / nb) % nb, bz = b / (nb * nb);
+  const int fy = 2 * kRBrick * by + (threadIdx.x & 15), fz = 2 * kRBrick * bz + (threadIdx.x >> 4);
+  int m = 0;
+  if (fy < n && fz < n && 2 * kRBrick * bx < n) {
+    const uint4 v = *reinterpret_cast<const uint4*>(R + fine_index(2 * kRBrick * bx, fy, fz, n));
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) m = max(m, (int)(int8_t)((w[k] >> (8 * j)) & 0xffu));
   }
-}
-
-// 1 for the triangles of the crop mesh whose centroid lies in the dirty box
-// (fine-voxel units relative to the crop origin): the patch of this edit
-__global__ void k_patch_mask(const float* __restrict__ V, const uint32_t* __restrict__ T, int64_t nt, float ox,
-                             float oy, float oz, float inv_cs, float lx, float ly, float lz, float hx, float hy,
-                             float hz, uint8_t* __restrict__ keep) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
-    float c[3] = {0.f, 0.f, 0.f};
-    for (int j = 0; j < 3; j++) {
-      const uint32_t v = T[3 * t + j];
-      c[0] += V[3 * (size_t)v];
-      c[1] += V[3 * (size_t)v + 1];
-      c[2] += V[3 * (size_t)v + 2];
-    }
-    const float x = (c[0] / 3.f - ox) * inv_cs, y = (c[1] / 3.f - oy) * inv_cs, z = (c[2] / 3.f - oz) * inv_cs;
-    keep[t] = (x >= lx && x < hx && y >= ly && y < hy && z >= lz && z < hz) ? 1 : 0;
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ int wm[8];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int k = 0; k < 8; k++) t = max(t, wm[k]);
+    out[b] = (uint8_t)t;
   }
 }
 
@@ -94,9 +87,8 @@ struct Slot {
   uint32_t* h_tot = nullptr;  // pinned: the crop mesh's four totals
   int phase = 0;              // 0 idle, 1 closing + counting, 2 emitting
   MeshArgs ma;
-  uint8_t *Xc = nullptr, *Cc = nullptr, *ws = nullptr, *keep = nullptr;
+  uint8_t *Xc = nullptr, *Cc = nullptr, *ws = nullptr;
   int8_t* Rc = nullptr;
-  size_t keep_cap = 0;
   MeshBuffers mesh;
   bool busy = false;
   uint64_t ticket = 0;
@@ -124,6 +116,11 @@ struct Server {
   int mode = 0;
   int rmax = 2;
   int max_cres = 0;
+  // host map of an upper bound of the radius in each 8-cell brick: exact at
+  // creation, raised at each dispatched brush (MAX and ZERO brushes can
+  // raise radii up to their target, MIN brushes only lower them)
+  std::vector<uint8_t> rmap;
+  int rnb = 0;  // bricks per axis
   int bilateral = 0;
   std::vector<Slot> slots;
   std::deque<Pending> queue;
@@ -136,46 +133,154 @@ static double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-static int margin_cells(int rmax) { return (2 * rmax + 8 + 1) / 2 + 1; }
+struct Plan {
+  Box3 dirty, crop;
+  int cres;
+  int rclose;  // radius bound of the crop's closing
+};
 
-// dirty box and crop of an edit; false when it needs a crop above max_cres
-static bool plan_edit(const Server& s, const gm_edit& e, Box3& dirty, Box3& crop, int& cres) {
-  const int res = s.desc.res;
-  const float cs_f = 0.5f * s.desc.cell_size;  // fine voxel size (scale-field cell)
+// largest mapped radius over the bricks meeting the cell box [lo, hi), or
+// over those of it that do not meet the box `ex` (when given)
+static int map_max(const Server& s, const int lo[3], const int hi[3], const Box3* ex) {
+  int b0[3], b1[3], e0[3] = {0, 0, 0}, e1[3] = {-1, -1, -1};
+  for (int a = 0; a < 3; a++) {
+    const int l = lo[a] < 0 ? 0 : lo[a], h = hi[a] > s.desc.res ? s.desc.res : hi[a];
+    if (l >= h) return 2;
+    b0[a] = l / kRBrick;
+    b1[a] = (h - 1) / kRBrick;
+    if (ex) {
+      e0[a] = (ex->lo[a] < 0 ? 0 : ex->lo[a]) / kRBrick;
+      e1[a] = ((ex->hi[a] > s.desc.res ? s.desc.res : ex->hi[a]) - 1) / kRBrick;
+    }
+  }
+  int m = 2;
+  for (int z = b0[2]; z <= b1[2]; z++)
+    for (int y = b0[1]; y <= b1[1]; y++) {
+      const uint8_t* row = &s.rmap[((size_t)z * s.rnb + y) * s.rnb];
+      const bool in_yz = ex && z >= e0[2] && z <= e1[2] && y >= e0[1] && y <= e1[1];
+      for (int x = b0[0]; x <= b1[0]; x++) {
+        if (in_yz && x >= e0[0] && x <= e1[0]) continue;
+        m = row[x] > m ? row[x] : m;
+      }
+    }
+  return m;
+}
+
+// radius an edit's brush can write (upper bound), or 0 when it only lowers
+static int brush_raise(const Server& s, const gm_edit& e) {
+  if (e.mode == GM_BRUSH_MIN) return 0;
+  const float cs_f = 0.5f * s.desc.cell_size;
+  const float t = (e.mode == GM_BRUSH_ZERO ? e.global_scale : e.scale) / cs_f;
+  const float c = ceilf(t);
+  return c > 127.f ? 127 : (c < 0.f ? 0 : (int)c);
+}
+
+// fine-voxel box the brush kernel may change (same bounds as the kernel)
+static void brush_box(const Server& s, const gm_edit& e, int lo[3], int hi[3]) {
+  const float cs_f = 0.5f * s.desc.cell_size;
   const float v = e.scale;
   const float h = (e.support - v) / sqrtf(1.f - sqrtf(0.5f));
   const float reach = v + h;
-  const int M = margin_cells(s.rmax);
+  for (int a = 0; a < 3; a++) {
+    lo[a] = (int)floorf((e.center[a] - reach - s.desc.bbox_min[a]) / cs_f) - 1;
+    hi[a] = (int)ceilf((e.center[a] + reach - s.desc.bbox_min[a]) / cs_f) + 1;
+  }
+}
+
+// Exact local re-closing plan of an edit (fine-voxel distances; r_in bounds
+// the radii, old and new, in the brush cells B grown by 2, r_out those of
+// the bricks around it that do not meet B + 2):
+//  * the closing can change only in dirty = B + Md, Md = (r_in + 2)/2 + 4
+//    cells (one block cell, one contour cell, erosion reach, refinement),
+//    and at least 9 so that bricks meeting B + 2 lie inside it;
+//  * a crop is exact on the cells at least Mc from its open sides,
+//    Mc = max(r_out + 8, (max(r_in, r_out) + 6)/2 + 1): wrong dilations next
+//    to an open side reach (r_out + 3)/2 + 2 cells in, the contour one more,
+//    erosion and refinement (r_out - 1)/2 + 2 more, and no dilation inside
+//    the dirty box reaches an open side;
+//  * two more cells for the mesh of the dirty box (cube corners one cell
+//    past it, cubes of one more cell tagged).
+// Crops are cubes whose edge is a multiple of 32 cells (or the whole grid).
+static bool plan_edit(const Server& s, const gm_edit& e, Plan& p) {
+  const int res = s.desc.res;
+  int flo[3], fhi[3];
+  brush_box(s, e, flo, fhi);
+  Box3 B;
+  for (int a = 0; a < 3; a++) {
+    B.lo[a] = (flo[a] >= 0 ? flo[a] / 2 : -((-flo[a] + 1) / 2)) - 1;  // floor(flo/2) - 1
+    B.hi[a] = (fhi[a] >= 0 ? fhi[a] / 2 : -((-fhi[a] + 1) / 2)) + 2;  // floor(fhi/2) + 2
+  }
+  Box3 B2 = B;
+  for (int a = 0; a < 3; a++) { B2.lo[a] -= 2; B2.hi[a] += 2; }
+  int r_in = map_max(s, B2.lo, B2.hi, nullptr);
+  const int raise = brush_raise(s, e);
+  r_in = raise > r_in ? raise : r_in;
+  int Md = (r_in + 2) / 2 + 4;
+  Md = Md < 9 ? 9 : Md;
+  const int Mc0 = s.rmax + 10;
+  int rlo[3], rhi[3];
+  for (int a = 0; a < 3; a++) { rlo[a] = B.lo[a] - Md - Mc0; rhi[a] = B.hi[a] + Md + Mc0; }
+  const int r_out = map_max(s, rlo, rhi, &B2);
+  const int rc = r_in > r_out ? r_in : r_out;
+  int Mc = (rc + 6) / 2 + 1;
+  Mc = r_out + 8 > Mc ? r_out + 8 : Mc;
+  Mc += 2;
   int span = 0;
   for (int a = 0; a < 3; a++) {
-    const float lo = (e.center[a] - reach - s.desc.bbox_min[a]) / cs_f;
-    const float hi = (e.center[a] + reach - s.desc.bbox_min[a]) / cs_f;
-    int blo = (int)floorf(lo) / 2 - 1, bhi = (int)ceilf(hi) / 2 + 2;  // brush box in cells
-    dirty.lo[a] = blo - M < 0 ? 0 : blo - M;
-    dirty.hi[a] = bhi + M > res ? res : bhi + M;
-    if (dirty.lo[a] >= dirty.hi[a]) { dirty.lo[a] = 0; dirty.hi[a] = 0; }
-    const int need = dirty.hi[a] - dirty.lo[a] + 2 * M;
+    int lo = B.lo[a] - Md, hi = B.hi[a] + Md;
+    lo = lo < 0 ? 0 : lo;
+    hi = hi > res ? res : hi;
+    if (lo >= hi) { lo = 0; hi = 0; }
+    p.dirty.lo[a] = lo;
+    p.dirty.hi[a] = hi;
+    const int need = hi - lo + 2 * Mc;
     span = need > span ? need : span;
   }
-  cres = 16;
-  while (cres < span) cres *= 2;
-  if (cres > res) cres = res;
+  int cres = (span + 31) / 32 * 32;
+  if (cres >= res) cres = res;
   if (cres > s.max_cres) return false;
   for (int a = 0; a < 3; a++) {
-    int c0 = dirty.lo[a] - M;
-    const int room = cres - (dirty.hi[a] - dirty.lo[a]);
-    c0 = dirty.lo[a] - room / 2;  // centre the dirty box in the crop
+    const int room = cres - (p.dirty.hi[a] - p.dirty.lo[a]);
+    int c0 = p.dirty.lo[a] - room / 2;  // centre the dirty box in the crop
     if (c0 < 0) c0 = 0;
     if (c0 + cres > res) c0 = res - cres;
-    crop.lo[a] = c0;
-    crop.hi[a] = c0 + cres;
+    p.crop.lo[a] = c0;
+    p.crop.hi[a] = c0 + cres;
   }
+  p.cres = cres;
+  p.rclose = cres == res ? s.rmax : (rc > s.rmax ? s.rmax : rc);
   return true;
 }
 
-static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Box3& dirty, const Box3& crop, int cres) {
+// raise the radius map over the bricks the brush can change
+static void map_raise(Server& s, const gm_edit& e) {
+  const int raise = brush_raise(s, e);
+  if (raise == 0) return;
+  int flo[3], fhi[3], b0[3], b1[3];
+  brush_box(s, e, flo, fhi);
+  const int n = 2 * s.desc.res;
+  for (int a = 0; a < 3; a++) {
+    const int l = flo[a] < 0 ? 0 : flo[a], h = fhi[a] > n - 1 ? n - 1 : fhi[a];
+    if (l > h) return;
+    b0[a] = l / (2 * kRBrick);
+    b1[a] = h / (2 * kRBrick);
+  }
+  for (int z = b0[2]; z <= b1[2]; z++)
+    for (int y = b0[1]; y <= b1[1]; y++)
+      for (int x = b0[0]; x <= b1[0]; x++) {
+        uint8_t& v = s.rmap[((size_t)z * s.rnb + y) * s.rnb + x];
+        v = raise > v ? (uint8_t)raise : v;
+      }
+}
+
+static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& pl) {
   const gm_edit& e = p.edit;
+  const int res = s.desc.res;
+  const Box3& dirty = pl.dirty;
+  const Box3& crop = pl.crop;
+  const int cres = pl.cres;
   cudaError_t err;
+  map_raise(s, e);
   sl.busy = true;
   sl.ticket = p.ticket;
   sl.crop = crop;
@@ -186,16 +291,18 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Box3& d
   cudaEventRecord(sl.t0, sl.st);
   // 1. brush the resident radius field (bounded box kernel)
   const float bmin[3] = {s.desc.bbox_min[0], s.desc.bbox_min[1], s.desc.bbox_min[2]};
-  if ((err = launch_scale_brush(s.R, 2 * s.desc.res, bmin, 0.5f * s.desc.cell_size, e.center, e.scale, e.support,
+  if ((err = launch_scale_brush(s.R, 2 * res, bmin, 0.5f * s.desc.cell_size, e.center, e.scale, e.support,
                                 e.global_scale, e.mode, sl.st, s.kc)) != cudaSuccess)
     return err;
-  // 2. crop, 3. close the crop
-  const int64_t ccells = (int64_t)cres * cres * cres;
-  int blocks = (int)((ccells + 255) / 256);
-  if (blocks > s.sms * 32) blocks = s.sms * 32;
-  GM_LAUNCH(s.kc, "k_crop", sl.st,
-            k_crop<<<blocks, 256, 0, sl.st>>>(s.X, s.R, s.desc.res, crop.lo[0], crop.lo[1], crop.lo[2], cres, sl.Xc,
-                                              sl.Rc));
+  // 2. crop the packed grid and the radius field
+  GM_LAUNCH(s.kc, "k_box_copy", sl.st,
+            k_box_copy<<<dim3(cres, cres), 128, 0, sl.st>>>(s.X, res, crop.lo[0], crop.lo[1], crop.lo[2], sl.Xc, cres,
+                                                            0, 0, 0, cres));
+  GM_LAUNCH(s.kc, "k_box_copy", sl.st,
+            k_box_copy<<<dim3(2 * cres, 2 * cres), 256, 0, sl.st>>>(
+                reinterpret_cast<const uint8_t*>(s.R), 2 * res, 2 * crop.lo[0], 2 * crop.lo[1], 2 * crop.lo[2],
+                reinterpret_cast<uint8_t*>(sl.Rc), 2 * cres, 0, 0, 0, 2 * cres));
+  // 3. close the crop
   CloseArgs a;
   a.res = cres;
   for (int k = 0; k < 3; k++) {
@@ -205,7 +312,7 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Box3& d
   a.X = sl.Xc;
   a.R = sl.Rc;
   a.uniform_r = 0;
-  a.rmax = s.rmax;
+  a.rmax = pl.rclose;
   a.mode = s.mode;
   a.se = 0;
   a.C_out = sl.Cc;
@@ -215,24 +322,30 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Box3& d
   a.num_sms = s.sms;
   if ((err = launch_close(a, sl.st, s.kc)) != cudaSuccess) return err;
   // 4. write back the dirty box
-  const int64_t dcells = (int64_t)(dirty.hi[0] - dirty.lo[0]) * (dirty.hi[1] - dirty.lo[1]) * (dirty.hi[2] - dirty.lo[2]);
-  if (dcells > 0) {
-    int b2 = (int)((dcells + 255) / 256);
-    if (b2 > s.sms * 32) b2 = s.sms * 32;
-    GM_LAUNCH(s.kc, "k_writeback", sl.st,
-              k_writeback<<<b2, 256, 0, sl.st>>>(sl.Cc, cres, crop.lo[0], crop.lo[1], crop.lo[2], s.C, s.desc.res,
-                                                 dirty.lo[0], dirty.lo[1], dirty.lo[2], dirty.hi[0], dirty.hi[1],
-                                                 dirty.hi[2]));
-  }
-  // 5. re-mesh the crop; the dirty box's triangles form the patch
+  const int wx = dirty.hi[0] - dirty.lo[0], wy = dirty.hi[1] - dirty.lo[1], wz = dirty.hi[2] - dirty.lo[2];
+  if (wx > 0 && wy > 0 && wz > 0)
+    GM_LAUNCH(s.kc, "k_box_copy", sl.st,
+              k_box_copy<<<dim3(wy, wz), 128, 0, sl.st>>>(sl.Cc, cres, dirty.lo[0] - crop.lo[0], dirty.lo[1] - crop.lo[1],
+                                                          dirty.lo[2] - crop.lo[2], s.C, res, dirty.lo[0], dirty.lo[1],
+                                                          dirty.lo[2], wx));
+  // 5. mesh the dirty box of the crop (vertices in global coordinates)
   MeshArgs ma;
   ma.res = cres;
   ma.C = sl.Cc;
-  for (int k = 0; k < 3; k++) ma.bbox_min[k] = s.desc.bbox_min[k] + crop.lo[k] * s.desc.cell_size;
+  for (int k = 0; k < 3; k++) ma.bbox_min[k] = s.desc.bbox_min[k];
   ma.cell_size = s.desc.cell_size;
   ma.isovalue = 0.95f;
   ma.bilateral_iters = s.bilateral;
   ma.num_sms = s.sms;
+  ma.gres = res;
+  for (int k = 0; k < 3; k++) {
+    ma.off[k] = crop.lo[k];
+    ma.emit_lo[k] = dirty.lo[k] - crop.lo[k];
+    ma.emit_hi[k] = dirty.hi[k] - crop.lo[k];
+    ma.tag_lo[k] = ma.emit_lo[k];
+    ma.tag_hi[k] = ma.emit_hi[k] + 1 < cres ? ma.emit_hi[k] + 1 : cres;
+  }
+  ma.zero_isolated = 1;
   sl.ma = ma;
   if ((err = mesh_count_launch(ma, sl.mesh, sl.st, s.kc, sl.h_tot)) != cudaSuccess) return err;
   cudaEventRecord(sl.counted, sl.st);
@@ -243,28 +356,8 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Box3& d
 // second half of an edit, once its mesh counts are on the host
 static cudaError_t finish_mesh(Server& s, Slot& sl) {
   cudaError_t err;
-  const Box3& dirty = sl.dirty;
-  const Box3& crop = sl.crop;
   if ((err = mesh_count_finish(sl.mesh, sl.h_tot, &sl.nv, &sl.nt)) != cudaSuccess) return err;
   if ((err = mesh_emit(sl.ma, sl.mesh, sl.nv, sl.nt, sl.st, s.kc)) != cudaSuccess) return err;
-  if ((size_t)sl.nt > sl.keep_cap) {
-    cudaFree(sl.keep);
-    sl.keep = nullptr;
-    sl.keep_cap = 0;
-    if ((err = cudaMalloc(&sl.keep, (size_t)sl.nt + 1024)) != cudaSuccess) return err;
-    sl.keep_cap = (size_t)sl.nt + 1024;
-  }
-  if (sl.nt > 0) {
-    const float cs_f = 0.5f * s.desc.cell_size;
-    int b3 = (int)((sl.nt + 255) / 256);
-    if (b3 > s.sms * 32) b3 = s.sms * 32;
-    GM_LAUNCH(s.kc, "k_patch_mask", sl.st,
-              k_patch_mask<<<b3, 256, 0, sl.st>>>(sl.mesh.V, sl.mesh.T, sl.nt, sl.ma.bbox_min[0], sl.ma.bbox_min[1],
-                                                  sl.ma.bbox_min[2], 1.f / cs_f, 2.f * (dirty.lo[0] - crop.lo[0]),
-                                                  2.f * (dirty.lo[1] - crop.lo[1]), 2.f * (dirty.lo[2] - crop.lo[2]),
-                                                  2.f * (dirty.hi[0] - crop.lo[0]), 2.f * (dirty.hi[1] - crop.lo[1]),
-                                                  2.f * (dirty.hi[2] - crop.lo[2]), sl.keep));
-  }
   sl.phase = 2;
   cudaEventRecord(sl.t1, sl.st);
   return cudaGetLastError();
@@ -306,12 +399,12 @@ static void progress(Server& s) {
       r.dirty_lo[a] = 2 * sl.dirty.lo[a];
       r.dirty_hi[a] = 2 * sl.dirty.hi[a];
     }
+    r.crop_res = sl.cres;
     r.patch.vertices = sl.mesh.V;
     r.patch.normals = sl.mesh.N;
     r.patch.triangles = sl.mesh.T;
     r.patch.num_vertices = sl.nv;
     r.patch.num_triangles = sl.nt;
-    r.patch_keep = sl.keep;
     s.done.push_back(r);
     sl.busy = false;
     sl.phase = 0;
@@ -319,9 +412,8 @@ static void progress(Server& s) {
   // dispatch queued edits in order while slots are free and crops disjoint
   while (!s.queue.empty()) {
     const Pending& p = s.queue.front();
-    Box3 dirty, crop;
-    int cres;
-    if (!plan_edit(s, p.edit, dirty, crop, cres)) {
+    Plan pl;
+    if (!plan_edit(s, p.edit, pl)) {
       gm_edit_result r = {};
       r.ticket = p.ticket;
       r.status = GM_ERR_CAPACITY;
@@ -332,13 +424,13 @@ static void progress(Server& s) {
     bool conflict = false;
     Slot* free_slot = nullptr;
     for (Slot& sl : s.slots) {
-      if (sl.busy && sl.crop.overlaps(crop)) conflict = true;
+      if (sl.busy && sl.crop.overlaps(pl.crop)) conflict = true;
       if (!sl.busy && !free_slot) free_slot = &sl;
     }
     if (conflict || !free_slot) break;
     const Pending pe = p;
     s.queue.pop_front();
-    if (dispatch(s, *free_slot, pe, dirty, crop, cres) != cudaSuccess) {
+    if (dispatch(s, *free_slot, pe, pl) != cudaSuccess) {
       cudaGetLastError();
       fail_slot(s, *free_slot, GM_ERR_CUDA);
     }
@@ -362,8 +454,9 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
                            const gm_server_opts* opts, gm_server** out) {
   if (!desc || !d_input || !d_scale || !opts || !out) return GM_ERR_INVALID_ARGUMENT;
   if (!pow2i(desc->res) || desc->res < 16 || desc->res > 1024) return GM_ERR_INVALID_ARGUMENT;
-  if (opts->slots < 1 || opts->slots > 16 || !pow2i(opts->max_crop_res) || opts->max_crop_res < 16 ||
-      opts->max_crop_res > desc->res || opts->rmax < 2 || opts->rmax > 127)
+  const bool crop_ok = opts->max_crop_res == desc->res || (opts->max_crop_res >= 32 && opts->max_crop_res % 32 == 0);
+  if (opts->slots < 1 || opts->slots > 16 || !crop_ok || opts->max_crop_res > desc->res || opts->rmax < 2 ||
+      opts->rmax > 127)
     return GM_ERR_INVALID_ARGUMENT;
   gm_server* srv = new gm_server();
   gm::Server& s = srv->s;
@@ -388,6 +481,20 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
     if (h > s.rmax) s.rmax = h;  // the bound must cover the field as loaded
   }
   cudaFree(d_r);
+  // radius map (8-cell bricks)
+  if (e == cudaSuccess) {
+    s.rnb = (desc->res + gm::kRBrick - 1) / gm::kRBrick;
+    const size_t nb = (size_t)s.rnb * s.rnb * s.rnb;
+    s.rmap.assign(nb, 0);
+    uint8_t* d_map = nullptr;
+    e = cudaMalloc(&d_map, nb);
+    if (e == cudaSuccess) {
+      GM_LAUNCH(s.kc, "k_brick_rmax", 0,
+                gm::k_brick_rmax<<<(unsigned)nb, 256, 0, 0>>>(d_scale, 2 * desc->res, s.rnb, d_map));
+      e = cudaMemcpy(s.rmap.data(), d_map, nb, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d_map);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&s.ws_full, gm::close_workspace_bytes(desc->res));
   // initial full closing of the resident grid
   if (e == cudaSuccess) {
@@ -450,7 +557,6 @@ gm_status gm_server_destroy(gm_server* srv) {
     cudaFree(sl.Cc);
     cudaFree(sl.Rc);
     cudaFree(sl.ws);
-    cudaFree(sl.keep);
     sl.mesh.release();
   }
   cudaFree(s.C);
@@ -500,5 +606,20 @@ int32_t gm_server_pending(gm_server* srv) {
 const uint8_t* gm_server_closing(gm_server* srv) { return srv ? srv->s.C : nullptr; }
 
 long long gm_server_kernel_launches(gm_server* srv) { return srv ? srv->kc.launches : -1; }
+
+gm_status gm_server_profile(gm_server* srv, int32_t enable) {
+  if (!srv) return GM_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(srv->s.device);
+  srv->kc.flush();
+  srv->kc.totals.clear();
+  srv->kc.profiling = enable != 0;
+  return GM_OK;
+}
+
+int64_t gm_server_profile_read(gm_server* srv, char* buf, int64_t cap) {
+  if (!srv) return -1;
+  cudaSetDevice(srv->s.device);
+  return gm::profile_json(srv->kc, buf, cap);
+}
 
 }  // extern "C"

@@ -214,7 +214,7 @@ typedef struct gm_server gm_server;
 
 typedef struct {
   int32_t slots;            /* concurrent edits (1..16) */
-  int32_t max_crop_res;     /* largest local re-closing, base cells per axis (power of two) */
+  int32_t max_crop_res;     /* largest local re-closing, base cells per axis (a multiple of 32, or res) */
   int32_t rmax;             /* radius bound (fine voxels) for edits and field */
   int32_t mode;             /* gm_mode of the closing */
   int32_t bilateral_iters;  /* normal filtering of the re-meshed patches */
@@ -235,8 +235,11 @@ typedef struct {
   float device_ms;         /* GPU time of the edit */
   int32_t dirty_lo[3];     /* fine-voxel box whose closing was recomputed */
   int32_t dirty_hi[3];
-  gm_mesh_view patch;      /* mesh of the re-closed crop (device, valid until its slot is reused) */
-  const uint8_t* patch_keep; /* per triangle: 1 when it lies in the dirty box */
+  int32_t crop_res;        /* edge (base cells) of the crop that was re-closed */
+  /* mesh of the dirty box (device, valid until its slot is reused): the
+   * triangles the whole grid's mesh has in these cells, with bit-identical
+   * vertex positions; vertices no patch triangle uses get a zero normal */
+  gm_mesh_view patch;
 } gm_edit_result;
 
 /* d_input and d_scale stay owned by the caller and must outlive the server;
@@ -252,6 +255,10 @@ int32_t gm_server_pending(gm_server* srv);
 /* The resident closed grid (device, res^3 bytes). */
 const uint8_t* gm_server_closing(gm_server* srv);
 long long gm_server_kernel_launches(gm_server* srv);
+/* Per-kernel device time of the server's launches (CUDA events around each
+ * launch on its slot stream), same JSON form as gm_ctx_profile_read. */
+gm_status gm_server_profile(gm_server* srv, int32_t enable);
+int64_t gm_server_profile_read(gm_server* srv, char* buf, int64_t cap);
 
 /* ---------------------------------------------------------------- a18 */
 /* BVH over the set fine voxels of a packed grid (BVH::BuildFromSEList,

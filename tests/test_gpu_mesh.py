@@ -76,6 +76,26 @@ def test_normals_match_oracle(gm_ctx, iters):
     np.testing.assert_allclose(N, No, atol=NORMAL_ATOL, rtol=0)
 
 
+@pytest.mark.parametrize("iters", [0, 20])
+def test_border_solid_matches_oracle(gm_ctx, iters):
+    # A solid cut by the grid border: cubes of border cells are never
+    # tagged, so the reference's triangles next to them take vertex index 0
+    # for the missing edges and vertex 0 collects thousands of corners.
+    res = 64
+    N = 2 * res
+    rng = np.random.default_rng(121)
+    z, y, x = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    occ = (x + 0.3 * y < 0.7 * N) | (rng.random((N, N, N)) < 0.002)
+    Cg = synth.pack_dense(occ)
+    V, N_, T, desc = _mesh(gm_ctx, res, Cg, iters)
+    Vo, To = O.mc(Cg, res, np.array(desc.bbox_min), desc.cell_size)
+    assert np.array_equal(T, To)
+    assert (To == 0).sum() > 1000
+    np.testing.assert_allclose(V, Vo, rtol=VERT_RTOL, atol=0)
+    No = O.normals(Vo, To, iters)
+    np.testing.assert_allclose(N_, No, atol=NORMAL_ATOL, rtol=0, equal_nan=True)
+
+
 def test_empty_mesh(gm_ctx):
     res = 16
     V, N, T, _ = _mesh(gm_ctx, res, np.zeros(res ** 3, np.uint8), 20)

@@ -21,13 +21,16 @@ def _setup(res=128, seed=301):
 
 
 def _edits(res, n=12, seed=7):
+    """Brush edits whose crops (rmax 8) are 64 or 96 cells: not powers of two
+    as well as powers of two."""
     rng = np.random.default_rng(seed)
     cs = 0.5 / res  # fine voxel (scale-field cell)
     out = []
     for i in range(n):
         c = rng.uniform(0.25, 0.75, size=3)
-        r_new = int(rng.integers(1, 9))
-        Rb = float(rng.uniform(3, 12))  # brush reach in fine voxels
+        small = i % 2 == 0
+        r_new = int(rng.integers(1, 5 if small else 9))
+        Rb = float(rng.uniform(2, 6) if small else rng.uniform(20, 30))  # brush reach in fine voxels
         scale = r_new * cs
         support = scale + max(Rb - r_new, 1.0) * cs * np.sqrt(1 - np.sqrt(0.5))
         mode = L.GM_BRUSH_MAX if r_new >= 4 else L.GM_BRUSH_MIN
@@ -38,7 +41,7 @@ def _edits(res, n=12, seed=7):
 def _run(slots, edits, res=128):
     import torch
     desc, X, R = _setup(res)
-    srv = api.Server(desc, X, R, slots=slots, max_crop_res=64, rmax=8, mode=L.GM_REF)
+    srv = api.Server(desc, X, R, slots=slots, max_crop_res=96, rmax=8, mode=L.GM_REF)
     results = []
     for c, scale, support, mode in edits:
         srv.submit(c, scale, support, 0.0, mode)
@@ -54,6 +57,7 @@ def test_local_reclosing_equals_full_closing(gm_ctx):
     edits = _edits(128)
     desc, X, R, C, results, srv = _run(3, edits)
     assert len(results) == len(edits) and all(r["status"] == L.GM_OK for r in results)
+    assert {64, 96} <= {r["crop_res"] for r in results}
     full = gm_ctx.close(desc, X, R, 0, L.GM_REF, L.GM_SE_SPHERE)
     torch.cuda.synchronize()
     assert torch.equal(C, full)
@@ -71,30 +75,58 @@ def test_same_alone_and_in_the_mix():
     s4.destroy()
 
 
+def _case91_cubes(C, res, lo_cell, hi_cell):
+    """MC cubes of value 91 with their min corner in the cell box (fine
+    corner order 000,100,110,010,001,101,111,011)."""
+    occ = synth.unpack_dense(C, res)  # [z, y, x]
+    N = 2 * res
+    o = np.zeros((N + 1,) * 3, dtype=np.uint8)
+    o[:N, :N, :N] = occ
+    v = np.zeros((N, N, N), dtype=np.int32)
+    for bit, (dx, dy, dz) in enumerate([(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0),
+                                        (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]):
+        v |= o[dz:dz + N, dy:dy + N, dx:dx + N].astype(np.int32) << bit
+    f0, f1 = 2 * np.asarray(lo_cell), 2 * np.asarray(hi_cell)
+    sub = v[f0[2]:f1[2], f0[1]:f1[1], f0[0]:f1[0]]
+    return int((sub == 91).sum())
+
+
 def test_patch_matches_full_mesh(gm_ctx):
+    """The patch holds exactly the whole mesh's triangles emitted by the cubes
+    of the dirty box, with bit-identical vertices (up to the reference's
+    case-91 late write, which lands on the next triangle slot of the run)."""
     import torch
-    desc, X, R = _setup(128, seed=305)
-    srv = api.Server(desc, X, R, slots=2, max_crop_res=64, rmax=8, mode=L.GM_REF)
+    res = 128
+    desc, X, R = _setup(res, seed=305)
+    srv = api.Server(desc, X, R, slots=2, max_crop_res=96, rmax=8, mode=L.GM_REF)
     c = np.array([0.5, 0.5, 0.5])
-    cs = 0.5 / 128
-    srv.submit(c, 6 * cs, 6 * cs + 4 * cs * np.sqrt(1 - np.sqrt(0.5)), 0.0, L.GM_BRUSH_MAX)
-    res = srv.drain()
-    assert len(res) == 1 and res[0]["status"] == L.GM_OK
-    r = res[0]
+    cs = 0.5 / res
+    srv.submit(c, 6 * cs, 6 * cs + 10 * cs * np.sqrt(1 - np.sqrt(0.5)), 0.0, L.GM_BRUSH_MAX)
+    out = srv.drain()
+    assert len(out) == 1 and out[0]["status"] == L.GM_OK
+    r = out[0]
     pv = torch.as_tensor(api.DevicePtrArray(r["patch"].vertices, (r["patch"].num_vertices, 3), "<f4"), device="cuda")
     pt = torch.as_tensor(api.DevicePtrArray(r["patch"].triangles, (r["patch"].num_triangles, 3), "<u4"),
                          device="cuda")
-    keep = torch.as_tensor(api.DevicePtrArray(r["patch_keep"], (r["patch"].num_triangles,), "|u1"), device="cuda")
-    tri_patch = pv[pt[keep.bool()].long()].cpu().numpy()  # (k, 3, 3) triangle corner positions
-    V, N, T = gm_ctx.mesh(desc, srv.closing().clone(), 0)
+    tri_patch = pv.cpu().numpy()[pt.view(torch.int32).cpu().numpy()]  # (k, 3, 3) corner positions
+    Cres = srv.closing().clone()
+    V, N, T = gm_ctx.mesh(desc, Cres, 0)
     torch.cuda.synchronize()
-    tri_full = V[T.long()].cpu().numpy()
-    lo, hi = np.array(r["dirty_lo"]), np.array(r["dirty_hi"])
-    cen = tri_full.mean(1) / cs
-    sel = np.all((cen >= lo) & (cen < hi), axis=1)
-    def rows(t):
-        m = np.round(t.reshape(len(t), -1) / cs, 3)
-        return m[np.lexsort(m.T[::-1])]
-    a, b = rows(tri_patch), rows(tri_full[sel])
-    assert len(a) > 0 and a.shape == b.shape and np.allclose(a, b, atol=1e-3)
+    tri_full = V.cpu().numpy()[T.view(torch.int32).cpu().numpy()]
+    lo_cell, hi_cell = np.array(r["dirty_lo"]) // 2, np.array(r["dirty_hi"]) // 2
+    # emitting cube of a triangle: floor of its smallest vertex coordinates
+    # (fine units; every vertex has one non-integer coordinate, x.05 or x.95)
+    cube = np.floor(tri_full.min(axis=1) / cs).astype(np.int64)
+    cell = cube // 2
+    sel = np.all((cell >= lo_cell) & (cell < hi_cell), axis=1)
+
+    def keyset(t):
+        from collections import Counter
+        return Counter(map(bytes, np.ascontiguousarray(t.reshape(len(t), -1)).view(np.uint8).reshape(len(t), -1)))
+
+    a, b = keyset(tri_patch), keyset(tri_full[sel])
+    diff = sum(((a - b) + (b - a)).values())
+    n91 = _case91_cubes(Cres.cpu().numpy(), res, lo_cell, hi_cell)
+    assert len(tri_patch) > 1000
+    assert diff <= 4 * n91, (diff, n91)
     srv.destroy()
