@@ -118,6 +118,15 @@ KERNEL_BYTES_PER_VOXEL = {
 }
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# one ncu capture of each kernel, scaled to the 1024^3 workload by the
+# units processed (see profiles/).
+TRAFFIC = {
+    "k_bilateral": 599_000_000,     # 137.3 MB at 1.10M vertices / 2.19M triangles, x4.366
+    "k_pass_dil_z": 3_354_000_000,  # 419.3 MB at 512^3 fine voxels, x8
+}
+
+
 def run_ours(args, rank, world):
     import torch
     from broxy_gb300 import api
@@ -215,18 +224,28 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
     hbm, peak_kind = peaks()
     top = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else (None, None)
     roof = None
-    if top[0] is not None:
-        name, rec = top
+    def kernel_roof(name, rec):
         per_launch_ms = rec["ms"] / rec["launches"]
-        bpv = KERNEL_BYTES_PER_VOXEL.get(name)
-        if bpv is not None:
-            ach = bpv * V / (per_launch_ms * 1e-3) / 1e9
-            roof = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                    "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": None,
-                    "bytes_per_voxel": round(bpv, 4), "per_launch_ms": round(per_launch_ms, 4)}
+        if name == "k_bilateral":
+            # per iteration: normal in + out and row pointer per vertex (16 + 16 + 4 B), the two
+            # neighbour ids and position weights per corner (8 + 8 B)
+            nbytes, model = 36 * nv + 48 * nt, "36 B/vertex + 48 B/triangle per iteration"
+        elif name in KERNEL_BYTES_PER_VOXEL:
+            nbytes, model = KERNEL_BYTES_PER_VOXEL[name] * V, "%.4f B/fine voxel" % KERNEL_BYTES_PER_VOXEL[name]
         else:
-            roof = {"kernel": name, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
+            return {"kernel": name, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
                     "peak_kind": peak_kind, "traffic": None, "per_launch_ms": round(per_launch_ms, 4)}
+        ach = nbytes / (per_launch_ms * 1e-3) / 1e9
+        return {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": TRAFFIC.get(name),
+                "algorithmic_bytes_per_launch": int(nbytes), "bytes_model": model,
+                "per_launch_ms": round(per_launch_ms, 4)}
+
+    if top[0] is not None:
+        roof = kernel_roof(*top)
+    morph_top = max(((k, v) for k, v in prof.items() if k in KERNEL_BYTES_PER_VOXEL), key=lambda kv: kv[1]["ms"],
+                    default=(None, None))
+    morph_roof = kernel_roof(*morph_top) if morph_top[0] is not None else None
     morph_kernels = [k for k in prof if not k.startswith(("k_mc", "k_adj", "k_scan", "k_vertex", "k_bilateral"))]
     morph_ms = sum(prof[k]["ms"] for k in morph_kernels) / args.steps
     mesh_ms = sum(prof[k]["ms"] for k in prof if k not in morph_kernels) / args.steps
@@ -249,6 +268,7 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
                 "d2h_bytes_per_step": int(24 * nv + 12 * nt)},
         "gpu_launches": int(launches),
         "roofline": roof,
+        "roofline_morphology_top": morph_roof,
         "morphology": {"ms": round(morph_ms, 3), "algorithmic_bytes": int(morph_bytes),
                        "achieved_gbs": round(morph_gbs, 1) if morph_gbs else None,
                        "frac_of_peak": round(morph_gbs / hbm, 4) if morph_gbs else None},

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
-SOURCES = ["morpho.cu", "mc.cu", "pyramid.cu", "scalefield.cu", "voxelize.cu", "capi.cu", "close_noalloc.cu", "bvh.cu", "batch.cu", "serve.cu"]
+SOURCES = ["morpho.cu", "mc.cu", "pyramid.cu", "scalefield.cu", "voxelize.cu", "capi.cu", "close_noalloc.cu", "bvh.cu", "batch.cu", "serve.cu", "crop.cu"]
 HOST_SOURCES = ["gmorpho_classes.cpp"]
 
 

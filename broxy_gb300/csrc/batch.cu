@@ -10,6 +10,15 @@
 // the same lanes with a single host synchronisation for all the vertex and
 // triangle counts.  The lane count is chosen by a small autotuner (timed
 // candidates 1, 2, 4, 8, 16 on the first call of a signature).
+//
+// Each grid is closed on its occupied extent only: the cube at the origin
+// holding every non-empty cell plus the dilation reach, rounded up to 32
+// cells.  The closing is empty beyond the dilation of the input, and inside
+// that cube it equals the whole grid's (no input is cut off, and the border
+// rules of the last cells act on empty cells), so the result embedded back
+// into the grid, and its mesh, are the whole-grid ones.  A grid of edge E
+// stored in a power-of-two cube P (the reference's requirement) costs E^3
+// instead of P^3.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -27,6 +36,8 @@ struct BatchLane {
   cudaEvent_t done = nullptr;
   uint8_t* ws = nullptr;
   size_t ws_bytes = 0;
+  uint8_t *Xc = nullptr, *Cc = nullptr, *Rc = nullptr;  // crop buffers
+  size_t crop_cells = 0, crop_fine = 0;
 };
 
 struct BatchState {
@@ -38,6 +49,9 @@ struct BatchState {
   int* d_rmax = nullptr;      // one int per instance
   int* h_rmax = nullptr;      // pinned
   int rmax_cap = 0;
+  unsigned* d_ext = nullptr;  // occupied extent, 3 per instance
+  unsigned* h_ext = nullptr;  // pinned
+  int ext_cap = 0;
   cudaEvent_t fork = nullptr;
   cudaStream_t cap_st = nullptr;  // capture / replay stream (the caller's may be the legacy stream)
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -54,11 +68,16 @@ void batch_release(void* p) {
     if (l.st) cudaStreamDestroy(l.st);
     if (l.done) cudaEventDestroy(l.done);
     cudaFree(l.ws);
+    cudaFree(l.Xc);
+    cudaFree(l.Cc);
+    cudaFree(l.Rc);
   }
   for (MeshBuffers& m : b->meshes) m.release();
   if (b->h_tot) cudaFreeHost(b->h_tot);
   if (b->h_rmax) cudaFreeHost(b->h_rmax);
   cudaFree(b->d_rmax);
+  if (b->h_ext) cudaFreeHost(b->h_ext);
+  cudaFree(b->d_ext);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->cap_st) cudaStreamDestroy(b->cap_st);
   if (b->ev_in) cudaEventDestroy(b->ev_in);
@@ -72,7 +91,7 @@ static uint64_t mix(uint64_t h, uint64_t v) {
   return h;
 }
 
-static uint64_t signature(int n, const gm_batch_item* it, int mode, int se, int lanes) {
+static uint64_t signature(int n, const gm_batch_item* it, const std::vector<int>& ext, int mode, int se, int lanes) {
   uint64_t h = mix(0, (uint64_t)n);
   h = mix(h, (uint64_t)mode);
   h = mix(h, (uint64_t)se);
@@ -84,6 +103,7 @@ static uint64_t signature(int n, const gm_batch_item* it, int mode, int se, int 
     h = mix(h, (uint64_t)(uintptr_t)it[i].d_scale);
     h = mix(h, (uint64_t)(uintptr_t)it[i].d_closing);
     h = mix(h, (uint64_t)it[i].uniform_radius);
+    h = mix(h, (uint64_t)ext[i]);
   }
   return h;
 }
@@ -106,47 +126,60 @@ static cudaError_t ensure_lanes(BatchState* b, int L) {
 }
 
 // largest grids first onto the least-loaded lane
-static std::vector<int> assign(int n, const gm_batch_item* it, int L) {
+static std::vector<int> assign(int n, const std::vector<int>& ext, int L) {
   std::vector<int> order(n), lane(n, 0);
   for (int i = 0; i < n; i++) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return it[a].desc.res > it[b].desc.res; });
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ext[a] > ext[b]; });
   std::vector<double> load(L, 0.0);
   for (int i : order) {
     int best = 0;
     for (int l = 1; l < L; l++)
       if (load[l] < load[best]) best = l;
     lane[i] = best;
-    load[best] += (double)it[i].desc.res * it[i].desc.res * it[i].desc.res;
+    load[best] += (double)ext[i] * ext[i] * ext[i];
   }
   return lane;
 }
 
 // The closing phase: fork from `st`, every lane runs its instances, join.
-static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* it, const int* rmax, int mode, int se,
-                                    int L, const std::vector<int>& lane, int sms, cudaStream_t st,
-                                    KernelCounter* kc) {
+static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* it, const int* rmax,
+                                    const std::vector<int>& ext, int mode, int se, int L, const std::vector<int>& lane,
+                                    int sms, cudaStream_t st, KernelCounter* kc) {
   cudaError_t e = cudaEventRecord(b->fork, st);
   if (e != cudaSuccess) return e;
   for (int l = 0; l < L; l++)
     if ((e = cudaStreamWaitEvent(b->lanes[l].st, b->fork, 0)) != cudaSuccess) return e;
   for (int i = 0; i < n; i++) {
     BatchLane& ln = b->lanes[lane[i]];
+    const int res = it[i].desc.res, E = ext[i];
+    const bool crop = E < res;
     CloseArgs a;
-    a.res = it[i].desc.res;
-    for (int k = 0; k < 3; k++) a.data_res[k] = it[i].desc.data_res[k];
+    a.res = E;
+    for (int k = 0; k < 3; k++) a.data_res[k] = it[i].desc.data_res[k] < E ? it[i].desc.data_res[k] : E;
     a.X = it[i].d_input;
     a.R = it[i].d_scale;
+    if (crop) {
+      const int zero[3] = {0, 0, 0}, e3[3] = {E, E, E}, f3[3] = {2 * E, 2 * E, 2 * E};
+      if ((e = launch_box_copy(it[i].d_input, res, zero, ln.Xc, E, zero, e3, ln.st, kc)) != cudaSuccess) return e;
+      a.X = ln.Xc;
+      if (it[i].d_scale) {
+        if ((e = launch_box_copy(reinterpret_cast<const uint8_t*>(it[i].d_scale), 2 * res, zero,
+                                 reinterpret_cast<uint8_t*>(ln.Rc), 2 * E, zero, f3, ln.st, kc)) != cudaSuccess)
+          return e;
+        a.R = reinterpret_cast<const int8_t*>(ln.Rc);
+      }
+    }
     a.uniform_r = it[i].uniform_radius;
     a.rmax = rmax[i];
     a.mode = mode;
     a.se = se;
-    a.C_out = it[i].d_closing;
+    a.C_out = crop ? ln.Cc : it[i].d_closing;
     a.D_out = nullptr;
     a.S_out = nullptr;
     a.workspace = ln.ws;
     a.num_sms = sms;
     if ((e = launch_close(a, ln.st, kc)) != cudaSuccess) return e;
+    if (crop && (e = launch_embed(ln.Cc, E, it[i].d_closing, res, ln.st, kc)) != cudaSuccess) return e;
   }
   for (int l = 0; l < L; l++) {
     if ((e = cudaEventRecord(b->lanes[l].done, b->lanes[l].st)) != cudaSuccess) return e;
@@ -168,32 +201,53 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     rmax[i] = clamp_radius(it[i].uniform_radius);
     if (it[i].d_scale) all_uniform = false;
   }
-  if (!all_uniform) {
-    if (b->rmax_cap < n) {
-      cudaFree(b->d_rmax);
-      if (b->h_rmax) cudaFreeHost(b->h_rmax);
-      b->d_rmax = nullptr;
-      b->h_rmax = nullptr;
-      if ((e = cudaMalloc(&b->d_rmax, sizeof(int) * n)) != cudaSuccess) return e;
-      if ((e = cudaMallocHost(&b->h_rmax, sizeof(int) * n)) != cudaSuccess) return e;
-      b->rmax_cap = n;
+  if (!all_uniform && b->rmax_cap < n) {
+    cudaFree(b->d_rmax);
+    if (b->h_rmax) cudaFreeHost(b->h_rmax);
+    b->d_rmax = nullptr;
+    b->h_rmax = nullptr;
+    if ((e = cudaMalloc(&b->d_rmax, sizeof(int) * n)) != cudaSuccess) return e;
+    if ((e = cudaMallocHost(&b->h_rmax, sizeof(int) * n)) != cudaSuccess) return e;
+    b->rmax_cap = n;
+  }
+  if (b->ext_cap < n) {
+    cudaFree(b->d_ext);
+    if (b->h_ext) cudaFreeHost(b->h_ext);
+    b->d_ext = nullptr;
+    b->h_ext = nullptr;
+    if ((e = cudaMalloc(&b->d_ext, sizeof(unsigned) * 3 * n)) != cudaSuccess) return e;
+    if ((e = cudaMallocHost(&b->h_ext, sizeof(unsigned) * 3 * n)) != cudaSuccess) return e;
+    b->ext_cap = n;
+  }
+  // one round trip: radius bounds of radius fields, occupied extents
+  for (int i = 0; i < n; i++) {
+    const int64_t cells = (int64_t)it[i].desc.res * it[i].desc.res * it[i].desc.res;
+    if (it[i].d_scale) {
+      if ((e = launch_rmax(it[i].d_scale, 8 * cells, b->d_rmax + i, sms, st, kc)) != cudaSuccess) return e;
+      if ((e = cudaMemcpyAsync(b->h_rmax + i, b->d_rmax + i, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        return e;
     }
-    for (int i = 0; i < n; i++)
-      if (it[i].d_scale) {
-        if ((e = launch_rmax(it[i].d_scale, (int64_t)8 * it[i].desc.res * it[i].desc.res * it[i].desc.res,
-                             b->d_rmax + i, sms, st, kc)) != cudaSuccess)
-          return e;
-        if ((e = cudaMemcpyAsync(b->h_rmax + i, b->d_rmax + i, sizeof(int), cudaMemcpyDeviceToHost, st)) !=
-            cudaSuccess)
-          return e;
-      }
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
-    for (int i = 0; i < n; i++)
-      if (it[i].d_scale) rmax[i] = b->h_rmax[i];
+    if ((e = launch_occ_extent(it[i].d_input, it[i].desc.res, b->d_ext + 3 * i, sms, st, kc)) != cudaSuccess) return e;
+  }
+  if ((e = cudaMemcpyAsync(b->h_ext, b->d_ext, sizeof(unsigned) * 3 * n, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  for (int i = 0; i < n; i++)
+    if (it[i].d_scale) rmax[i] = b->h_rmax[i];
+  // closing extents: occupied cells + dilation reach ((r+1) fine, one block
+  // cell, one contour cell, one to spare), a multiple of 32 cells
+  std::vector<int> ext(n);
+  for (int i = 0; i < n; i++) {
+    const unsigned* x = b->h_ext + 3 * i;
+    const int occ = (int)std::max(x[0], std::max(x[1], x[2]));
+    const int reach = occ == 0 ? 0 : occ + (rmax[i] + 2) / 2 + 3;
+    int E = (std::max(reach, 32) + 31) / 32 * 32;
+    if (se == GM_SE_CUBE) E = (std::max(reach + 1, 32) + 31) / 32 * 32;
+    ext[i] = E >= it[i].desc.res ? it[i].desc.res : E;
   }
   // lane count: requested, tuned for this signature, or tuned now
   int L = lanes_req;
-  const uint64_t tune_sig = signature(n, it, mode, se, 0);
+  const uint64_t tune_sig = signature(n, it, ext, mode, se, 0);
   if (L <= 0) {
     auto f = b->tuned.find(tune_sig);
     if (f != b->tuned.end()) L = f->second;
@@ -202,18 +256,44 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
   const int cands[5] = {1, 2, 4, 8, 16};
   const int maxL = tune ? 16 : std::max(1, std::min(L, 64));
   if ((e = ensure_lanes(b, maxL)) != cudaSuccess) return e;
-  // per-lane workspaces sized for the largest grid of the batch
-  int maxres = 16;
-  for (int i = 0; i < n; i++) maxres = std::max(maxres, (int)it[i].desc.res);
-  const size_t wsb = close_workspace_bytes(maxres);
-  for (int l = 0; l < maxL; l++)
-    if (b->lanes[l].ws_bytes < wsb) {
-      cudaFree(b->lanes[l].ws);
-      b->lanes[l].ws = nullptr;
-      b->lanes[l].ws_bytes = 0;
-      if ((e = cudaMalloc(&b->lanes[l].ws, wsb)) != cudaSuccess) return e;
-      b->lanes[l].ws_bytes = wsb;
+  // per-lane workspaces and crop buffers sized for the largest closing
+  int maxres = 16, maxcrop = 0;
+  bool crop_field = false;
+  for (int i = 0; i < n; i++) {
+    maxres = std::max(maxres, ext[i]);
+    if (ext[i] < it[i].desc.res) {
+      maxcrop = std::max(maxcrop, ext[i]);
+      crop_field |= it[i].d_scale != nullptr;
     }
+  }
+  const size_t wsb = close_workspace_bytes(maxres);
+  const size_t ccells = (size_t)maxcrop * maxcrop * maxcrop;
+  for (int l = 0; l < maxL; l++) {
+    BatchLane& ln = b->lanes[l];
+    if (ln.ws_bytes < wsb) {
+      cudaFree(ln.ws);
+      ln.ws = nullptr;
+      ln.ws_bytes = 0;
+      if ((e = cudaMalloc(&ln.ws, wsb)) != cudaSuccess) return e;
+      ln.ws_bytes = wsb;
+    }
+    if (ln.crop_cells < ccells) {
+      cudaFree(ln.Xc);
+      cudaFree(ln.Cc);
+      ln.Xc = ln.Cc = nullptr;
+      ln.crop_cells = 0;
+      if ((e = cudaMalloc(&ln.Xc, ccells)) != cudaSuccess) return e;
+      if ((e = cudaMalloc(&ln.Cc, ccells)) != cudaSuccess) return e;
+      ln.crop_cells = ccells;
+    }
+    if (crop_field && ln.crop_fine < 8 * ccells) {
+      cudaFree(ln.Rc);
+      ln.Rc = nullptr;
+      ln.crop_fine = 0;
+      if ((e = cudaMalloc(&ln.Rc, 8 * ccells)) != cudaSuccess) return e;
+      ln.crop_fine = 8 * ccells;
+    }
+  }
   if (tune) {
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);
@@ -221,11 +301,11 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     float best_ms = 1e30f;
     int best = 1;
     for (int c : cands) {
-      const std::vector<int> lane = assign(n, it, c);
+      const std::vector<int> lane = assign(n, ext, c);
       // one untimed pass (first-touch, function attributes), one timed
       for (int rep = 0; rep < 2; rep++) {
         cudaEventRecord(t0, st);
-        if ((e = enqueue_closings(b, n, it, rmax.data(), mode, se, c, lane, sms, st, nullptr)) != cudaSuccess) {
+        if ((e = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, c, lane, sms, st, nullptr)) != cudaSuccess) {
           cudaEventDestroy(t0);
           cudaEventDestroy(t1);
           return e;
@@ -242,9 +322,9 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     L = best;
     b->tuned[tune_sig] = L;
   }
-  const std::vector<int> lane = assign(n, it, L);
+  const std::vector<int> lane = assign(n, ext, L);
   // closing phase: replay the captured graph when the batch is unchanged
-  const uint64_t sig = signature(n, it, mode, se, L);
+  const uint64_t sig = signature(n, it, ext, mode, se, L);
   const bool graphable = all_uniform && !(kc && kc->profiling);
   if (graphable) {
     if (!b->graph || b->graph_sig != sig) {
@@ -255,7 +335,7 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
       cudaGraph_t g = nullptr;
       KernelCounter cap;  // counts the kernels the graph holds
       if ((e = cudaStreamBeginCapture(b->cap_st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-      const cudaError_t ec = enqueue_closings(b, n, it, rmax.data(), mode, se, L, lane, sms, b->cap_st, &cap);
+      const cudaError_t ec = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, b->cap_st, &cap);
       e = cudaStreamEndCapture(b->cap_st, &g);
       if (ec != cudaSuccess) return ec;
       if (e != cudaSuccess) return e;
@@ -272,7 +352,7 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     if ((e = cudaStreamWaitEvent(st, b->ev_out, 0)) != cudaSuccess) return e;
     if (kc) kc->launches += b->graph_kernels;
   } else {
-    if ((e = enqueue_closings(b, n, it, rmax.data(), mode, se, L, lane, sms, st, kc)) != cudaSuccess) return e;
+    if ((e = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, st, kc)) != cudaSuccess) return e;
   }
   if (!meshes) return cudaGetLastError();
   // meshing: counts on the lanes, one synchronisation, emission on the lanes
@@ -297,6 +377,13 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     a.isovalue = 0.95f;
     a.bilateral_iters = bilateral;
     a.num_sms = sms;
+    // the closing is empty beyond the extent: mesh only its cells (the
+    // whole grid's border rule, identical mesh)
+    a.gres = a.res;
+    for (int k = 0; k < 3; k++) {
+      a.tag_lo[k] = a.emit_lo[k] = 0;
+      a.tag_hi[k] = a.emit_hi[k] = ext[i];
+    }
     if ((e = mesh_count_launch(a, b->meshes[i], b->lanes[lane[i]].st, kc, b->h_tot + 4 * i)) != cudaSuccess) return e;
   }
   for (int l = 0; l < L; l++)

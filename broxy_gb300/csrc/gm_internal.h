@@ -66,6 +66,13 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc);
 
+// ---------------------------------------------------------------- crops
+cudaError_t launch_box_copy(const uint8_t* src, int sn, const int s0[3], uint8_t* dst, int dn, const int d0[3],
+                            const int ext[3], cudaStream_t st, KernelCounter* kc);
+cudaError_t launch_embed(const uint8_t* Cc, int ext, uint8_t* C, int res, cudaStream_t st, KernelCounter* kc);
+cudaError_t launch_occ_extent(const uint8_t* X, int res, unsigned* d_out3, int sms, cudaStream_t st,
+                              KernelCounter* kc);
+
 // ---------------------------------------------------------------- pyramid
 size_t pyramid_texels(int res);
 cudaError_t launch_pyramid(const uint8_t* grid, const int8_t* R, int uniform_r, int res, uint64_t* pyr,

@@ -32,18 +32,6 @@
 
 namespace gm {
 
-// Copy of the box [s, s + e) of a cubic byte volume of edge sn into the box
-// [d, d + e) of a cubic volume of edge dn (the crops of the packed grid and
-// of the radius field, and the write-back of the dirty box).  One block per
-// row; the boxes lie inside both volumes by construction.
-__global__ void k_box_copy(const uint8_t* __restrict__ src, int sn, int sx, int sy, int sz, uint8_t* __restrict__ dst,
-                           int dn, int dx, int dy, int dz, int ex) {
-  const int y = blockIdx.x, z = blockIdx.y;
-  const uint8_t* s = src + cell_index(sx, sy + y, sz + z, sn);
-  uint8_t* d = dst + cell_index(dx, dy + y, dz + z, dn);
-  for (int x = threadIdx.x; x < ex; x += blockDim.x) d[x] = s[x];
-}
-
 // Largest radius of each 8-cell brick (16^3 fine voxels) of the radius
 // field: one block per brick, one 16-byte row segment per thread.
 constexpr int kRBrick = 8;  // cells per radius-map brick edge
@@ -295,13 +283,15 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
                                 e.global_scale, e.mode, sl.st, s.kc)) != cudaSuccess)
     return err;
   // 2. crop the packed grid and the radius field
-  GM_LAUNCH(s.kc, "k_box_copy", sl.st,
-            k_box_copy<<<dim3(cres, cres), 128, 0, sl.st>>>(s.X, res, crop.lo[0], crop.lo[1], crop.lo[2], sl.Xc, cres,
-                                                            0, 0, 0, cres));
-  GM_LAUNCH(s.kc, "k_box_copy", sl.st,
-            k_box_copy<<<dim3(2 * cres, 2 * cres), 256, 0, sl.st>>>(
-                reinterpret_cast<const uint8_t*>(s.R), 2 * res, 2 * crop.lo[0], 2 * crop.lo[1], 2 * crop.lo[2],
-                reinterpret_cast<uint8_t*>(sl.Rc), 2 * cres, 0, 0, 0, 2 * cres));
+  {
+    const int zero[3] = {0, 0, 0};
+    const int ext[3] = {cres, cres, cres}, ext2[3] = {2 * cres, 2 * cres, 2 * cres};
+    const int f0[3] = {2 * crop.lo[0], 2 * crop.lo[1], 2 * crop.lo[2]};
+    if ((err = launch_box_copy(s.X, res, crop.lo, sl.Xc, cres, zero, ext, sl.st, s.kc)) != cudaSuccess) return err;
+    if ((err = launch_box_copy(reinterpret_cast<const uint8_t*>(s.R), 2 * res, f0, reinterpret_cast<uint8_t*>(sl.Rc),
+                               2 * cres, zero, ext2, sl.st, s.kc)) != cudaSuccess)
+      return err;
+  }
   // 3. close the crop
   CloseArgs a;
   a.res = cres;
@@ -322,12 +312,11 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
   a.num_sms = s.sms;
   if ((err = launch_close(a, sl.st, s.kc)) != cudaSuccess) return err;
   // 4. write back the dirty box
-  const int wx = dirty.hi[0] - dirty.lo[0], wy = dirty.hi[1] - dirty.lo[1], wz = dirty.hi[2] - dirty.lo[2];
-  if (wx > 0 && wy > 0 && wz > 0)
-    GM_LAUNCH(s.kc, "k_box_copy", sl.st,
-              k_box_copy<<<dim3(wy, wz), 128, 0, sl.st>>>(sl.Cc, cres, dirty.lo[0] - crop.lo[0], dirty.lo[1] - crop.lo[1],
-                                                          dirty.lo[2] - crop.lo[2], s.C, res, dirty.lo[0], dirty.lo[1],
-                                                          dirty.lo[2], wx));
+  {
+    const int src0[3] = {dirty.lo[0] - crop.lo[0], dirty.lo[1] - crop.lo[1], dirty.lo[2] - crop.lo[2]};
+    const int ext[3] = {dirty.hi[0] - dirty.lo[0], dirty.hi[1] - dirty.lo[1], dirty.hi[2] - dirty.lo[2]};
+    if ((err = launch_box_copy(sl.Cc, cres, src0, s.C, res, dirty.lo, ext, sl.st, s.kc)) != cudaSuccess) return err;
+  }
   // 5. mesh the dirty box of the crop (vertices in global coordinates)
   MeshArgs ma;
   ma.res = cres;

@@ -58,3 +58,35 @@ def test_batch_variable_radius(gm_ctx):
     torch.cuda.synchronize()
     for (d, X, R, r, out), ref in zip(items, refs):
         assert torch.equal(out, ref)
+
+
+@pytest.mark.parametrize("mode,se", [(L.GM_REF, L.GM_SE_SPHERE), (L.GM_EXACT, L.GM_SE_SPHERE),
+                                     (L.GM_REF, L.GM_SE_CUBE)])
+def test_batch_occupied_extent(gm_ctx, mode, se):
+    """Grids closed on their occupied extent (solid in a corner of a larger
+    cube, an empty grid, a grid full to its border, a radius field) equal
+    the whole-grid closings and meshes."""
+    import torch
+    rng = np.random.default_rng(77)
+    specs = [(128, synth._blob_box(128, 80, 901, 12, None), 5, None),
+             (128, np.zeros(128 ** 3, np.uint8), 3, None),
+             (64, synth.random_grid(64, 902), 2, None),
+             (128, synth._blob_box(128, 150, 903, 20, None), 0, rng.integers(0, 13, size=256 ** 3).astype(np.int8))]
+    items, descs = [], []
+    for res, X, r, R in specs:
+        d = api.make_desc(res, bbox_min=(0.25, -0.5, 0.125), cell_size=1.0 / res)
+        Xd = torch.as_tensor(np.ascontiguousarray(X)).cuda()
+        Rd = torch.as_tensor(R).cuda() if R is not None else None
+        descs.append(d)
+        items.append((d, Xd, Rd, r, torch.empty_like(Xd)))
+    meshes = gm_ctx.batch_close_mesh(items, mode=mode, se=se, bilateral_iters=2, lanes=2)
+    torch.cuda.synchronize()
+    got = [(items[i][4].cpu().numpy(), meshes[i][0].cpu().numpy(), meshes[i][2].cpu().numpy())
+           for i in range(len(items))]
+    for i, (d, Xd, Rd, r, _) in enumerate(items):
+        ref = gm_ctx.close(d, Xd, Rd, r, mode, se)
+        V, N, T = gm_ctx.mesh(d, ref, 2)
+        torch.cuda.synchronize()
+        assert np.array_equal(got[i][0], ref.cpu().numpy())
+        assert np.array_equal(got[i][2], T.cpu().numpy())
+        assert np.array_equal(got[i][1], V.cpu().numpy())
