@@ -237,7 +237,7 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
                     "peak_kind": peak_kind, "traffic": None, "per_launch_ms": round(per_launch_ms, 4)}
         ach = nbytes / (per_launch_ms * 1e-3) / 1e9
         return {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": TRAFFIC.get(name),
+                "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": TRAFFIC.get(name) if res == RES else None,
                 "algorithmic_bytes_per_launch": int(nbytes), "bytes_model": model,
                 "per_launch_ms": round(per_launch_ms, 4)}
 

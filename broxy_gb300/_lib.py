@@ -94,6 +94,9 @@ PROTOTYPES = {
     "gm_server_closing": (C.c_void_p, [_P]),
     "gm_server_kernel_launches": (C.c_longlong, [_P]),
     "gm_server_profile": (C.c_int, [_P, C.c_int32]),
+    "gm_server_snapshot": (C.c_int, [_P, _P, _P]),
+    "gm_server_restore": (C.c_int, [_P, _P, _P]),
+    "gm_mesh_store": (C.c_int, [C.c_char_p, _P, _P, C.c_int64, _P, C.c_int64, C.c_int32]),
     "gm_server_profile_read": (C.c_int64, [_P, C.c_char_p, C.c_int64]),
     "gm_bvh_build": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.POINTER(_P), C.POINTER(C.c_int64), _P]),
     "gm_bvh_destroy": (C.c_int, [_P]),

@@ -319,6 +319,39 @@ class Server:
     def kernel_launches(self):
         return int(self.lib.gm_server_kernel_launches(self.h))
 
+    def snapshot(self):
+        """Host copies (closed grid, radius field) of the resident state."""
+        n = self.desc.res ** 3
+        C_ = np.empty(n, np.uint8)
+        R_ = np.empty(8 * n, np.int8)
+        st = self.lib.gm_server_snapshot(self.h, C_.ctypes.data, R_.ctypes.data)
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_snapshot")
+        return C_, R_
+
+    def restore(self, closing, scale):
+        closing = np.ascontiguousarray(closing, np.uint8)
+        scale = np.ascontiguousarray(scale, np.int8)
+        st = self.lib.gm_server_restore(self.h, closing.ctypes.data, scale.ctypes.data)
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_restore")
+
+    def export_patch(self, result, path, drop_unused=True):
+        """Write an edit's patch (a poll() result) as OFF / PN / PLY."""
+        import torch
+        p = result["patch"]
+        nv, nt = p.num_vertices, p.num_triangles
+
+        def host(ptr, shape, typestr, dtype):
+            if shape[0] == 0:
+                return np.empty(shape, dtype)
+            return torch.as_tensor(DevicePtrArray(ptr, shape, typestr), device="cuda").cpu().numpy().view(dtype)
+
+        V = host(p.vertices, (nv, 3), "<f4", np.float32)
+        N = host(p.normals, (nv, 3), "<f4", np.float32)
+        T = host(p.triangles, (nt, 3), "<i4", np.uint32)
+        store_mesh(path, V, N, T, drop_unused=drop_unused)
+
     def profile(self, enable=True):
         st = self.lib.gm_server_profile(self.h, 1 if enable else 0)
         if st != L.GM_OK:
@@ -341,3 +374,19 @@ class Server:
             self.destroy()
         except Exception:
             pass
+
+
+def store_mesh(path, V, N, T, drop_unused=False):
+    """Write a host mesh (float32 V/N (n, 3), uint32 T (m, 3)) as OFF, PN or
+    PLY, by extension (gm_mesh_store)."""
+    lib = L.load()
+    V = np.ascontiguousarray(V, np.float32)
+    T = np.ascontiguousarray(T, np.uint32)
+    Np = None
+    if N is not None:
+        N = np.ascontiguousarray(N, np.float32)
+        Np = N.ctypes.data
+    st = lib.gm_mesh_store(str(path).encode(), V.ctypes.data if V.size else None, Np, V.shape[0],
+                           T.ctypes.data if T.size else None, T.shape[0], 1 if drop_unused else 0)
+    if st != L.GM_OK:
+        raise L.GMError(st, "gm_mesh_store")

@@ -24,7 +24,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-co
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
 SOURCES = ["morpho.cu", "mc.cu", "pyramid.cu", "scalefield.cu", "voxelize.cu", "capi.cu", "close_noalloc.cu", "bvh.cu", "batch.cu", "serve.cu", "crop.cu"]
-HOST_SOURCES = ["gmorpho_classes.cpp"]
+HOST_SOURCES = ["gmorpho_classes.cpp", "meshio.cpp"]
 
 
 def nvcc():

@@ -81,6 +81,64 @@ bool Mesh::storeOFF(const std::string& path) const {
   return (bool)out;
 }
 
+bool Mesh::loadPN(const std::string& path) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return false;
+  std::vector<float> buf;
+  float tmp[6];
+  while (std::fread(tmp, sizeof(float), 6, f) == 6) buf.insert(buf.end(), tmp, tmp + 6);
+  std::fclose(f);
+  const size_t n = buf.size() / 6;
+  P_.resize(n);
+  N_.resize(n);
+  T_.clear();
+  for (size_t i = 0; i < n; i++) {
+    P_[i] = Vec3f(buf[6 * i], buf[6 * i + 1], buf[6 * i + 2]);
+    N_[i] = Vec3f(buf[6 * i + 3], buf[6 * i + 4], buf[6 * i + 5]);
+  }
+  return true;
+}
+
+static bool store_via_abi(const Mesh& m, const std::string& path) {
+  std::vector<float> n;
+  const float* np = nullptr;
+  if (m.N().size() == m.P().size()) {
+    np = m.P().empty() ? nullptr : &m.N()[0][0];
+  } else {
+    n.assign(3 * m.P().size(), 0.f);  // no normals: zeros
+    np = n.empty() ? nullptr : n.data();
+  }
+  return gm_mesh_store(path.c_str(), m.P().empty() ? nullptr : &m.P()[0][0], np, (int64_t)m.P().size(),
+                       m.T().empty() ? nullptr : &m.T()[0][0], (int64_t)m.T().size(), 0) == GM_OK;
+}
+
+bool Mesh::storePN(const std::string& path) const { return store_via_abi(*this, path); }
+bool Mesh::storePLY(const std::string& path) const { return store_via_abi(*this, path); }
+
+static std::string extension(const std::string& path) {
+  const size_t dot = path.find_last_of('.');
+  return dot == std::string::npos ? std::string() : path.substr(dot);
+}
+
+void Mesh::load(const std::string& path) {
+  const std::string ext = extension(path);
+  bool ok;
+  if (ext == ".off") ok = loadOFF(path);
+  else if (ext == ".pn") ok = loadPN(path);
+  else throw Exception("Error loading mesh: unrecognized file format.");
+  if (!ok) throw Exception("Error loading mesh file: " + path);
+}
+
+void Mesh::store(const std::string& path) const {
+  const std::string ext = extension(path);
+  bool ok;
+  if (ext == ".off") ok = storeOFF(path);
+  else if (ext == ".pn") ok = storePN(path);
+  else if (ext == ".ply") ok = storePLY(path);
+  else throw Exception("Error storing mesh: unrecognized file format.");
+  if (!ok) throw Exception("Error storing mesh file: " + path);
+}
+
 // ------------------------------------------------------------------ Grid
 
 Grid::Grid() {}

@@ -121,6 +121,21 @@ static double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// (re)build the host radius map from the device radius field
+static cudaError_t build_radius_map(Server& s) {
+  s.rnb = (s.desc.res + kRBrick - 1) / kRBrick;
+  const size_t nb = (size_t)s.rnb * s.rnb * s.rnb;
+  s.rmap.assign(nb, 0);
+  uint8_t* d_map = nullptr;
+  cudaError_t e = cudaMalloc(&d_map, nb);
+  if (e == cudaSuccess) {
+    GM_LAUNCH(s.kc, "k_brick_rmax", 0, k_brick_rmax<<<(unsigned)nb, 256, 0, 0>>>(s.R, 2 * s.desc.res, s.rnb, d_map));
+    e = cudaMemcpy(s.rmap.data(), d_map, nb, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d_map);
+  return e;
+}
+
 struct Plan {
   Box3 dirty, crop;
   int cres;
@@ -470,20 +485,7 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
     if (h > s.rmax) s.rmax = h;  // the bound must cover the field as loaded
   }
   cudaFree(d_r);
-  // radius map (8-cell bricks)
-  if (e == cudaSuccess) {
-    s.rnb = (desc->res + gm::kRBrick - 1) / gm::kRBrick;
-    const size_t nb = (size_t)s.rnb * s.rnb * s.rnb;
-    s.rmap.assign(nb, 0);
-    uint8_t* d_map = nullptr;
-    e = cudaMalloc(&d_map, nb);
-    if (e == cudaSuccess) {
-      GM_LAUNCH(s.kc, "k_brick_rmax", 0,
-                gm::k_brick_rmax<<<(unsigned)nb, 256, 0, 0>>>(d_scale, 2 * desc->res, s.rnb, d_map));
-      e = cudaMemcpy(s.rmap.data(), d_map, nb, cudaMemcpyDeviceToHost);
-    }
-    cudaFree(d_map);
-  }
+  if (e == cudaSuccess) e = gm::build_radius_map(s);
   if (e == cudaSuccess) e = cudaMalloc(&s.ws_full, gm::close_workspace_bytes(desc->res));
   // initial full closing of the resident grid
   if (e == cudaSuccess) {
@@ -595,6 +597,39 @@ int32_t gm_server_pending(gm_server* srv) {
 const uint8_t* gm_server_closing(gm_server* srv) { return srv ? srv->s.C : nullptr; }
 
 long long gm_server_kernel_launches(gm_server* srv) { return srv ? srv->kc.launches : -1; }
+
+gm_status gm_server_snapshot(gm_server* srv, uint8_t* h_closing, int8_t* h_scale) {
+  if (!srv || (!h_closing && !h_scale)) return GM_ERR_INVALID_ARGUMENT;
+  gm::Server& s = srv->s;
+  if (gm_server_pending(srv) != 0) return GM_ERR_NOT_READY;
+  cudaSetDevice(s.device);
+  const size_t cells = (size_t)s.desc.res * s.desc.res * s.desc.res;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && h_closing) e = cudaMemcpy(h_closing, s.C, cells, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && h_scale) e = cudaMemcpy(h_scale, s.R, 8 * cells, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? GM_OK : GM_ERR_CUDA;
+}
+
+gm_status gm_server_restore(gm_server* srv, const uint8_t* h_closing, const int8_t* h_scale) {
+  if (!srv || !h_closing || !h_scale) return GM_ERR_INVALID_ARGUMENT;
+  gm::Server& s = srv->s;
+  if (gm_server_pending(srv) != 0) return GM_ERR_NOT_READY;
+  cudaSetDevice(s.device);
+  const size_t cells = (size_t)s.desc.res * s.desc.res * s.desc.res;
+  cudaError_t e = cudaDeviceSynchronize();
+  int* d_r = nullptr;
+  int h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(s.R, h_scale, 8 * cells, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&d_r, sizeof(int));
+  if (e == cudaSuccess) e = gm::launch_rmax(s.R, (int64_t)8 * cells, d_r, s.sms, 0, s.kc);
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d_r, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d_r);
+  if (e != cudaSuccess) return GM_ERR_CUDA;
+  if (h > s.rmax) return GM_ERR_CAPACITY;  // the field is in place but edits need a larger bound
+  e = cudaMemcpy(s.C, h_closing, cells, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = gm::build_radius_map(s);
+  return e == cudaSuccess ? GM_OK : GM_ERR_CUDA;
+}
 
 gm_status gm_server_profile(gm_server* srv, int32_t enable) {
   if (!srv) return GM_ERR_INVALID_ARGUMENT;

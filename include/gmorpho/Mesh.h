@@ -21,6 +21,15 @@ typedef Vec3<unsigned int> Vec3ui;
 
 class Mesh {
  public:
+  class Exception {
+   public:
+    inline Exception(const std::string& msg) : msg_("Mesh Error: " + msg) {}
+    inline const std::string& msg() const { return msg_; }
+
+   protected:
+    std::string msg_;
+  };
+
   std::vector<Vec3f>& P() { return P_; }
   const std::vector<Vec3f>& P() const { return P_; }
   std::vector<Vec3f>& N() { return N_; }
@@ -32,6 +41,16 @@ class Mesh {
   // OFF file I/O (reference Mesh::loadOFF / storeOFF)
   bool loadOFF(const std::string& path);
   bool storeOFF(const std::string& path) const;
+  // PN: float32 position + normal per vertex (reference Mesh::loadPN /
+  // storePN, Common/Mesh.h:638-673)
+  bool loadPN(const std::string& path);
+  bool storePN(const std::string& path) const;
+  // binary little-endian PLY with normals
+  bool storePLY(const std::string& path) const;
+  // by extension (".off", ".pn", ".ply" for store); throws Exception on
+  // an unknown format or an I/O failure (reference Mesh::load / store)
+  void load(const std::string& path);
+  void store(const std::string& path) const;
 
  private:
   std::vector<Vec3f> P_, N_;

@@ -255,10 +255,27 @@ int32_t gm_server_pending(gm_server* srv);
 /* The resident closed grid (device, res^3 bytes). */
 const uint8_t* gm_server_closing(gm_server* srv);
 long long gm_server_kernel_launches(gm_server* srv);
+/* Snapshot / restore of the resident state (the closed grid, res^3 bytes,
+ * and the radius field, (2 res)^3 bytes) through host buffers; either
+ * snapshot buffer may be NULL.  Both need an idle server (no edit queued or
+ * on the GPU: GM_ERR_NOT_READY otherwise).  The input grid stays the
+ * caller's.  A restored field above the server's radius bound is copied but
+ * answered with GM_ERR_CAPACITY. */
+gm_status gm_server_snapshot(gm_server* srv, uint8_t* h_closing, int8_t* h_scale);
+gm_status gm_server_restore(gm_server* srv, const uint8_t* h_closing, const int8_t* h_scale);
 /* Per-kernel device time of the server's launches (CUDA events around each
  * launch on its slot stream), same JSON form as gm_ctx_profile_read. */
 gm_status gm_server_profile(gm_server* srv, int32_t enable);
 int64_t gm_server_profile_read(gm_server* srv, char* buf, int64_t cap);
+
+/* Host mesh file output, format by extension: ".off" (the reference's
+ * Mesh::storeOFF text form, Common/Mesh.h:627-637), ".pn" (float32
+ * position + normal per vertex, the reference's PN form) or ".ply" (binary
+ * little-endian: float x y z nx ny nz, uchar-count uint faces).  N may be
+ * NULL for OFF.  With drop_unused, vertices no triangle uses are left out
+ * (indices renumbered), as for a served patch. */
+gm_status gm_mesh_store(const char* path, const float* V, const float* N, int64_t nv, const uint32_t* T, int64_t nt,
+                        int32_t drop_unused);
 
 /* ---------------------------------------------------------------- a18 */
 /* BVH over the set fine voxels of a packed grid (BVH::BuildFromSEList,

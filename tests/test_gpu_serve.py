@@ -130,3 +130,37 @@ def test_patch_matches_full_mesh(gm_ctx):
     assert len(tri_patch) > 1000
     assert diff <= 4 * n91, (diff, n91)
     srv.destroy()
+
+
+def test_snapshot_restore_and_patch_export(tmp_path):
+    """A server restored from a snapshot continues exactly like the original;
+    a patch exports as OFF with only the vertices its triangles use."""
+    import torch
+    edits = _edits(128, n=6, seed=21)
+    desc, X, R, C, results, srv = _run(2, edits[:3])
+    Cs, Rs = srv.snapshot()
+    p = tmp_path / "patch.off"
+    exported = None
+    for c, scale, support, mode in edits[3:]:
+        srv.submit(c, scale, support, 0.0, mode)
+        for r in srv.drain():
+            if r["patch_triangles"] > 0:
+                srv.export_patch(r, p)  # while its slot still holds it
+                exported = r
+    Ca = srv.closing().clone()
+    desc2, X2, R2 = _setup(128)
+    srv2 = api.Server(desc2, X2, R2, slots=2, max_crop_res=96, rmax=8, mode=L.GM_REF)
+    srv2.restore(Cs, Rs)
+    for c, scale, support, mode in edits[3:]:
+        srv2.submit(c, scale, support, 0.0, mode)
+    srv2.drain()
+    torch.cuda.synchronize()
+    assert torch.equal(srv2.closing(), Ca)
+    assert torch.equal(R2, R)
+    r = exported
+    assert r is not None
+    tok = open(p).read().split()
+    nv, nf = int(tok[1]), int(tok[2])
+    assert nf == r["patch_triangles"] and 0 < nv <= r["patch_vertices"]
+    srv.destroy()
+    srv2.destroy()
