@@ -176,27 +176,34 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
         if (R != nullptr)
           rq = clamp_radius(R[fine_index(x, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)]);
         site_pos[base + k] = ((uint32_t)r << 16) | (uint32_t)x;
-        site_u[base + k] = K - 4u * (uint32_t)((rq - 1) * (rq - 1));
+        // offset K - 4 (r-1)^2 (< 2^16) and the site's reach r - 1 (a point
+        // at |q - p| >= r(q) is never eroded by q: e >= 2 (r(q) - 1))
+        const int reach = rq - 1 < halo ? rq - 1 : halo;
+        site_u[base + k] = (K - 4u * (uint32_t)((rq - 1) * (rq - 1))) | ((uint32_t)reach << 16);
         k++;
       }
     }
     __syncthreads();
     const int ns = nsites;
-    const int taps = 2 * halo + 1;
-    for (int i = threadIdx.x; i < ns * taps; i += blockDim.x) {
-      const int sidx = i / taps, dq = i - sidx * taps - halo;
+    // one warp per site, lanes over its 2 reach + 1 taps
+    const int lane = threadIdx.x & 31;
+    for (int sidx = threadIdx.x >> 5; sidx < ns; sidx += blockDim.x >> 5) {
       const uint32_t sp = site_pos[sidx];
       const int r = (int)(sp >> 16), q = (int)(sp & 0xffffu);
-      const uint32_t u = site_u[sidx];
-      const int p = q - dq;  // output position, delta = q - p = dq
-      if (p < 0 || p >= N) continue;
-      const int ec = center_dist2(dq);
-      const uint32_t vc = u + (uint32_t)(ec * ec);
-      if (vc < K) atomicMin(&hc[r * N + p], vc);
-      if (p & 1) {
-        const int el = 2 * lattice_dist(dq);
-        const uint32_t vl = u + (uint32_t)(el * el);
-        if (vl < K) atomicMin(&hl[r * res + (p >> 1)], vl);
+      const uint32_t su = site_u[sidx];
+      const uint32_t u = su & 0xffffu;
+      const int reach = (int)(su >> 16);
+      for (int dq = lane - reach; dq <= reach; dq += 32) {
+        const int p = q - dq;  // output position, delta = q - p = dq
+        if (p < 0 || p >= N) continue;
+        const int ec = center_dist2(dq);
+        const uint32_t vc = u + (uint32_t)(ec * ec);
+        if (vc < K) atomicMin(&hc[r * N + p], vc);
+        if (p & 1) {
+          const int el = 2 * lattice_dist(dq);
+          const uint32_t vl = u + (uint32_t)(el * el);
+          if (vl < K) atomicMin(&hl[r * res + (p >> 1)], vl);
+        }
       }
     }
     __syncthreads();
@@ -475,11 +482,38 @@ size_t dpx_smem_bytes(int sub, int halo) {
   return (size_t)2 * span * 32 * sizeof(uint32_t);
 }
 
+// Radius bound of one tile of a dilation pass, from the map of the largest
+// raw radius per 16^3 fine voxels: over the tile's x columns and outputs,
+// and its two third-axis coordinates widened by `rext` (the y pass feeds z
+// outputs up to a halo away).  Block-uniform.
+__device__ int tile_radius(const uint8_t* __restrict__ rmap, int mb, int nx, int n3, int axis, int nout, int o0,
+                           int rext) {
+  __shared__ int rt_s;
+  if (threadIdx.x == 0) rt_s = 0;
+  __syncthreads();
+  const int xa = (blockIdx.x * kDpxCols) >> 4, xb = (min(blockIdx.x * kDpxCols + kDpxCols, nx) - 1) >> 4;
+  const int aa = o0 >> 4, ab = (min(o0 + kDpxOut, nout) - 1) >> 4;
+  const int ta = max(2 * (int)blockIdx.z - rext, 0) >> 4, tb = min(2 * (int)blockIdx.z + 1 + rext, n3 - 1) >> 4;
+  const int cx = xb - xa + 1, ca = ab - aa + 1, ct = tb - ta + 1;
+  int m = 0;
+  for (int i = threadIdx.x; i < cx * ca * ct; i += blockDim.x) {
+    const int ix = xa + i % cx, ia = aa + (i / cx) % ca, it = ta + i / (cx * ca);
+    const int my = axis == 1 ? ia : it, mz = axis == 1 ? it : ia;
+    const int v = rmap[ix + (int64_t)mb * (my + (int64_t)mb * mz)];
+    m = v > m ? v : m;
+  }
+  for (int o = 16; o > 0; o >>= 1) { const int t = __shfl_xor_sync(0xffffffffu, m, o); m = t > m ? t : m; }
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(&rt_s, m);
+  __syncthreads();
+  return clamp_radius(rt_s);
+}
+
 template <int G, typename TIn, int FIN>
 __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
                                                   int sub, int halo, uint32_t cap, const int8_t* __restrict__ R,
-                                                  int uniform_r, int res) {
+                                                  int uniform_r, int res, const uint8_t* __restrict__ rmap, int mb,
+                                                  int rext) {
   extern __shared__ uint32_t tileu[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tpar = w >> 2, grp = w & 3;
@@ -494,11 +528,22 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
   const int step = sub ? 2 : 1;
   const int lo = (sub ? 2 * o0 + 1 : o0) - halo;
   const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
+  // Dilation passes with a radius field use the tile's own radius bound:
+  // a smaller window (halo_e) and saturation value (cap_e).  Every output
+  // that reads this tile has r(p) <= rt, so terms >= (rt+1)^2 never decide.
+  int halo_e = halo;
+  if (rmap != nullptr && step == 1) {
+    const int rt = tile_radius(rmap, mb, nx, n3, axis, nout, o0, rext);
+    const uint32_t ct = G == KERN_CUBE ? (uint32_t)(rt + 1) : (uint32_t)((rt + 1) * (rt + 1));
+    cap = ct < cap ? ct : cap;
+    halo_e = rt + 2 < halo ? rt + 2 : halo;
+  }
+  const int skip = halo - halo_e;  // tile rows never read
   const uint32_t capp = cap | (cap << 16);
   uint32_t* tile = tileu + tpar * span * 32;
   const bool colok = x < nx && third < n3;
   int finite = 0;
-  for (int s = grp; s < span; s += 4) {
+  for (int s = skip + grp; s < span - skip; s += 4) {
     const int a = lo + s;
     uint32_t v = capp;
     if (colok && a >= 0 && a < na) v = load_pair<G, TIn>(in + x + sa * a + s3 * third, cap);
@@ -513,6 +558,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     // Register sliding windows: wp[(j + k) % 16] holds tile row sp0 + j + k
     // and wm[(j - k) mod 16] holds row sp0 + j - k, so that after tap k only
     // one new row per side is loaded (into the slot its leaving row frees).
+    // Rows read: sp0 - halo_e .. sp0 + 15 + halo_e, inside [skip, span - skip).
     const uint32_t* tcol = tile + lane;
     uint32_t wp[kDpxPer], wm[kDpxPer];
 #pragma unroll
@@ -523,20 +569,21 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     const uint32_t g0 = gpair<G>(0, cap);
 #pragma unroll
     for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tcol[(sp0 + j) * 32], g0, capp);
-    for (int kb = 0; kb <= halo; kb += kDpxPer) {
+    for (int kb = 0; kb <= halo_e; kb += kDpxPer) {
 #pragma unroll
       for (int u = 0; u < kDpxPer; u++) {
         const int k = kb + u;
         if (k == 0) continue;
-        if (k > halo) goto dpx_done;
+        if (k > halo_e) goto dpx_done;
         const uint32_t gp = gpair<G>(k, cap), gm_ = gpair<G>(-k, cap);
 #pragma unroll
         for (int j = 0; j < kDpxPer; j++) {
           best[j] = step_min<G>(wp[(j + u) % kDpxPer], gp, best[j]);
           best[j] = step_min<G>(wm[(j - u + kDpxPer) % kDpxPer], gm_, best[j]);
         }
+        if (k == halo_e) goto dpx_done;  // no further tap: load nothing past the window
         // rows sp0 + k + 16 and sp0 - k - 1 enter; the slots of rows
-        // sp0 + k and sp0 + 15 - k are free now (k <= halo keeps both in the tile)
+        // sp0 + k and sp0 + 15 - k are free now (k < halo_e keeps both in the window)
         wp[u] = tcol[(sp0 + k + kDpxPer) * 32];
         wm[(kDpxPer - 1 - u) % kDpxPer] = tcol[(sp0 - k - 1) * 32];
         if (u & 1) {
@@ -652,7 +699,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
 template <int G, typename TIn, int FIN>
 static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
                        int halo, uint32_t cap, const int8_t* R, int uniform_r, int res, cudaStream_t st,
-                       KernelCounter* kc, const char* name) {
+                       KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0) {
   const size_t smem = dpx_smem_bytes(sub, halo);
   static size_t configured = 0;
   if (smem > 48 * 1024 && smem > configured) {
@@ -665,7 +712,39 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, (n3 + 1) / 2);
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
-                                                          uniform_r, res));
+                                                          uniform_r, res, rmap, nx >> 4, rext));
+}
+
+// Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
+// field of edge n (a multiple of 16): one block per map cell, one 16-byte
+// row segment per thread.
+__global__ void __launch_bounds__(256) k_radius_map(const int8_t* __restrict__ R, int n, int mb,
+                                                     uint8_t* __restrict__ out) {
+  const int b = blockIdx.x;
+  const int bx = b % mb, by = (b / mb) % mb, bz = b / (mb * mb);
+  const int fy = 16 * by + (threadIdx.x & 15), fz = 16 * bz + (threadIdx.x >> 4);
+  const uint4 v = *reinterpret_cast<const uint4*>(R + fine_index(16 * bx, fy, fz, n));
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  int m = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) m = max(m, (int)(int8_t)((w[k] >> (8 * j)) & 0xffu));
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ int wm[8];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int k = 0; k < 8; k++) t = max(t, wm[k]);
+    out[b] = (uint8_t)t;
+  }
+}
+
+cudaError_t launch_radius_map(const int8_t* R, int n, uint8_t* out, cudaStream_t st, KernelCounter* kc) {
+  const int mb = n / 16;
+  GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<mb * mb * mb, 256, 0, st>>>(R, n, mb, out));
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------
@@ -950,8 +1029,8 @@ static int grid_stride_blocks(int64_t n, int threads, int sms) {
 
 size_t close_workspace_bytes(int res) {
   const size_t N = 2 * (size_t)res, V = N * N * N, cells = (size_t)res * res * res;
-  // buf16 x2, buf8, HL1, HL2, Df, Eb, Ef, S, D + slack for alignment
-  return 2 * V * 2 + V + (size_t)res * N * N * 2 + (size_t)res * res * N * 2 + 5 * cells + 16 * 256;
+  // buf16 x2, buf8, HL1, HL2, Df, Eb, Ef, S, D, radius map + slack for alignment
+  return 2 * V * 2 + V + (size_t)res * N * N * 2 + (size_t)res * res * N * 2 + 5 * cells + V / 4096 + 16 * 256;
 }
 
 static inline uint8_t* carve(uint8_t*& p, size_t bytes) {
@@ -974,6 +1053,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   uint8_t* Ef = carve(p, cells);
   uint8_t* S = carve(p, cells);
   uint8_t* D = a.D_out != nullptr ? a.D_out : carve(p, cells);
+  uint8_t* rmap = carve(p, V / 4096);
   const int rmax = a.rmax;
   DataRes dr{{a.data_res[0], a.data_res[1], a.data_res[2]}};
   const bool exact = a.mode == 1;
@@ -983,6 +1063,11 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const int dcap = (a.se == 1 ? rmax + 2 : dil_r + 1) < 255 ? (a.se == 1 ? rmax + 2 : dil_r + 1) : 255;
   const uint32_t dil_cap = a.se == 1 ? (uint32_t)(rmax + 1) : (uint32_t)(dil_r * dil_r);
   const int dil_halo = dil_r + 1;
+  const uint8_t* tile_map = nullptr;  // per-tile radius bounds of the dilation passes
+  if (a.R != nullptr) {
+    if (launch_radius_map(a.R, N, rmap, st, kc) != cudaSuccess) return cudaGetLastError();
+    tile_map = rmap;
+  }
   {
     const int W = N >> 5;
     GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x<<<dim3(res, res), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, res, dcap));
@@ -990,14 +1075,14 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     if (dil_cap <= 32767) {
       if (a.se == 1) {
         launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, nullptr, 0, res, st,
-                                          kc, "k_pass_dil_y");
+                                          kc, "k_pass_dil_y", tile_map, dil_halo);
         launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, N, N, N, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r,
-                                           res, st, kc, "k_pass_dil_z");
+                                           res, st, kc, "k_pass_dil_z", tile_map, 0);
       } else {
         launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, nullptr, 0, res, st,
-                                         kc, "k_pass_dil_y");
+                                         kc, "k_pass_dil_y", tile_map, dil_halo);
         launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, N, N, N, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r, res,
-                                          st, kc, "k_pass_dil_z");
+                                          st, kc, "k_pass_dil_z", tile_map, 0);
       }
     } else {
       const int span = kTileOut + 2 * dil_halo;
