@@ -26,6 +26,10 @@ GM_HD int64_t cell_index(int x, int y, int z, int res) {
 GM_HD int64_t fine_index(int x, int y, int z, int n) {
   return (int64_t)x + (int64_t)n * y + (int64_t)n * n * z;
 }
+// x-fastest index in a box of nx * ny * (any) elements
+GM_HD int64_t idx3(int x, int y, int z, int nx, int ny) {
+  return (int64_t)x + (int64_t)nx * y + (int64_t)nx * ny * z;
+}
 GM_HD int child_bit(int x, int y, int z) { return (x & 1) | ((y & 1) << 1) | ((z & 1) << 2); }
 
 // Morton code with 10 bits per axis, x in bit 0 (GMorpho/cuda_math.h:111-117,

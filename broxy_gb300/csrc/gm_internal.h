@@ -46,7 +46,8 @@ int64_t profile_json(KernelCounter& kc, char* buf, int64_t cap);
   } while (0)
 
 struct CloseArgs {
-  int res;            // base resolution (power of two, >= 16)
+  int res;            // base resolution of a cubic grid (a multiple of 16)
+  int dims[3] = {0, 0, 0};  // box grid rx, ry, rz (multiples of 16) when dims[0] > 0; res is then unused
   int data_res[3];    // cells with data (GMorpho/Voxelizer.cu:453-454)
   const uint8_t* X;   // input packed grid, res^3
   const int8_t* R;    // fine radius grid (2res)^3, or nullptr for uniform_r
@@ -62,6 +63,7 @@ struct CloseArgs {
 };
 
 size_t close_workspace_bytes(int res);
+size_t close_workspace_bytes_box(int rx, int ry, int rz);
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc);
@@ -80,7 +82,8 @@ cudaError_t launch_pyramid(const uint8_t* grid, const int8_t* R, int uniform_r, 
 
 // ---------------------------------------------------------------- mesh
 struct MeshArgs {
-  int res;
+  int res;              // cubic grid edge (cells), unless dims[0] > 0
+  int dims[3] = {0, 0, 0};  // box grid rx, ry, rz (multiples of 16) when dims[0] > 0
   const uint8_t* C;     // closed grid
   float bbox_min[3];
   float cell_size;      // base cell size (fine = cell_size / 2)

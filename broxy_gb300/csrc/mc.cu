@@ -48,22 +48,26 @@ __device__ __forceinline__ void brick_origin(int b, int& ox, int& oy, int& oz) {
   oz = (int)gather_bits3((uint32_t)b >> 2) * kBrick;
 }
 
-__device__ void load_tile(const uint8_t* __restrict__ C, int res, int ox, int oy, int oz, uint8_t* tile) {
+// grid dimensions in cells (x, y, z); x-fastest
+struct GDims { int x, y, z; };
+__device__ __forceinline__ int64_t gidx(int x, int y, int z, GDims d) { return idx3(x, y, z, d.x, d.y); }
+
+__device__ void load_tile(const uint8_t* __restrict__ C, GDims d, int ox, int oy, int oz, uint8_t* tile) {
   for (int i = threadIdx.x; i < kTileCells; i += blockDim.x) {
     const int lx = i % kTileE, ly = (i / kTileE) % kTileE, lz = i / (kTileE * kTileE);
     const int x = ox + lx, y = oy + ly, z = oz + lz;
-    tile[i] = (x < res && y < res && z < res) ? C[cell_index(x, y, z, res)] : (uint8_t)0;
+    tile[i] = (x < d.x && y < d.y && z < d.z) ? C[gidx(x, y, z, d)] : (uint8_t)0;
   }
 }
 
 // Loads the tile and tells (block-uniformly) whether it can hold a mixed
 // cube: a tile whose bytes are all 0x00 or all 0xff has none.
-__device__ bool load_tile_mixed(const uint8_t* __restrict__ C, int res, int ox, int oy, int oz, uint8_t* tile) {
+__device__ bool load_tile_mixed(const uint8_t* __restrict__ C, GDims d, int ox, int oy, int oz, uint8_t* tile) {
   int seen0 = 0, seen1 = 0, part = 0;
   for (int i = threadIdx.x; i < kTileCells; i += blockDim.x) {
     const int lx = i % kTileE, ly = (i / kTileE) % kTileE, lz = i / (kTileE * kTileE);
     const int x = ox + lx, y = oy + ly, z = oz + lz;
-    const uint8_t v = (x < res && y < res && z < res) ? C[cell_index(x, y, z, res)] : (uint8_t)0;
+    const uint8_t v = (x < d.x && y < d.y && z < d.z) ? C[gidx(x, y, z, d)] : (uint8_t)0;
     tile[i] = v;
     seen0 |= v == 0x00;
     seen1 |= v == 0xff;
@@ -122,7 +126,7 @@ __device__ __forceinline__ bool cell_uniform(const uint8_t* tile, int lx, int ly
 }
 
 // Tagging / emission window of one meshing run.  A whole grid is its own
-// window: off = 0, gres = res, tag and emit boxes = [0, res).  The edit
+// window: off = 0, gdim = its size, tag and emit boxes = the whole grid.  The edit
 // server meshes the dirty box of a crop: the crop's cells sit at global
 // cells off + local, the border rule uses the global resolution, cubes are
 // tagged (own vertices) in the dirty box plus one cell on the + side (the
@@ -130,7 +134,7 @@ __device__ __forceinline__ bool cell_uniform(const uint8_t* tile, int lx, int ly
 // from the dirty box only.
 struct McWin {
   int off[3];
-  int gres;
+  int gdim[3];         // global grid (cells): cubes of cells outside [1, gdim-2] are never tagged
   int tlo[3], thi[3];  // local cells whose cubes may be tagged, [lo, hi)
   int elo[3], ehi[3];  // local cells whose cubes emit triangles, [lo, hi)
 };
@@ -139,7 +143,7 @@ struct McWin {
 // Grid.cu:1334-1340)
 __device__ __forceinline__ bool win_tag(const McWin& w, int x, int y, int z) {
   const int gx = x + w.off[0], gy = y + w.off[1], gz = z + w.off[2];
-  return gx >= 1 && gy >= 1 && gz >= 1 && gx <= w.gres - 2 && gy <= w.gres - 2 && gz <= w.gres - 2 &&
+  return gx >= 1 && gy >= 1 && gz >= 1 && gx <= w.gdim[0] - 2 && gy <= w.gdim[1] - 2 && gz <= w.gdim[2] - 2 &&
          x >= w.tlo[0] && y >= w.tlo[1] && z >= w.tlo[2] && x < w.thi[0] && y < w.thi[1] && z < w.thi[2];
 }
 __device__ __forceinline__ bool win_emit(const McWin& w, int x, int y, int z) {
@@ -214,12 +218,12 @@ __device__ __forceinline__ CellCounts block_exclusive_scan(CellCounts v, CellCou
                     wpre[3] + inc[3] - a[3]};
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, int res, McWin w,
+__global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                           uint32_t* __restrict__ brick_tot) {
   __shared__ uint8_t tile[kTileCells];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, res, ox, oy, oz, tile)) {
+  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) {
     if (threadIdx.x < 4) brick_tot[4 * blockIdx.x + threadIdx.x] = 0;
     return;
   }
@@ -286,7 +290,7 @@ __device__ __forceinline__ float lerp_coord(float p1, float p2, float v1, float 
   return __fadd_rn(p1, __fdiv_rn(__fmul_rn(t, __fsub_rn(p2, p1)), __fsub_rn(v2, v1)));
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, int res, McWin w,
+__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                              const uint32_t* __restrict__ brick_off,
                                                              uint32_t* __restrict__ cell_voff,
                                                              float* __restrict__ V, float bx, float by, float bz,
@@ -294,7 +298,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
   __shared__ uint8_t tile[kTileCells];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, res, ox, oy, oz, tile)) return;
+  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) return;
   CellCounts acc{0, 0, 0, 0};
   for (int i = 0; i < kCellsPerThread; i++) {
     const int l = threadIdx.x * kCellsPerThread + i;
@@ -321,7 +325,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
     const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
     const int m = mixed_mask(vals, win_tag(w, gx, gy, gz));
     if (!m) continue;
-    cell_voff[cell_index(gx, gy, gz, res)] = vo;
+    cell_voff[gidx(gx, gy, gz, gd)] = vo;
     for (int s = 0; s < 8; s++) {
       if (!((m >> s) & 1)) continue;
       const int v = vals[s];
@@ -394,7 +398,7 @@ __device__ __forceinline__ long long cube_voff(uint32_t info, uint32_t cell_off,
   return (long long)off;
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __restrict__ C, int res, McWin w,
+__global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                               const uint32_t* __restrict__ brick_off,
                                                               const uint32_t* __restrict__ cell_voff,
                                                               uint32_t* __restrict__ T, uint32_t nt_total,
@@ -403,7 +407,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
   __shared__ uint32_t info[kInfoE * kInfoE * kInfoE];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
-  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, res, ox, oy, oz, tile)) return;
+  if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) return;
   for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) {
     const int lx = i % kInfoE, ly = (i / kInfoE) % kInfoE, lz = i / (kInfoE * kInfoE);
     info[i] = cell_info(tile, lx, ly, lz, win_tag(w, ox + lx, oy + ly, oz + lz));
@@ -434,7 +438,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
     if (!win_emit(w, gx, gy, gz)) continue;
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    uint32_t vo = cell_voff[cell_index(gx, gy, gz, res)];
+    uint32_t vo = cell_voff[gidx(gx, gy, gz, gd)];
     for (int s = 0; s < 8; s++) {
       if (!((m >> s) & 1)) continue;
       const int v = vals[s];
@@ -459,7 +463,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
         const uint32_t ninfo = info[cx + kInfoE * (cy + kInfoE * cz)];
         const int k = (nfx & 1) | ((nfy & 1) << 1) | ((nfz & 1) << 2);
         if (!((ninfo >> k) & 1)) { e0 = e3 = 0; return -1; }
-        return cube_voff(ninfo, cell_voff[cell_index(nfx >> 1, nfy >> 1, nfz >> 1, res)], k, e0, e3);
+        return cube_voff(ninfo, cell_voff[gidx(nfx >> 1, nfy >> 1, nfz >> 1, gd)], k, e0, e3);
       };
       int a0 = 0, a3 = 0;
       if (em & (2 | 512)) {
@@ -810,32 +814,41 @@ void MeshBuffers::release() {
 // Bricks are visited in Morton order over the smallest power-of-two cube of
 // bricks covering the grid; bricks outside the grid or the tag box return
 // at once.
-static int brick_count(int res) {
+static int brick_count(const int d[3]) {
+  const int m = d[0] > d[1] ? (d[0] > d[2] ? d[0] : d[2]) : (d[1] > d[2] ? d[1] : d[2]);
   int p = kBrick;
-  while (p < res) p *= 2;
+  while (p < m) p *= 2;
   const int e = p / kBrick;
   return e * e * e;
 }
 
+static void grid_dims(const MeshArgs& a, int d[3]) {
+  for (int k = 0; k < 3; k++) d[k] = a.dims[0] > 0 ? a.dims[k] : a.res;
+}
+
 static McWin window_of(const MeshArgs& a) {
   McWin w;
+  int d[3];
+  grid_dims(a, d);
   const bool crop = a.gres > 0;
-  w.gres = crop ? a.gres : a.res;
   for (int k = 0; k < 3; k++) {
+    w.gdim[k] = crop ? a.gres : d[k];
     w.off[k] = crop ? a.off[k] : 0;
     w.tlo[k] = crop ? a.tag_lo[k] : 0;
-    w.thi[k] = crop ? a.tag_hi[k] : a.res;
+    w.thi[k] = crop ? a.tag_hi[k] : d[k];
     w.elo[k] = crop ? a.emit_lo[k] : 0;
-    w.ehi[k] = crop ? a.emit_hi[k] : a.res;
+    w.ehi[k] = crop ? a.emit_hi[k] : d[k];
   }
   return w;
 }
 
 cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
                               uint32_t* h_tot4) {
-  const int res = a.res;
-  const int64_t cells = (int64_t)res * res * res;
-  const int nb = brick_count(res);
+  int d[3];
+  grid_dims(a, d);
+  const GDims gd{d[0], d[1], d[2]};
+  const int64_t cells = (int64_t)d[0] * d[1] * d[2];
+  const int nb = brick_count(d);
   cudaError_t e;
   if (nb + 1 > b.bricks_cap) {
     if (b.brick_tot) cudaFree(b.brick_tot);
@@ -851,7 +864,7 @@ cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st
     if (e != cudaSuccess) return e;
     b.cells_cap = cells;
   }
-  GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, res, window_of(a), b.brick_tot));
+  GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, gd, window_of(a), b.brick_tot));
   GM_LAUNCH(kc, "k_scan_bricks", st, k_scan_bricks<<<1, 1024, 0, st>>>(b.brick_tot, nb));
   return cudaMemcpyAsync(h_tot4, b.brick_tot + 4 * (size_t)nb, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
 }
@@ -885,8 +898,10 @@ cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, Kerne
 
 cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt, cudaStream_t st,
                       KernelCounter* kc) {
-  const int res = a.res;
-  const int nb = brick_count(res);
+  int d[3];
+  grid_dims(a, d);
+  const GDims gd{d[0], d[1], d[2]};
+  const int nb = brick_count(d);
   const McWin w = window_of(a);
   cudaError_t e;
   // per-vertex buffers share one capacity, per-triangle buffers another
@@ -920,9 +935,9 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   }
   const float cs = 0.5f * a.cell_size;  // exact: scaling by a power of two
   cudaMemsetAsync(b.fix, 0, sizeof(uint32_t), st);
-  GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, res, w, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],
+  GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],
                                            a.bbox_min[2], cs, a.isovalue));
-  GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, 0, st>>>(a.C, res, w, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
+  GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, 0, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
                                             b.fix_cap));
   GM_LAUNCH(kc, "k_mc_fix91", st, k_mc_fix91<<<1, 256, 0, st>>>(b.fix, b.fix_cap, b.T));
   if (nv == 0 || nt == 0) return cudaGetLastError();

@@ -37,13 +37,13 @@ namespace gm {
 // then the corner sets L = bits | bits << 1 (the lattice points that bound
 // an occupied voxel), then the nearest set bit of L for every x.
 __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ X, uint8_t* __restrict__ A,
-                                                    int res, int dcap) {
+                                                    int rx, int ry, int dcap) {
   extern __shared__ uint32_t sm_words[];
-  const int N = 2 * res, W = N >> 5;
+  const int N = 2 * rx, Ny = 2 * ry, W = N >> 5;
   const int cy = blockIdx.x, cz = blockIdx.y;
   uint32_t* bits = sm_words;            // [4][W]
   uint32_t* corner = sm_words + 4 * W;  // [4][W]
-  const uint8_t* row = X + (int64_t)res * cy + (int64_t)res * res * cz;
+  const uint8_t* row = X + idx3(0, cy, cz, rx, ry);
   int any = 0, all = 1;
   // word w of a fine row covers bytes 16w .. 16w+15 of the byte row
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
     const uint32_t v = !any ? (uint32_t)dcap * 0x01010101u : 0u;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {  // 4 rows x N/4 words
       const int r = i / (N >> 2), p4 = 4 * (i - r * (N >> 2));
-      *reinterpret_cast<uint32_t*>(A + fine_index(p4, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)) = v;
+      *reinterpret_cast<uint32_t*>(A + idx3(p4, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)) = v;
     }
     return;
   }
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
       if (d > dcap) d = dcap;
       packed |= (uint32_t)d << (8 * j);
     }
-    *reinterpret_cast<uint32_t*>(A + fine_index(p4, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)) = packed;
+    *reinterpret_cast<uint32_t*>(A + idx3(p4, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)) = packed;
   }
 }
 
@@ -128,10 +128,11 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
 // contribution u(q) + e(q - p)^2 to the outputs within reach with shared
 // atomicMin, instead of every output scanning the window.
 __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ S, const int8_t* __restrict__ R,
-                                                    int uniform_r, int res, int halo, uint32_t K,
+                                                    int uniform_r, int rx, int ry, int halo, uint32_t K,
                                                     uint16_t* __restrict__ HC, uint16_t* __restrict__ HL) {
   extern __shared__ uint32_t sm_words[];
-  const int N = 2 * res, W = N >> 5;
+  const int res = rx;  // cells along x
+  const int N = 2 * rx, Ny = 2 * ry, W = N >> 5;
   const int cy = blockIdx.x, cz = blockIdx.y;
   uint32_t* bits = sm_words;              // [4][W]
   uint32_t* hc = sm_words + 4 * W;        // [4][N] centre outputs
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
   uint32_t* site_pos = hl + 4 * res;      // compacted sites: (row << 16) | x
   uint32_t* site_u = site_pos + 4 * N;    // their offsets K - 4 (r-1)^2
   __shared__ int nsites;
-  const uint8_t* row = S + (int64_t)res * cy + (int64_t)res * res * cz;
+  const uint8_t* row = S + idx3(0, cy, cz, rx, ry);
   if (threadIdx.x == 0) nsites = 0;
   __syncthreads();
   int any = 0;
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
         m &= m - 1;
         int rq = ru;
         if (R != nullptr)
-          rq = clamp_radius(R[fine_index(x, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)]);
+          rq = clamp_radius(R[idx3(x, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)]);
         site_pos[base + k] = ((uint32_t)r << 16) | (uint32_t)x;
         // offset K - 4 (r-1)^2 (< 2^16) and the site's reach r - 1 (a point
         // at |q - p| >= r(q) is never eroded by q: e >= 2 (r(q) - 1))
@@ -212,13 +213,12 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
   for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) {
     const int r = i / (N >> 1), p2 = 2 * (i - r * (N >> 1));
     const uint32_t v = any ? (hc[r * N + p2] | (hc[r * N + p2 + 1] << 16)) : (K | (K << 16));
-    *reinterpret_cast<uint32_t*>(HC + fine_index(p2, 2 * cy + (r & 1), 2 * cz + (r >> 1), N)) = v;
+    *reinterpret_cast<uint32_t*>(HC + idx3(p2, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)) = v;
   }
   for (int i = threadIdx.x; i < 2 * res; i += blockDim.x) {
     const int r = i / (res >> 1), c2 = 2 * (i - r * (res >> 1));
     const uint32_t v = any ? (hl[r * res + c2] | (hl[r * res + c2 + 1] << 16)) : (K | (K << 16));
-    *reinterpret_cast<uint32_t*>(HL + (int64_t)c2 + (int64_t)res * (2 * cy + (r & 1)) +
-                                 (int64_t)res * N * (2 * cz + (r >> 1))) = v;
+    *reinterpret_cast<uint32_t*>(HL + idx3(c2, 2 * cy + (r & 1), 2 * cz + (r >> 1), rx, Ny)) = v;
   }
 }
 
@@ -320,10 +320,10 @@ enum Fin { FIN_DIL = 0, FIN_ERO = 1 };
 
 template <int G, int F>
 __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in, uint8_t* __restrict__ out_cells,
-                                                 const int8_t* __restrict__ R, int uniform_r, int res, int halo,
-                                                 uint32_t cap) {
+                                                 const int8_t* __restrict__ R, int uniform_r, int rx, int ry, int rz,
+                                                 int halo, uint32_t cap) {
   extern __shared__ uint16_t tile2[];  // [2][span][32]
-  const int N = 2 * res;
+  const int Nx = 2 * rx, Ny = 2 * ry, N = 2 * rz;  // N: fine extent along the pass axis z
   const int tx = threadIdx.x, yp = threadIdx.y & 1, zg = threadIdx.y >> 1;
   const int x = blockIdx.x * 32 + tx;
   const int y = 2 * blockIdx.z + yp;
@@ -335,8 +335,8 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
   for (int s = zg; s < span; s += 4) {
     const int a = lo + s;
     uint16_t v = (uint16_t)cap;
-    if (x < N && a >= 0 && a < N) {
-      const uint32_t t = in[fine_index(x, y, a, N)];
+    if (x < Nx && a >= 0 && a < N) {
+      const uint32_t t = in[idx3(x, y, a, Nx, Ny)];
       v = (uint16_t)(t < cap ? t : cap);
     }
     tile[s * 32 + tx] = v;
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
   // each thread: 16 consecutive z = z0 + 16 zg + j
   uint32_t bits = 0;
   const int ru = clamp_radius(uniform_r);
-  if (x < N) {
+  if (x < Nx) {
 #pragma unroll 1
     for (int j = 0; j < 16; j++) {
       const int z = z0 + 16 * zg + j;
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
       const uint32_t v = column_min<G>(tile + tx, z - lo, span, halo);
       bool b;
       if (F == FIN_DIL) {
-        const int r = R != nullptr ? clamp_radius(R[fine_index(x, y, z, N)]) : ru;
+        const int r = R != nullptr ? clamp_radius(R[idx3(x, y, z, Nx, Ny)]) : ru;
         if (G == KERN_CUBE) b = v <= (uint32_t)r;
         else b = v < (uint32_t)((r + 1) * (r + 1));
       } else {
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
   ex[yp][zg][tx][1] = packed_hi;
   __syncthreads();
   (void)ybits;
-  if (yp == 0 && (tx & 1) == 0 && x < N) {
+  if (yp == 0 && (tx & 1) == 0 && x < Nx) {
     const uint32_t w0 = packed | ex[1][zg][tx][0];
     const uint32_t w1 = packed_hi | ex[1][zg][tx][1];
     const int cx = x >> 1, cyy = y >> 1;
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
       const int zc = (z0 + 16 * zg) / 2 + q;
       if (2 * zc > z_last) break;
       const uint32_t byte = q < 4 ? (w0 >> (8 * q)) & 0xffu : (w1 >> (8 * (q - 4))) & 0xffu;
-      out_cells[cell_index(cx, cyy, zc, res)] = (uint8_t)byte;
+      out_cells[idx3(cx, cyy, zc, rx, ry)] = (uint8_t)byte;
     }
   }
 }
@@ -399,30 +399,30 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
 // final z pass of the base erosion: lattice points 2c+1 only; one flag byte
 // per base cell (1 = the cell centre is eroded).
 __global__ void __launch_bounds__(256) k_final_z_base(const uint16_t* __restrict__ in, uint8_t* __restrict__ flags,
-                                                      int res, int halo, uint32_t cap) {
+                                                      int rx, int ry, int rz, int halo, uint32_t cap) {
   extern __shared__ uint16_t tile[];
-  const int N = 2 * res;
+  const int N = 2 * rz;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x = blockIdx.x * 32 + tx;  // cx
   const int cyy = blockIdx.z;
   const int o0 = blockIdx.y * kTileOut;
-  const int o_last = min(o0 + kTileOut, res) - 1;
+  const int o_last = min(o0 + kTileOut, rz) - 1;
   const int lo = 2 * o0 + 1 - halo;
   const int span = 2 * o_last + 1 + halo - lo + 1;
   for (int s = ty; s < span; s += kRows) {
     const int a = lo + s;
     uint16_t v = (uint16_t)cap;
-    if (x < res && a >= 0 && a < N) {
-      const uint32_t t = in[(int64_t)x + (int64_t)res * cyy + (int64_t)res * res * a];
+    if (x < rx && a >= 0 && a < N) {
+      const uint32_t t = in[idx3(x, cyy, a, rx, ry)];
       v = (uint16_t)(t < cap ? t : cap);
     }
     tile[s * 32 + tx] = v;
   }
   __syncthreads();
-  if (x >= res) return;
+  if (x >= rx) return;
   for (int o = o0 + ty; o <= o_last; o += kRows) {
     const uint32_t v = column_min<KERN_LAT2>(tile + tx, 2 * o + 1 - lo, span, halo);
-    flags[cell_index(x, cyy, o, res)] = v < cap ? 1 : 0;
+    flags[idx3(x, cyy, o, rx, ry)] = v < cap ? 1 : 0;
   }
 }
 
@@ -486,8 +486,8 @@ size_t dpx_smem_bytes(int sub, int halo) {
 // raw radius per 16^3 fine voxels: over the tile's x columns and outputs,
 // and its two third-axis coordinates widened by `rext` (the y pass feeds z
 // outputs up to a halo away).  Block-uniform.
-__device__ int tile_radius(const uint8_t* __restrict__ rmap, int mb, int nx, int n3, int axis, int nout, int o0,
-                           int rext) {
+__device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, int nx, int n3, int axis, int nout,
+                           int o0, int rext) {
   __shared__ int rt_s;
   if (threadIdx.x == 0) rt_s = 0;
   __syncthreads();
@@ -499,7 +499,7 @@ __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mb, int nx, int
   for (int i = threadIdx.x; i < cx * ca * ct; i += blockDim.x) {
     const int ix = xa + i % cx, ia = aa + (i / cx) % ca, it = ta + i / (cx * ca);
     const int my = axis == 1 ? ia : it, mz = axis == 1 ? it : ia;
-    const int v = rmap[ix + (int64_t)mb * (my + (int64_t)mb * mz)];
+    const int v = rmap[idx3(ix, my, mz, mbx, mby)];
     m = v > m ? v : m;
   }
   for (int o = 16; o > 0; o >>= 1) { const int t = __shfl_xor_sync(0xffffffffu, m, o); m = t > m ? t : m; }
@@ -512,7 +512,7 @@ template <int G, typename TIn, int FIN>
 __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
                                                   int sub, int halo, uint32_t cap, const int8_t* __restrict__ R,
-                                                  int uniform_r, int res, const uint8_t* __restrict__ rmap, int mb,
+                                                  int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
                                                   int rext) {
   extern __shared__ uint32_t tileu[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
   // that reads this tile has r(p) <= rt, so terms >= (rt+1)^2 never decide.
   int halo_e = halo;
   if (rmap != nullptr && step == 1) {
-    const int rt = tile_radius(rmap, mb, nx, n3, axis, nout, o0, rext);
+    const int rt = tile_radius(rmap, nx >> 4, ny >> 4, nx, n3, axis, nout, o0, rext);
     const uint32_t ct = G == KERN_CUBE ? (uint32_t)(rt + 1) : (uint32_t)((rt + 1) * (rt + 1));
     cap = ct < cap ? ct : cap;
     halo_e = rt + 2 < halo ? rt + 2 : halo;
@@ -641,14 +641,14 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
       const int o = obase + j;
       if (o >= nout) continue;
       const uint32_t v = best[j];
-      uint8_t* dst = out8 + cell_index(x, third, o, res);
+      uint8_t* dst = out8 + idx3(x, third, o, rx, ry);
       dst[0] = (v & 0xffffu) < cap ? 1 : 0;
       dst[1] = (v >> 16) < cap ? 1 : 0;
     }
   } else {
     // threshold then pack 2 (x) x 2 (y = third pair) x 2 (z) bits per byte
     __shared__ uint32_t xch[4][32][2];
-    const int N = 2 * res;
+    const int N = nz;  // fine extent along the pass axis (z)
     const int ru = clamp_radius(uniform_r);
     uint32_t bytes[2] = {0u, 0u};  // 8 z pairs: bytes q = 0..7
 #pragma unroll
@@ -659,7 +659,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
       if (FIN == 1) {
         int rlo = ru, rhi = ru;
         if (R != nullptr && colok && z < N) {
-          const uint16_t rr = *reinterpret_cast<const uint16_t*>(R + fine_index(x, third, z, N));
+          const uint16_t rr = *reinterpret_cast<const uint16_t*>(R + idx3(x, third, z, nx, ny));
           rlo = clamp_radius((int)(int8_t)(rr & 0xff));
           rhi = clamp_radius((int)(int8_t)(rr >> 8));
         }
@@ -690,7 +690,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
 #pragma unroll
       for (int q = 0; q < kDpxPer / 2; q++) {
         const int cz = obase / 2 + q;
-        if (2 * cz < N) out8[cell_index(cx, cy, cz, res)] = (uint8_t)((bytes[q >> 2] >> (8 * (q & 3))) & 0xffu);
+        if (2 * cz < N) out8[idx3(cx, cy, cz, rx, ry)] = (uint8_t)((bytes[q >> 2] >> (8 * (q & 3))) & 0xffu);
       }
     }
   }
@@ -698,7 +698,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
 
 template <int G, typename TIn, int FIN>
 static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
-                       int halo, uint32_t cap, const int8_t* R, int uniform_r, int res, cudaStream_t st,
+                       int halo, uint32_t cap, const int8_t* R, int uniform_r, int rx, int ry, cudaStream_t st,
                        KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0) {
   const size_t smem = dpx_smem_bytes(sub, halo);
   static size_t configured = 0;
@@ -712,18 +712,18 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, (n3 + 1) / 2);
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
-                                                          uniform_r, res, rmap, nx >> 4, rext));
+                                                          uniform_r, rx, ry, rmap, rext));
 }
 
 // Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
 // field of edge n (a multiple of 16): one block per map cell, one 16-byte
 // row segment per thread.
-__global__ void __launch_bounds__(256) k_radius_map(const int8_t* __restrict__ R, int n, int mb,
+__global__ void __launch_bounds__(256) k_radius_map(const int8_t* __restrict__ R, int nx, int ny, int mbx, int mby,
                                                      uint8_t* __restrict__ out) {
   const int b = blockIdx.x;
-  const int bx = b % mb, by = (b / mb) % mb, bz = b / (mb * mb);
+  const int bx = b % mbx, by = (b / mbx) % mby, bz = b / (mbx * mby);
   const int fy = 16 * by + (threadIdx.x & 15), fz = 16 * bz + (threadIdx.x >> 4);
-  const uint4 v = *reinterpret_cast<const uint4*>(R + fine_index(16 * bx, fy, fz, n));
+  const uint4 v = *reinterpret_cast<const uint4*>(R + idx3(16 * bx, fy, fz, nx, ny));
   const uint32_t w[4] = {v.x, v.y, v.z, v.w};
   int m = 0;
 #pragma unroll
@@ -741,9 +741,10 @@ __global__ void __launch_bounds__(256) k_radius_map(const int8_t* __restrict__ R
   }
 }
 
-cudaError_t launch_radius_map(const int8_t* R, int n, uint8_t* out, cudaStream_t st, KernelCounter* kc) {
-  const int mb = n / 16;
-  GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<mb * mb * mb, 256, 0, st>>>(R, n, mb, out));
+cudaError_t launch_radius_map(const int8_t* R, int nx, int ny, int nz, uint8_t* out, cudaStream_t st,
+                              KernelCounter* kc) {
+  const int mbx = nx / 16, mby = ny / 16, mbz = nz / 16;
+  GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<mbx * mby * mbz, 256, 0, st>>>(R, nx, ny, mbx, mby, out));
   return cudaGetLastError();
 }
 
@@ -766,26 +767,6 @@ __device__ __forceinline__ uint8_t base_dil(const uint8_t* X, const uint8_t* Df,
   return (inside && x != 0xff && (Df[c] & 1)) ? (uint8_t)0xff : x;
 }
 
-__global__ void k_dil_select(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
-                             uint8_t* __restrict__ D, int res, DataRes dr) {
-  const int64_t total = (int64_t)res * res * res;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
-    const int x = (int)(c % res), y = (int)((c / res) % res), z = (int)(c / ((int64_t)res * res));
-    const uint8_t d0 = base_dil(X, Df, c, in_box(x, y, z, dr.v));
-    bool tag = false;
-    if (x <= res - 2 && y <= res - 2 && z <= res - 2) {
-      int full = d0 == 0xff;
-#pragma unroll
-      for (int k = 1; k < 8; k++) {
-        const int xx = x + (k & 1), yy = y + ((k >> 1) & 1), zz = z + (k >> 2);
-        full += base_dil(X, Df, cell_index(xx, yy, zz, res), in_box(xx, yy, zz, dr.v)) == 0xff;
-      }
-      tag = full != 0 && full != 8;
-    }
-    D[c] = tag ? Df[c] : d0;
-  }
-}
-
 // Contour of the dilation: fine voxels outside D that are 6-adjacent to D.
 // GM_REF: only for cells in [1, res-2]^3 whose byte is not 0xff
 // (TagVoxelsContourByErosion, Grid.cu:1230-1327); GM_EXACT: whole grid.
@@ -800,25 +781,6 @@ __device__ __forceinline__ uint8_t adj6(uint8_t v, uint8_t xm, uint8_t xp, uint8
   return (uint8_t)t;
 }
 
-__global__ void k_contour(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, int res, int exact) {
-  const int64_t total = (int64_t)res * res * res;
-  const int64_t s1 = res, s2 = (int64_t)res * res;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
-    const int x = (int)(c % res), y = (int)((c / res) % res), z = (int)(c / s2);
-    const uint8_t v = D[c];
-    uint8_t out = 0;
-    if (exact) {
-      const uint8_t xm = x > 0 ? D[c - 1] : 0, xp = x < res - 1 ? D[c + 1] : 0;
-      const uint8_t ym = y > 0 ? D[c - s1] : 0, yp = y < res - 1 ? D[c + s1] : 0;
-      const uint8_t zm = z > 0 ? D[c - s2] : 0, zp = z < res - 1 ? D[c + s2] : 0;
-      out = adj6(v, xm, xp, ym, yp, zm, zp) & (uint8_t)~v;
-    } else if (x >= 1 && y >= 1 && z >= 1 && x <= res - 2 && y <= res - 2 && z <= res - 2 && v != 0xff) {
-      out = adj6(v, D[c - 1], D[c + 1], D[c - s1], D[c + s1], D[c - s2], D[c + s2]) & (uint8_t)~v;
-    }
-    S[c] = out;
-  }
-}
-
 // GM_REF erosion select: base pass (cells inside data_res with D != 0 and
 // X != 0xff are cleared when the centre 2c+1 is eroded, GMorpho.cu:4360-4370,
 // 4644-4646), then cells whose byte differs from a 6-neighbour
@@ -829,43 +791,24 @@ __device__ __forceinline__ uint8_t base_ero(const uint8_t* X, const uint8_t* D, 
   return (inside && d != 0 && X[c] != 0xff && Eb[c]) ? (uint8_t)0 : d;
 }
 
-__global__ void k_ero_select(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
-                             const uint8_t* __restrict__ Eb, const uint8_t* __restrict__ Ef,
-                             uint8_t* __restrict__ C, int res, DataRes dr, int exact) {
-  const int64_t total = (int64_t)res * res * res;
-  const int64_t s1 = res, s2 = (int64_t)res * res;
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
-    if (exact) { C[c] = D[c] & (uint8_t)~Ef[c]; continue; }
-    const int x = (int)(c % res), y = (int)((c / res) % res), z = (int)(c / s2);
-    const uint8_t c0 = base_ero(X, D, Eb, c, in_box(x, y, z, dr.v));
-    bool tag = false;
-    if (x >= 1 && y >= 1 && z >= 1 && x <= res - 2 && y <= res - 2 && z <= res - 2) {
-      tag = base_ero(X, D, Eb, c - 1, in_box(x - 1, y, z, dr.v)) != c0 ||
-            base_ero(X, D, Eb, c + 1, in_box(x + 1, y, z, dr.v)) != c0 ||
-            base_ero(X, D, Eb, c - s1, in_box(x, y - 1, z, dr.v)) != c0 ||
-            base_ero(X, D, Eb, c + s1, in_box(x, y + 1, z, dr.v)) != c0 ||
-            base_ero(X, D, Eb, c - s2, in_box(x, y, z - 1, dr.v)) != c0 ||
-            base_ero(X, D, Eb, c + s2, in_box(x, y, z + 1, dr.v)) != c0;
-    }
-    C[c] = tag ? (uint8_t)(0xff & ~Ef[c]) : c0;
-  }
-}
-
 // ---------------------------------------------------------------------
 // the same cell-level kernels, four consecutive cells (one u32) per thread
 // block (64, 4): x quads along threadIdx.x, y along threadIdx.y, z = blockIdx.z
 // ---------------------------------------------------------------------
 
-__device__ __forceinline__ uint32_t ld4(const uint8_t* g, int x4, int y, int z, int res) {
-  return *reinterpret_cast<const uint32_t*>(g + cell_index(x4, y, z, res));
+// cell grids of this section are boxes of rx * ry * rz cells (Dims)
+struct Dims { int x, y, z; };
+__device__ __forceinline__ int64_t cidx(int x, int y, int z, Dims d) { return idx3(x, y, z, d.x, d.y); }
+__device__ __forceinline__ uint32_t ld4(const uint8_t* g, int x4, int y, int z, Dims d) {
+  return *reinterpret_cast<const uint32_t*>(g + cidx(x4, y, z, d));
 }
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
 
 __global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
-                                                     uint8_t* __restrict__ D, int res, DataRes dr) {
+                                                     uint8_t* __restrict__ D, Dims g, DataRes dr) {
   const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
   const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= res || y >= res) return;
+  if (x4 >= g.x || y >= g.y) return;
   // full flags of the base-pass byte for x in [x4, x4+4], (y, y+1) x (z, z+1)
   uint32_t full[2][2];
   uint32_t center = 0, dfc = 0;
@@ -875,15 +818,15 @@ __global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__
     for (int dy = 0; dy < 2; dy++) {
       const int yy = y + dy, zz = z + dz;
       uint32_t f = 0;
-      if (yy < res && zz < res) {
-        const uint32_t xw = ld4(X, x4, yy, zz, res), dw = ld4(Df, x4, yy, zz, res);
+      if (yy < g.y && zz < g.z) {
+        const uint32_t xw = ld4(X, x4, yy, zz, g), dw = ld4(Df, x4, yy, zz, g);
         const bool iyz = yy < dr.v[1] && zz < dr.v[2];
 #pragma unroll
         for (int i = 0; i < 5; i++) {
           const int xx = x4 + i;
-          if (xx >= res) break;
-          const uint32_t xb = i < 4 ? byte_of(xw, i) : X[cell_index(xx, yy, zz, res)];
-          const uint32_t db = i < 4 ? byte_of(dw, i) : Df[cell_index(xx, yy, zz, res)];
+          if (xx >= g.x) break;
+          const uint32_t xb = i < 4 ? byte_of(xw, i) : X[cidx(xx, yy, zz, g)];
+          const uint32_t db = i < 4 ? byte_of(dw, i) : Df[cidx(xx, yy, zz, g)];
           const bool inside = iyz && xx < dr.v[0];
           const uint32_t d0 = (inside && xb != 0xffu && (db & 1u)) ? 0xffu : xb;
           f |= (uint32_t)(d0 == 0xffu) << i;
@@ -898,40 +841,40 @@ __global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__
   for (int i = 0; i < 4; i++) {
     const int x = x4 + i;
     bool tag = false;
-    if (x <= res - 2 && y <= res - 2 && z <= res - 2) {
+    if (x <= g.x - 2 && y <= g.y - 2 && z <= g.z - 2) {
       const uint32_t m = 3u << i;
       const int n = __popc(full[0][0] & m) + __popc(full[0][1] & m) + __popc(full[1][0] & m) + __popc(full[1][1] & m);
       tag = n != 0 && n != 8;
     }
     out |= (tag ? byte_of(dfc, i) : byte_of(center, i)) << (8 * i);
   }
-  *reinterpret_cast<uint32_t*>(D + cell_index(x4, y, z, res)) = out;
+  *reinterpret_cast<uint32_t*>(D + cidx(x4, y, z, g)) = out;
 }
 
-__global__ void __launch_bounds__(256) k_contour4(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, int res,
+__global__ void __launch_bounds__(256) k_contour4(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, Dims g,
                                                   int exact) {
   const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
   const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= res || y >= res) return;
-  const uint32_t v4 = ld4(D, x4, y, z, res);
-  const uint32_t xm = x4 > 0 ? D[cell_index(x4 - 1, y, z, res)] : 0u;
-  const uint32_t xp = x4 + 4 < res ? D[cell_index(x4 + 4, y, z, res)] : 0u;
-  const uint32_t ym4 = y > 0 ? ld4(D, x4, y - 1, z, res) : 0u, yp4 = y < res - 1 ? ld4(D, x4, y + 1, z, res) : 0u;
-  const uint32_t zm4 = z > 0 ? ld4(D, x4, y, z - 1, res) : 0u, zp4 = z < res - 1 ? ld4(D, x4, y, z + 1, res) : 0u;
+  if (x4 >= g.x || y >= g.y) return;
+  const uint32_t v4 = ld4(D, x4, y, z, g);
+  const uint32_t xm = x4 > 0 ? D[cidx(x4 - 1, y, z, g)] : 0u;
+  const uint32_t xp = x4 + 4 < g.x ? D[cidx(x4 + 4, y, z, g)] : 0u;
+  const uint32_t ym4 = y > 0 ? ld4(D, x4, y - 1, z, g) : 0u, yp4 = y < g.y - 1 ? ld4(D, x4, y + 1, z, g) : 0u;
+  const uint32_t zm4 = z > 0 ? ld4(D, x4, y, z - 1, g) : 0u, zp4 = z < g.z - 1 ? ld4(D, x4, y, z + 1, g) : 0u;
   uint32_t out = 0;
-  const bool yz_in = y >= 1 && z >= 1 && y <= res - 2 && z <= res - 2;
+  const bool yz_in = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
 #pragma unroll
   for (int i = 0; i < 4; i++) {
     const int x = x4 + i;
     const uint32_t v = byte_of(v4, i);
     const uint32_t l = i == 0 ? xm : byte_of(v4, i - 1), r = i == 3 ? xp : byte_of(v4, i + 1);
     uint32_t o = 0;
-    if (exact || (yz_in && x >= 1 && x <= res - 2 && v != 0xffu))
+    if (exact || (yz_in && x >= 1 && x <= g.x - 2 && v != 0xffu))
       o = adj6((uint8_t)v, (uint8_t)l, (uint8_t)r, (uint8_t)byte_of(ym4, i), (uint8_t)byte_of(yp4, i),
                (uint8_t)byte_of(zm4, i), (uint8_t)byte_of(zp4, i)) & ~v & 0xffu;
     out |= o << (8 * i);
   }
-  *reinterpret_cast<uint32_t*>(S + cell_index(x4, y, z, res)) = out;
+  *reinterpret_cast<uint32_t*>(S + cidx(x4, y, z, g)) = out;
 }
 
 __device__ __forceinline__ uint32_t c0_of(uint32_t x, uint32_t d, uint32_t eb, bool inside) {
@@ -940,38 +883,38 @@ __device__ __forceinline__ uint32_t c0_of(uint32_t x, uint32_t d, uint32_t eb, b
 
 __global__ void __launch_bounds__(256) k_ero_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
                                                      const uint8_t* __restrict__ Eb, const uint8_t* __restrict__ Ef,
-                                                     uint8_t* __restrict__ C, int res, DataRes dr, int exact) {
+                                                     uint8_t* __restrict__ C, Dims g, DataRes dr, int exact) {
   const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
   const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= res || y >= res) return;
-  const uint32_t d4 = ld4(D, x4, y, z, res), ef4 = ld4(Ef, x4, y, z, res);
+  if (x4 >= g.x || y >= g.y) return;
+  const uint32_t d4 = ld4(D, x4, y, z, g), ef4 = ld4(Ef, x4, y, z, g);
   if (exact) {
-    *reinterpret_cast<uint32_t*>(C + cell_index(x4, y, z, res)) = d4 & ~ef4;
+    *reinterpret_cast<uint32_t*>(C + cidx(x4, y, z, g)) = d4 & ~ef4;
     return;
   }
-  const uint32_t x4v = ld4(X, x4, y, z, res), eb4 = ld4(Eb, x4, y, z, res);
+  const uint32_t x4v = ld4(X, x4, y, z, g), eb4 = ld4(Eb, x4, y, z, g);
   const bool iyz = y < dr.v[1] && z < dr.v[2];
   // C0 along the row at x4-1 .. x4+4
   uint32_t row[6];
 #pragma unroll
   for (int i = 0; i < 6; i++) {
     const int xx = x4 - 1 + i;
-    if (xx < 0 || xx >= res) { row[i] = 0u; continue; }
+    if (xx < 0 || xx >= g.x) { row[i] = 0u; continue; }
     uint32_t xb, db, eb;
     if (i >= 1 && i <= 4) { xb = byte_of(x4v, i - 1); db = byte_of(d4, i - 1); eb = byte_of(eb4, i - 1); }
-    else { const int64_t c = cell_index(xx, y, z, res); xb = X[c]; db = D[c]; eb = Eb[c]; }
+    else { const int64_t c = cidx(xx, y, z, g); xb = X[c]; db = D[c]; eb = Eb[c]; }
     row[i] = c0_of(xb, db, eb, iyz && xx < dr.v[0]);
   }
   // C0 of the four y/z neighbour rows
   uint32_t nb[4] = {0u, 0u, 0u, 0u};
   const int ny[4] = {y - 1, y + 1, y, y};
   const int nz[4] = {z, z, z - 1, z + 1};
-  const bool interior_yz = y >= 1 && z >= 1 && y <= res - 2 && z <= res - 2;
+  const bool interior_yz = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
   if (interior_yz) {
 #pragma unroll
     for (int n = 0; n < 4; n++) {
-      const uint32_t xw = ld4(X, x4, ny[n], nz[n], res), dw = ld4(D, x4, ny[n], nz[n], res),
-                     ew = ld4(Eb, x4, ny[n], nz[n], res);
+      const uint32_t xw = ld4(X, x4, ny[n], nz[n], g), dw = ld4(D, x4, ny[n], nz[n], g),
+                     ew = ld4(Eb, x4, ny[n], nz[n], g);
       const bool in_yz = ny[n] < dr.v[1] && nz[n] < dr.v[2];
       uint32_t w = 0;
 #pragma unroll
@@ -986,16 +929,16 @@ __global__ void __launch_bounds__(256) k_ero_select4(const uint8_t* __restrict__
     const int x = x4 + i;
     const uint32_t c0 = row[i + 1];
     bool tag = false;
-    if (interior_yz && x >= 1 && x <= res - 2) {
+    if (interior_yz && x >= 1 && x <= g.x - 2) {
       tag = row[i] != c0 || row[i + 2] != c0 || byte_of(nb[0], i) != c0 || byte_of(nb[1], i) != c0 ||
             byte_of(nb[2], i) != c0 || byte_of(nb[3], i) != c0;
     }
     out |= (tag ? (0xffu & ~byte_of(ef4, i)) : c0) << (8 * i);
   }
-  *reinterpret_cast<uint32_t*>(C + cell_index(x4, y, z, res)) = out;
+  *reinterpret_cast<uint32_t*>(C + cidx(x4, y, z, g)) = out;
 }
 
-static dim3 quad_grid(int res) { return dim3((res / 4 + 63) / 64, (res + 3) / 4, res); }
+static dim3 quad_grid(Dims g) { return dim3((g.x / 4 + 63) / 64, (g.y + 3) / 4, g.z); }
 
 // max clamped radius over the fine radius grid
 __global__ void k_rmax(const int8_t* __restrict__ R, int64_t n, int* __restrict__ out) {
@@ -1027,11 +970,14 @@ static int grid_stride_blocks(int64_t n, int threads, int sms) {
   return (int)(b < cap ? b : cap);
 }
 
-size_t close_workspace_bytes(int res) {
-  const size_t N = 2 * (size_t)res, V = N * N * N, cells = (size_t)res * res * res;
-  // buf16 x2, buf8, HL1, HL2, Df, Eb, Ef, S, D, radius map + slack for alignment
-  return 2 * V * 2 + V + (size_t)res * N * N * 2 + (size_t)res * res * N * 2 + 5 * cells + V / 4096 + 16 * 256;
+size_t close_workspace_bytes_box(int rx, int ry, int rz) {
+  const size_t Nx = 2 * (size_t)rx, Ny = 2 * (size_t)ry, Nz = 2 * (size_t)rz, V = Nx * Ny * Nz;
+  const size_t cells = (size_t)rx * ry * rz;
+  // buf16 x2, buf8, HL1 (rx, Ny, Nz), HL2 (rx, ry, Nz), Df, Eb, Ef, S, D, radius map + alignment slack
+  return 2 * V * 2 + V + (size_t)rx * Ny * Nz * 2 + (size_t)rx * ry * Nz * 2 + 5 * cells + V / 4096 + 16 * 256;
 }
+
+size_t close_workspace_bytes(int res) { return close_workspace_bytes_box(res, res, res); }
 
 static inline uint8_t* carve(uint8_t*& p, size_t bytes) {
   uint8_t* r = p;
@@ -1040,14 +986,19 @@ static inline uint8_t* carve(uint8_t*& p, size_t bytes) {
 }
 
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc) {
-  const int res = a.res, N = 2 * res;
-  const size_t V = (size_t)N * N * N, cells = (size_t)res * res * res;
+  const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
+  const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
+  const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
+  if (rx % 16 != 0 || ry % 16 != 0 || rz % 16 != 0 || rx <= 0 || ry <= 0 || rz <= 0) return cudaErrorInvalidValue;
+  const Dims g{rx, ry, rz};
+  const int Nx = 2 * rx, Ny = 2 * ry, Nz = 2 * rz;
+  const size_t V = (size_t)Nx * Ny * Nz, cells = (size_t)rx * ry * rz;
   uint8_t* p = a.workspace;
   uint16_t* buf16a = reinterpret_cast<uint16_t*>(carve(p, V * 2));
   uint16_t* buf16b = reinterpret_cast<uint16_t*>(carve(p, V * 2));
   uint8_t* buf8 = carve(p, V);
-  uint16_t* HL1 = reinterpret_cast<uint16_t*>(carve(p, (size_t)res * N * N * 2));
-  uint16_t* HL2 = reinterpret_cast<uint16_t*>(carve(p, (size_t)res * res * N * 2));
+  uint16_t* HL1 = reinterpret_cast<uint16_t*>(carve(p, (size_t)rx * Ny * Nz * 2));
+  uint16_t* HL2 = reinterpret_cast<uint16_t*>(carve(p, (size_t)rx * ry * Nz * 2));
   uint8_t* Df = carve(p, cells);
   uint8_t* Eb = carve(p, cells);
   uint8_t* Ef = carve(p, cells);
@@ -1065,92 +1016,94 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const int dil_halo = dil_r + 1;
   const uint8_t* tile_map = nullptr;  // per-tile radius bounds of the dilation passes
   if (a.R != nullptr) {
-    if (launch_radius_map(a.R, N, rmap, st, kc) != cudaSuccess) return cudaGetLastError();
+    if (launch_radius_map(a.R, Nx, Ny, Nz, rmap, st, kc) != cudaSuccess) return cudaGetLastError();
     tile_map = rmap;
   }
   {
-    const int W = N >> 5;
-    GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x<<<dim3(res, res), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, res, dcap));
+    const int W = Nx >> 5;
+    GM_LAUNCH(kc, "k_dil_pass_x", st,
+              k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, dcap));
     uint8_t* dst = exact ? D : Df;
     if (dil_cap <= 32767) {
       if (a.se == 1) {
-        launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, nullptr, 0, res, st,
-                                          kc, "k_pass_dil_y", tile_map, dil_halo);
-        launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, N, N, N, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r,
-                                           res, st, kc, "k_pass_dil_z", tile_map, 0);
+        launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, nullptr, 0, rx,
+                                          ry, st, kc, "k_pass_dil_y", tile_map, dil_halo);
+        launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r,
+                                           rx, ry, st, kc, "k_pass_dil_z", tile_map, 0);
       } else {
-        launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, nullptr, 0, res, st,
-                                         kc, "k_pass_dil_y", tile_map, dil_halo);
-        launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, N, N, N, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r, res,
-                                          st, kc, "k_pass_dil_z", tile_map, 0);
+        launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, nullptr, 0, rx,
+                                         ry, st, kc, "k_pass_dil_y", tile_map, dil_halo);
+        launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r,
+                                          rx, ry, st, kc, "k_pass_dil_z", tile_map, 0);
       }
     } else {
       const int span = kTileOut + 2 * dil_halo;
-      dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
+      dim3 gy(cdiv(Nx, 32), cdiv(Ny, kTileOut), Nz);
       if (a.se == 1)
-        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CUBE, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(
-                                             buf8, buf16a, N, N, N, 1, 0, dil_halo, dil_cap));
+        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CUBE, uint8_t><<<gy, dim3(32, kRows), span * 32 * 2, st>>>(
+                                             buf8, buf16a, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap));
       else
-        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT, uint8_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(
-                                             buf8, buf16a, N, N, N, 1, 0, dil_halo, dil_cap));
-      dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
+        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT, uint8_t><<<gy, dim3(32, kRows), span * 32 * 2, st>>>(
+                                             buf8, buf16a, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap));
+      dim3 gz(cdiv(Nx, 32), cdiv(Nz, kTileOut), Ny / 2);
       if (a.se == 1)
         GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CUBE, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                           buf16a, dst, a.R, a.uniform_r, res, dil_halo, dil_cap));
+                                           buf16a, dst, a.R, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
       else
         GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                           buf16a, dst, a.R, a.uniform_r, res, dil_halo, dil_cap));
+                                           buf16a, dst, a.R, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
     }
     if (!exact) {
-      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(res), dim3(64, 4), 0, st>>>(a.X, Df, D, res, dr));
+      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr));
     }
   }
   // ---- contour ----
-  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(res), dim3(64, 4), 0, st>>>(D, S, res, exact ? 1 : 0));
+  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact ? 1 : 0));
   // ---- erosion ----
   {
     const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
     const int ehalo = rmax + 1;
-    const int W = N >> 5;
+    const int W = Nx >> 5;
     // bits, centre and lattice accumulators, compacted sites
-    const size_t smem = sizeof(uint32_t) * (4 * (size_t)W + 4 * (size_t)N + 4 * (size_t)res + 8 * (size_t)N);
+    const size_t smem = sizeof(uint32_t) * (4 * (size_t)W + 4 * (size_t)Nx + 4 * (size_t)rx + 8 * (size_t)Nx);
     static size_t ero_x_configured = 0;
     if (smem > 48 * 1024 && smem > ero_x_configured) {
       cudaFuncSetAttribute(k_ero_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       ero_x_configured = smem;
     }
-    GM_LAUNCH(kc, "k_ero_pass_x", st, k_ero_pass_x<<<dim3(res, res), 256, smem, st>>>(S, a.R, a.uniform_r, res, ehalo, K, buf16a, HL1));
+    GM_LAUNCH(kc, "k_ero_pass_x", st,
+              k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, a.R, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1));
     if (K <= 32767) {
-      launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, N, N, N, 1, 0, ehalo, K, nullptr, 0, res, st, kc,
-                                         "k_pass_ero_y");
-      launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, N, N, N, 2, 0, ehalo, K, nullptr, 0, res, st, kc,
+      launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, nullptr, 0, rx, ry, st,
+                                         kc, "k_pass_ero_y");
+      launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, nullptr, 0, rx, ry, st, kc,
                                          "k_pass_ero_z");
       if (!exact) {
-        launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, res, N, N, 1, 1, ehalo, K, nullptr, 0, res, st, kc,
+        launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, nullptr, 0, rx, ry, st, kc,
                                            "k_pass_erob_y");
-        launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, res, res, N, 2, 1, ehalo, K, nullptr, 0, res, st, kc,
+        launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, nullptr, 0, rx, ry, st, kc,
                                            "k_pass_erob_z");
       }
     } else {
       const int span = kTileOut + 2 * ehalo;
-      dim3 g(cdiv(N, 32), cdiv(N, kTileOut), N);
-      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CEN2, uint16_t><<<g, dim3(32, kRows), span * 32 * 2, st>>>(
-                                           buf16a, buf16b, N, N, N, 1, 0, ehalo, K));
-      dim3 gz(cdiv(N, 32), cdiv(N, kTileOut), N / 2);
+      dim3 gy(cdiv(Nx, 32), cdiv(Ny, kTileOut), Nz);
+      GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CEN2, uint16_t><<<gy, dim3(32, kRows), span * 32 * 2, st>>>(
+                                           buf16a, buf16b, Nx, Ny, Nz, 1, 0, ehalo, K));
+      dim3 gz(cdiv(Nx, 32), cdiv(Nz, kTileOut), Ny / 2);
       GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CEN2, FIN_ERO><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                         buf16b, Ef, nullptr, 0, res, ehalo, K));
+                                         buf16b, Ef, nullptr, 0, rx, ry, rz, ehalo, K));
       if (!exact) {
         const int span_s = 2 * kTileOut + 2 * ehalo;
-        dim3 gy(cdiv(res, 32), cdiv(res, kTileOut), N);
-        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT2, uint16_t><<<gy, dim3(32, kRows), span_s * 32 * 2, st>>>(
-                                             HL1, HL2, res, N, N, 1, 1, ehalo, K));
-        dim3 gzb(cdiv(res, 32), cdiv(res, kTileOut), res);
+        dim3 gyb(cdiv(rx, 32), cdiv(ry, kTileOut), Nz);
+        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT2, uint16_t><<<gyb, dim3(32, kRows), span_s * 32 * 2, st>>>(
+                                             HL1, HL2, rx, Ny, Nz, 1, 1, ehalo, K));
+        dim3 gzb(cdiv(rx, 32), cdiv(rz, kTileOut), ry);
         GM_LAUNCH(kc, "k_final_z_base", st, k_final_z_base<<<gzb, dim3(32, kRows), span_s * 32 * 2, st>>>(
-                                                HL2, Eb, res, ehalo, K));
+                                                HL2, Eb, rx, ry, rz, ehalo, K));
       }
     }
-    GM_LAUNCH(kc, "k_ero_select", st, k_ero_select4<<<quad_grid(res), dim3(64, 4), 0, st>>>(a.X, D, Eb, Ef, a.C_out, res, dr,
-                                                                                         exact ? 1 : 0));
+    GM_LAUNCH(kc, "k_ero_select", st,
+              k_ero_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0));
   }
   if (a.S_out) {
     cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
@@ -1159,7 +1112,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
 }
 
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc) {
-  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(res), dim3(64, 4), 0, st>>>(D, S, res, exact));
+  const Dims g{res, res, res};
+  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact));
   return cudaGetLastError();
 }
 
