@@ -32,6 +32,16 @@ class MeshView(C.Structure):
                 ("num_vertices", C.c_int64), ("num_triangles", C.c_int64)]
 
 
+class BoxDesc(C.Structure):
+    _fields_ = [("bbox_min", C.c_float * 3), ("cell_size", C.c_float), ("dims", C.c_int32 * 3),
+                ("data_res", C.c_int32 * 3)]
+
+
+class MeshWindow(C.Structure):
+    _fields_ = [("origin", C.c_int32 * 3), ("global_res", C.c_int32), ("emit_lo", C.c_int32 * 3),
+                ("emit_hi", C.c_int32 * 3)]
+
+
 class BatchItem(C.Structure):
     _fields_ = [("desc", GridDesc), ("d_input", C.c_void_p), ("d_scale", C.c_void_p), ("uniform_radius", C.c_int32),
                 ("d_closing", C.c_void_p)]
@@ -96,6 +106,8 @@ PROTOTYPES = {
     "gm_server_profile": (C.c_int, [_P, C.c_int32]),
     "gm_server_snapshot": (C.c_int, [_P, _P, _P]),
     "gm_server_restore": (C.c_int, [_P, _P, _P]),
+    "gm_close_box": (C.c_int, [_P, C.POINTER(BoxDesc), _P, _P, C.c_int32, C.c_int, C.c_int, _P, _P]),
+    "gm_mesh_box": (C.c_int, [_P, C.POINTER(BoxDesc), _P, C.POINTER(MeshWindow), C.c_int32, C.POINTER(MeshView), _P]),
     "gm_mesh_store": (C.c_int, [C.c_char_p, _P, _P, C.c_int64, _P, C.c_int64, C.c_int32]),
     "gm_server_profile_read": (C.c_int64, [_P, C.c_char_p, C.c_int64]),
     "gm_bvh_build": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.POINTER(_P), C.POINTER(C.c_int64), _P]),

@@ -40,6 +40,16 @@ def make_desc(res, data_res=None, bbox_min=(0.0, 0.0, 0.0), cell_size=None):
     return d
 
 
+def make_box(dims, data_res=None, bbox_min=(0.0, 0.0, 0.0), cell_size=1.0):
+    b = L.BoxDesc()
+    for a in range(3):
+        b.bbox_min[a] = bbox_min[a]
+        b.dims[a] = int(dims[a])
+        b.data_res[a] = int(dims[a] if data_res is None else data_res[a])
+    b.cell_size = cell_size
+    return b
+
+
 def grid_attributes(points, base_res, margin):
     P = np.ascontiguousarray(points, dtype=np.float32)
     d = L.GridDesc()
@@ -109,6 +119,29 @@ class Context:
         out = grid if inplace else torch.empty_like(grid)
         self._check(self.lib.gm_contour(self.ctx, C.byref(desc), _ptr(grid), _ptr(out), mode, _stream()))
         return out
+
+    # box grids (slabs, crops, non-power-of-two instances)
+    def close_box(self, box, X, R=None, uniform_radius=4, mode=L.GM_REF, se=L.GM_SE_SPHERE, out=None):
+        import torch
+        if out is None:
+            out = torch.empty_like(X)
+        self._check(self.lib.gm_close_box(self.ctx, C.byref(box), _ptr(X), _ptr(R), int(uniform_radius), mode, se,
+                                          _ptr(out), _stream()))
+        return out
+
+    def mesh_box(self, box, Cg, bilateral_iters=20, window=None):
+        """window: None or L.MeshWindow.  Returns zero-copy (V, N, T) owned by
+        the context until the next mesh-producing call."""
+        import torch
+        mv = L.MeshView()
+        wp = C.byref(window) if window is not None else None
+        self._check(self.lib.gm_mesh_box(self.ctx, C.byref(box), _ptr(Cg), wp, int(bilateral_iters), C.byref(mv),
+                                         _stream()))
+        nv, nt = mv.num_vertices, mv.num_triangles
+        V = torch.as_tensor(DevicePtrArray(mv.vertices, (nv, 3), "<f4"), device="cuda")
+        N = torch.as_tensor(DevicePtrArray(mv.normals, (nv, 3), "<f4"), device="cuda")
+        T = torch.as_tensor(DevicePtrArray(mv.triangles, (nt, 3), "<u4"), device="cuda")
+        return V, N, T
 
     # a12..a16
     def mesh(self, desc, Cg, bilateral_iters=20):

@@ -410,6 +410,121 @@ gm_status gm_contour(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_gri
   return GM_OK;
 }
 
+// ------------------------------------------------------------------ box grids
+
+static gm_status check_box(gm_ctx* ctx, const gm_box_desc* b) {
+  if (!b) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "box descriptor is NULL");
+  for (int a = 0; a < 3; a++) {
+    if (b->dims[a] < 16 || b->dims[a] % 16 != 0 || b->dims[a] > 2048)
+      return fail(ctx, GM_ERR_INVALID_ARGUMENT, "box dims must be multiples of 16 in [16, 2048]");
+    if (b->data_res[a] < 0 || b->data_res[a] > b->dims[a])
+      return fail(ctx, GM_ERR_INVALID_ARGUMENT, "data_res must lie in [0, dims]");
+  }
+  if (!(b->cell_size > 0.f)) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "cell_size must be positive");
+  return GM_OK;
+}
+
+gm_status gm_close_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
+                       int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_box(ctx, box);
+  if (s != GM_OK) return s;
+  if (!d_input || !d_closing) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_box: NULL input or output");
+  if (!aligned16(d_input) || (d_scale && !aligned16(d_scale)))
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_box: device buffers must be 16-byte aligned");
+  if (mode != GM_REF && mode != GM_EXACT) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_box: unknown mode");
+  if (se != GM_SE_SPHERE && se != GM_SE_CUBE) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_box: unknown se");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int rx = box->dims[0], ry = box->dims[1], rz = box->dims[2];
+  int rmax;
+  if (d_scale) {
+    GM_CHECK_CUDA(ctx, gm::launch_rmax(d_scale, (int64_t)8 * rx * ry * rz, ctx->d_int, ctx->num_sms, st, &ctx->kc),
+                  "radius bound");
+    int h = 0;
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_int, sizeof(int), cudaMemcpyDeviceToHost, st), "radius bound");
+    GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "radius bound");
+    rmax = h;
+  } else {
+    rmax = gm::clamp_radius(uniform_radius);
+  }
+  if ((s = ensure(ctx, (void**)&ctx->ws, ctx->ws_bytes, gm::close_workspace_bytes_box(rx, ry, rz),
+                  "closing workspace")) != GM_OK)
+    return s;
+  gm::CloseArgs a;
+  a.res = 0;
+  a.dims[0] = rx;
+  a.dims[1] = ry;
+  a.dims[2] = rz;
+  for (int i = 0; i < 3; i++) a.data_res[i] = box->data_res[i];
+  a.X = d_input;
+  a.R = d_scale;
+  a.uniform_r = uniform_radius;
+  a.rmax = rmax;
+  a.mode = (int)mode;
+  a.se = (int)se;
+  a.C_out = d_closing;
+  a.D_out = nullptr;
+  a.S_out = nullptr;
+  a.workspace = ctx->ws;
+  a.num_sms = ctx->num_sms;
+  GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close_box");
+  return GM_OK;
+}
+
+gm_status gm_mesh_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_closing, const gm_mesh_window* win,
+                      int32_t bilateral_iters, gm_mesh_view* out, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_box(ctx, box);
+  if (s != GM_OK) return s;
+  if (!d_closing || !out || bilateral_iters < 0)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh_box: NULL buffer or negative iteration count");
+  if (win) {
+    if (win->global_res < 1) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh_box: global_res must be positive");
+    for (int a = 0; a < 3; a++)
+      if (win->emit_lo[a] < 0 || win->emit_hi[a] > box->dims[a] || win->emit_lo[a] > win->emit_hi[a] ||
+          win->origin[a] < 0 || win->origin[a] + box->dims[a] > win->global_res)
+        return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh_box: window outside the box or the global grid");
+  }
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  gm::MeshArgs a;
+  a.res = 0;
+  for (int k = 0; k < 3; k++) a.dims[k] = box->dims[k];
+  a.C = d_closing;
+  for (int i = 0; i < 3; i++) a.bbox_min[i] = box->bbox_min[i];
+  a.cell_size = box->cell_size;
+  a.isovalue = 0.95f;  // GMorpho.cu:6922
+  a.bilateral_iters = bilateral_iters;
+  a.num_sms = ctx->num_sms;
+  if (win) {
+    a.gres = win->global_res;
+    for (int k = 0; k < 3; k++) {
+      a.off[k] = win->origin[k];
+      a.emit_lo[k] = win->emit_lo[k];
+      a.emit_hi[k] = win->emit_hi[k];
+      a.tag_lo[k] = win->emit_lo[k];
+      a.tag_hi[k] = win->emit_hi[k] + 1 < box->dims[k] ? win->emit_hi[k] + 1 : box->dims[k];
+    }
+    a.zero_isolated = 1;
+  }
+  int64_t nv = 0, nt = 0;
+  ctx->has_mesh = false;
+  GM_CHECK_CUDA(ctx, gm::mesh_count(a, ctx->mesh, st, &ctx->kc, &nv, &nt), "gm_mesh_box (count)");
+  if (nv > 0xfffffff0LL || nt > 0x7ffffff0LL)
+    return fail(ctx, GM_ERR_CAPACITY, "gm_mesh_box: mesh exceeds 32-bit vertex/triangle indexing");
+  GM_CHECK_CUDA(ctx, gm::mesh_emit(a, ctx->mesh, nv, nt, st, &ctx->kc), "gm_mesh_box (emit)");
+  ctx->nv = nv;
+  ctx->nt = nt;
+  ctx->has_mesh = true;
+  out->vertices = ctx->mesh.V;
+  out->normals = ctx->mesh.N;
+  out->triangles = ctx->mesh.T;
+  out->num_vertices = nv;
+  out->num_triangles = nt;
+  return GM_OK;
+}
+
 // ------------------------------------------------------------------ a12..a16
 
 static gm_status mesh_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closing, int iters,

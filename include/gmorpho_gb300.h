@@ -268,6 +268,39 @@ gm_status gm_server_restore(gm_server* srv, const uint8_t* h_closing, const int8
 gm_status gm_server_profile(gm_server* srv, int32_t enable);
 int64_t gm_server_profile_read(gm_server* srv, char* buf, int64_t cap);
 
+/* ---------------------------------------------------------------- boxes
+ * Grids that are boxes of rx * ry * rz base cells (each a multiple of 16),
+ * x-fastest, packed like gm_grid_desc grids: a slab of a larger grid on one
+ * GPU, a crop, or an instance whose edges are not powers of two.  The
+ * closing is the same algorithm with the box's own border (cells outside
+ * [1, dims-2] are never contour cells); a box cut out of a larger grid with
+ * a margin of rmax + 8 cells on each cut side is exact on its interior. */
+typedef struct {
+  float bbox_min[3];    /* world position of the box's cell (0,0,0) corner */
+  float cell_size;      /* base cell edge */
+  int32_t dims[3];      /* rx, ry, rz */
+  int32_t data_res[3];  /* cells with data (<= dims) */
+} gm_box_desc;
+
+gm_status gm_close_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
+                       int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, void* stream);
+
+/* Where a box sits in a cubic global grid, and which of its cells to mesh:
+ * triangles of cells [emit_lo, emit_hi), the global grid's border rule and
+ * global vertex coordinates (box->bbox_min must then be the GLOBAL grid's
+ * corner), so that the meshes of adjacent windows hold exactly the global
+ * mesh's triangles.  Vertices no triangle of the window uses (one layer past
+ * emit_hi) get a zero normal. */
+typedef struct {
+  int32_t origin[3];    /* global cell of the box's cell (0,0,0) */
+  int32_t global_res;
+  int32_t emit_lo[3], emit_hi[3];
+} gm_mesh_window;
+
+/* Mesh of a closed box (win NULL: the whole box, its own border rule). */
+gm_status gm_mesh_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_closing, const gm_mesh_window* win,
+                      int32_t bilateral_iters, gm_mesh_view* out, void* stream);
+
 /* Host mesh file output, format by extension: ".off" (the reference's
  * Mesh::storeOFF text form, Common/Mesh.h:627-637), ".pn" (float32
  * position + normal per vertex, the reference's PN form) or ".ply" (binary
