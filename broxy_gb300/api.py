@@ -300,7 +300,7 @@ class Server:
     re-closing and re-meshing, continuous batching over `slots`."""
 
     def __init__(self, desc, X, R, slots=4, max_crop_res=256, rmax=32, mode=L.GM_REF, bilateral_iters=0):
-        """max_crop_res: largest crop edge in cells (a multiple of 32, or
+        """max_crop_res: largest crop edge in cells (a multiple of 16, or
         desc.res); an edit needing more is answered with GM_ERR_CAPACITY."""
         self.lib = L.load()
         self.desc, self.X, self.R = desc, X, R  # keep the device buffers alive

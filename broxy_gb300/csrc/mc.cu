@@ -285,12 +285,16 @@ __global__ void __launch_bounds__(1024) k_scan_bricks(uint32_t* __restrict__ bt,
 // Float expressions of findIntersection (MarchingCubesMesher.cu:98-100) with
 // the corner point minC + idx * cellSize (MarchingCubesMesher.cu:1329-1331),
 // evaluated with explicit rounding so that host and device agree bit for bit.
+// The corner values are 0 or 1 and differ along an edge, so v2 - v1 is +1 or
+// -1 and the IEEE quotient is the numerator or its negation, exactly
+// (signed zeros included): no division is issued.
 __device__ __forceinline__ float lerp_coord(float p1, float p2, float v1, float v2, float iso) {
   const float t = __fsub_rn(iso, v1);
-  return __fadd_rn(p1, __fdiv_rn(__fmul_rn(t, __fsub_rn(p2, p1)), __fsub_rn(v2, v1)));
+  const float num = __fmul_rn(t, __fsub_rn(p2, p1));
+  return __fadd_rn(p1, __fsub_rn(v2, v1) > 0.f ? num : -num);
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, GDims gd, McWin w,
+__global__ void __launch_bounds__(kMcThreads, 4) k_mc_vertices(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                              const uint32_t* __restrict__ brick_off,
                                                              uint32_t* __restrict__ cell_voff,
                                                              float* __restrict__ V, float bx, float by, float bz,

@@ -453,6 +453,22 @@ __device__ __forceinline__ uint32_t gpair(int delta, uint32_t cap) {
   return g | (g << 16);
 }
 
+// kernel value at delta = k >= 1 (the +side), without the general
+// lattice_dist; the -side of LAT and CUBE at -k equals the +side at k - 1,
+// and CEN2 is symmetric
+template <int G>
+__device__ __forceinline__ uint32_t kern_pos(int k) {
+  if (G == KERN_LAT) return (uint32_t)(k * k);
+  if (G == KERN_LAT2) return (uint32_t)(4 * k * k);
+  if (G == KERN_CEN2) return (uint32_t)((2 * k - 1) * (2 * k - 1));
+  return (uint32_t)k;  // KERN_CUBE
+}
+
+__device__ __forceinline__ uint32_t pack_cap(uint32_t g, uint32_t cap) {
+  g = g < cap ? g : cap;
+  return g | (g << 16);
+}
+
 template <int G>
 __device__ __forceinline__ uint32_t step_min(uint32_t row, uint32_t g, uint32_t best) {
   if (G == KERN_CUBE) return __vminu2(__vmaxu2(row, g), best);
@@ -569,13 +585,17 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     const uint32_t g0 = gpair<G>(0, cap);
 #pragma unroll
     for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tcol[(sp0 + j) * 32], g0, capp);
+    uint32_t gprev = g0;  // +side kernel of the previous tap (the -side of this one for LAT, CUBE)
     for (int kb = 0; kb <= halo_e; kb += kDpxPer) {
 #pragma unroll
       for (int u = 0; u < kDpxPer; u++) {
         const int k = kb + u;
         if (k == 0) continue;
         if (k > halo_e) goto dpx_done;
-        const uint32_t gp = gpair<G>(k, cap), gm_ = gpair<G>(-k, cap);
+        const uint32_t graw = kern_pos<G>(k);
+        const uint32_t gp = pack_cap(graw, cap);
+        const uint32_t gm_ = G == KERN_CEN2 ? gp : gprev;
+        gprev = gp;
 #pragma unroll
         for (int j = 0; j < kDpxPer; j++) {
           best[j] = step_min<G>(wp[(j + u) % kDpxPer], gp, best[j]);
@@ -586,13 +606,13 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
         // sp0 + k and sp0 + 15 - k are free now (k < halo_e keeps both in the window)
         wp[u] = tcol[(sp0 + k + kDpxPer) * 32];
         wm[(kDpxPer - 1 - u) % kDpxPer] = tcol[(sp0 - k - 1) * 32];
-        if (u & 1) {
+        if ((u & 3) == 3) {  // every fourth tap: leave once no output can improve
           uint32_t m = best[0];
 #pragma unroll
           for (int j = 1; j < kDpxPer; j++) m = __vmaxu2(m, best[j]);
           const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
-          const uint32_t np = kern_g<G>(k + 1), nm = kern_g<G>(-(k + 1));
-          const uint32_t nxt = np < nm ? np : nm;
+          // smallest kernel value of the taps to come (k + 1 on either side)
+          const uint32_t nxt = G == KERN_CEN2 ? kern_pos<G>(k + 1) : graw;
           if (__all_sync(0xffffffffu, nxt >= mx)) goto dpx_done;
         }
       }

@@ -203,7 +203,7 @@ static void brush_box(const Server& s, const gm_edit& e, int lo[3], int hi[3]) {
 //    the dirty box reaches an open side;
 //  * two more cells for the mesh of the dirty box (cube corners one cell
 //    past it, cubes of one more cell tagged).
-// Crops are cubes whose edge is a multiple of 32 cells (or the whole grid).
+// Crops are cubes whose edge is a multiple of 16 cells (or the whole grid).
 static bool plan_edit(const Server& s, const gm_edit& e, Plan& p) {
   const int res = s.desc.res;
   int flo[3], fhi[3];
@@ -239,7 +239,7 @@ static bool plan_edit(const Server& s, const gm_edit& e, Plan& p) {
     const int need = hi - lo + 2 * Mc;
     span = need > span ? need : span;
   }
-  int cres = (span + 31) / 32 * 32;
+  int cres = (span + 15) / 16 * 16;
   if (cres >= res) cres = res;
   if (cres > s.max_cres) return false;
   for (int a = 0; a < 3; a++) {
@@ -458,7 +458,7 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
                            const gm_server_opts* opts, gm_server** out) {
   if (!desc || !d_input || !d_scale || !opts || !out) return GM_ERR_INVALID_ARGUMENT;
   if (!pow2i(desc->res) || desc->res < 16 || desc->res > 1024) return GM_ERR_INVALID_ARGUMENT;
-  const bool crop_ok = opts->max_crop_res == desc->res || (opts->max_crop_res >= 32 && opts->max_crop_res % 32 == 0);
+  const bool crop_ok = opts->max_crop_res == desc->res || (opts->max_crop_res >= 16 && opts->max_crop_res % 16 == 0);
   if (opts->slots < 1 || opts->slots > 16 || !crop_ok || opts->max_crop_res > desc->res || opts->rmax < 2 ||
       opts->rmax > 127)
     return GM_ERR_INVALID_ARGUMENT;

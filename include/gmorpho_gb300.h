@@ -214,7 +214,7 @@ typedef struct gm_server gm_server;
 
 typedef struct {
   int32_t slots;            /* concurrent edits (1..16) */
-  int32_t max_crop_res;     /* largest local re-closing, base cells per axis (a multiple of 32, or res) */
+  int32_t max_crop_res;     /* largest local re-closing, base cells per axis (a multiple of 16, or res) */
   int32_t rmax;             /* radius bound (fine voxels) for edits and field */
   int32_t mode;             /* gm_mode of the closing */
   int32_t bilateral_iters;  /* normal filtering of the re-meshed patches */

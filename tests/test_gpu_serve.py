@@ -21,8 +21,8 @@ def _setup(res=128, seed=301):
 
 
 def _edits(res, n=12, seed=7):
-    """Brush edits whose crops (rmax 8) are 64 or 96 cells: not powers of two
-    as well as powers of two."""
+    """Brush edits of two sizes: crops (rmax 8) of several edges, not only
+    powers of two."""
     rng = np.random.default_rng(seed)
     cs = 0.5 / res  # fine voxel (scale-field cell)
     out = []
@@ -57,7 +57,8 @@ def test_local_reclosing_equals_full_closing(gm_ctx):
     edits = _edits(128)
     desc, X, R, C, results, srv = _run(3, edits)
     assert len(results) == len(edits) and all(r["status"] == L.GM_OK for r in results)
-    assert {64, 96} <= {r["crop_res"] for r in results}
+    crops = {r["crop_res"] for r in results}
+    assert len(crops) >= 2 and any(c & (c - 1) for c in crops)  # several sizes, not only powers of two
     full = gm_ctx.close(desc, X, R, 0, L.GM_REF, L.GM_SE_SPHERE)
     torch.cuda.synchronize()
     assert torch.equal(C, full)
