@@ -36,8 +36,8 @@ struct BatchLane {
   cudaEvent_t done = nullptr;
   uint8_t* ws = nullptr;
   size_t ws_bytes = 0;
-  uint8_t *Xc = nullptr, *Cc = nullptr, *Rc = nullptr;  // crop buffers
-  size_t crop_cells = 0, crop_fine = 0;
+  uint8_t *Xc = nullptr, *Cc = nullptr;  // crop buffers (radius fields are read in place)
+  size_t crop_cells = 0;
 };
 
 struct BatchState {
@@ -70,7 +70,6 @@ void batch_release(void* p) {
     cudaFree(l.ws);
     cudaFree(l.Xc);
     cudaFree(l.Cc);
-    cudaFree(l.Rc);
   }
   for (MeshBuffers& m : b->meshes) m.release();
   if (b->h_tot) cudaFreeHost(b->h_tot);
@@ -159,15 +158,12 @@ static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* i
     a.X = it[i].d_input;
     a.R = it[i].d_scale;
     if (crop) {
-      const int zero[3] = {0, 0, 0}, e3[3] = {E, E, E}, f3[3] = {2 * E, 2 * E, 2 * E};
+      const int zero[3] = {0, 0, 0}, e3[3] = {E, E, E};
       if ((e = launch_box_copy(it[i].d_input, res, zero, ln.Xc, E, zero, e3, ln.st, kc)) != cudaSuccess) return e;
       a.X = ln.Xc;
-      if (it[i].d_scale) {
-        if ((e = launch_box_copy(reinterpret_cast<const uint8_t*>(it[i].d_scale), 2 * res, zero,
-                                 reinterpret_cast<uint8_t*>(ln.Rc), 2 * E, zero, f3, ln.st, kc)) != cudaSuccess)
-          return e;
-        a.R = reinterpret_cast<const int8_t*>(ln.Rc);
-      }
+      // the radius field is read in place, with the instance grid's strides
+      a.r_sy = 2 * (int64_t)res;
+      a.r_sz = 4 * (int64_t)res * res;
     }
     a.uniform_r = it[i].uniform_radius;
     a.rmax = rmax[i];
@@ -258,12 +254,10 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
   if ((e = ensure_lanes(b, maxL)) != cudaSuccess) return e;
   // per-lane workspaces and crop buffers sized for the largest closing
   int maxres = 16, maxcrop = 0;
-  bool crop_field = false;
   for (int i = 0; i < n; i++) {
     maxres = std::max(maxres, ext[i]);
     if (ext[i] < it[i].desc.res) {
       maxcrop = std::max(maxcrop, ext[i]);
-      crop_field |= it[i].d_scale != nullptr;
     }
   }
   const size_t wsb = close_workspace_bytes(maxres);
@@ -285,13 +279,6 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
       if ((e = cudaMalloc(&ln.Xc, ccells)) != cudaSuccess) return e;
       if ((e = cudaMalloc(&ln.Cc, ccells)) != cudaSuccess) return e;
       ln.crop_cells = ccells;
-    }
-    if (crop_field && ln.crop_fine < 8 * ccells) {
-      cudaFree(ln.Rc);
-      ln.Rc = nullptr;
-      ln.crop_fine = 0;
-      if ((e = cudaMalloc(&ln.Rc, 8 * ccells)) != cudaSuccess) return e;
-      ln.crop_fine = 8 * ccells;
     }
   }
   if (tune) {

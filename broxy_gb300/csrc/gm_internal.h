@@ -51,6 +51,7 @@ struct CloseArgs {
   int data_res[3];    // cells with data (GMorpho/Voxelizer.cu:453-454)
   const uint8_t* X;   // input packed grid, res^3
   const int8_t* R;    // fine radius grid (2res)^3, or nullptr for uniform_r
+  int64_t r_sy = 0, r_sz = 0;  // its y / z strides in bytes when it is a view into a larger field (0: dense)
   int uniform_r;      // radius when R == nullptr
   int rmax;           // upper bound of the clamped radius over the grid
   int mode;           // 0 = GM_REF, 1 = GM_EXACT
@@ -135,6 +136,9 @@ cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, Kerne
 cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
                               uint32_t* h_tot4);
 cudaError_t mesh_count_finish(MeshBuffers& b, const uint32_t* tot, int64_t* nv, int64_t* nt);
+// Allocate up front for meshes of a cubic grid of edge res with up to nv
+// vertices and nt triangles (later meshes only grow the buffers further).
+cudaError_t mesh_reserve(MeshBuffers& b, int res, int64_t nv, int64_t nt);
 // Phase 2: emission into b (capacities must be >= counts).
 cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt, cudaStream_t st,
                       KernelCounter* kc);

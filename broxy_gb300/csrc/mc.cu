@@ -846,13 +846,8 @@ static McWin window_of(const MeshArgs& a) {
   return w;
 }
 
-cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
-                              uint32_t* h_tot4) {
-  int d[3];
-  grid_dims(a, d);
-  const GDims gd{d[0], d[1], d[2]};
-  const int64_t cells = (int64_t)d[0] * d[1] * d[2];
-  const int nb = brick_count(d);
+// capacity helpers: buffers grow (never shrink) to the sizes asked for
+static cudaError_t ensure_grid_buffers(MeshBuffers& b, int64_t cells, int nb) {
   cudaError_t e;
   if (nb + 1 > b.bricks_cap) {
     if (b.brick_tot) cudaFree(b.brick_tot);
@@ -868,6 +863,64 @@ cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st
     if (e != cudaSuccess) return e;
     b.cells_cap = cells;
   }
+  return cudaSuccess;
+}
+
+static cudaError_t ensure_vertex_buffers(MeshBuffers& b, int64_t nv) {
+  cudaError_t e;
+  if (b.v_cap < nv || b.V == nullptr) {
+    cudaFree(b.V); cudaFree(b.N); cudaFree(b.N4a); cudaFree(b.N4b); cudaFree(b.rowptr); cudaFree(b.cursor);
+    b.V = b.N = nullptr;
+    b.N4a = b.N4b = nullptr;
+    b.rowptr = b.cursor = nullptr;
+    b.v_cap = 0;
+    const int64_t c = nv + nv / 4 + 1024;
+    if ((e = cudaMalloc(&b.V, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.N, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.N4a, sizeof(float4) * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.N4b, sizeof(float4) * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.rowptr, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.cursor, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
+    b.v_cap = c;
+  }
+  return cudaSuccess;
+}
+
+static cudaError_t ensure_triangle_buffers(MeshBuffers& b, int64_t nt) {
+  cudaError_t e;
+  if (b.t_cap < nt || b.T == nullptr) {
+    cudaFree(b.T); cudaFree(b.adj); cudaFree(b.nbr); cudaFree(b.wpos);
+    b.T = b.adj = nullptr;
+    b.nbr = nullptr;
+    b.wpos = nullptr;
+    b.t_cap = 0;
+    const int64_t c = nt + nt / 4 + 1024;
+    if ((e = cudaMalloc(&b.T, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.adj, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.nbr, sizeof(uint2) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.wpos, sizeof(float2) * 3 * (size_t)c)) != cudaSuccess) return e;
+    b.t_cap = c;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t mesh_reserve(MeshBuffers& b, int res, int64_t nv, int64_t nt) {
+  const int d[3] = {res, res, res};
+  cudaError_t e = ensure_grid_buffers(b, (int64_t)res * res * res, brick_count(d));
+  if (e == cudaSuccess) e = ensure_vertex_buffers(b, nv);
+  if (e == cudaSuccess) e = ensure_triangle_buffers(b, nt);
+  return e;
+}
+
+cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
+                              uint32_t* h_tot4) {
+  int d[3];
+  grid_dims(a, d);
+  const GDims gd{d[0], d[1], d[2]};
+  const int64_t cells = (int64_t)d[0] * d[1] * d[2];
+  const int nb = brick_count(d);
+  cudaError_t e = ensure_grid_buffers(b, cells, nb);
+  if (e != cudaSuccess) return e;
   GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, gd, window_of(a), b.brick_tot));
   GM_LAUNCH(kc, "k_scan_bricks", st, k_scan_bricks<<<1, 1024, 0, st>>>(b.brick_tot, nb));
   return cudaMemcpyAsync(h_tot4, b.brick_tot + 4 * (size_t)nb, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -909,34 +962,8 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   const McWin w = window_of(a);
   cudaError_t e;
   // per-vertex buffers share one capacity, per-triangle buffers another
-  if (b.v_cap < nv || b.V == nullptr) {
-    cudaFree(b.V); cudaFree(b.N); cudaFree(b.N4a); cudaFree(b.N4b); cudaFree(b.rowptr); cudaFree(b.cursor);
-    b.V = b.N = nullptr;
-    b.N4a = b.N4b = nullptr;
-    b.rowptr = b.cursor = nullptr;
-    b.v_cap = 0;
-    const int64_t c = nv + nv / 4 + 1024;
-    if ((e = cudaMalloc(&b.V, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.N, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.N4a, sizeof(float4) * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.N4b, sizeof(float4) * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.rowptr, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.cursor, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
-    b.v_cap = c;
-  }
-  if (b.t_cap < nt || b.T == nullptr) {
-    cudaFree(b.T); cudaFree(b.adj); cudaFree(b.nbr); cudaFree(b.wpos);
-    b.T = b.adj = nullptr;
-    b.nbr = nullptr;
-    b.wpos = nullptr;
-    b.t_cap = 0;
-    const int64_t c = nt + nt / 4 + 1024;
-    if ((e = cudaMalloc(&b.T, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.adj, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.nbr, sizeof(uint2) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.wpos, sizeof(float2) * 3 * (size_t)c)) != cudaSuccess) return e;
-    b.t_cap = c;
-  }
+  if ((e = ensure_vertex_buffers(b, nv)) != cudaSuccess) return e;
+  if ((e = ensure_triangle_buffers(b, nt)) != cudaSuccess) return e;
   const float cs = 0.5f * a.cell_size;  // exact: scaling by a power of two
   cudaMemsetAsync(b.fix, 0, sizeof(uint32_t), st);
   GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],

@@ -27,6 +27,16 @@
 
 namespace gm {
 
+// A radius field read in place: element (x, y, z) at p[x + y sy + z sz]
+// (a whole field, or a crop of a larger one without copying it).
+struct RField {
+  const int8_t* p;
+  int64_t sy, sz;
+};
+__device__ __forceinline__ int rget(const RField& f, int x, int y, int z) {
+  return f.p[(int64_t)x + (int64_t)y * f.sy + (int64_t)z * f.sz];
+}
+
 // ---------------------------------------------------------------------
 // pass X of the dilation: 1-D lattice distance to the nearest occupied
 // voxel along each fine row, from the packed byte grid.
@@ -127,7 +137,7 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
 // Sites are sparse (the contour shell), so each site splats its
 // contribution u(q) + e(q - p)^2 to the outputs within reach with shared
 // atomicMin, instead of every output scanning the window.
-__global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ S, const int8_t* __restrict__ R,
+__global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ S, RField R,
                                                     int uniform_r, int rx, int ry, int halo, uint32_t K,
                                                     uint16_t* __restrict__ HC, uint16_t* __restrict__ HL) {
   extern __shared__ uint32_t sm_words[];
@@ -174,8 +184,7 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
         const int x = (w << 5) + __ffs(m) - 1;
         m &= m - 1;
         int rq = ru;
-        if (R != nullptr)
-          rq = clamp_radius(R[idx3(x, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)]);
+        if (R.p != nullptr) rq = clamp_radius(rget(R, x, 2 * cy + (r & 1), 2 * cz + (r >> 1)));
         site_pos[base + k] = ((uint32_t)r << 16) | (uint32_t)x;
         // offset K - 4 (r-1)^2 (< 2^16) and the site's reach r - 1 (a point
         // at |q - p| >= r(q) is never eroded by q: e >= 2 (r(q) - 1))
@@ -320,7 +329,7 @@ enum Fin { FIN_DIL = 0, FIN_ERO = 1 };
 
 template <int G, int F>
 __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in, uint8_t* __restrict__ out_cells,
-                                                 const int8_t* __restrict__ R, int uniform_r, int rx, int ry, int rz,
+                                                 RField R, int uniform_r, int rx, int ry, int rz,
                                                  int halo, uint32_t cap) {
   extern __shared__ uint16_t tile2[];  // [2][span][32]
   const int Nx = 2 * rx, Ny = 2 * ry, N = 2 * rz;  // N: fine extent along the pass axis z
@@ -354,7 +363,7 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
       const uint32_t v = column_min<G>(tile + tx, z - lo, span, halo);
       bool b;
       if (F == FIN_DIL) {
-        const int r = R != nullptr ? clamp_radius(R[idx3(x, y, z, Nx, Ny)]) : ru;
+        const int r = R.p != nullptr ? clamp_radius(rget(R, x, y, z)) : ru;
         if (G == KERN_CUBE) b = v <= (uint32_t)r;
         else b = v < (uint32_t)((r + 1) * (r + 1));
       } else {
@@ -527,7 +536,7 @@ __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, i
 template <int G, typename TIn, int FIN>
 __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
-                                                  int sub, int halo, uint32_t cap, const int8_t* __restrict__ R,
+                                                  int sub, int halo, uint32_t cap, RField R,
                                                   int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
                                                   int rext) {
   extern __shared__ uint32_t tileu[];
@@ -678,8 +687,9 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
       uint32_t blo, bhi;
       if (FIN == 1) {
         int rlo = ru, rhi = ru;
-        if (R != nullptr && colok && z < N) {
-          const uint16_t rr = *reinterpret_cast<const uint16_t*>(R + idx3(x, third, z, nx, ny));
+        if (R.p != nullptr && colok && z < N) {
+          // x even and even strides: a 2-byte aligned pair
+          const uint16_t rr = *reinterpret_cast<const uint16_t*>(R.p + (int64_t)x + third * R.sy + z * R.sz);
           rlo = clamp_radius((int)(int8_t)(rr & 0xff));
           rhi = clamp_radius((int)(int8_t)(rr >> 8));
         }
@@ -718,7 +728,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
 
 template <int G, typename TIn, int FIN>
 static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
-                       int halo, uint32_t cap, const int8_t* R, int uniform_r, int rx, int ry, cudaStream_t st,
+                       int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry, cudaStream_t st,
                        KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0) {
   const size_t smem = dpx_smem_bytes(sub, halo);
   static size_t configured = 0;
@@ -738,18 +748,24 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
 // Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
 // field of edge n (a multiple of 16): one block per map cell, one 16-byte
 // row segment per thread.
-__global__ void __launch_bounds__(256) k_radius_map(const int8_t* __restrict__ R, int nx, int ny, int mbx, int mby,
+__global__ void __launch_bounds__(256) k_radius_map(RField R, int mbx, int mby, int aligned,
                                                      uint8_t* __restrict__ out) {
   const int b = blockIdx.x;
   const int bx = b % mbx, by = (b / mbx) % mby, bz = b / (mbx * mby);
   const int fy = 16 * by + (threadIdx.x & 15), fz = 16 * bz + (threadIdx.x >> 4);
-  const uint4 v = *reinterpret_cast<const uint4*>(R + idx3(16 * bx, fy, fz, nx, ny));
-  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  const int8_t* row = R.p + (int64_t)16 * bx + fy * R.sy + fz * R.sz;
   int m = 0;
+  if (aligned) {
+    const uint4 v = *reinterpret_cast<const uint4*>(row);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-  for (int k = 0; k < 4; k++)
+    for (int k = 0; k < 4; k++)
 #pragma unroll
-    for (int j = 0; j < 4; j++) m = max(m, (int)(int8_t)((w[k] >> (8 * j)) & 0xffu));
+      for (int j = 0; j < 4; j++) m = max(m, (int)(int8_t)((w[k] >> (8 * j)) & 0xffu));
+  } else {
+#pragma unroll
+    for (int j = 0; j < 16; j++) m = max(m, (int)row[j]);
+  }
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   __shared__ int wm[8];
   if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
@@ -761,10 +777,10 @@ __global__ void __launch_bounds__(256) k_radius_map(const int8_t* __restrict__ R
   }
 }
 
-cudaError_t launch_radius_map(const int8_t* R, int nx, int ny, int nz, uint8_t* out, cudaStream_t st,
-                              KernelCounter* kc) {
+cudaError_t launch_radius_map(RField R, int nx, int ny, int nz, uint8_t* out, cudaStream_t st, KernelCounter* kc) {
   const int mbx = nx / 16, mby = ny / 16, mbz = nz / 16;
-  GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<mbx * mby * mbz, 256, 0, st>>>(R, nx, ny, mbx, mby, out));
+  const int aligned = ((uintptr_t)R.p % 16 == 0 && R.sy % 16 == 0 && R.sz % 16 == 0) ? 1 : 0;
+  GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<mbx * mby * mbz, 256, 0, st>>>(R, mbx, mby, aligned, out));
   return cudaGetLastError();
 }
 
@@ -1028,6 +1044,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const int rmax = a.rmax;
   DataRes dr{{a.data_res[0], a.data_res[1], a.data_res[2]}};
   const bool exact = a.mode == 1;
+  const RField RF{a.R, a.r_sy > 0 ? a.r_sy : (int64_t)Nx, a.r_sz > 0 ? a.r_sz : (int64_t)Nx * Ny};
+  const RField RNONE{nullptr, 0, 0};
 
   // ---- dilation ----
   const int dil_r = rmax + 1;  // "Safety Measure" radius + 1 (GMorpho.cu:2864)
@@ -1036,7 +1054,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const int dil_halo = dil_r + 1;
   const uint8_t* tile_map = nullptr;  // per-tile radius bounds of the dilation passes
   if (a.R != nullptr) {
-    if (launch_radius_map(a.R, Nx, Ny, Nz, rmap, st, kc) != cudaSuccess) return cudaGetLastError();
+    if (launch_radius_map(RF, Nx, Ny, Nz, rmap, st, kc) != cudaSuccess) return cudaGetLastError();
     tile_map = rmap;
   }
   {
@@ -1046,14 +1064,14 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     uint8_t* dst = exact ? D : Df;
     if (dil_cap <= 32767) {
       if (a.se == 1) {
-        launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, nullptr, 0, rx,
+        launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
                                           ry, st, kc, "k_pass_dil_y", tile_map, dil_halo);
-        launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r,
+        launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
                                            rx, ry, st, kc, "k_pass_dil_z", tile_map, 0);
       } else {
-        launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, nullptr, 0, rx,
+        launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
                                          ry, st, kc, "k_pass_dil_y", tile_map, dil_halo);
-        launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, a.R, a.uniform_r,
+        launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
                                           rx, ry, st, kc, "k_pass_dil_z", tile_map, 0);
       }
     } else {
@@ -1068,10 +1086,10 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       dim3 gz(cdiv(Nx, 32), cdiv(Nz, kTileOut), Ny / 2);
       if (a.se == 1)
         GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CUBE, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                           buf16a, dst, a.R, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
+                                           buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
       else
         GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                           buf16a, dst, a.R, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
+                                           buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
     }
     if (!exact) {
       GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr));
@@ -1092,16 +1110,16 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       ero_x_configured = smem;
     }
     GM_LAUNCH(kc, "k_ero_pass_x", st,
-              k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, a.R, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1));
+              k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, RF, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1));
     if (K <= 32767) {
-      launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, nullptr, 0, rx, ry, st,
+      launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
                                          kc, "k_pass_ero_y");
-      launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, nullptr, 0, rx, ry, st, kc,
+      launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
                                          "k_pass_ero_z");
       if (!exact) {
-        launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, nullptr, 0, rx, ry, st, kc,
+        launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
                                            "k_pass_erob_y");
-        launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, nullptr, 0, rx, ry, st, kc,
+        launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
                                            "k_pass_erob_z");
       }
     } else {
@@ -1111,7 +1129,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                            buf16a, buf16b, Nx, Ny, Nz, 1, 0, ehalo, K));
       dim3 gz(cdiv(Nx, 32), cdiv(Nz, kTileOut), Ny / 2);
       GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CEN2, FIN_ERO><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                         buf16b, Ef, nullptr, 0, rx, ry, rz, ehalo, K));
+                                         buf16b, Ef, RNONE, 0, rx, ry, rz, ehalo, K));
       if (!exact) {
         const int span_s = 2 * kTileOut + 2 * ehalo;
         dim3 gyb(cdiv(rx, 32), cdiv(ry, kTileOut), Nz);

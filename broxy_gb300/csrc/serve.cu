@@ -76,7 +76,6 @@ struct Slot {
   int phase = 0;              // 0 idle, 1 closing + counting, 2 emitting
   MeshArgs ma;
   uint8_t *Xc = nullptr, *Cc = nullptr, *ws = nullptr;
-  int8_t* Rc = nullptr;
   MeshBuffers mesh;
   bool busy = false;
   uint64_t ticket = 0;
@@ -116,6 +115,8 @@ struct Server {
   uint64_t next_ticket = 1;
   KernelCounter* kc = nullptr;
 };
+
+constexpr int kLookAhead = 64;  // queued edits examined per dispatch round
 
 static double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -297,15 +298,11 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
   if ((err = launch_scale_brush(s.R, 2 * res, bmin, 0.5f * s.desc.cell_size, e.center, e.scale, e.support,
                                 e.global_scale, e.mode, sl.st, s.kc)) != cudaSuccess)
     return err;
-  // 2. crop the packed grid and the radius field
+  // 2. crop the packed grid (the radius field is read in place)
   {
     const int zero[3] = {0, 0, 0};
-    const int ext[3] = {cres, cres, cres}, ext2[3] = {2 * cres, 2 * cres, 2 * cres};
-    const int f0[3] = {2 * crop.lo[0], 2 * crop.lo[1], 2 * crop.lo[2]};
+    const int ext[3] = {cres, cres, cres};
     if ((err = launch_box_copy(s.X, res, crop.lo, sl.Xc, cres, zero, ext, sl.st, s.kc)) != cudaSuccess) return err;
-    if ((err = launch_box_copy(reinterpret_cast<const uint8_t*>(s.R), 2 * res, f0, reinterpret_cast<uint8_t*>(sl.Rc),
-                               2 * cres, zero, ext2, sl.st, s.kc)) != cudaSuccess)
-      return err;
   }
   // 3. close the crop
   CloseArgs a;
@@ -315,7 +312,10 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
     a.data_res[k] = d < 0 ? 0 : (d > cres ? cres : d);
   }
   a.X = sl.Xc;
-  a.R = sl.Rc;
+  const int64_t N = 2 * (int64_t)res;
+  a.R = s.R + 2 * crop.lo[0] + N * 2 * crop.lo[1] + N * N * 2 * crop.lo[2];
+  a.r_sy = N;
+  a.r_sz = N * N;
   a.uniform_r = 0;
   a.rmax = pl.rclose;
   a.mode = s.mode;
@@ -413,27 +413,38 @@ static void progress(Server& s) {
     sl.busy = false;
     sl.phase = 0;
   }
-  // dispatch queued edits in order while slots are free and crops disjoint
-  while (!s.queue.empty()) {
-    const Pending& p = s.queue.front();
+  // Dispatch queued edits while slots are free.  An edit whose crop meets
+  // the crop of an edit on the GPU, or of an earlier edit still queued,
+  // waits (its result depends on that edit); later edits independent of
+  // everything before them go ahead of it (bounded look-ahead).
+  std::vector<Box3> waiting;  // crops of the earlier edits that stay queued
+  int looked = 0;
+  for (auto it = s.queue.begin(); it != s.queue.end() && looked < kLookAhead; looked++) {
+    Slot* free_slot = nullptr;
+    for (Slot& sl : s.slots)
+      if (!sl.busy) { free_slot = &sl; break; }
+    if (!free_slot) break;
     Plan pl;
-    if (!plan_edit(s, p.edit, pl)) {
+    if (!plan_edit(s, it->edit, pl)) {
       gm_edit_result r = {};
-      r.ticket = p.ticket;
+      r.ticket = it->ticket;
       r.status = GM_ERR_CAPACITY;
       s.done.push_back(r);
-      s.queue.pop_front();
+      it = s.queue.erase(it);
       continue;
     }
     bool conflict = false;
-    Slot* free_slot = nullptr;
-    for (Slot& sl : s.slots) {
+    for (const Slot& sl : s.slots)
       if (sl.busy && sl.crop.overlaps(pl.crop)) conflict = true;
-      if (!sl.busy && !free_slot) free_slot = &sl;
+    for (const Box3& w : waiting)
+      if (w.overlaps(pl.crop)) conflict = true;
+    if (conflict) {
+      waiting.push_back(pl.crop);
+      ++it;
+      continue;
     }
-    if (conflict || !free_slot) break;
-    const Pending pe = p;
-    s.queue.pop_front();
+    const Pending pe = *it;
+    it = s.queue.erase(it);
     if (dispatch(s, *free_slot, pe, pl) != cudaSuccess) {
       cudaGetLastError();
       fail_slot(s, *free_slot, GM_ERR_CUDA);
@@ -520,8 +531,11 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
     if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tot, 4 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&sl.Xc, ccells);
     if (e == cudaSuccess) e = cudaMalloc(&sl.Cc, ccells);
-    if (e == cudaSuccess) e = cudaMalloc(&sl.Rc, 8 * ccells);
     if (e == cudaSuccess) e = cudaMalloc(&sl.ws, gm::close_workspace_bytes(s.max_cres));
+    // mesh buffers for a patch of a few surface layers across the largest
+    // crop, so that the first large edits do not allocate
+    const int64_t nt = 16 * (int64_t)s.max_cres * s.max_cres;
+    if (e == cudaSuccess) e = gm::mesh_reserve(sl.mesh, s.max_cres, nt / 2, nt);
     s.slots.push_back(sl);
   }
   if (e != cudaSuccess) {
@@ -546,7 +560,6 @@ gm_status gm_server_destroy(gm_server* srv) {
     if (sl.h_tot) cudaFreeHost(sl.h_tot);
     cudaFree(sl.Xc);
     cudaFree(sl.Cc);
-    cudaFree(sl.Rc);
     cudaFree(sl.ws);
     sl.mesh.release();
   }
