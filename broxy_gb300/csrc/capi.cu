@@ -102,6 +102,8 @@ struct gm_ctx {
   int* d_int = nullptr;
   // voxelizer scratch
   uint8_t* vox = nullptr;
+  uint8_t* rmap = nullptr;  // 16^3-block radius map of the last radius field
+  size_t rmap_bytes = 0;
   size_t vox_bytes = 0;
   // batched closing + meshing state (lanes, per-instance meshes, graph)
   void* batch = nullptr;
@@ -205,6 +207,7 @@ gm_status gm_ctx_destroy(gm_ctx* ctx) {
   cudaFree(ctx->d_R);
   cudaFree(ctx->d_C);
   cudaFree(ctx->d_int);
+  cudaFree(ctx->rmap);
   cudaFree(ctx->vox);
   ctx->mesh.release();
   gm::batch_release(ctx->batch);
@@ -345,11 +348,16 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   const int64_t fine = (int64_t)8 * res * res * res;
   int rmax;
   if (d_scale) {
-    GM_CHECK_CUDA(ctx, gm::launch_rmax(d_scale, fine, ctx->d_int, ctx->num_sms, st, &ctx->kc), "radius bound");
+    // the radius bound and the per-tile radius map in one pass over the field
+    if ((s = ensure(ctx, (void**)&ctx->rmap, ctx->rmap_bytes, (size_t)fine / 4096 + 16, "radius map")) != GM_OK)
+      return s;
+    GM_CHECK_CUDA(ctx, gm::launch_radius_map_dense(d_scale, 2 * res, 2 * res, 2 * res, ctx->rmap, ctx->d_int, st,
+                                                   &ctx->kc),
+                  "radius bound");
     int h = 0;
     GM_CHECK_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_int, sizeof(int), cudaMemcpyDeviceToHost, st), "radius bound");
     GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "radius bound");
-    rmax = h;
+    rmax = h < 2 ? 2 : h;
   } else {
     rmax = gm::clamp_radius(uniform_radius);
   }
@@ -369,6 +377,7 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   a.S_out = d_contour;
   a.workspace = ctx->ws;
   a.num_sms = ctx->num_sms;
+  a.rmap_in = d_scale ? ctx->rmap : nullptr;
   GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close");
   return GM_OK;
 }

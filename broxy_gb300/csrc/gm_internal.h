@@ -52,6 +52,7 @@ struct CloseArgs {
   const uint8_t* X;   // input packed grid, res^3
   const int8_t* R;    // fine radius grid (2res)^3, or nullptr for uniform_r
   int64_t r_sy = 0, r_sz = 0;  // its y / z strides in bytes when it is a view into a larger field (0: dense)
+  const uint8_t* rmap_in = nullptr;  // its 16^3-block radius map when already built (launch_radius_map_dense)
   int uniform_r;      // radius when R == nullptr
   int rmax;           // upper bound of the clamped radius over the grid
   int mode;           // 0 = GM_REF, 1 = GM_EXACT
@@ -68,6 +69,11 @@ size_t close_workspace_bytes_box(int rx, int ry, int rz);
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc);
+// The 16^3-block map of the largest raw radius of a dense field of nx*ny*nz
+// fine voxels ((nx/16)(ny/16)(nz/16) bytes), and its largest clamped radius
+// into *d_rmax (when given).
+cudaError_t launch_radius_map_dense(const int8_t* R, int nx, int ny, int nz, uint8_t* out, int* d_rmax,
+                                    cudaStream_t st, KernelCounter* kc);
 
 // ---------------------------------------------------------------- crops
 cudaError_t launch_box_copy(const uint8_t* src, int sn, const int s0[3], uint8_t* dst, int dn, const int d0[3],

@@ -538,7 +538,8 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
                                                   int sub, int halo, uint32_t cap, RField R,
                                                   int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
-                                                  int rext) {
+                                                  int rext, const uint8_t* __restrict__ dmap, int mdx, int mdy,
+                                                  int mdz) {
   extern __shared__ uint32_t tileu[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tpar = w >> 2, grp = w & 3;
@@ -563,7 +564,29 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     cap = ct < cap ? ct : cap;
     halo_e = rt + 2 < halo ? rt + 2 : halo;
   }
-  const int skip = halo - halo_e;  // tile rows never read
+  // Erosion outputs matter only where the dilation has voxels: the centre
+  // flags on D grown by one cell (the refinement tags cells next to D), the
+  // lattice flags on D.  A tile whose cells (so grown) hold no voxel of D,
+  // by the 8^3-cell occupancy map of D, writes "not eroded" without work.
+  bool needed = true;
+  if ((FIN == 2 || FIN == 3) && dmap != nullptr) {
+    const int grow = FIN == 2 ? 1 : 0;
+    const int cx0 = FIN == 2 ? (int)(blockIdx.x * kDpxCols) / 2 : (int)(blockIdx.x * kDpxCols);
+    const int cx1 = cx0 + (FIN == 2 ? kDpxCols / 2 : kDpxCols) - 1;
+    const int cy0 = FIN == 2 ? (int)blockIdx.z : 2 * (int)blockIdx.z, cy1 = FIN == 2 ? cy0 : cy0 + 1;
+    const int cz0 = FIN == 2 ? o0 / 2 : o0, cz1 = cz0 + (FIN == 2 ? kDpxOut / 2 : kDpxOut) - 1;
+    const int ax = max(cx0 - grow, 0) >> 3, bx = min((cx1 + grow) >> 3, mdx - 1);
+    const int ay = max(cy0 - grow, 0) >> 3, by = min((cy1 + grow) >> 3, mdy - 1);
+    const int az = max(cz0 - grow, 0) >> 3, bz = min((cz1 + grow) >> 3, mdz - 1);
+    const int cnx = bx - ax + 1, cny = by - ay + 1, cnz = bz - az + 1;
+    int any = 0;
+    for (int i = threadIdx.x; i < cnx * cny * cnz; i += blockDim.x) {
+      const int ix = ax + i % cnx, iy = ay + (i / cnx) % cny, iz = az + i / (cnx * cny);
+      any |= dmap[idx3(ix, iy, iz, mdx, mdy)];
+    }
+    needed = __syncthreads_or(any) != 0;
+  }
+  const int skip = needed ? halo - halo_e : span;  // tile rows never read
   const uint32_t capp = cap | (cap << 16);
   uint32_t* tile = tileu + tpar * span * 32;
   const bool colok = x < nx && third < n3;
@@ -729,7 +752,8 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
 template <int G, typename TIn, int FIN>
 static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
                        int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry, cudaStream_t st,
-                       KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0) {
+                       KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0,
+                       const uint8_t* dmap = nullptr, int mdx = 0, int mdy = 0, int mdz = 0) {
   const size_t smem = dpx_smem_bytes(sub, halo);
   static size_t configured = 0;
   if (smem > 48 * 1024 && smem > configured) {
@@ -742,46 +766,88 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, (n3 + 1) / 2);
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
-                                                          uniform_r, rx, ry, rmap, rext));
+                                                          uniform_r, rx, ry, rmap, rext, dmap, mdx, mdy, mdz));
 }
 
 // Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
 // field of edge n (a multiple of 16): one block per map cell, one 16-byte
 // row segment per thread.
+// Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
+// field (nx, ny, nz multiples of 16).  One block per (map y, map z) row of
+// map cells; a lane owns a map cell along x and a warp 32 of the 256 fine
+// rows, so each warp load is 32 consecutive 16-byte segments.  With
+// d_rmax, the largest clamped radius is folded into *d_rmax as well.
 __global__ void __launch_bounds__(256) k_radius_map(RField R, int mbx, int mby, int aligned,
-                                                     uint8_t* __restrict__ out) {
-  const int b = blockIdx.x;
-  const int bx = b % mbx, by = (b / mbx) % mby, bz = b / (mbx * mby);
-  const int fy = 16 * by + (threadIdx.x & 15), fz = 16 * bz + (threadIdx.x >> 4);
-  const int8_t* row = R.p + (int64_t)16 * bx + fy * R.sy + fz * R.sz;
-  int m = 0;
-  if (aligned) {
-    const uint4 v = *reinterpret_cast<const uint4*>(row);
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+                                                     uint8_t* __restrict__ out, int* __restrict__ d_rmax) {
+  const int my = blockIdx.x, mz = blockIdx.y;
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ int part[8][32];
+  int gmax = 0;
+  for (int cb = 0; cb < mbx; cb += 32) {
+    const int cx = cb + lane;
+    int m = 0;
+    if (cx < mbx) {
+      for (int r = wid; r < 256; r += 8) {
+        const int8_t* row = R.p + (int64_t)16 * cx + (int64_t)(16 * my + (r & 15)) * R.sy +
+                            (int64_t)(16 * mz + (r >> 4)) * R.sz;
+        if (aligned) {
+          const uint4 v = *reinterpret_cast<const uint4*>(row);
+          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int k = 0; k < 4; k++)
+          for (int k = 0; k < 4; k++)
 #pragma unroll
-      for (int j = 0; j < 4; j++) m = max(m, (int)(int8_t)((w[k] >> (8 * j)) & 0xffu));
-  } else {
+            for (int j = 0; j < 4; j++) m = max(m, (int)(int8_t)((w[k] >> (8 * j)) & 0xffu));
+        } else {
 #pragma unroll
-    for (int j = 0; j < 16; j++) m = max(m, (int)row[j]);
+          for (int j = 0; j < 16; j++) m = max(m, (int)row[j]);
+        }
+      }
+    }
+    part[wid][lane] = m;
+    __syncthreads();
+    if (wid == 0) {
+      int t = 0;
+      for (int k = 0; k < 8; k++) t = max(t, part[k][lane]);
+      if (cx < mbx) out[cx + (int64_t)mbx * (my + (int64_t)mby * mz)] = (uint8_t)t;
+      gmax = max(gmax, t);
+    }
+    __syncthreads();
   }
-  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __shared__ int wm[8];
-  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int t = 0;
-    for (int k = 0; k < 8; k++) t = max(t, wm[k]);
-    out[b] = (uint8_t)t;
+  if (d_rmax != nullptr && wid == 0) {
+    for (int o = 16; o > 0; o >>= 1) gmax = max(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+    if (lane == 0) atomicMax(d_rmax, clamp_radius(gmax));
   }
 }
 
-cudaError_t launch_radius_map(RField R, int nx, int ny, int nz, uint8_t* out, cudaStream_t st, KernelCounter* kc) {
+cudaError_t launch_radius_map(RField R, int nx, int ny, int nz, uint8_t* out, int* d_rmax, cudaStream_t st,
+                              KernelCounter* kc) {
   const int mbx = nx / 16, mby = ny / 16, mbz = nz / 16;
   const int aligned = ((uintptr_t)R.p % 16 == 0 && R.sy % 16 == 0 && R.sz % 16 == 0) ? 1 : 0;
-  GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<mbx * mby * mbz, 256, 0, st>>>(R, mbx, mby, aligned, out));
+  if (d_rmax) cudaMemsetAsync(d_rmax, 0, sizeof(int), st);
+  GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<dim3(mby, mbz), 256, 0, st>>>(R, mbx, mby, aligned, out, d_rmax));
   return cudaGetLastError();
+}
+
+cudaError_t launch_radius_map_dense(const int8_t* R, int nx, int ny, int nz, uint8_t* out, int* d_rmax,
+                                    cudaStream_t st, KernelCounter* kc) {
+  return launch_radius_map(RField{R, (int64_t)nx, (int64_t)nx * ny}, nx, ny, nz, out, d_rmax, st, kc);
+}
+
+// 1 for each 8^3 block of cells of a cell grid (rx, ry, rz multiples of
+// 16) holding a non-zero byte: one warp per block, two 8-byte rows a lane.
+__global__ void __launch_bounds__(256) k_occ_map8(const uint8_t* __restrict__ G, int rx, int ry, int mdx, int mdy,
+                                                  int nblocks, uint8_t* __restrict__ out) {
+  const int b = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (b >= nblocks) return;
+  const int bx = b % mdx, by = (b / mdx) % mdy, bz = b / (mdx * mdy);
+  uint64_t acc = 0;
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int r = lane + 32 * k;  // row r of the block: y = r & 7, z = r >> 3
+    acc |= *reinterpret_cast<const uint64_t*>(G + idx3(8 * bx, 8 * by + (r & 7), 8 * bz + (r >> 3), rx, ry));
+  }
+  const int any = __any_sync(0xffffffffu, acc != 0);
+  if (lane == 0) out[b] = any ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------
@@ -1010,7 +1076,8 @@ size_t close_workspace_bytes_box(int rx, int ry, int rz) {
   const size_t Nx = 2 * (size_t)rx, Ny = 2 * (size_t)ry, Nz = 2 * (size_t)rz, V = Nx * Ny * Nz;
   const size_t cells = (size_t)rx * ry * rz;
   // buf16 x2, buf8, HL1 (rx, Ny, Nz), HL2 (rx, ry, Nz), Df, Eb, Ef, S, D, radius map + alignment slack
-  return 2 * V * 2 + V + (size_t)rx * Ny * Nz * 2 + (size_t)rx * ry * Nz * 2 + 5 * cells + V / 4096 + 16 * 256;
+  return 2 * V * 2 + V + (size_t)rx * Ny * Nz * 2 + (size_t)rx * ry * Nz * 2 + 5 * cells + V / 4096 + cells / 512 +
+         16 * 256;
 }
 
 size_t close_workspace_bytes(int res) { return close_workspace_bytes_box(res, res, res); }
@@ -1041,6 +1108,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   uint8_t* S = carve(p, cells);
   uint8_t* D = a.D_out != nullptr ? a.D_out : carve(p, cells);
   uint8_t* rmap = carve(p, V / 4096);
+  const int mdx = rx / 8, mdy = ry / 8, mdz = rz / 8;
+  uint8_t* dmap = carve(p, (size_t)mdx * mdy * mdz);
   const int rmax = a.rmax;
   DataRes dr{{a.data_res[0], a.data_res[1], a.data_res[2]}};
   const bool exact = a.mode == 1;
@@ -1053,8 +1122,10 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const uint32_t dil_cap = a.se == 1 ? (uint32_t)(rmax + 1) : (uint32_t)(dil_r * dil_r);
   const int dil_halo = dil_r + 1;
   const uint8_t* tile_map = nullptr;  // per-tile radius bounds of the dilation passes
-  if (a.R != nullptr) {
-    if (launch_radius_map(RF, Nx, Ny, Nz, rmap, st, kc) != cudaSuccess) return cudaGetLastError();
+  if (a.R != nullptr && a.rmap_in != nullptr) {
+    tile_map = a.rmap_in;  // built by the caller together with the radius bound
+  } else if (a.R != nullptr) {
+    if (launch_radius_map(RF, Nx, Ny, Nz, rmap, nullptr, st, kc) != cudaSuccess) return cudaGetLastError();
     tile_map = rmap;
   }
   {
@@ -1095,6 +1166,11 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr));
     }
   }
+  // ---- occupancy map of D (erosion outputs are needed on D only) ----
+  {
+    const int nb = mdx * mdy * mdz;
+    GM_LAUNCH(kc, "k_occ_map8", st, k_occ_map8<<<(nb + 7) / 8, 256, 0, st>>>(D, rx, ry, mdx, mdy, nb, dmap));
+  }
   // ---- contour ----
   GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact ? 1 : 0));
   // ---- erosion ----
@@ -1115,12 +1191,12 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
                                          kc, "k_pass_ero_y");
       launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                         "k_pass_ero_z");
+                                         "k_pass_ero_z", nullptr, 0, dmap, mdx, mdy, mdz);
       if (!exact) {
         launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
                                            "k_pass_erob_y");
         launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_z");
+                                           "k_pass_erob_z", nullptr, 0, dmap, mdx, mdy, mdz);
       }
     } else {
       const int span = kTileOut + 2 * ehalo;
