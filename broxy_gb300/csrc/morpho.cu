@@ -37,6 +37,21 @@ __device__ __forceinline__ int rget(const RField& f, int x, int y, int z) {
   return f.p[(int64_t)x + (int64_t)y * f.sy + (int64_t)z * f.sz];
 }
 
+// The two x-bits of fine row r (y parity r & 1, z parity r >> 1) of four
+// packed bytes, gathered into 8 bits (byte b -> bits 2b, 2b+1).
+__device__ __forceinline__ uint32_t row_bits8(uint32_t w, int r) {
+  uint32_t x = (w >> (2 * r)) & 0x03030303u;
+  x = (x | (x >> 6)) & 0x000f000fu;
+  return (x | (x >> 12)) & 0xffu;
+}
+
+// The four fine rows of 16 packed bytes as 32-bit words (one per row).
+__device__ __forceinline__ void rows_of_16_bytes(const uint4 q, uint32_t o[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; r++)
+    o[r] = row_bits8(q.x, r) | (row_bits8(q.y, r) << 8) | (row_bits8(q.z, r) << 16) | (row_bits8(q.w, r) << 24);
+}
+
 // ---------------------------------------------------------------------
 // pass X of the dilation: 1-D lattice distance to the nearest occupied
 // voxel along each fine row, from the packed byte grid.
@@ -54,34 +69,29 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
   uint32_t* bits = sm_words;            // [4][W]
   uint32_t* corner = sm_words + 4 * W;  // [4][W]
   const uint8_t* row = X + idx3(0, cy, cz, rx, ry);
-  int any = 0, all = 1;
-  // word w of a fine row covers bytes 16w .. 16w+15 of the byte row
-  for (int w = threadIdx.x; w < W; w += blockDim.x) {
-    const uint4 q = *reinterpret_cast<const uint4*>(row + 16 * w);
-    const uint32_t by[4] = {q.x, q.y, q.z, q.w};
-    uint32_t o[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int b = 0; b < 16; b++) {
-      const uint32_t v = (by[b >> 2] >> (8 * (b & 3))) & 0xffu;
-#pragma unroll
-      for (int r = 0; r < 4; r++) o[r] |= ((v >> (2 * r)) & 3u) << (2 * b);
-    }
-#pragma unroll
-    for (int r = 0; r < 4; r++) bits[r * W + w] = o[r];
-    any |= (q.x | q.y | q.z | q.w) != 0u;
-    all &= (q.x & q.y & q.z & q.w) == 0xffffffffu;
-  }
-  any = __syncthreads_or(any);
-  all = __syncthreads_and(all);
+  // word w of a fine row covers bytes 16w .. 16w+15 of the byte row (W <= 256)
+  uint4 q = make_uint4(0u, 0u, 0u, 0u);
+  const bool has = threadIdx.x < W;
+  if (has) q = *reinterpret_cast<const uint4*>(row + 16 * threadIdx.x);
+  const int any = __syncthreads_or(has && (q.x | q.y | q.z | q.w) != 0u);
+  const int all = __syncthreads_and(!has || (q.x & q.y & q.z & q.w) == 0xffffffffu);
   if (!any || all) {
     // empty rows: nothing within reach; full rows: every corner is a site
     const uint32_t v = !any ? (uint32_t)dcap * 0x01010101u : 0u;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {  // 4 rows x N/4 words
-      const int r = i / (N >> 2), p4 = 4 * (i - r * (N >> 2));
-      *reinterpret_cast<uint32_t*>(A + idx3(p4, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)) = v;
+    const uint4 v4 = make_uint4(v, v, v, v);
+    for (int i = threadIdx.x; i < N >> 2; i += blockDim.x) {  // 4 rows x N/16 vectors
+      const int r = i / (N >> 4), p16 = 16 * (i - r * (N >> 4));
+      *reinterpret_cast<uint4*>(A + idx3(p16, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)) = v4;
     }
     return;
   }
+  if (has) {
+    uint32_t o[4];
+    rows_of_16_bytes(q, o);
+#pragma unroll
+    for (int r = 0; r < 4; r++) bits[r * W + threadIdx.x] = o[r];
+  }
+  __syncthreads();
   for (int i = threadIdx.x; i < 4 * W; i += blockDim.x) {
     const int r = i / W, w = i - r * W;
     const uint32_t b = bits[i];
@@ -152,25 +162,34 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
   __shared__ int nsites;
   const uint8_t* row = S + idx3(0, cy, cz, rx, ry);
   if (threadIdx.x == 0) nsites = 0;
-  __syncthreads();
-  int any = 0;
-  for (int w = threadIdx.x; w < W; w += blockDim.x) {
-    const uint4 q = *reinterpret_cast<const uint4*>(row + 16 * w);
-    const uint32_t by[4] = {q.x, q.y, q.z, q.w};
-    uint32_t o[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int b = 0; b < 16; b++) {
-      const uint32_t v = (by[b >> 2] >> (8 * (b & 3))) & 0xffu;
-#pragma unroll
-      for (int r = 0; r < 4; r++) o[r] |= ((v >> (2 * r)) & 3u) << (2 * b);
+  // word w of a fine row covers bytes 16w .. 16w+15 of the byte row (W <= 256)
+  uint4 q16 = make_uint4(0u, 0u, 0u, 0u);
+  const bool has = threadIdx.x < W;
+  if (has) q16 = *reinterpret_cast<const uint4*>(row + 16 * threadIdx.x);
+  const int any = __syncthreads_or(has && (q16.x | q16.y | q16.z | q16.w) != 0u);
+  if (!any) {
+    // no site in these rows: every output keeps the saturation value K
+    const uint32_t k2 = K | (K << 16);
+    const uint4 v4 = make_uint4(k2, k2, k2, k2);
+    for (int i = threadIdx.x; i < N >> 1; i += blockDim.x) {  // 4 rows x N/8 vectors
+      const int r = i / (N >> 3), p8 = 8 * (i - r * (N >> 3));
+      *reinterpret_cast<uint4*>(HC + idx3(p8, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)) = v4;
     }
-#pragma unroll
-    for (int r = 0; r < 4; r++) bits[r * W + w] = o[r];
-    any |= (q.x | q.y | q.z | q.w) != 0u;
+    for (int i = threadIdx.x; i < res >> 1; i += blockDim.x) {  // 4 rows x rx/8 vectors
+      const int r = i / (res >> 3), c8 = 8 * (i - r * (res >> 3));
+      *reinterpret_cast<uint4*>(HL + idx3(c8, 2 * cy + (r & 1), 2 * cz + (r >> 1), rx, Ny)) = v4;
+    }
+    return;
   }
-  any = __syncthreads_or(any);
+  if (has) {
+    uint32_t o[4];
+    rows_of_16_bytes(q16, o);
+#pragma unroll
+    for (int r = 0; r < 4; r++) bits[r * W + threadIdx.x] = o[r];
+  }
+  __syncthreads();
   const int ru = clamp_radius(uniform_r);
-  if (any) {
+  {
     for (int i = threadIdx.x; i < 4 * N; i += blockDim.x) hc[i] = K;
     for (int i = threadIdx.x; i < 4 * res; i += blockDim.x) hl[i] = K;
     // compact the sites with their offsets
@@ -221,12 +240,12 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
   // write out (u16 pairs)
   for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) {
     const int r = i / (N >> 1), p2 = 2 * (i - r * (N >> 1));
-    const uint32_t v = any ? (hc[r * N + p2] | (hc[r * N + p2 + 1] << 16)) : (K | (K << 16));
+    const uint32_t v = hc[r * N + p2] | (hc[r * N + p2 + 1] << 16);
     *reinterpret_cast<uint32_t*>(HC + idx3(p2, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny)) = v;
   }
   for (int i = threadIdx.x; i < 2 * res; i += blockDim.x) {
     const int r = i / (res >> 1), c2 = 2 * (i - r * (res >> 1));
-    const uint32_t v = any ? (hl[r * res + c2] | (hl[r * res + c2 + 1] << 16)) : (K | (K << 16));
+    const uint32_t v = hl[r * res + c2] | (hl[r * res + c2 + 1] << 16);
     *reinterpret_cast<uint32_t*>(HL + idx3(c2, 2 * cy + (r & 1), 2 * cz + (r >> 1), rx, Ny)) = v;
   }
 }
