@@ -787,8 +787,10 @@ __global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __re
       const uint2 bc = nbr[i];
       const float2 wp = wpos[i];
       const float4 nb = Nin[bc.x], nc = Nin[bc.y];
-      const float w1 = expf(-__fadd_rn(wp.x, __fdiv_rn(dist2n(na, nb), sn2)));
-      const float w2 = expf(-__fadd_rn(wp.y, __fdiv_rn(dist2n(na, nc), sn2)));
+      // the reference library is built with -use_fast_math (GMorpho/cuda.prf:47),
+      // so its exp and division here are the fast forms
+      const float w1 = __expf(-__fadd_rn(wp.x, __fdividef(dist2n(na, nb), sn2)));
+      const float w2 = __expf(-__fadd_rn(wp.y, __fdividef(dist2n(na, nc), sn2)));
       acc.x = __fadd_rn(acc.x, __fadd_rn(__fmul_rn(w1, nb.x), __fmul_rn(w2, nc.x)));
       acc.y = __fadd_rn(acc.y, __fadd_rn(__fmul_rn(w1, nb.y), __fmul_rn(w2, nc.y)));
       acc.z = __fadd_rn(acc.z, __fadd_rn(__fmul_rn(w1, nb.z), __fmul_rn(w2, nc.z)));

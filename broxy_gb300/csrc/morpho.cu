@@ -504,21 +504,16 @@ __device__ __forceinline__ uint32_t step_min(uint32_t row, uint32_t g, uint32_t 
 }
 
 template <int G, typename TIn>
-__device__ __forceinline__ uint32_t load_pair(const TIn* p, uint32_t cap) {
-  uint32_t a, b;
+__device__ __forceinline__ uint32_t load_pair(const TIn* p, uint32_t capp) {
+  uint32_t v;
   if (sizeof(TIn) == 1) {
-    const uint16_t v = *reinterpret_cast<const uint16_t*>(p);
-    a = v & 0xffu;
-    b = v >> 8;
-    if (G != KERN_CUBE) { a = a * a; b = b * b; }
+    const uint32_t w = *reinterpret_cast<const uint16_t*>(p);
+    const uint32_t a = w & 0xffu, b = w >> 8;
+    v = G != KERN_CUBE ? (a * a) | ((b * b) << 16) : a | (b << 16);
   } else {
-    const uint32_t v = *reinterpret_cast<const uint32_t*>(p);
-    a = v & 0xffffu;
-    b = v >> 16;
+    v = *reinterpret_cast<const uint32_t*>(p);
   }
-  a = a < cap ? a : cap;
-  b = b < cap ? b : cap;
-  return a | (b << 16);
+  return __vminu2(v, capp);  // both lanes saturated at cap
 }
 
 size_t dpx_smem_bytes(int sub, int halo) {
@@ -613,7 +608,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
   for (int s = skip + grp; s < span - skip; s += 4) {
     const int a = lo + s;
     uint32_t v = capp;
-    if (colok && a >= 0 && a < na) v = load_pair<G, TIn>(in + x + sa * a + s3 * third, cap);
+    if (colok && a >= 0 && a < na) v = load_pair<G, TIn>(in + x + sa * a + s3 * third, capp);
     tile[s * 32 + lane] = v;
     finite |= v != capp;
   }
@@ -726,29 +721,32 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     for (int j = 0; j < kDpxPer; j++) {
       const int z = obase + j;
       const uint32_t v = best[j];
-      uint32_t blo, bhi;
+      // per-lane thresholds T (bit = value < T)
+      uint32_t tpair;
       if (FIN == 1) {
-        int rlo = ru, rhi = ru;
+        uint32_t r2;  // the two clamped radii, one per u16 lane
         if (R.p != nullptr && colok && z < N) {
           // x even and even strides: a 2-byte aligned pair
-          const uint16_t rr = *reinterpret_cast<const uint16_t*>(R.p + (int64_t)x + third * R.sy + z * R.sz);
-          rlo = clamp_radius((int)(int8_t)(rr & 0xff));
-          rhi = clamp_radius((int)(int8_t)(rr >> 8));
-        }
-        if (G == KERN_CUBE) {
-          blo = (v & 0xffffu) <= (uint32_t)rlo;
-          bhi = (v >> 16) <= (uint32_t)rhi;
+          const uint32_t rr = *reinterpret_cast<const uint16_t*>(R.p + (int64_t)x + third * R.sy + z * R.sz);
+          const uint32_t c = __vmins4(__vmaxs4(rr, 0x02020202u), 0x7f7f7f7fu);  // clamp to [2, 127] per byte
+          r2 = __byte_perm(c, 0u, 0x4140);
         } else {
-          blo = (v & 0xffffu) < (uint32_t)((rlo + 1) * (rlo + 1));
-          bhi = (v >> 16) < (uint32_t)((rhi + 1) * (rhi + 1));
+          r2 = (uint32_t)ru | ((uint32_t)ru << 16);
+        }
+        const uint32_t r1 = r2 + 0x00010001u;  // r + 1 per lane (<= 128)
+        if (G == KERN_CUBE) {
+          tpair = r1;  // value <= r
+        } else {
+          const uint32_t lo = r1 & 0xffffu, hi = r1 >> 16;
+          tpair = (lo * lo) | ((hi * hi) << 16);  // value < (r + 1)^2
         }
       } else {
-        blo = (v & 0xffffu) < cap;
-        bhi = (v >> 16) < cap;
+        tpair = capp;
       }
+      const uint32_t m = __vcmpltu2(v, tpair);  // 0xffff per lane below its threshold
+      const uint32_t b2 = (m & 1u) | ((m >> 15) & 2u);
       const int q = j >> 1, zb = j & 1;
-      const uint32_t bits = (blo << (2 * tpar + 4 * zb)) | (bhi << (1 + 2 * tpar + 4 * zb));
-      bytes[q >> 2] |= bits << (8 * (q & 3));
+      bytes[q >> 2] |= (b2 << (2 * tpar + 4 * zb)) << (8 * (q & 3));
     }
     if (tpar == 1) {
       xch[grp][lane][0] = bytes[0];

@@ -7,7 +7,8 @@ triples (connectivity and emission order), vertices within 1e-6 relative.
 Normals after bilateral filtering: within 2e-3 absolute per component (the
 reference accumulates them with float atomics, so their order and last
 bits are not fixed; the GPU path sums in triangle order like the oracle and
-differs only through expf rounding).
+differs through the fast exp and division of the bilateral weights, which
+the reference's own fast-math build uses too).
 """
 import numpy as np
 import pytest
