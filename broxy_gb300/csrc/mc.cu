@@ -218,24 +218,90 @@ __device__ __forceinline__ CellCounts block_exclusive_scan(CellCounts v, CellCou
                     wpre[3] + inc[3] - a[3]};
 }
 
+// block-wide exclusive scan of one counter (256 threads); total in `total`
+__device__ __forceinline__ uint32_t block_scan1(uint32_t v, uint32_t& total) {
+  __shared__ uint32_t wt[kMcThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += t;
+  }
+  if (lane == 31) wt[wid] = x;
+  __syncthreads();
+  uint32_t pre = 0, tot = 0;
+#pragma unroll
+  for (int k = 0; k < kMcThreads / 32; k++) {
+    pre += k < wid ? wt[k] : 0u;
+    tot += wt[k];
+  }
+  __syncthreads();
+  total = tot;
+  return pre + x - v;
+}
+
+// The brick's own cells that may hold a tagged mixed cube (not uniform,
+// inside the tag window), in Morton order, into list[]; returns how many
+// (block-uniform).  The cube work then runs over this list with every lane
+// busy, instead of each thread walking its 16 cells and the warp taking the
+// slow path whenever one lane needs it.
+__device__ int brick_candidates(const uint8_t* tile, const McWin& w, int ox, int oy, int oz, uint16_t* list) {
+  uint32_t mask = 0;
+#pragma unroll 4
+  for (int i = 0; i < kCellsPerThread; i++) {
+    const int l = threadIdx.x * kCellsPerThread + i;
+    int lx, ly, lz;
+    local_coords(l, lx, ly, lz);
+    if (!cell_uniform(tile, lx, ly, lz) && win_tag(w, ox + lx, oy + ly, oz + lz)) mask |= 1u << i;
+  }
+  uint32_t total;
+  uint32_t k = block_scan1(__popc(mask), total);
+  while (mask) {
+    const int i = __ffs(mask) - 1;
+    mask &= mask - 1;
+    list[k++] = (uint16_t)(threadIdx.x * kCellsPerThread + i);
+  }
+  __syncthreads();
+  return (int)total;
+}
+
+// exclusive prefix sums of cnt[0..n) in place (list order), per-thread
+// contiguous chunks; returns the total
+__device__ uint32_t block_prefix_inplace(uint32_t* cnt, int n) {
+  const int per = (n + kMcThreads - 1) / kMcThreads;
+  const int b0 = threadIdx.x * per, b1 = min(n, b0 + per);
+  uint32_t sum = 0;
+  for (int j = b0; j < b1; j++) sum += cnt[j];
+  uint32_t total;
+  uint32_t run = block_scan1(sum, total);
+  for (int j = b0; j < b1; j++) {
+    const uint32_t c = cnt[j];
+    cnt[j] = run;
+    run += c;
+  }
+  __syncthreads();
+  return total;
+}
+
 __global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                           uint32_t* __restrict__ brick_tot) {
   __shared__ uint8_t tile[kTileCells];
+  __shared__ uint16_t list[kCellsPerBrick];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
   if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) {
     if (threadIdx.x < 4) brick_tot[4 * blockIdx.x + threadIdx.x] = 0;
     return;
   }
+  const int nc = brick_candidates(tile, w, ox, oy, oz, list);
   CellCounts acc{0, 0, 0, 0};
-  for (int i = 0; i < kCellsPerThread; i++) {
-    const int l = threadIdx.x * kCellsPerThread + i;
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
     int lx, ly, lz;
-    local_coords(l, lx, ly, lz);
-    if (cell_uniform(tile, lx, ly, lz)) continue;
+    local_coords(list[j], lx, ly, lz);
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, win_tag(w, ox + lx, oy + ly, oz + lz));
+    const int m = mixed_mask(vals, true);
     if (!m) continue;
     const CellCounts c = cell_counts(vals, m);
     acc.cubes += c.cubes; acc.verts += c.verts;
@@ -294,41 +360,39 @@ __device__ __forceinline__ float lerp_coord(float p1, float p2, float v1, float 
   return __fadd_rn(p1, __fsub_rn(v2, v1) > 0.f ? num : -num);
 }
 
-__global__ void __launch_bounds__(kMcThreads, 4) k_mc_vertices(const uint8_t* __restrict__ C, GDims gd, McWin w,
-                                                             const uint32_t* __restrict__ brick_off,
-                                                             uint32_t* __restrict__ cell_voff,
-                                                             float* __restrict__ V, float bx, float by, float bz,
-                                                             float cs, float iso) {
+__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, GDims gd, McWin w,
+                                                          const uint32_t* __restrict__ brick_off,
+                                                          uint32_t* __restrict__ cell_voff,
+                                                          float* __restrict__ V, float bx, float by, float bz,
+                                                          float cs, float iso) {
   __shared__ uint8_t tile[kTileCells];
+  __shared__ uint16_t list[kCellsPerBrick];
+  __shared__ uint32_t offs[kCellsPerBrick];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
   if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) return;
-  CellCounts acc{0, 0, 0, 0};
-  for (int i = 0; i < kCellsPerThread; i++) {
-    const int l = threadIdx.x * kCellsPerThread + i;
+  const int nc = brick_candidates(tile, w, ox, oy, oz, list);
+  // vertices per candidate, then their offsets in Morton order
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
     int lx, ly, lz;
-    local_coords(l, lx, ly, lz);
-    if (cell_uniform(tile, lx, ly, lz)) continue;
+    local_coords(list[j], lx, ly, lz);
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, win_tag(w, ox + lx, oy + ly, oz + lz));
-    if (!m) continue;
-    const CellCounts c = cell_counts(vals, m);
-    acc.verts += c.verts;
+    const int m = mixed_mask(vals, true);
+    offs[j] = m ? cell_counts(vals, m).verts : 0u;
   }
-  CellCounts tot;
-  const CellCounts pre = block_exclusive_scan(acc, tot);
-  uint32_t vo = brick_off[4 * blockIdx.x + 1] + pre.verts;
-  for (int i = 0; i < kCellsPerThread; i++) {
-    const int l = threadIdx.x * kCellsPerThread + i;
+  __syncthreads();
+  block_prefix_inplace(offs, nc);
+  const uint32_t base = brick_off[4 * blockIdx.x + 1];
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
     int lx, ly, lz;
-    local_coords(l, lx, ly, lz);
-    if (cell_uniform(tile, lx, ly, lz)) continue;
+    local_coords(list[j], lx, ly, lz);
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    const int m = mixed_mask(vals, win_tag(w, gx, gy, gz));
+    const int m = mixed_mask(vals, true);
     if (!m) continue;
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
+    uint32_t vo = base + offs[j];
     cell_voff[gidx(gx, gy, gz, gd)] = vo;
     for (int s = 0; s < 8; s++) {
       if (!((m >> s) & 1)) continue;
@@ -390,6 +454,23 @@ __device__ __forceinline__ uint32_t cell_info(const uint8_t* tile, int lx, int l
 
 constexpr int kInfoE = kBrick + 1;  // cells 0..16 of the brick (own + one neighbour layer)
 
+__device__ __forceinline__ uint32_t info_of(const int vals[8], int m) {
+  uint32_t info = (uint32_t)m;
+#pragma unroll
+  for (int s = 0; s < 8; s++) {
+    if (!((m >> s) & 1)) continue;
+    const int em = edge_mask(vals[s]);
+    info |= (uint32_t)(em & 1) << (8 + s);
+    info |= (uint32_t)((em >> 3) & 1) << (16 + s);
+    info |= (uint32_t)((em >> 8) & 1) << (24 + s);
+  }
+  return info;
+}
+
+// dynamic shared memory of k_mc_triangles
+constexpr size_t kTriSmem = sizeof(uint32_t) * (kInfoE * kInfoE * kInfoE + kCellsPerBrick) +
+                            sizeof(uint16_t) * kCellsPerBrick + kTileCells;
+
 // Vertex offset of cube k of the cell whose summary is `info` (absent: -1),
 // with its edge-0 / edge-3 ownership.
 __device__ __forceinline__ long long cube_voff(uint32_t info, uint32_t cell_off, int k, int& e0, int& e3) {
@@ -407,37 +488,42 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
                                                               const uint32_t* __restrict__ cell_voff,
                                                               uint32_t* __restrict__ T, uint32_t nt_total,
                                                               uint32_t* __restrict__ fix, int fix_cap) {
-  __shared__ uint8_t tile[kTileCells];
-  __shared__ uint32_t info[kInfoE * kInfoE * kInfoE];
+  extern __shared__ uint32_t mc_smem[];
+  uint32_t* info = mc_smem;                                   // [17^3]
+  uint32_t* offs = info + kInfoE * kInfoE * kInfoE;           // [4096]
+  uint16_t* list = reinterpret_cast<uint16_t*>(offs + kCellsPerBrick);  // [4096]
+  uint8_t* tile = reinterpret_cast<uint8_t*>(list + kCellsPerBrick);    // [18^3]
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
   if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) return;
+  for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) info[i] = 0u;
+  const int nc = brick_candidates(tile, w, ox, oy, oz, list);
+  // summaries of the own candidates, and their triangle counts
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+    int lx, ly, lz;
+    local_coords(list[j], lx, ly, lz);
+    int vals[8];
+    cube_values(tile, lx, ly, lz, vals);
+    const int m = mixed_mask(vals, true);
+    info[lx + kInfoE * (ly + kInfoE * lz)] = info_of(vals, m);
+    offs[j] = (m && win_emit(w, ox + lx, oy + ly, oz + lz)) ? cell_counts(vals, m).tris : 0u;
+  }
+  // the neighbour layer (cells 16 along some axis)
   for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) {
     const int lx = i % kInfoE, ly = (i / kInfoE) % kInfoE, lz = i / (kInfoE * kInfoE);
+    if (lx < kBrick && ly < kBrick && lz < kBrick) continue;
     info[i] = cell_info(tile, lx, ly, lz, win_tag(w, ox + lx, oy + ly, oz + lz));
   }
   __syncthreads();
-  CellCounts acc{0, 0, 0, 0};
-  for (int i = 0; i < kCellsPerThread; i++) {
-    const int l = threadIdx.x * kCellsPerThread + i;
+  block_prefix_inplace(offs, nc);
+  const uint32_t tbase = brick_off[4 * blockIdx.x + 2];
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
     int lx, ly, lz;
-    local_coords(l, lx, ly, lz);
-    if (!(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu)) continue;
-    if (!win_emit(w, ox + lx, oy + ly, oz + lz)) continue;
-    int vals[8];
-    cube_values(tile, lx, ly, lz, vals);
-    acc.tris += cell_counts(vals, (int)(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu)).tris;
-  }
-  CellCounts tot;
-  const CellCounts pre = block_exclusive_scan(acc, tot);
-  uint32_t to = brick_off[4 * blockIdx.x + 2] + pre.tris;
-  for (int i = 0; i < kCellsPerThread; i++) {
-    const int l = threadIdx.x * kCellsPerThread + i;
-    int lx, ly, lz;
-    local_coords(l, lx, ly, lz);
+    local_coords(list[j], lx, ly, lz);
     const uint32_t myinfo = info[lx + kInfoE * (ly + kInfoE * lz)];
     const int m = (int)(myinfo & 0xffu);
     if (!m) continue;
+    uint32_t to = tbase + offs[j];
     const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
     if (!win_emit(w, gx, gy, gz)) continue;
     int vals[8];
@@ -970,7 +1056,12 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   cudaMemsetAsync(b.fix, 0, sizeof(uint32_t), st);
   GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],
                                            a.bbox_min[2], cs, a.isovalue));
-  GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, 0, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
+  static bool tri_smem_set = false;  // > 48 KB of dynamic shared memory
+  if (!tri_smem_set) {
+    cudaFuncSetAttribute(k_mc_triangles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTriSmem);
+    tri_smem_set = true;
+  }
+  GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, kTriSmem, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
                                             b.fix_cap));
   GM_LAUNCH(kc, "k_mc_fix91", st, k_mc_fix91<<<1, 256, 0, st>>>(b.fix, b.fix_cap, b.T));
   if (nv == 0 || nt == 0) return cudaGetLastError();
