@@ -6,10 +6,11 @@ plus contour marching cubes (with normals and 20 bilateral iterations) of a
 
 One JSON line on rank 0.  ``value`` is whole-job Gvoxel/s with the inputs
 resident in HBM (device-timed with CUDA events); ``e2e`` is the same metric
-through the host-buffer C ABI call gm_update + gm_mesh_download (pinned host
+through the host-buffer C ABI call gm_update_to_host (pinned host
 buffers, H2D of the grid and the radius field and D2H of the mesh inside the
-timed region).  Under torchrun every rank closes its own replica (weak
-scaling, no collective on the data path).
+timed region; gm_update_to_host overlaps them with the work).  Under
+torchrun every rank closes its own replica (weak scaling, no collective on
+the data path).
 
 Two more objects ride on rank 0's line: ``batch`` (64 uneven grids, edges
 log-uniform in [64, 512], own radius U{1..24}: one batched call against 64
@@ -172,7 +173,7 @@ def run_ours(args, rank, world):
         ms_max = float(t.item())
     value = world * V / (ms_max * 1e-3) / 1e9
 
-    # ---- e2e through the host-buffer C ABI (gm_update + gm_mesh_download)
+    # ---- e2e through the host-buffer C ABI (gm_update_to_host)
     if args.no_e2e:
         e2e_ms, nv2, nt2 = float("nan"), nv, nt
     else:
@@ -193,14 +194,10 @@ def run_e2e(args, ctx, desc, X, R, nv, nt, world, dev):
     hV = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True)
     hN = torch.empty((nv, 3), dtype=torch.float32, pin_memory=True)
     hT = torch.empty((nt, 3), dtype=torch.int32, pin_memory=True)
-    import ctypes as C
-
     def e2e_step():
-        nv2, nt2 = ctx.update(desc, hX, hR, gs)
-        st_ = ctx.lib.gm_mesh_download(ctx.ctx, C.c_void_p(hV.data_ptr()), C.c_void_p(hN.data_ptr()),
-                                       C.c_void_p(hT.data_ptr()), api._stream())
-        api.L.check(ctx.ctx, st_)
-        return nv2, nt2
+        # gm_update_to_host: grid and radius field up, closing + mesh, mesh
+        # down into the pinned buffers, copies overlapped with the work
+        return ctx.update_to_host(desc, hX, hR, gs, hV, hN, hT)
 
     for _ in range(max(1, args.warmup - 1)):
         e2e_step()

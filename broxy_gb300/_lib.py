@@ -92,6 +92,8 @@ PROTOTYPES = {
     "gm_mesh": (C.c_int, [_P, C.POINTER(GridDesc), _P, C.c_int32, C.POINTER(MeshView), _P]),
     "gm_update": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_float, C.POINTER(UpdateOpts),
                             C.POINTER(C.c_int64), C.POINTER(C.c_int64), _P]),
+    "gm_update_to_host": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_float, C.POINTER(UpdateOpts), _P, _P, _P,
+                                    C.c_int64, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _P]),
     "gm_mesh_download": (C.c_int, [_P, _P, _P, _P, _P]),
     "gm_batch_close_mesh": (C.c_int, [_P, C.c_int32, C.POINTER(BatchItem), C.c_int, C.c_int, C.c_int32, C.c_int32,
                                        C.POINTER(MeshView), _P]),

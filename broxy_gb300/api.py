@@ -181,6 +181,26 @@ class Context:
         self._check(st)
         return nv.value, nt.value
 
+    def update_to_host(self, desc, h_X, h_R, global_scale, hV, hN, hT, asymmetric=False, bilateral=True,
+                       mode=L.GM_REF):
+        """Update from host buffers straight into host mesh buffers (pinned
+        tensors or numpy arrays of shape (cap, 3)); returns (nv, nt)."""
+        o = L.UpdateOpts(1 if asymmetric else 0, 1 if bilateral else 0, mode)
+        nv = C.c_int64(0)
+        nt = C.c_int64(0)
+
+        def ptr(a):
+            if a is None:
+                return None
+            return C.c_void_p(a.data_ptr()) if hasattr(a, "data_ptr") else a.ctypes.data_as(C.c_void_p)
+
+        vcap = hV.shape[0] if hV is not None else (hN.shape[0] if hN is not None else 0)
+        tcap = hT.shape[0] if hT is not None else 0
+        st = self.lib.gm_update_to_host(self.ctx, C.byref(desc), ptr(h_X), ptr(h_R), float(global_scale), C.byref(o),
+                                        ptr(hV), ptr(hN), ptr(hT), vcap, tcap, C.byref(nv), C.byref(nt), _stream())
+        self._check(st)
+        return nv.value, nt.value
+
     # a4
     def pyramid(self, desc, grid, R=None, uniform_radius=4):
         import torch

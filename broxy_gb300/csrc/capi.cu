@@ -107,6 +107,9 @@ struct gm_ctx {
   size_t vox_bytes = 0;
   // batched closing + meshing state (lanes, per-instance meshes, graph)
   void* batch = nullptr;
+  // host-buffer updates: a copy stream and its events
+  cudaStream_t copy_st = nullptr;
+  cudaEvent_t ev_copy = nullptr, ev_geom = nullptr;
   // last mesh
   gm::MeshBuffers mesh;
   int64_t nv = 0, nt = 0;
@@ -209,6 +212,9 @@ gm_status gm_ctx_destroy(gm_ctx* ctx) {
   cudaFree(ctx->d_int);
   cudaFree(ctx->rmap);
   cudaFree(ctx->vox);
+  if (ctx->copy_st) cudaStreamDestroy(ctx->copy_st);
+  if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+  if (ctx->ev_geom) cudaEventDestroy(ctx->ev_geom);
   ctx->mesh.release();
   gm::batch_release(ctx->batch);
   ctx->kc.release();
@@ -342,7 +348,7 @@ gm_status gm_pyramid_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t*
 
 static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
                             int32_t uniform_radius, int mode, int se, uint8_t* d_closing, uint8_t* d_dilation,
-                            uint8_t* d_contour, cudaStream_t st) {
+                            uint8_t* d_contour, cudaStream_t st, bool xpass_done = false) {
   gm_status s;
   const int res = desc->res;
   const int64_t fine = (int64_t)8 * res * res * res;
@@ -378,6 +384,7 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   a.workspace = ctx->ws;
   a.num_sms = ctx->num_sms;
   a.rmap_in = d_scale ? ctx->rmap : nullptr;
+  a.xpass_done = xpass_done;
   GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close");
   return GM_OK;
 }
@@ -537,7 +544,7 @@ gm_status gm_mesh_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_clos
 // ------------------------------------------------------------------ a12..a16
 
 static gm_status mesh_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closing, int iters,
-                           cudaStream_t st) {
+                           cudaStream_t st, cudaEvent_t geometry_done = nullptr) {
   gm::MeshArgs a;
   a.res = desc->res;
   a.C = d_closing;
@@ -546,6 +553,7 @@ static gm_status mesh_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t*
   a.isovalue = 0.95f;  // GMorpho.cu:6922
   a.bilateral_iters = iters;
   a.num_sms = ctx->num_sms;
+  a.geometry_done = geometry_done;
   int64_t nv = 0, nt = 0;
   ctx->has_mesh = false;
   GM_CHECK_CUDA(ctx, gm::mesh_count(a, ctx->mesh, st, &ctx->kc, &nv, &nt), "gm_mesh (count)");
@@ -577,6 +585,93 @@ gm_status gm_mesh(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closin
 
 // ------------------------------------------------------------------ a17
 
+// Host-buffer update.  The input grid goes up first and the dilation's x
+// pass (which reads only the grid) runs while the radius field is still
+// being copied on a second stream; with host mesh buffers, the vertices and
+// triangles come down on that stream while the normals are filtered.
+static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_input, const int8_t* h_scale,
+                             float global_scale, const gm_update_opts* opts, float* h_V, float* h_N, uint32_t* h_T,
+                             int64_t v_cap, int64_t t_cap, int64_t* num_vertices, int64_t* num_triangles,
+                             cudaStream_t st) {
+  gm_status s;
+  const int res = desc->res;
+  const size_t cells = (size_t)res * res * res;
+  const int asym = opts ? opts->use_asymmetric_closing : 0;
+  const int bil = opts ? opts->bilateral_filtering : 1;
+  const int mode = opts ? opts->mode : GM_REF;
+  if (!ctx->copy_st) {
+    GM_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_st, cudaStreamNonBlocking), "copy stream");
+    GM_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming), "copy event");
+    GM_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_geom, cudaEventDisableTiming), "geometry event");
+  }
+  if ((s = ensure(ctx, (void**)&ctx->d_X, ctx->X_bytes, cells, "input grid")) != GM_OK) return s;
+  if ((s = ensure(ctx, (void**)&ctx->d_C, ctx->C_bytes, cells, "closing grid")) != GM_OK) return s;
+  if (h_scale && (s = ensure(ctx, (void**)&ctx->d_R, ctx->R_bytes, 8 * cells, "scale grid")) != GM_OK) return s;
+  // the radius field's upload waits only for the work already on the stream
+  // (earlier uses of the buffer), then runs beside the grid's upload and x pass
+  // (the grid is issued first: copies of one direction are served in order)
+  GM_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev_copy, st), "gm_update");
+  GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_X, h_input, cells, cudaMemcpyHostToDevice, st), "gm_update H2D");
+  if (h_scale) {
+    GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_st, ctx->ev_copy, 0), "gm_update");
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_R, h_scale, 8 * cells, cudaMemcpyHostToDevice, ctx->copy_st),
+                  "gm_update H2D");
+    GM_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev_copy, ctx->copy_st), "gm_update");
+  }
+  // uniform radius in fine voxels: floor(global_scale / (cell_size / 2))
+  // (GMorpho/ScaleField.cu:143-146 with cell_size_sf = cell_size / 2)
+  const float gate = std::floor(2.f * global_scale / desc->cell_size);
+  const int uniform = (int)std::floor(global_scale / (0.5f * desc->cell_size));
+  const bool morph = gate > 1.f;
+  bool xpass = false;
+  if (morph) {
+    if ((s = ensure(ctx, (void**)&ctx->ws, ctx->ws_bytes, gm::close_workspace_bytes(res), "closing workspace")) !=
+        GM_OK)
+      return s;
+    gm::CloseArgs a;
+    a.res = res;
+    a.X = ctx->d_X;
+    a.workspace = ctx->ws;
+    GM_CHECK_CUDA(ctx, gm::launch_close_xpass(a, st, &ctx->kc), "gm_update x pass");
+    xpass = true;
+  }
+  const int8_t* d_scale = nullptr;
+  if (h_scale) {
+    GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_copy, 0), "gm_update");
+    d_scale = ctx->d_R;
+  }
+  if (morph) {
+    s = close_impl(ctx, desc, ctx->d_X, d_scale, uniform, mode, asym ? GM_SE_CUBE : GM_SE_SPHERE, ctx->d_C, nullptr,
+                   nullptr, st, xpass);
+    if (s != GM_OK) return s;
+  } else {
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_C, ctx->d_X, cells, cudaMemcpyDeviceToDevice, st), "gm_update copy");
+  }
+  const int iters = bil ? (asym ? 200 : 20) : 0;  // GMorpho.cu:7808-7811
+  const bool to_host = h_V != nullptr || h_N != nullptr || h_T != nullptr;
+  if ((s = mesh_impl(ctx, desc, ctx->d_C, iters, st, to_host ? ctx->ev_geom : nullptr)) != GM_OK) return s;
+  if (num_vertices) *num_vertices = ctx->nv;
+  if (num_triangles) *num_triangles = ctx->nt;
+  if (!to_host) return GM_OK;
+  if (ctx->nv > v_cap || ctx->nt > t_cap) {
+    GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "gm_update_to_host");
+    return fail(ctx, GM_ERR_CAPACITY, "gm_update_to_host: host mesh buffers too small (mesh kept on the device)");
+  }
+  // geometry down on the copy stream while the normals are filtered
+  GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_st, ctx->ev_geom, 0), "gm_update_to_host");
+  if (h_V && ctx->nv)
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(h_V, ctx->mesh.V, 12 * (size_t)ctx->nv, cudaMemcpyDeviceToHost, ctx->copy_st),
+                  "D2H");
+  if (h_T && ctx->nt)
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(h_T, ctx->mesh.T, 12 * (size_t)ctx->nt, cudaMemcpyDeviceToHost, ctx->copy_st),
+                  "D2H");
+  if (h_N && ctx->nv)
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(h_N, ctx->mesh.N, 12 * (size_t)ctx->nv, cudaMemcpyDeviceToHost, st), "D2H");
+  GM_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->copy_st), "gm_update_to_host");
+  GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "gm_update_to_host");
+  return GM_OK;
+}
+
 gm_status gm_update(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_input, const int8_t* h_scale,
                     float global_scale, const gm_update_opts* opts, int64_t* num_vertices, int64_t* num_triangles,
                     void* stream) {
@@ -585,37 +680,22 @@ gm_status gm_update(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_inpu
   if (s != GM_OK) return s;
   if (!h_input) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_update: NULL input grid");
   if ((s = set_device(ctx)) != GM_OK) return s;
-  cudaStream_t st = (cudaStream_t)stream;
-  const int res = desc->res;
-  const size_t cells = (size_t)res * res * res;
-  const int asym = opts ? opts->use_asymmetric_closing : 0;
-  const int bil = opts ? opts->bilateral_filtering : 1;
-  const int mode = opts ? opts->mode : GM_REF;
-  if ((s = ensure(ctx, (void**)&ctx->d_X, ctx->X_bytes, cells, "input grid")) != GM_OK) return s;
-  if ((s = ensure(ctx, (void**)&ctx->d_C, ctx->C_bytes, cells, "closing grid")) != GM_OK) return s;
-  GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_X, h_input, cells, cudaMemcpyHostToDevice, st), "gm_update H2D");
-  const int8_t* d_scale = nullptr;
-  if (h_scale) {
-    if ((s = ensure(ctx, (void**)&ctx->d_R, ctx->R_bytes, 8 * cells, "scale grid")) != GM_OK) return s;
-    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_R, h_scale, 8 * cells, cudaMemcpyHostToDevice, st), "gm_update H2D");
-    d_scale = ctx->d_R;
-  }
-  // uniform radius in fine voxels: floor(global_scale / (cell_size / 2))
-  // (GMorpho/ScaleField.cu:143-146 with cell_size_sf = cell_size / 2)
-  const float gate = std::floor(2.f * global_scale / desc->cell_size);
-  const int uniform = (int)std::floor(global_scale / (0.5f * desc->cell_size));
-  if (gate > 1.f) {
-    s = close_impl(ctx, desc, ctx->d_X, d_scale, uniform, mode, asym ? GM_SE_CUBE : GM_SE_SPHERE, ctx->d_C, nullptr,
-                   nullptr, st);
-    if (s != GM_OK) return s;
-  } else {
-    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_C, ctx->d_X, cells, cudaMemcpyDeviceToDevice, st), "gm_update copy");
-  }
-  const int iters = bil ? (asym ? 200 : 20) : 0;  // GMorpho.cu:7808-7811
-  if ((s = mesh_impl(ctx, desc, ctx->d_C, iters, st)) != GM_OK) return s;
-  if (num_vertices) *num_vertices = ctx->nv;
-  if (num_triangles) *num_triangles = ctx->nt;
-  return GM_OK;
+  return update_impl(ctx, desc, h_input, h_scale, global_scale, opts, nullptr, nullptr, nullptr, 0, 0, num_vertices,
+                     num_triangles, (cudaStream_t)stream);
+}
+
+gm_status gm_update_to_host(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_input, const int8_t* h_scale,
+                            float global_scale, const gm_update_opts* opts, float* h_V, float* h_N, uint32_t* h_T,
+                            int64_t vertex_capacity, int64_t triangle_capacity, int64_t* num_vertices,
+                            int64_t* num_triangles, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!h_input || (!h_V && !h_N && !h_T) || vertex_capacity < 0 || triangle_capacity < 0)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_update_to_host: NULL input or no output buffer");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  return update_impl(ctx, desc, h_input, h_scale, global_scale, opts, h_V, h_N, h_T, vertex_capacity,
+                     triangle_capacity, num_vertices, num_triangles, (cudaStream_t)stream);
 }
 
 gm_status gm_mesh_download(gm_ctx* ctx, float* h_V, float* h_N, uint32_t* h_T, void* stream) {

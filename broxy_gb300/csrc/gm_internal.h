@@ -53,6 +53,7 @@ struct CloseArgs {
   const int8_t* R;    // fine radius grid (2res)^3, or nullptr for uniform_r
   int64_t r_sy = 0, r_sz = 0;  // its y / z strides in bytes when it is a view into a larger field (0: dense)
   const uint8_t* rmap_in = nullptr;  // its 16^3-block radius map when already built (launch_radius_map_dense)
+  bool xpass_done = false;  // the dilation's x pass already ran (launch_close_xpass) into the workspace
   int uniform_r;      // radius when R == nullptr
   int rmax;           // upper bound of the clamped radius over the grid
   int mode;           // 0 = GM_REF, 1 = GM_EXACT
@@ -67,6 +68,10 @@ struct CloseArgs {
 size_t close_workspace_bytes(int res);
 size_t close_workspace_bytes_box(int rx, int ry, int rz);
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
+// The dilation's x pass alone (it reads only the input grid), with the
+// saturation of the largest radius, so that it can run before the radius
+// field is on the device; launch_close then skips it (xpass_done).
+cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc);
 // The 16^3-block map of the largest raw radius of a dense field of nx*ny*nz
@@ -108,6 +113,7 @@ struct MeshArgs {
   int tag_lo[3] = {0, 0, 0}, tag_hi[3] = {0, 0, 0};
   int emit_lo[3] = {0, 0, 0}, emit_hi[3] = {0, 0, 0};
   int zero_isolated = 0;  // (0,0,0) normal for vertices no triangle uses
+  cudaEvent_t geometry_done = nullptr;  // recorded once vertices and triangles are final (before normals)
 };
 
 // Device-side mesh buffers, grown on demand by the caller of launch_mesh.

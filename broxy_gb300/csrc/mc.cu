@@ -1064,6 +1064,7 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, kTriSmem, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
                                             b.fix_cap));
   GM_LAUNCH(kc, "k_mc_fix91", st, k_mc_fix91<<<1, 256, 0, st>>>(b.fix, b.fix_cap, b.T));
+  if (a.geometry_done) cudaEventRecord(a.geometry_done, st);
   if (nv == 0 || nt == 0) return cudaGetLastError();
   // normals
   const int sms = a.num_sms;

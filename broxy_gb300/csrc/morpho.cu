@@ -1147,8 +1147,9 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   }
   {
     const int W = Nx >> 5;
-    GM_LAUNCH(kc, "k_dil_pass_x", st,
-              k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, dcap));
+    if (!a.xpass_done)
+      GM_LAUNCH(kc, "k_dil_pass_x", st,
+                k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, dcap));
     uint8_t* dst = exact ? D : Df;
     if (dil_cap <= 32767) {
       if (a.se == 1) {
@@ -1239,6 +1240,24 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   if (a.S_out) {
     cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounter* kc) {
+  const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
+  const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
+  const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
+  if (rx % 16 != 0 || ry % 16 != 0 || rz % 16 != 0 || rx <= 0 || ry <= 0 || rz <= 0) return cudaErrorInvalidValue;
+  const size_t V = (size_t)8 * rx * ry * rz;
+  uint8_t* p = a.workspace;
+  carve(p, V * 2);
+  carve(p, V * 2);
+  uint8_t* buf8 = carve(p, V);  // same place as in launch_close
+  const int W = (2 * rx) >> 5;
+  // saturation of the largest clamped radius (127): exact distances up to
+  // 129, so any radius bound found later is covered
+  GM_LAUNCH(kc, "k_dil_pass_x", st,
+            k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, 129));
   return cudaGetLastError();
 }
 

@@ -175,6 +175,17 @@ gm_status gm_update(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_inpu
                     int64_t* num_triangles, void* stream);
 /* Copy the context's last mesh to host buffers (GMorpho.cu:6992-7000);
  * any pointer may be NULL to skip that array. */
+/* gm_update that also brings the mesh into the caller's host buffers (3
+ * floats per vertex for h_V / h_N, 3 indices per triangle; any may be NULL),
+ * overlapping the copies with the work: the dilation's first pass runs
+ * while the radius field is uploaded, and vertices and triangles come down
+ * while the normals are filtered.  When the mesh exceeds the capacities,
+ * GM_ERR_CAPACITY is returned with the counts set and the mesh kept on the
+ * device (gm_mesh_download fetches it into larger buffers). */
+gm_status gm_update_to_host(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* h_input, const int8_t* h_scale,
+                            float global_scale, const gm_update_opts* opts, float* h_V, float* h_N, uint32_t* h_T,
+                            int64_t vertex_capacity, int64_t triangle_capacity, int64_t* num_vertices,
+                            int64_t* num_triangles, void* stream);
 gm_status gm_mesh_download(gm_ctx* ctx, float* h_vertices, float* h_normals, uint32_t* h_triangles, void* stream);
 
 /* ---------------------------------------------------------------- batch */

@@ -171,6 +171,30 @@ def test_update_host_buffers_match_oracle(gm_ctx):
     np.testing.assert_allclose(N, O.normals(Vo, To, 20), atol=NORMAL_ATOL)
 
 
+@pytest.mark.parametrize("with_field", [False, True])
+def test_update_to_host_equals_update_and_download(gm_ctx, with_field):
+    """The overlapped host-buffer update gives the same mesh as gm_update +
+    gm_mesh_download; too small buffers answer GM_ERR_CAPACITY with the
+    counts and keep the mesh on the device."""
+    res = 64
+    X = synth.random_grid(res, 141)
+    R = np.random.default_rng(3).integers(0, 9, size=(2 * res) ** 3).astype(np.int8) if with_field else None
+    desc = api.make_desc(res, cell_size=0.01)
+    nv, nt = gm_ctx.update(desc, X, R, 0.02)
+    V, N, T = gm_ctx.mesh_download(nv, nt)
+    hV = np.zeros((nv + 5, 3), np.float32)
+    hN = np.zeros((nv + 5, 3), np.float32)
+    hT = np.zeros((nt + 5, 3), np.uint32)
+    assert gm_ctx.update_to_host(desc, X, R, 0.02, hV, hN, hT) == (nv, nt)
+    assert np.array_equal(hT[:nt], T) and np.array_equal(hV[:nv], V)
+    assert np.array_equal(hN[:nv], N, equal_nan=True)  # border geometry: the reference's NaN normals
+    small = np.zeros((nv - 1, 3), np.float32)
+    with pytest.raises(L.GMError):
+        gm_ctx.update_to_host(desc, X, R, 0.02, small, None, hT)
+    V2, N2, T2 = gm_ctx.mesh_download(nv, nt)
+    assert np.array_equal(T2, T)
+
+
 def test_update_gate_skips_morphology(gm_ctx):
     # floor(2 * gs / cell) <= 1 leaves the input unchanged (GMorpho.cu:7783)
     res = 16
