@@ -521,6 +521,43 @@ size_t dpx_smem_bytes(int sub, int halo) {
   return (size_t)2 * span * 32 * sizeof(uint32_t);
 }
 
+// Where a pass's outputs are needed: tiles whose cells, grown by (gx, ga,
+// gt) cells along (x, pass axis, third axis), hold no non-empty cell of the
+// 8^3-cell occupancy map of the dilation are skipped.  The x coordinate and
+// the third coordinate are fine voxels (shift 1) or cells (shift 0); the
+// outputs along the pass axis are fine voxels (sub = 0) or cells (sub = 1).
+struct NeedMap {
+  const uint8_t* dmap;  // nullptr: every tile is needed
+  int mdx, mdy, mdz;
+  int x_shift, t_shift;
+  int gx, ga, gt;
+};
+
+__device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int nout) {
+  const int x0 = (int)blockIdx.x * kDpxCols;
+  const int cx0 = x0 >> nm.x_shift, cx1 = (x0 + kDpxCols - 1) >> nm.x_shift;
+  const int oa = o0, ob = min(o0 + kDpxOut, nout) - 1;
+  const int ca0 = sub ? oa : oa >> 1, ca1 = sub ? ob : ob >> 1;
+  const int ct0 = (2 * (int)blockIdx.z) >> nm.t_shift, ct1 = (2 * (int)blockIdx.z + 1) >> nm.t_shift;
+  // (a, t) are (y, z) for the y pass and (z, y) for the z pass
+  const int lo[3] = {cx0 - nm.gx, (axis == 1 ? ca0 - nm.ga : ct0 - nm.gt), (axis == 1 ? ct0 - nm.gt : ca0 - nm.ga)};
+  const int hi[3] = {cx1 + nm.gx, (axis == 1 ? ca1 + nm.ga : ct1 + nm.gt), (axis == 1 ? ct1 + nm.gt : ca1 + nm.ga)};
+  const int md[3] = {nm.mdx, nm.mdy, nm.mdz};
+  int a[3], b[3], c[3];
+  for (int k = 0; k < 3; k++) {
+    a[k] = max(lo[k], 0) >> 3;
+    b[k] = min(hi[k] >> 3, md[k] - 1);
+    c[k] = b[k] - a[k] + 1;
+  }
+  int any = 0;
+  if (c[0] > 0 && c[1] > 0 && c[2] > 0)
+    for (int i = threadIdx.x; i < c[0] * c[1] * c[2]; i += blockDim.x) {
+      const int ix = a[0] + i % c[0], iy = a[1] + (i / c[0]) % c[1], iz = a[2] + i / (c[0] * c[1]);
+      any |= nm.dmap[idx3(ix, iy, iz, nm.mdx, nm.mdy)];
+    }
+  return __syncthreads_or(any) != 0;
+}
+
 // Radius bound of one tile of a dilation pass, from the map of the largest
 // raw radius per 16^3 fine voxels: over the tile's x columns and outputs,
 // and its two third-axis coordinates widened by `rext` (the y pass feeds z
@@ -552,8 +589,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
                                                   int sub, int halo, uint32_t cap, RField R,
                                                   int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
-                                                  int rext, const uint8_t* __restrict__ dmap, int mdx, int mdy,
-                                                  int mdz) {
+                                                  int rext, NeedMap need) {
   extern __shared__ uint32_t tileu[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tpar = w >> 2, grp = w & 3;
@@ -578,28 +614,10 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     cap = ct < cap ? ct : cap;
     halo_e = rt + 2 < halo ? rt + 2 : halo;
   }
-  // Erosion outputs matter only where the dilation has voxels: the centre
-  // flags on D grown by one cell (the refinement tags cells next to D), the
-  // lattice flags on D.  A tile whose cells (so grown) hold no voxel of D,
-  // by the 8^3-cell occupancy map of D, writes "not eroded" without work.
-  bool needed = true;
-  if ((FIN == 2 || FIN == 3) && dmap != nullptr) {
-    const int grow = FIN == 2 ? 1 : 0;
-    const int cx0 = FIN == 2 ? (int)(blockIdx.x * kDpxCols) / 2 : (int)(blockIdx.x * kDpxCols);
-    const int cx1 = cx0 + (FIN == 2 ? kDpxCols / 2 : kDpxCols) - 1;
-    const int cy0 = FIN == 2 ? (int)blockIdx.z : 2 * (int)blockIdx.z, cy1 = FIN == 2 ? cy0 : cy0 + 1;
-    const int cz0 = FIN == 2 ? o0 / 2 : o0, cz1 = cz0 + (FIN == 2 ? kDpxOut / 2 : kDpxOut) - 1;
-    const int ax = max(cx0 - grow, 0) >> 3, bx = min((cx1 + grow) >> 3, mdx - 1);
-    const int ay = max(cy0 - grow, 0) >> 3, by = min((cy1 + grow) >> 3, mdy - 1);
-    const int az = max(cz0 - grow, 0) >> 3, bz = min((cz1 + grow) >> 3, mdz - 1);
-    const int cnx = bx - ax + 1, cny = by - ay + 1, cnz = bz - az + 1;
-    int any = 0;
-    for (int i = threadIdx.x; i < cnx * cny * cnz; i += blockDim.x) {
-      const int ix = ax + i % cnx, iy = ay + (i / cnx) % cny, iz = az + i / (cnx * cny);
-      any |= dmap[idx3(ix, iy, iz, mdx, mdy)];
-    }
-    needed = __syncthreads_or(any) != 0;
-  }
+  // Erosion outputs matter only where the dilation has voxels (and the
+  // passes feeding them within their window): a tile outside writes its
+  // saturation value ("not eroded") without work.
+  const bool needed = need.dmap == nullptr || tile_needed(need, axis, sub, o0, nout);
   const int skip = needed ? halo - halo_e : span;  // tile rows never read
   const uint32_t capp = cap | (cap << 16);
   uint32_t* tile = tileu + tpar * span * 32;
@@ -770,7 +788,7 @@ template <int G, typename TIn, int FIN>
 static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
                        int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry, cudaStream_t st,
                        KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0,
-                       const uint8_t* dmap = nullptr, int mdx = 0, int mdy = 0, int mdz = 0) {
+                       NeedMap need = NeedMap{nullptr, 0, 0, 0, 0, 0, 0, 0, 0}) {
   const size_t smem = dpx_smem_bytes(sub, halo);
   static size_t configured = 0;
   if (smem > 48 * 1024 && smem > configured) {
@@ -783,7 +801,7 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, (n3 + 1) / 2);
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
-                                                          uniform_r, rx, ry, rmap, rext, dmap, mdx, mdy, mdz));
+                                                          uniform_r, rx, ry, rmap, rext, need));
 }
 
 // Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
@@ -1206,15 +1224,21 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     GM_LAUNCH(kc, "k_ero_pass_x", st,
               k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, RF, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1));
     if (K <= 32767) {
+      // ero z needs its outputs on D grown by one cell (the refinement tags
+      // cells next to D), ero y its outputs there and within the z window
+      // (ehalo fine voxels) of it
+      const int gz = (ehalo + 1) / 2 + 1;
       launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
-                                         kc, "k_pass_ero_y");
+                                         kc, "k_pass_ero_y", nullptr, 0,
+                                         NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1 + gz});
       launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                         "k_pass_ero_z", nullptr, 0, dmap, mdx, mdy, mdz);
+                                         "k_pass_ero_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1});
       if (!exact) {
+        // erob z needs its flags on D only, erob y within its z window
         launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_y");
+                                           "k_pass_erob_y", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 1, 0, 0, gz});
         launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_z", nullptr, 0, dmap, mdx, mdy, mdz);
+                                           "k_pass_erob_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 0, 0, 0, 0});
       }
     } else {
       const int span = kTileOut + 2 * ehalo;
