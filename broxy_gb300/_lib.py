@@ -109,6 +109,8 @@ PROTOTYPES = {
     "gm_server_snapshot": (C.c_int, [_P, _P, _P]),
     "gm_server_restore": (C.c_int, [_P, _P, _P]),
     "gm_close_box": (C.c_int, [_P, C.POINTER(BoxDesc), _P, _P, C.c_int32, C.c_int, C.c_int, _P, _P]),
+    "gm_close_box_region": (C.c_int, [_P, C.POINTER(BoxDesc), _P, _P, C.c_int32, C.c_int, C.c_int,
+                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32), _P, _P]),
     "gm_mesh_box": (C.c_int, [_P, C.POINTER(BoxDesc), _P, C.POINTER(MeshWindow), C.c_int32, C.POINTER(MeshView), _P]),
     "gm_mesh_store": (C.c_int, [C.c_char_p, _P, _P, C.c_int64, _P, C.c_int64, C.c_int32]),
     "gm_server_profile_read": (C.c_int64, [_P, C.c_char_p, C.c_int64]),

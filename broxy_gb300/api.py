@@ -129,6 +129,19 @@ class Context:
                                           _ptr(out), _stream()))
         return out
 
+    def close_box_region(self, box, X, roi_lo, roi_hi, R=None, uniform_radius=4, mode=L.GM_REF,
+                         se=L.GM_SE_SPHERE, out=None):
+        """The closing on cells [roi_lo, roi_hi) of the box only (other cells
+        of `out` are unspecified)."""
+        import torch
+        if out is None:
+            out = torch.empty_like(X)
+        lo = (C.c_int32 * 3)(*[int(v) for v in roi_lo])
+        hi = (C.c_int32 * 3)(*[int(v) for v in roi_hi])
+        self._check(self.lib.gm_close_box_region(self.ctx, C.byref(box), _ptr(X), _ptr(R), int(uniform_radius), mode,
+                                                 se, lo, hi, _ptr(out), _stream()))
+        return out
+
     def mesh_box(self, box, Cg, bilateral_iters=20, window=None):
         """window: None or L.MeshWindow.  Returns zero-copy (V, N, T) owned by
         the context until the next mesh-producing call."""

@@ -440,8 +440,9 @@ static gm_status check_box(gm_ctx* ctx, const gm_box_desc* b) {
   return GM_OK;
 }
 
-gm_status gm_close_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
-                       int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, void* stream) {
+static gm_status close_box_impl(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
+                                int32_t uniform_radius, gm_mode mode, gm_se se, const int32_t* roi_lo,
+                                const int32_t* roi_hi, uint8_t* d_closing, void* stream) {
   if (!ctx) return GM_ERR_INVALID_ARGUMENT;
   gm_status s = check_box(ctx, box);
   if (s != GM_OK) return s;
@@ -484,8 +485,29 @@ gm_status gm_close_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_inp
   a.S_out = nullptr;
   a.workspace = ctx->ws;
   a.num_sms = ctx->num_sms;
+  if (roi_lo && roi_hi)
+    for (int k = 0; k < 3; k++) {
+      a.roi_lo[k] = roi_lo[k];
+      a.roi_hi[k] = roi_hi[k];
+    }
   GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close_box");
   return GM_OK;
+}
+
+gm_status gm_close_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
+                       int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, void* stream) {
+  return close_box_impl(ctx, box, d_input, d_scale, uniform_radius, mode, se, nullptr, nullptr, d_closing, stream);
+}
+
+gm_status gm_close_box_region(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
+                              int32_t uniform_radius, gm_mode mode, gm_se se, const int32_t roi_lo[3],
+                              const int32_t roi_hi[3], uint8_t* d_closing, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  if (!roi_lo || !roi_hi) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_box_region: NULL region");
+  for (int k = 0; k < 3; k++)
+    if (roi_lo[k] < 0 || roi_hi[k] <= roi_lo[k] || (box && roi_hi[k] > box->dims[k]))
+      return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_box_region: empty region or region outside the box");
+  return close_box_impl(ctx, box, d_input, d_scale, uniform_radius, mode, se, roi_lo, roi_hi, d_closing, stream);
 }
 
 gm_status gm_mesh_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_closing, const gm_mesh_window* win,

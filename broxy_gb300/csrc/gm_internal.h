@@ -54,6 +54,10 @@ struct CloseArgs {
   int64_t r_sy = 0, r_sz = 0;  // its y / z strides in bytes when it is a view into a larger field (0: dense)
   const uint8_t* rmap_in = nullptr;  // its 16^3-block radius map when already built (launch_radius_map_dense)
   bool xpass_done = false;  // the dilation's x pass already ran (launch_close_xpass) into the workspace
+  // Cells [roi_lo, roi_hi) where the caller needs the closing (roi_hi[0] == 0:
+  // everywhere).  Work that cannot reach them is skipped, and the closing and
+  // the optional D / S outputs hold no meaningful values outside them.
+  int roi_lo[3] = {0, 0, 0}, roi_hi[3] = {0, 0, 0};
   int uniform_r;      // radius when R == nullptr
   int rmax;           // upper bound of the clamped radius over the grid
   int mode;           // 0 = GM_REF, 1 = GM_EXACT

@@ -37,6 +37,15 @@ __device__ __forceinline__ int rget(const RField& f, int x, int y, int z) {
   return f.p[(int64_t)x + (int64_t)y * f.sy + (int64_t)z * f.sz];
 }
 
+// A box of cells [lo, hi) where a pass's outputs are needed (the whole grid
+// unless the caller needs the closing on part of it only).
+struct CBox {
+  int lo[3], hi[3];
+};
+__host__ __device__ __forceinline__ bool cbox_meets(const CBox& b, int x0, int x1, int y0, int y1, int z0, int z1) {
+  return x1 >= b.lo[0] && x0 < b.hi[0] && y1 >= b.lo[1] && y0 < b.hi[1] && z1 >= b.lo[2] && z0 < b.hi[2];
+}
+
 // The two x-bits of fine row r (y parity r & 1, z parity r >> 1) of four
 // packed bytes, gathered into 8 bits (byte b -> bits 2b, 2b+1).
 __device__ __forceinline__ uint32_t row_bits8(uint32_t w, int r) {
@@ -62,10 +71,11 @@ __device__ __forceinline__ void rows_of_16_bytes(const uint4 q, uint32_t o[4]) {
 // then the corner sets L = bits | bits << 1 (the lattice points that bound
 // an occupied voxel), then the nearest set bit of L for every x.
 __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ X, uint8_t* __restrict__ A,
-                                                    int rx, int ry, int dcap) {
+                                                    int rx, int ry, int dcap, CBox rows) {
   extern __shared__ uint32_t sm_words[];
   const int N = 2 * rx, Ny = 2 * ry, W = N >> 5;
   const int cy = blockIdx.x, cz = blockIdx.y;
+  if (cy < rows.lo[1] || cy >= rows.hi[1] || cz < rows.lo[2] || cz >= rows.hi[2]) return;  // rows nobody reads
   uint32_t* bits = sm_words;            // [4][W]
   uint32_t* corner = sm_words + 4 * W;  // [4][W]
   const uint8_t* row = X + idx3(0, cy, cz, rx, ry);
@@ -149,11 +159,12 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
 // atomicMin, instead of every output scanning the window.
 __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ S, RField R,
                                                     int uniform_r, int rx, int ry, int halo, uint32_t K,
-                                                    uint16_t* __restrict__ HC, uint16_t* __restrict__ HL) {
+                                                    uint16_t* __restrict__ HC, uint16_t* __restrict__ HL, CBox rows) {
   extern __shared__ uint32_t sm_words[];
   const int res = rx;  // cells along x
   const int N = 2 * rx, Ny = 2 * ry, W = N >> 5;
   const int cy = blockIdx.x, cz = blockIdx.y;
+  if (cy < rows.lo[1] || cy >= rows.hi[1] || cz < rows.lo[2] || cz >= rows.hi[2]) return;  // rows nobody reads
   uint32_t* bits = sm_words;              // [4][W]
   uint32_t* hc = sm_words + 4 * W;        // [4][N] centre outputs
   uint32_t* hl = hc + 4 * N;              // [4][res] lattice outputs (x = 2c+1)
@@ -527,10 +538,11 @@ size_t dpx_smem_bytes(int sub, int halo) {
 // the third coordinate are fine voxels (shift 1) or cells (shift 0); the
 // outputs along the pass axis are fine voxels (sub = 0) or cells (sub = 1).
 struct NeedMap {
-  const uint8_t* dmap;  // nullptr: every tile is needed
+  const uint8_t* dmap;  // nullptr: no occupancy test
   int mdx, mdy, mdz;
   int x_shift, t_shift;
   int gx, ga, gt;
+  CBox roi;             // tiles whose own cells miss it are skipped as well
 };
 
 __device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int nout) {
@@ -540,6 +552,12 @@ __device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int no
   const int ca0 = sub ? oa : oa >> 1, ca1 = sub ? ob : ob >> 1;
   const int ct0 = (2 * (int)blockIdx.z) >> nm.t_shift, ct1 = (2 * (int)blockIdx.z + 1) >> nm.t_shift;
   // (a, t) are (y, z) for the y pass and (z, y) for the z pass
+  {
+    const int ya = axis == 1 ? ca0 : ct0, yb = axis == 1 ? ca1 : ct1;
+    const int za = axis == 1 ? ct0 : ca0, zb = axis == 1 ? ct1 : ca1;
+    if (!cbox_meets(nm.roi, cx0, cx1, ya, yb, za, zb)) return false;  // block-uniform
+  }
+  if (nm.dmap == nullptr) return true;
   const int lo[3] = {cx0 - nm.gx, (axis == 1 ? ca0 - nm.ga : ct0 - nm.gt), (axis == 1 ? ct0 - nm.gt : ca0 - nm.ga)};
   const int hi[3] = {cx1 + nm.gx, (axis == 1 ? ca1 + nm.ga : ct1 + nm.gt), (axis == 1 ? ct1 + nm.gt : ca1 + nm.ga)};
   const int md[3] = {nm.mdx, nm.mdy, nm.mdz};
@@ -617,7 +635,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
   // Erosion outputs matter only where the dilation has voxels (and the
   // passes feeding them within their window): a tile outside writes its
   // saturation value ("not eroded") without work.
-  const bool needed = need.dmap == nullptr || tile_needed(need, axis, sub, o0, nout);
+  const bool needed = tile_needed(need, axis, sub, o0, nout);
   const int skip = needed ? halo - halo_e : span;  // tile rows never read
   const uint32_t capp = cap | (cap << 16);
   uint32_t* tile = tileu + tpar * span * 32;
@@ -788,7 +806,7 @@ template <int G, typename TIn, int FIN>
 static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
                        int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry, cudaStream_t st,
                        KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0,
-                       NeedMap need = NeedMap{nullptr, 0, 0, 0, 0, 0, 0, 0, 0}) {
+                       NeedMap need = NeedMap{nullptr, 0, 0, 0, 0, 0, 0, 0, 0, CBox{{0, 0, 0}, {1 << 30, 1 << 30, 1 << 30}}}) {
   const size_t smem = dpx_smem_bytes(sub, halo);
   static size_t configured = 0;
   if (smem > 48 * 1024 && smem > configured) {
@@ -942,10 +960,10 @@ __device__ __forceinline__ uint32_t ld4(const uint8_t* g, int x4, int y, int z, 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
 
 __global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
-                                                     uint8_t* __restrict__ D, Dims g, DataRes dr) {
+                                                     uint8_t* __restrict__ D, Dims g, DataRes dr, CBox roi) {
   const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
   const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= g.x || y >= g.y) return;
+  if (x4 >= g.x || y >= g.y || !cbox_meets(roi, x4, x4 + 3, y, y, z, z)) return;
   // full flags of the base-pass byte for x in [x4, x4+4], (y, y+1) x (z, z+1)
   uint32_t full[2][2];
   uint32_t center = 0, dfc = 0;
@@ -989,10 +1007,10 @@ __global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__
 }
 
 __global__ void __launch_bounds__(256) k_contour4(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, Dims g,
-                                                  int exact) {
+                                                  int exact, CBox roi) {
   const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
   const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= g.x || y >= g.y) return;
+  if (x4 >= g.x || y >= g.y || !cbox_meets(roi, x4, x4 + 3, y, y, z, z)) return;
   const uint32_t v4 = ld4(D, x4, y, z, g);
   const uint32_t xm = x4 > 0 ? D[cidx(x4 - 1, y, z, g)] : 0u;
   const uint32_t xp = x4 + 4 < g.x ? D[cidx(x4 + 4, y, z, g)] : 0u;
@@ -1020,10 +1038,10 @@ __device__ __forceinline__ uint32_t c0_of(uint32_t x, uint32_t d, uint32_t eb, b
 
 __global__ void __launch_bounds__(256) k_ero_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
                                                      const uint8_t* __restrict__ Eb, const uint8_t* __restrict__ Ef,
-                                                     uint8_t* __restrict__ C, Dims g, DataRes dr, int exact) {
+                                                     uint8_t* __restrict__ C, Dims g, DataRes dr, int exact, CBox roi) {
   const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
   const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= g.x || y >= g.y) return;
+  if (x4 >= g.x || y >= g.y || !cbox_meets(roi, x4, x4 + 3, y, y, z, z)) return;
   const uint32_t d4 = ld4(D, x4, y, z, g), ef4 = ld4(Ef, x4, y, z, g);
   if (exact) {
     *reinterpret_cast<uint32_t*>(C + cidx(x4, y, z, g)) = d4 & ~ef4;
@@ -1107,6 +1125,26 @@ static int grid_stride_blocks(int64_t n, int threads, int sms) {
   return (int)(b < cap ? b : cap);
 }
 
+// tile-need test by output box only (x and third coordinates in fine voxels
+// or cells by the shifts)
+static NeedMap roi_only(const CBox& b, int x_shift, int t_shift) {
+  return NeedMap{nullptr, 0, 0, 0, x_shift, t_shift, 0, 0, 0, b};
+}
+
+// box grown by g cells along each axis flagged in `axes` (bit a), clamped
+static CBox cbox_grow(const CBox& b, int g, int axes, const int dims[3]) {
+  CBox r = b;
+  for (int a = 0; a < 3; a++) {
+    if ((axes >> a) & 1) {
+      r.lo[a] = b.lo[a] - g;
+      r.hi[a] = b.hi[a] + g;
+    }
+    r.lo[a] = r.lo[a] < 0 ? 0 : r.lo[a];
+    r.hi[a] = r.hi[a] > dims[a] ? dims[a] : r.hi[a];
+  }
+  return r;
+}
+
 size_t close_workspace_bytes_box(int rx, int ry, int rz) {
   const size_t Nx = 2 * (size_t)rx, Ny = 2 * (size_t)ry, Nz = 2 * (size_t)rz, V = Nx * Ny * Nz;
   const size_t cells = (size_t)rx * ry * rz;
@@ -1150,6 +1188,25 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const bool exact = a.mode == 1;
   const RField RF{a.R, a.r_sy > 0 ? a.r_sy : (int64_t)Nx, a.r_sz > 0 ? a.r_sz : (int64_t)Nx * Ny};
   const RField RNONE{nullptr, 0, 0};
+  // Output boxes of the passes (cells).  F: where the caller needs the
+  // closing.  Working backwards: the erosion flags on F (centres) and F + 1
+  // (lattice points, read by the neighbour test), the contour within the
+  // erosion reach of those, the dilation one cell further (contour
+  // neighbours) and its fine flags one more (forward 2x2x2 block); each
+  // y (z) pass also within the window of the following pass.
+  const int dims[3] = {rx, ry, rz};
+  CBox F{{0, 0, 0}, {rx, ry, rz}};
+  if (a.roi_hi[0] > 0)
+    for (int k = 0; k < 3; k++) {
+      F.lo[k] = a.roi_lo[k] < 0 ? 0 : a.roi_lo[k];
+      F.hi[k] = a.roi_hi[k] > dims[k] ? dims[k] : a.roi_hi[k];
+    }
+  const int win = (rmax + 3) / 2 + 2;  // cells covering a pass window (rmax + 2 fine voxels) with rounding
+  const CBox R_Ef = F, R_Eb = cbox_grow(F, 1, 7, dims);
+  const CBox R_S = cbox_grow(F, win + 2, 7, dims), R_D = cbox_grow(R_S, 1, 7, dims), R_Df = cbox_grow(R_D, 1, 7, dims);
+  const CBox B_dil_y = cbox_grow(R_Df, win, 4, dims), B_dil_x = cbox_grow(R_Df, win, 6, dims);
+  const CBox B_ero_y = cbox_grow(R_Ef, win, 4, dims), B_erob_y = cbox_grow(R_Eb, win, 4, dims);
+  const CBox B_ero_x = cbox_grow(R_Eb, win, 6, dims);
 
   // ---- dilation ----
   const int dil_r = rmax + 1;  // "Safety Measure" radius + 1 (GMorpho.cu:2864)
@@ -1167,19 +1224,19 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     const int W = Nx >> 5;
     if (!a.xpass_done)
       GM_LAUNCH(kc, "k_dil_pass_x", st,
-                k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, dcap));
+                k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, dcap, B_dil_x));
     uint8_t* dst = exact ? D : Df;
     if (dil_cap <= 32767) {
       if (a.se == 1) {
         launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
-                                          ry, st, kc, "k_pass_dil_y", tile_map, dil_halo);
+                                          ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
         launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
-                                           rx, ry, st, kc, "k_pass_dil_z", tile_map, 0);
+                                           rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
       } else {
         launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
-                                         ry, st, kc, "k_pass_dil_y", tile_map, dil_halo);
+                                         ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
         launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
-                                          rx, ry, st, kc, "k_pass_dil_z", tile_map, 0);
+                                          rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
       }
     } else {
       const int span = kTileOut + 2 * dil_halo;
@@ -1199,7 +1256,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                            buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
     }
     if (!exact) {
-      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr));
+      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr, R_D));
     }
   }
   // ---- occupancy map of D (erosion outputs are needed on D only) ----
@@ -1208,7 +1265,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     GM_LAUNCH(kc, "k_occ_map8", st, k_occ_map8<<<(nb + 7) / 8, 256, 0, st>>>(D, rx, ry, mdx, mdy, nb, dmap));
   }
   // ---- contour ----
-  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact ? 1 : 0));
+  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact ? 1 : 0, R_S));
   // ---- erosion ----
   {
     const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
@@ -1222,7 +1279,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       ero_x_configured = smem;
     }
     GM_LAUNCH(kc, "k_ero_pass_x", st,
-              k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, RF, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1));
+              k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, RF, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1,
+                                                            B_ero_x));
     if (K <= 32767) {
       // ero z needs its outputs on D grown by one cell (the refinement tags
       // cells next to D), ero y its outputs there and within the z window
@@ -1230,15 +1288,15 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       const int gz = (ehalo + 1) / 2 + 1;
       launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
                                          kc, "k_pass_ero_y", nullptr, 0,
-                                         NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1 + gz});
+                                         NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1 + gz, B_ero_y});
       launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                         "k_pass_ero_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1});
+                                         "k_pass_ero_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1, R_Ef});
       if (!exact) {
         // erob z needs its flags on D only, erob y within its z window
         launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_y", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 1, 0, 0, gz});
+                                           "k_pass_erob_y", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 1, 0, 0, gz, B_erob_y});
         launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 0, 0, 0, 0});
+                                           "k_pass_erob_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 0, 0, 0, 0, R_Eb});
       }
     } else {
       const int span = kTileOut + 2 * ehalo;
@@ -1259,7 +1317,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       }
     }
     GM_LAUNCH(kc, "k_ero_select", st,
-              k_ero_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0));
+              k_ero_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0,
+                                                                          F));
   }
   if (a.S_out) {
     cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
@@ -1281,13 +1340,14 @@ cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounte
   // saturation of the largest clamped radius (127): exact distances up to
   // 129, so any radius bound found later is covered
   GM_LAUNCH(kc, "k_dil_pass_x", st,
-            k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, 129));
+            k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, 129,
+                                                                               CBox{{0, 0, 0}, {rx, ry, rz}}));
   return cudaGetLastError();
 }
 
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc) {
   const Dims g{res, res, res};
-  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact));
+  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact, CBox{{0, 0, 0}, {res, res, res}}));
   return cudaGetLastError();
 }
 

@@ -325,6 +325,12 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
   a.S_out = nullptr;
   a.workspace = sl.ws;
   a.num_sms = s.sms;
+  // only the dirty box and the two cells the mesh reads around it are used
+  if (dirty.hi[0] > dirty.lo[0] && dirty.hi[1] > dirty.lo[1] && dirty.hi[2] > dirty.lo[2])
+    for (int k = 0; k < 3; k++) {
+      a.roi_lo[k] = dirty.lo[k] - crop.lo[k] - 2;
+      a.roi_hi[k] = dirty.hi[k] - crop.lo[k] + 2;
+    }
   if ((err = launch_close(a, sl.st, s.kc)) != cudaSuccess) return err;
   // 4. write back the dirty box
   {

@@ -3,7 +3,7 @@ GPU (no reference counterpart: the reference runs on one GPU).
 
 Every rank owns the cells [z0, z1) of the grid and receives, up front, its
 slab of the input grid (and radius field) with a halo on each cut side.  It
-closes the slab as a box grid (``gm_close_box``; the closing is local, so a
+closes the slab as a box grid (``gm_close_box_region``; the closing is local, so a
 slab cut with rmax + 8 cells of margin is exact on its owned cells) and
 meshes it with a window in global coordinates (``gm_mesh_box``): triangles
 of a guard band around the owned cells are kept long enough for the normals
@@ -176,7 +176,11 @@ def close_mesh_slab(ctx, slab, desc, X, R=None, uniform_radius=4, mode=0, se=0, 
     res = slab.res
     dr = [desc.data_res[0], desc.data_res[1], min(max(desc.data_res[2] - slab.zlo, 0), slab.depth)]
     box = make_box((res, res, slab.depth), dr, bbox_min=tuple(desc.bbox_min), cell_size=desc.cell_size)
-    Cb = ctx.close_box(box, X, R, uniform_radius, mode, se)
+    # only the mesh window and the two cells its cubes read around it are
+    # closed; the rest of the box is the halo the closing reads
+    zr0 = max(slab.z0 - slab.guard - 2, slab.zlo) - slab.zlo
+    zr1 = min(slab.z1 + slab.guard + 2, slab.zhi) - slab.zlo
+    Cb = ctx.close_box_region(box, X, (0, 0, zr0), (res, res, zr1), R, uniform_radius, mode, se)
     win = L.MeshWindow()
     win.global_res = res
     for a in range(3):

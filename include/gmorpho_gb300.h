@@ -296,6 +296,15 @@ typedef struct {
 gm_status gm_close_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
                        int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing, void* stream);
 
+/* The closing of a box on the cells [roi_lo, roi_hi) only (no reference
+ * counterpart: a local re-closing after an edit, or a slab's owned cells).
+ * Those cells are bit-identical to gm_close_box's; d_closing holds
+ * unspecified bytes elsewhere.  Passes skip the tiles that cannot reach the
+ * region (the dilation within its erosion and dilation reach). */
+gm_status gm_close_box_region(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_input, const int8_t* d_scale,
+                              int32_t uniform_radius, gm_mode mode, gm_se se, const int32_t roi_lo[3],
+                              const int32_t roi_hi[3], uint8_t* d_closing, void* stream);
+
 /* Where a box sits in a cubic global grid, and which of its cells to mesh:
  * triangles of cells [emit_lo, emit_hi), the global grid's border rule and
  * global vertex coordinates (box->bbox_min must then be the GLOBAL grid's
