@@ -352,6 +352,8 @@ class Server:
         return t.value
 
     def poll(self, cap=256):
+        """Finished edits; a result's patch (device mesh) stays valid until the
+        next poll."""
         arr = (L.EditResult * cap)()
         n = C.c_int32(0)
         st = self.lib.gm_server_poll(self.h, arr, cap, C.byref(n))

@@ -641,14 +641,45 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
   uint32_t* tile = tileu + tpar * span * 32;
   const bool colok = x < nx && third < n3;
   int finite = 0;
+  constexpr bool kTileMin = G == KERN_CEN2 || G == KERN_LAT2;
+  uint32_t vmin = 0xffffffffu;  // smallest loaded value (both lanes)
   for (int s = skip + grp; s < span - skip; s += 4) {
     const int a = lo + s;
     uint32_t v = capp;
     if (colok && a >= 0 && a < na) v = load_pair<G, TIn>(in + x + sa * a + s3 * third, capp);
     tile[s * 32 + lane] = v;
     finite |= v != capp;
+    if (kTileMin) vmin = __vminu2(vmin, v);
+  }
+  __shared__ uint32_t warp_min[8];
+  if (kTileMin) {
+    const uint32_t m2 = (vmin & 0xffffu) < (vmin >> 16) ? (vmin & 0xffffu) : (vmin >> 16);
+    const uint32_t mw = __reduce_min_sync(0xffffffffu, m2);
+    if (lane == 0) warp_min[w] = mw;
   }
   finite = __syncthreads_or(finite);
+  // Every tile value is >= tmin, so a tap whose kernel value reaches
+  // cap - tmin cannot bring an output below the saturation value cap: the
+  // window of this tile ends at the last tap below it (kernels grow with
+  // |delta|).  Erosion passes only: their inputs carry the per-site offset
+  // K - 4 (r - 1)^2, so tiles whose sites all have small radii need short
+  // windows; dilation tiles next to a surface hold zeros (and use their
+  // radius bound instead).
+  uint32_t tmin = 0;
+  int halo_t = step == 1 ? halo_e : halo;
+  if (kTileMin) {
+    tmin = warp_min[0];
+#pragma unroll
+    for (int i = 1; i < 8; i++) tmin = warp_min[i] < tmin ? warp_min[i] : tmin;
+  }
+  if (kTileMin && finite) {
+    int hm = 1;
+    while (hm < halo_t && (step == 1 ? kern_pos<G>(hm)
+                                     : (kern_g<G>(hm) < kern_g<G>(-hm) ? kern_g<G>(hm) : kern_g<G>(-hm))) +
+                                  tmin < cap)
+      hm++;
+    halo_t = hm < halo_t ? hm : halo_t;
+  }
   const int obase = o0 + grp * kDpxPer;
   const int sp0 = (sub ? 2 * obase + 1 : obase) - lo;
   uint32_t best[kDpxPer];
@@ -656,7 +687,9 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     // Register sliding windows: wp[(j + k) % 16] holds tile row sp0 + j + k
     // and wm[(j - k) mod 16] holds row sp0 + j - k, so that after tap k only
     // one new row per side is loaded (into the slot its leaving row frees).
-    // Rows read: sp0 - halo_e .. sp0 + 15 + halo_e, inside [skip, span - skip).
+    // Rows read: sp0 - halo_t .. sp0 + 15 + halo_t (halo_t <= halo_e, and
+    // at least the rows sp0 - 1 and sp0 + 16 of the first window), inside
+    // [skip, span - skip).
     const uint32_t* tcol = tile + lane;
     uint32_t wp[kDpxPer], wm[kDpxPer];
 #pragma unroll
@@ -668,12 +701,12 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
 #pragma unroll
     for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tcol[(sp0 + j) * 32], g0, capp);
     uint32_t gprev = g0;  // +side kernel of the previous tap (the -side of this one for LAT, CUBE)
-    for (int kb = 0; kb <= halo_e; kb += kDpxPer) {
+    for (int kb = 0; kb <= halo_t; kb += kDpxPer) {
 #pragma unroll
       for (int u = 0; u < kDpxPer; u++) {
         const int k = kb + u;
         if (k == 0) continue;
-        if (k > halo_e) goto dpx_done;
+        if (k > halo_t) goto dpx_done;
         const uint32_t graw = kern_pos<G>(k);
         const uint32_t gp = pack_cap(graw, cap);
         const uint32_t gm_ = G == KERN_CEN2 ? gp : gprev;
@@ -683,7 +716,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
           best[j] = step_min<G>(wp[(j + u) % kDpxPer], gp, best[j]);
           best[j] = step_min<G>(wm[(j - u + kDpxPer) % kDpxPer], gm_, best[j]);
         }
-        if (k == halo_e) goto dpx_done;  // no further tap: load nothing past the window
+        if (k == halo_t) goto dpx_done;  // no further tap: load nothing past the window
         // rows sp0 + k + 16 and sp0 - k - 1 enter; the slots of rows
         // sp0 + k and sp0 + 15 - k are free now (k < halo_e keeps both in the window)
         wp[u] = tcol[(sp0 + k + kDpxPer) * 32];
@@ -695,7 +728,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
           const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
           // smallest kernel value of the taps to come (k + 1 on either side)
           const uint32_t nxt = G == KERN_CEN2 ? kern_pos<G>(k + 1) : graw;
-          if (__all_sync(0xffffffffu, nxt >= mx)) goto dpx_done;
+          if (__all_sync(0xffffffffu, nxt + tmin >= mx)) goto dpx_done;
         }
       }
     }
@@ -704,7 +737,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
     const uint32_t g0 = gpair<G>(0, cap);
 #pragma unroll
     for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tile[(sp0 + step * j) * 32 + lane], g0, capp);
-    for (int k = 1; k <= halo; k++) {
+    for (int k = 1; k <= halo_t; k++) {
       const uint32_t gp = gpair<G>(k, cap), gm_ = gpair<G>(-k, cap);
 #pragma unroll
       for (int j = 0; j < kDpxPer; j++) {
@@ -719,7 +752,7 @@ __global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, ui
         const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
         const uint32_t np = kern_g<G>(k + 1), nm = kern_g<G>(-(k + 1));
         const uint32_t nxt = np < nm ? np : nm;
-        if (__all_sync(0xffffffffu, nxt >= mx)) break;
+        if (__all_sync(0xffffffffu, nxt + tmin >= mx)) break;
       }
     }
   } else {

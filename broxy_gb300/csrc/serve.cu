@@ -17,8 +17,9 @@
 //
 // Continuous batching: each slot owns a stream, crop buffers and a mesh
 // buffer.  Queued edits are dispatched in arrival order as slots free up; an
-// edit whose crop overlaps the crop of an edit still on the GPU waits (its
-// result depends on the earlier one), disjoint edits run concurrently.
+// edit whose crop overlaps the crop of an edit still on the GPU is queued
+// behind it on the GPU (its stream waits for the earlier edit's write back),
+// disjoint edits run concurrently.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -72,12 +73,14 @@ struct Box3 {
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr, counted = nullptr;
+  cudaEvent_t written = nullptr;  // the edit's closing is in the resident grid (later overlapping edits wait on it)
   uint32_t* h_tot = nullptr;  // pinned: the crop mesh's four totals
   int phase = 0;              // 0 idle, 1 closing + counting, 2 emitting
   MeshArgs ma;
   uint8_t *Xc = nullptr, *Cc = nullptr, *ws = nullptr;
   MeshBuffers mesh;
   bool busy = false;
+  bool held = false;  // result returned by the last poll: its patch stays valid until the next poll
   uint64_t ticket = 0;
   Box3 crop, dirty;
   int cres = 0;
@@ -277,7 +280,7 @@ static void map_raise(Server& s, const gm_edit& e) {
       }
 }
 
-static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& pl) {
+static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& pl, const std::vector<cudaEvent_t>& deps) {
   const gm_edit& e = p.edit;
   const int res = s.desc.res;
   const Box3& dirty = pl.dirty;
@@ -292,6 +295,9 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
   sl.cres = cres;
   sl.t_submit = p.t_submit;
   sl.status = 0;
+  // overlapping edits dispatched earlier: their brush, closing and write
+  // back come first (stream order on the GPU, no host round trip)
+  for (cudaEvent_t d : deps) cudaStreamWaitEvent(sl.st, d, 0);
   cudaEventRecord(sl.t0, sl.st);
   // 1. brush the resident radius field (bounded box kernel)
   const float bmin[3] = {s.desc.bbox_min[0], s.desc.bbox_min[1], s.desc.bbox_min[2]};
@@ -338,6 +344,7 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
     const int ext[3] = {dirty.hi[0] - dirty.lo[0], dirty.hi[1] - dirty.lo[1], dirty.hi[2] - dirty.lo[2]};
     if ((err = launch_box_copy(sl.Cc, cres, src0, s.C, res, dirty.lo, ext, sl.st, s.kc)) != cudaSuccess) return err;
   }
+  cudaEventRecord(sl.written, sl.st);
   // 5. mesh the dirty box of the crop (vertices in global coordinates)
   MeshArgs ma;
   ma.res = cres;
@@ -383,6 +390,7 @@ static void fail_slot(Server& s, Slot& sl, int status) {
 }
 
 static void progress(Server& s) {
+  for (Slot& sl : s.slots) sl.held = false;
   // slots whose counts arrived go on to emission (no host wait)
   for (Slot& sl : s.slots) {
     if (!sl.busy || sl.phase != 1) continue;
@@ -417,18 +425,22 @@ static void progress(Server& s) {
     r.patch.num_triangles = sl.nt;
     s.done.push_back(r);
     sl.busy = false;
+    sl.held = true;
     sl.phase = 0;
   }
   // Dispatch queued edits while slots are free.  An edit whose crop meets
-  // the crop of an edit on the GPU, or of an earlier edit still queued,
-  // waits (its result depends on that edit); later edits independent of
-  // everything before them go ahead of it (bounded look-ahead).
+  // the crop of an earlier edit still queued waits (its result depends on
+  // that edit); later edits independent of everything queued before them go
+  // ahead of it (bounded look-ahead).  One whose crop meets edits on the GPU
+  // is dispatched behind them: its stream waits for their write back (its
+  // brush then follows their reads of the radius field, its crop sees their
+  // brushes and its write back lands after theirs).
   std::vector<Box3> waiting;  // crops of the earlier edits that stay queued
   int looked = 0;
   for (auto it = s.queue.begin(); it != s.queue.end() && looked < kLookAhead; looked++) {
     Slot* free_slot = nullptr;
     for (Slot& sl : s.slots)
-      if (!sl.busy) { free_slot = &sl; break; }
+      if (!sl.busy && !sl.held) { free_slot = &sl; break; }
     if (!free_slot) break;
     Plan pl;
     if (!plan_edit(s, it->edit, pl)) {
@@ -440,8 +452,9 @@ static void progress(Server& s) {
       continue;
     }
     bool conflict = false;
+    std::vector<cudaEvent_t> deps;
     for (const Slot& sl : s.slots)
-      if (sl.busy && sl.crop.overlaps(pl.crop)) conflict = true;
+      if (sl.busy && sl.crop.overlaps(pl.crop)) deps.push_back(sl.written);
     for (const Box3& w : waiting)
       if (w.overlaps(pl.crop)) conflict = true;
     if (conflict) {
@@ -451,7 +464,7 @@ static void progress(Server& s) {
     }
     const Pending pe = *it;
     it = s.queue.erase(it);
-    if (dispatch(s, *free_slot, pe, pl) != cudaSuccess) {
+    if (dispatch(s, *free_slot, pe, pl, deps) != cudaSuccess) {
       cudaGetLastError();
       fail_slot(s, *free_slot, GM_ERR_CUDA);
     }
@@ -534,6 +547,7 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
     if (e == cudaSuccess) e = cudaEventCreate(&sl.t0);
     if (e == cudaSuccess) e = cudaEventCreate(&sl.t1);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.counted, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.written, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tot, 4 * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&sl.Xc, ccells);
     if (e == cudaSuccess) e = cudaMalloc(&sl.Cc, ccells);
@@ -563,6 +577,7 @@ gm_status gm_server_destroy(gm_server* srv) {
     if (sl.t0) cudaEventDestroy(sl.t0);
     if (sl.t1) cudaEventDestroy(sl.t1);
     if (sl.counted) cudaEventDestroy(sl.counted);
+    if (sl.written) cudaEventDestroy(sl.written);
     if (sl.h_tot) cudaFreeHost(sl.h_tot);
     cudaFree(sl.Xc);
     cudaFree(sl.Cc);

@@ -219,8 +219,9 @@ int32_t gm_batch_lanes(gm_ctx* ctx);
  * resident radius field, followed by an exact LOCAL re-closing of the
  * region it can change and a re-mesh of that region.  Edits are admitted as
  * slots free up (continuous batching); edits whose regions overlap an edit
- * still on the GPU wait for it, disjoint edits run concurrently.  The
- * server uses the current device; all calls come from one host thread. */
+ * still on the GPU are queued behind it on the GPU (stream order), disjoint
+ * edits run concurrently.  The server uses the current device; all calls
+ * come from one host thread. */
 typedef struct gm_server gm_server;
 
 typedef struct {
@@ -247,7 +248,7 @@ typedef struct {
   int32_t dirty_lo[3];     /* fine-voxel box whose closing was recomputed */
   int32_t dirty_hi[3];
   int32_t crop_res;        /* edge (base cells) of the crop that was re-closed */
-  /* mesh of the dirty box (device, valid until its slot is reused): the
+  /* mesh of the dirty box (device, valid until the next gm_server_poll): the
    * triangles the whole grid's mesh has in these cells, with bit-identical
    * vertex positions; vertices no patch triangle uses get a zero normal */
   gm_mesh_view patch;
