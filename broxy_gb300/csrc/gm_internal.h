@@ -58,6 +58,12 @@ struct CloseArgs {
   // everywhere).  Work that cannot reach them is skipped, and the closing and
   // the optional D / S outputs hold no meaningful values outside them.
   int roi_lo[3] = {0, 0, 0}, roi_hi[3] = {0, 0, 0};
+  // Resident squared lattice distance field of the input grid (launch_edt,
+  // saturated for a radius bound >= every radius of R), as a view with y / z
+  // strides in elements: the sphere dilation is then its per-voxel threshold
+  // instead of three passes.
+  const uint16_t* edt = nullptr;
+  int64_t e_sy = 0, e_sz = 0;
   int uniform_r;      // radius when R == nullptr
   int rmax;           // upper bound of the clamped radius over the grid
   int mode;           // 0 = GM_REF, 1 = GM_EXACT
@@ -77,6 +83,12 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
 // field is on the device; launch_close then skips it (xpass_done).
 cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
+// The squared lattice distance field of a cubic grid: per fine voxel p (u16,
+// x-fastest, (2 res)^3), the smallest squared distance from lattice point p
+// to an occupied fine voxel box, saturated at (rmax + 1)^2 — what the sphere
+// dilation's z pass thresholds.  Workspace: close_workspace_bytes(res).
+cudaError_t launch_edt(const uint8_t* X, int res, int rmax, uint8_t* workspace, uint16_t* E, cudaStream_t st,
+                       KernelCounter* kc);
 cudaError_t launch_rmax(const int8_t* R, int64_t n, int* d_out, int sms, cudaStream_t st, KernelCounter* kc);
 // The 16^3-block map of the largest raw radius of a dense field of nx*ny*nz
 // fine voxels ((nx/16)(ny/16)(nz/16) bytes), and its largest clamped radius

@@ -1039,6 +1039,42 @@ __global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__
   *reinterpret_cast<uint32_t*>(D + cidx(x4, y, z, g)) = out;
 }
 
+// Dilation flags from a resident squared lattice distance field E of the
+// input grid (u16 per fine voxel: the value the dilation's z pass computes,
+// saturated at (rmax + 1)^2 for a bound rmax of every radius asked for).
+// The flag of fine voxel p is E(p) < (r(p) + 1)^2, the z pass's own test, so
+// the bytes equal the passes' output.  Four cells per thread, bit
+// x + 2y + 4z of the 2x2x2 fine voxels of a cell.
+__global__ void __launch_bounds__(256) k_dil_threshold(const uint16_t* __restrict__ E, int64_t esy, int64_t esz,
+                                                       RField R, int uniform_r, Dims g, uint8_t* __restrict__ out,
+                                                       CBox roi) {
+  const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
+  const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
+  if (x4 >= g.x || y >= g.y || !cbox_meets(roi, x4, x4 + 3, y, y, z, z)) return;
+  const int ru = clamp_radius(uniform_r);
+  uint32_t out4 = 0;
+#pragma unroll
+  for (int r = 0; r < 4; r++) {  // fine row: y parity r & 1, z parity r >> 1
+    const int fy = 2 * y + (r & 1), fz = 2 * z + (r >> 1);
+    const uint16_t* er = E + fy * esy + fz * esz + 2 * x4;
+    const int8_t* rr = R.p != nullptr ? R.p + fy * R.sy + fz * R.sz + 2 * x4 : nullptr;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {  // fine x 2(x4 + i) and 2(x4 + i) + 1
+      const uint32_t e2 = *reinterpret_cast<const uint32_t*>(er + 2 * i);
+      int r0 = ru, r1 = ru;
+      if (rr != nullptr) {
+        const uint32_t w = *reinterpret_cast<const uint16_t*>(rr + 2 * i);
+        r0 = clamp_radius((int)(int8_t)(w & 0xffu));
+        r1 = clamp_radius((int)(int8_t)(w >> 8));
+      }
+      const uint32_t b0 = (e2 & 0xffffu) < (uint32_t)((r0 + 1) * (r0 + 1)) ? 1u : 0u;
+      const uint32_t b1 = (e2 >> 16) < (uint32_t)((r1 + 1) * (r1 + 1)) ? 2u : 0u;
+      out4 |= (b0 | b1) << (2 * r + 8 * i);
+    }
+  }
+  *reinterpret_cast<uint32_t*>(out + cidx(x4, y, z, g)) = out4;
+}
+
 __global__ void __launch_bounds__(256) k_contour4(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, Dims g,
                                                   int exact, CBox roi) {
   const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
@@ -1247,13 +1283,20 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const uint32_t dil_cap = a.se == 1 ? (uint32_t)(rmax + 1) : (uint32_t)(dil_r * dil_r);
   const int dil_halo = dil_r + 1;
   const uint8_t* tile_map = nullptr;  // per-tile radius bounds of the dilation passes
-  if (a.R != nullptr && a.rmap_in != nullptr) {
+  if (a.edt != nullptr) {
+    // resident distance field: the dilation is its per-voxel threshold
+    if (a.se != 0) return cudaErrorInvalidValue;
+  } else if (a.R != nullptr && a.rmap_in != nullptr) {
     tile_map = a.rmap_in;  // built by the caller together with the radius bound
   } else if (a.R != nullptr) {
     if (launch_radius_map(RF, Nx, Ny, Nz, rmap, nullptr, st, kc) != cudaSuccess) return cudaGetLastError();
     tile_map = rmap;
   }
-  {
+  if (a.edt != nullptr) {
+    GM_LAUNCH(kc, "k_dil_threshold", st,
+              k_dil_threshold<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.edt, a.e_sy, a.e_sz, RF, a.uniform_r, g,
+                                                                    exact ? D : Df, R_Df));
+  } else {
     const int W = Nx >> 5;
     if (!a.xpass_done)
       GM_LAUNCH(kc, "k_dil_pass_x", st,
@@ -1288,9 +1331,9 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
         GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
                                            buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
     }
-    if (!exact) {
-      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr, R_D));
-    }
+  }
+  if (!exact) {
+    GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr, R_D));
   }
   // ---- occupancy map of D (erosion outputs are needed on D only) ----
   {
@@ -1356,6 +1399,31 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   if (a.S_out) {
     cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_edt(const uint8_t* X, int res, int rmax, uint8_t* workspace, uint16_t* E, cudaStream_t st,
+                       KernelCounter* kc) {
+  if (res % 16 != 0 || res <= 0 || rmax < 2 || rmax > 127) return cudaErrorInvalidValue;
+  const int N = 2 * res;
+  const size_t V = (size_t)N * N * N;
+  uint8_t* p = workspace;
+  uint16_t* buf16a = reinterpret_cast<uint16_t*>(carve(p, V * 2));
+  carve(p, V * 2);
+  uint8_t* buf8 = carve(p, V);
+  // the sphere dilation's passes with the saturation of the largest radius
+  // and no per-tile radius bound (every radius up to rmax may be asked)
+  const int dil_r = rmax + 1, dil_halo = dil_r + 1, dcap = dil_r + 1;
+  const uint32_t dil_cap = (uint32_t)(dil_r * dil_r);
+  const RField RNONE{nullptr, 0, 0};
+  const int W = N >> 5;
+  GM_LAUNCH(kc, "k_dil_pass_x", st,
+            k_dil_pass_x<<<dim3(res, res), 256, 8 * W * sizeof(uint32_t), st>>>(X, buf8, res, res, dcap,
+                                                                               CBox{{0, 0, 0}, {res, res, res}}));
+  launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, RNONE, 0, res, res, st,
+                                   kc, "k_pass_dil_y");
+  launch_dpx<KERN_LAT, uint16_t, 0>(buf16a, E, nullptr, N, N, N, 2, 0, dil_halo, dil_cap, RNONE, 0, res, res, st,
+                                    kc, "k_pass_edt_z");
   return cudaGetLastError();
 }
 

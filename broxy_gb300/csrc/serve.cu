@@ -102,6 +102,10 @@ struct Server {
   const uint8_t* X = nullptr;
   int8_t* R = nullptr;
   uint8_t* C = nullptr;        // resident closing (owned)
+  // resident squared lattice distance field of the input grid (owned, u16
+  // per fine voxel, saturated for rmax): the input grid never changes, so
+  // the dilation of any crop is a per-voxel threshold of it by the radii
+  uint16_t* E = nullptr;
   uint8_t* ws_full = nullptr;  // workspace of the initial full closing
   int mode = 0;
   int rmax = 2;
@@ -200,13 +204,18 @@ static void brush_box(const Server& s, const gm_edit& e, int lo[3], int hi[3]) {
 //  * the closing can change only in dirty = B + Md, Md = (r_in + 2)/2 + 4
 //    cells (one block cell, one contour cell, erosion reach, refinement),
 //    and at least 9 so that bricks meeting B + 2 lie inside it;
-//  * a crop is exact on the cells at least Mc from its open sides,
-//    Mc = max(r_out + 8, (max(r_in, r_out) + 6)/2 + 1): wrong dilations next
-//    to an open side reach (r_out + 3)/2 + 2 cells in, the contour one more,
-//    erosion and refinement (r_out - 1)/2 + 2 more, and no dilation inside
-//    the dirty box reaches an open side;
+//  * the dilation of a crop is the threshold of the whole grid's distance
+//    field, exact on every cell except the last layer of each open high side
+//    (the tight contour rule reads the forward 2x2x2 block); the contour is
+//    then exact except within two cells of an open high side and one of an
+//    open low side;
+//  * a cell is eroded only by sites within (r - 1)/2 + 1 cells of it, and
+//    the sites outside B + 2 have radii <= r_out, so the closing is exact on
+//    the cells at least (r_out + 1)/2 + 4 (erosion reach, refinement
+//    neighbours, contour) from the open sides;
 //  * two more cells for the mesh of the dirty box (cube corners one cell
-//    past it, cubes of one more cell tagged).
+//    past it, cubes of one more cell tagged) and two spare:
+//    Mc = (r_out + 1)/2 + 8.
 // Crops are cubes whose edge is a multiple of 16 cells (or the whole grid).
 static bool plan_edit(const Server& s, const gm_edit& e, Plan& p) {
   const int res = s.desc.res;
@@ -229,9 +238,7 @@ static bool plan_edit(const Server& s, const gm_edit& e, Plan& p) {
   for (int a = 0; a < 3; a++) { rlo[a] = B.lo[a] - Md - Mc0; rhi[a] = B.hi[a] + Md + Mc0; }
   const int r_out = map_max(s, rlo, rhi, &B2);
   const int rc = r_in > r_out ? r_in : r_out;
-  int Mc = (rc + 6) / 2 + 1;
-  Mc = r_out + 8 > Mc ? r_out + 8 : Mc;
-  Mc += 2;
+  const int Mc = (r_out + 1) / 2 + 8;
   int span = 0;
   for (int a = 0; a < 3; a++) {
     int lo = B.lo[a] - Md, hi = B.hi[a] + Md;
@@ -331,6 +338,9 @@ static cudaError_t dispatch(Server& s, Slot& sl, const Pending& p, const Plan& p
   a.S_out = nullptr;
   a.workspace = sl.ws;
   a.num_sms = s.sms;
+  a.edt = s.E + 2 * crop.lo[0] + N * 2 * crop.lo[1] + N * N * 2 * crop.lo[2];
+  a.e_sy = N;
+  a.e_sz = N * N;
   // only the dirty box and the two cells the mesh reads around it are used
   if (dirty.hi[0] > dirty.lo[0] && dirty.hi[1] > dirty.lo[1] && dirty.hi[2] > dirty.lo[2])
     for (int k = 0; k < 3; k++) {
@@ -517,7 +527,10 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
   cudaFree(d_r);
   if (e == cudaSuccess) e = gm::build_radius_map(s);
   if (e == cudaSuccess) e = cudaMalloc(&s.ws_full, gm::close_workspace_bytes(desc->res));
-  // initial full closing of the resident grid
+  if (e == cudaSuccess) e = cudaMalloc(&s.E, (size_t)8 * cells * sizeof(uint16_t));
+  if (e == cudaSuccess) e = gm::launch_edt(d_input, desc->res, s.rmax, s.ws_full, s.E, 0, s.kc);
+  // initial full closing of the resident grid (its dilation from the
+  // distance field, like every edit's)
   if (e == cudaSuccess) {
     gm::CloseArgs a;
     a.res = desc->res;
@@ -533,6 +546,9 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
     a.S_out = nullptr;
     a.workspace = s.ws_full;
     a.num_sms = s.sms;
+    a.edt = s.E;
+    a.e_sy = 2 * (int64_t)desc->res;
+    a.e_sz = a.e_sy * a.e_sy;
     e = gm::launch_close(a, 0, s.kc);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
   }
@@ -585,6 +601,7 @@ gm_status gm_server_destroy(gm_server* srv) {
     sl.mesh.release();
   }
   cudaFree(s.C);
+  cudaFree(s.E);
   cudaFree(s.ws_full);
   srv->kc.release();
   delete srv;
