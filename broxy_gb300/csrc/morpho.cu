@@ -148,6 +148,154 @@ __global__ void __launch_bounds__(256) k_dil_pass_x(const uint8_t* __restrict__ 
   }
 }
 
+// The same pass with one warp per packed byte-row (four fine rows) and no
+// shared memory: lane l holds words l, l + 32, .. (WPL per lane) of each
+// fine row's corner set, the nearest corner in the words before / after its
+// own comes from a warp prefix max / suffix min, and each lane writes the
+// 32 distances of each of its words as two 16-byte stores.
+constexpr int kBig = 1 << 24;
+
+template <int WPL>
+__global__ void __launch_bounds__(256) k_dil_pass_x_w(const uint8_t* __restrict__ X, uint8_t* __restrict__ A,
+                                                      int rx, int ry, int rz, int dcap, CBox rows) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row_id = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (row_id >= (int64_t)ry * rz) return;
+  const int cy = (int)(row_id % ry), cz = (int)(row_id / ry);
+  if (cy < rows.lo[1] || cy >= rows.hi[1] || cz < rows.lo[2] || cz >= rows.hi[2]) return;  // rows nobody reads
+  const int N = 2 * rx, Ny = 2 * ry, W = N >> 5;
+  const uint8_t* row = X + idx3(0, cy, cz, rx, ry);
+  uint32_t L[4][WPL];
+  bool any = false, all = true;
+#pragma unroll
+  for (int k = 0; k < WPL; k++) {
+    const int w = lane + 32 * k;
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    if (w < W) {
+      q = *reinterpret_cast<const uint4*>(row + 16 * w);
+      all = all && (q.x & q.y & q.z & q.w) == 0xffffffffu;
+    }
+    any = any || (q.x | q.y | q.z | q.w) != 0u;
+    uint32_t o[4];
+    rows_of_16_bytes(q, o);
+#pragma unroll
+    for (int r = 0; r < 4; r++) L[r][k] = o[r];
+  }
+  any = __any_sync(0xffffffffu, any);
+  all = __all_sync(0xffffffffu, all);
+  if (!any || all) {
+    // empty rows: nothing within reach; full rows: every corner is a site
+    const uint32_t v = !any ? (uint32_t)dcap * 0x01010101u : 0u;
+    const uint4 v4 = make_uint4(v, v, v, v);
+#pragma unroll
+    for (int k = 0; k < WPL; k++) {
+      const int w = lane + 32 * k;
+      if (w >= W) continue;
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        uint4* dst = reinterpret_cast<uint4*>(A + idx3(32 * w, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny));
+        dst[0] = v4;
+        dst[1] = v4;
+      }
+    }
+    return;
+  }
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    // corner sets: lattice point p bounds voxels p - 1 and p
+    uint32_t bits[WPL];
+#pragma unroll
+    for (int k = 0; k < WPL; k++) bits[k] = L[r][k];
+    int first[WPL], last[WPL];
+#pragma unroll
+    for (int k = 0; k < WPL; k++) {
+      // the previous word: lane - 1's, or for lane 0 the last word of the
+      // group before (none for word 0)
+      uint32_t prev = __shfl_up_sync(0xffffffffu, bits[k], 1);
+      const uint32_t tail = k > 0 ? __shfl_sync(0xffffffffu, bits[k > 0 ? k - 1 : 0], 31) : 0u;
+      if (lane == 0) prev = tail;
+      const uint32_t c = bits[k] | (bits[k] << 1) | (prev >> 31);
+      L[r][k] = c;
+      const int w = lane + 32 * k;
+      first[k] = c ? 32 * w + __ffs(c) - 1 : kBig;
+      last[k] = c ? 32 * w + 31 - __clz(c) : -kBig;
+    }
+    // nearest corner after / before each word
+    int nxt[WPL], prv[WPL];
+    int after = kBig, before = -kBig;  // over the word groups past / ahead of the current one
+#pragma unroll
+    for (int k = WPL - 1; k >= 0; k--) {
+      int s = first[k];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_down_sync(0xffffffffu, s, o);
+        if (lane + o < 32) s = t < s ? t : s;
+      }
+      int ex = __shfl_down_sync(0xffffffffu, s, 1);
+      if (lane == 31) ex = kBig;
+      nxt[k] = ex < after ? ex : after;
+      const int tot = __shfl_sync(0xffffffffu, s, 0);
+      after = tot < after ? tot : after;
+    }
+#pragma unroll
+    for (int k = 0; k < WPL; k++) {
+      int s = last[k];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s = t > s ? t : s;
+      }
+      int ex = __shfl_up_sync(0xffffffffu, s, 1);
+      if (lane == 0) ex = -kBig;
+      prv[k] = ex > before ? ex : before;
+      const int tot = __shfl_sync(0xffffffffu, s, 31);
+      before = tot > before ? tot : before;
+    }
+#pragma unroll
+    for (int k = 0; k < WPL; k++) {
+      const int w = lane + 32 * k;
+      if (w >= W) continue;
+      const uint32_t c = L[r][k];
+      uint32_t out[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        uint32_t packed = 0;
+#pragma unroll
+        for (int j4 = 0; j4 < 4; j4++) {
+          const int b = 4 * q + j4, pos = 32 * w + b;
+          const uint32_t mr = c >> b, ml = c << (31 - b);
+          const int dr = mr ? __ffs(mr) - 1 : nxt[k] - pos;
+          const int dl = ml ? __clz(ml) : pos - prv[k];
+          int d = dr < dl ? dr : dl;
+          d = d < dcap ? d : dcap;
+          packed |= (uint32_t)d << (8 * j4);
+        }
+        out[q] = packed;
+      }
+      uint4* dst = reinterpret_cast<uint4*>(A + idx3(32 * w, 2 * cy + (r & 1), 2 * cz + (r >> 1), N, Ny));
+      dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
+      dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
+    }
+  }
+}
+
+// launch of the dilation's x pass over the rows of `rows`
+static cudaError_t launch_dil_pass_x(const uint8_t* X, uint8_t* A, int rx, int ry, int rz, int dcap, CBox rows,
+                                     cudaStream_t st, KernelCounter* kc) {
+  const int W = (2 * rx) >> 5;
+  const int64_t nrows = (int64_t)ry * rz;
+  const unsigned blocks = (unsigned)((nrows + 7) / 8);
+  if (W <= 32) {
+    GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x_w<1><<<blocks, 256, 0, st>>>(X, A, rx, ry, rz, dcap, rows));
+  } else if (W <= 64) {
+    GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x_w<2><<<blocks, 256, 0, st>>>(X, A, rx, ry, rz, dcap, rows));
+  } else {
+    GM_LAUNCH(kc, "k_dil_pass_x", st,
+              k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(X, A, rx, ry, dcap, rows));
+  }
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------
 // pass X of the erosion: sites are the contour voxels of one fine row;
 // outputs the half-voxel-unit partial sums at every voxel centre (HC) and
@@ -1297,10 +1445,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
               k_dil_threshold<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.edt, a.e_sy, a.e_sz, RF, a.uniform_r, g,
                                                                     exact ? D : Df, R_Df));
   } else {
-    const int W = Nx >> 5;
-    if (!a.xpass_done)
-      GM_LAUNCH(kc, "k_dil_pass_x", st,
-                k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, dcap, B_dil_x));
+    if (!a.xpass_done && launch_dil_pass_x(a.X, buf8, rx, ry, rz, dcap, B_dil_x, st, kc) != cudaSuccess)
+      return cudaGetLastError();
     uint8_t* dst = exact ? D : Df;
     if (dil_cap <= 32767) {
       if (a.se == 1) {
@@ -1416,10 +1562,8 @@ cudaError_t launch_edt(const uint8_t* X, int res, int rmax, uint8_t* workspace, 
   const int dil_r = rmax + 1, dil_halo = dil_r + 1, dcap = dil_r + 1;
   const uint32_t dil_cap = (uint32_t)(dil_r * dil_r);
   const RField RNONE{nullptr, 0, 0};
-  const int W = N >> 5;
-  GM_LAUNCH(kc, "k_dil_pass_x", st,
-            k_dil_pass_x<<<dim3(res, res), 256, 8 * W * sizeof(uint32_t), st>>>(X, buf8, res, res, dcap,
-                                                                               CBox{{0, 0, 0}, {res, res, res}}));
+  if (launch_dil_pass_x(X, buf8, res, res, res, dcap, CBox{{0, 0, 0}, {res, res, res}}, st, kc) != cudaSuccess)
+    return cudaGetLastError();
   launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, N, N, N, 1, 0, dil_halo, dil_cap, RNONE, 0, res, res, st,
                                    kc, "k_pass_dil_y");
   launch_dpx<KERN_LAT, uint16_t, 0>(buf16a, E, nullptr, N, N, N, 2, 0, dil_halo, dil_cap, RNONE, 0, res, res, st,
@@ -1437,13 +1581,9 @@ cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounte
   carve(p, V * 2);
   carve(p, V * 2);
   uint8_t* buf8 = carve(p, V);  // same place as in launch_close
-  const int W = (2 * rx) >> 5;
   // saturation of the largest clamped radius (127): exact distances up to
   // 129, so any radius bound found later is covered
-  GM_LAUNCH(kc, "k_dil_pass_x", st,
-            k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(a.X, buf8, rx, ry, 129,
-                                                                               CBox{{0, 0, 0}, {rx, ry, rz}}));
-  return cudaGetLastError();
+  return launch_dil_pass_x(a.X, buf8, rx, ry, rz, 129, CBox{{0, 0, 0}, {rx, ry, rz}}, st, kc);
 }
 
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc) {

@@ -76,3 +76,43 @@ def test_region_rejects_bad_regions(gm_ctx):
         with pytest.raises(L.GMError):
             gm_ctx.close_box_region(box, X, lo, hi, None, 4)
     torch.cuda.synchronize()
+
+
+def _swap_xz_bytes(C, dims):
+    """Box bytes (z, y, x) -> the box with x and z exchanged, bits moved
+    from x + 2y + 4z to z + 2y + 4x."""
+    import torch
+    lut = torch.zeros(256, dtype=torch.uint8)
+    for v in range(256):
+        o = 0
+        for k in range(8):
+            if v >> k & 1:
+                x, y, z = k & 1, k >> 1 & 1, k >> 2 & 1
+                o |= 1 << (z + 2 * y + 4 * x)
+        lut[v] = o
+    B = C.view(dims[2], dims[1], dims[0]).permute(2, 1, 0).contiguous()
+    return lut.to(C.device)[B.long()].view(-1)
+
+
+@pytest.mark.parametrize("mode", [L.GM_REF, L.GM_EXACT])
+def test_long_rows_equal_transposed_box(gm_ctx, mode):
+    """Rows of 2048 fine voxels (two 32-bit words per lane in the x pass)
+    against the same grid with x and z exchanged (short rows): the closing
+    commutes with the exchange."""
+    import torch
+    long_dims, short_dims = (1024, 32, 32), (32, 32, 1024)
+    g = torch.Generator().manual_seed(9500)
+    X = torch.zeros(long_dims[2], long_dims[1], long_dims[0], dtype=torch.uint8)
+    # random blocks and sparse voxels away from the y / z borders
+    X[6:26, 6:26, :] = torch.where(torch.rand(20, 20, 1024, generator=g) < 0.08,
+                                   torch.randint(0, 256, (20, 20, 1024), generator=g, dtype=torch.uint8),
+                                   torch.zeros(20, 20, 1024, dtype=torch.uint8))
+    X[10:20, 12:18, 100:180] = 0xFF
+    X[8:24, 8:24, 700:705] = 0xFF
+    X = X.view(-1).cuda()
+    Xt = _swap_xz_bytes(X, long_dims)
+    C_long = gm_ctx.close_box(api.make_box(long_dims), X, None, 5, mode, L.GM_SE_SPHERE)
+    C_short = gm_ctx.close_box(api.make_box(short_dims), Xt, None, 5, mode, L.GM_SE_SPHERE)
+    torch.cuda.synchronize()
+    assert C_long.sum().item() > 0
+    assert torch.equal(_swap_xz_bytes(C_long, long_dims), C_short)
