@@ -409,6 +409,111 @@ __global__ void __launch_bounds__(256) k_ero_pass_x(const uint8_t* __restrict__ 
   }
 }
 
+// The erosion x pass with one warp per packed byte-row (four fine rows,
+// handled one after the other) and no block barrier: the warp's own slice
+// of shared memory holds one fine row's outputs (u16) and its site list;
+// the warp splats one site at a time, lanes over the site's taps, so the
+// lanes of a splat touch distinct outputs and need no atomics.  Rows
+// without sites are written as K straight away.  Rows of up to 2048 fine
+// voxels (two 32-bit words of sites per lane).
+constexpr int kEroXWarps = 8;
+
+__host__ __device__ inline size_t ero_x_w_warp_bytes(int rx) {
+  const size_t N = 2 * (size_t)rx;
+  return N * 2 + (size_t)rx * 2 + N * 4;  // outputs at centres, at lattice points, sites
+}
+
+__global__ void __launch_bounds__(256) k_ero_pass_x_w(const uint8_t* __restrict__ S, RField R, int uniform_r, int rx,
+                                                      int ry, int rz, int halo, uint32_t K,
+                                                      uint16_t* __restrict__ HC, uint16_t* __restrict__ HL,
+                                                      CBox rows) {
+  extern __shared__ uint4 sm_ero[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int N = 2 * rx, Ny = 2 * ry, W = N >> 5;
+  const int64_t row_id = (int64_t)blockIdx.x * kEroXWarps + wid;
+  if (row_id >= (int64_t)ry * rz) return;
+  const int cy = (int)(row_id % ry), cz = (int)(row_id / ry);
+  if (cy < rows.lo[1] || cy >= rows.hi[1] || cz < rows.lo[2] || cz >= rows.hi[2]) return;  // rows nobody reads
+  uint8_t* mine = reinterpret_cast<uint8_t*>(sm_ero) + (size_t)wid * ero_x_w_warp_bytes(rx);
+  uint16_t* hc = reinterpret_cast<uint16_t*>(mine);
+  uint16_t* hl = reinterpret_cast<uint16_t*>(mine + 2 * (size_t)N);
+  uint32_t* sites = reinterpret_cast<uint32_t*>(mine + 2 * (size_t)N + 2 * (size_t)rx);
+  const uint8_t* srow = S + idx3(0, cy, cz, rx, ry);
+  uint32_t bits[4][2];
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    const int w = lane + 32 * k;
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    if (w < W) q = *reinterpret_cast<const uint4*>(srow + 16 * w);
+    uint32_t o[4];
+    rows_of_16_bytes(q, o);
+#pragma unroll
+    for (int r = 0; r < 4; r++) bits[r][k] = o[r];
+  }
+  const uint32_t k2 = K | (K << 16);
+  const uint4 K4 = make_uint4(k2, k2, k2, k2);
+  const int ru = clamp_radius(uniform_r);
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const int fy = 2 * cy + (r & 1), fz = 2 * cz + (r >> 1);
+    uint4* hcrow = reinterpret_cast<uint4*>(HC + idx3(0, fy, fz, N, Ny));
+    uint4* hlrow = reinterpret_cast<uint4*>(HL + idx3(0, fy, fz, rx, Ny));
+    const int c = __popc(bits[r][0]) + __popc(bits[r][1]);
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int ns = __shfl_sync(0xffffffffu, incl, 31);
+    if (ns == 0) {
+      // no site in this row: every output keeps the saturation value K
+      for (int i = lane; i < N >> 3; i += 32) hcrow[i] = K4;
+      for (int i = lane; i < rx >> 3; i += 32) hlrow[i] = K4;
+      continue;
+    }
+    for (int i = lane; i < N >> 3; i += 32) reinterpret_cast<uint4*>(hc)[i] = K4;
+    for (int i = lane; i < rx >> 3; i += 32) reinterpret_cast<uint4*>(hl)[i] = K4;
+    // site list: position, r - 1 and reach (a point at |q - p| >= r(q) is
+    // never eroded by q: e >= 2 (r(q) - 1))
+    int idx = incl - c;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      uint32_t m = bits[r][k];
+      while (m) {
+        const int x = 32 * (lane + 32 * k) + __ffs(m) - 1;
+        m &= m - 1;
+        int rq = ru;
+        if (R.p != nullptr) rq = clamp_radius(rget(R, x, fy, fz));
+        const int reach = rq - 1 < halo ? rq - 1 : halo;
+        sites[idx++] = (uint32_t)x | ((uint32_t)(rq - 1) << 12) | ((uint32_t)reach << 20);
+      }
+    }
+    __syncwarp();
+    for (int s = 0; s < ns; s++) {
+      const uint32_t sw = sites[s];
+      const int q = (int)(sw & 0xfffu), rm1 = (int)((sw >> 12) & 0xffu), reach = (int)(sw >> 20);
+      const uint32_t u = K - 4u * (uint32_t)(rm1 * rm1);
+      for (int dq = lane - reach; dq <= reach; dq += 32) {
+        const int p = q - dq;  // output position, delta = q - p = dq
+        if (p < 0 || p >= N) continue;
+        const int ec = center_dist2(dq);
+        const uint32_t vc = u + (uint32_t)(ec * ec);
+        if (vc < K && vc < hc[p]) hc[p] = (uint16_t)vc;
+        if (p & 1) {
+          const int el = 2 * lattice_dist(dq);
+          const uint32_t vl = u + (uint32_t)(el * el);
+          if (vl < K && vl < hl[p >> 1]) hl[p >> 1] = (uint16_t)vl;
+        }
+      }
+      __syncwarp();
+    }
+    for (int i = lane; i < N >> 3; i += 32) hcrow[i] = reinterpret_cast<const uint4*>(hc)[i];
+    for (int i = lane; i < rx >> 3; i += 32) hlrow[i] = reinterpret_cast<const uint4*>(hl)[i];
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------------
 // generic axis pass (y or z): out(o) = min over delta of
 //     in(pos(o) + delta) (+) g(delta)
@@ -1495,14 +1600,27 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     const int W = Nx >> 5;
     // bits, centre and lattice accumulators, compacted sites
     const size_t smem = sizeof(uint32_t) * (4 * (size_t)W + 4 * (size_t)Nx + 4 * (size_t)rx + 8 * (size_t)Nx);
-    static size_t ero_x_configured = 0;
-    if (smem > 48 * 1024 && smem > ero_x_configured) {
-      cudaFuncSetAttribute(k_ero_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      ero_x_configured = smem;
+    if (W <= 64) {
+      const size_t smem_w = kEroXWarps * ero_x_w_warp_bytes(rx);
+      static size_t ero_xw_configured = 0;
+      if (smem_w > 48 * 1024 && smem_w > ero_xw_configured) {
+        cudaFuncSetAttribute(k_ero_pass_x_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
+        ero_xw_configured = smem_w;
+      }
+      const unsigned blocks = (unsigned)(((int64_t)ry * rz + kEroXWarps - 1) / kEroXWarps);
+      GM_LAUNCH(kc, "k_ero_pass_x", st,
+                k_ero_pass_x_w<<<blocks, 32 * kEroXWarps, smem_w, st>>>(S, RF, a.uniform_r, rx, ry, rz, ehalo, K,
+                                                                        buf16a, HL1, B_ero_x));
+    } else {
+      static size_t ero_x_configured = 0;
+      if (smem > 48 * 1024 && smem > ero_x_configured) {
+        cudaFuncSetAttribute(k_ero_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        ero_x_configured = smem;
+      }
+      GM_LAUNCH(kc, "k_ero_pass_x", st,
+                k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, RF, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1,
+                                                              B_ero_x));
     }
-    GM_LAUNCH(kc, "k_ero_pass_x", st,
-              k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, RF, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1,
-                                                            B_ero_x));
     if (K <= 32767) {
       // ero z needs its outputs on D grown by one cell (the refinement tags
       // cells next to D), ero y its outputs there and within the z window
