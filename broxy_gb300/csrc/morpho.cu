@@ -1193,104 +1193,15 @@ __global__ void __launch_bounds__(256) k_occ_map8(const uint8_t* __restrict__ G,
 // cell-level kernels
 // ---------------------------------------------------------------------
 
-__device__ __forceinline__ bool in_box(int x, int y, int z, const int* dr) {
-  return x < dr[0] && y < dr[1] && z < dr[2];
-}
-
 struct DataRes { int v[3]; };
 
-// GM_REF dilation select: base pass (cells inside data_res that are not
-// full take 0xff when their child-0 corner is dilated, GMorpho.cu:2848-2927)
-// then the tight contour (forward 2x2x2 block mixes full and non-full,
-// Grid.cu:1589-1607) takes the fine per-voxel byte (GMorpho.cu:2930-3056).
-__device__ __forceinline__ uint8_t base_dil(const uint8_t* X, const uint8_t* Df, int64_t c, bool inside) {
-  const uint8_t x = X[c];
-  return (inside && x != 0xff && (Df[c] & 1)) ? (uint8_t)0xff : x;
-}
-
-// Contour of the dilation: fine voxels outside D that are 6-adjacent to D.
-// GM_REF: only for cells in [1, res-2]^3 whose byte is not 0xff
-// (TagVoxelsContourByErosion, Grid.cu:1230-1327); GM_EXACT: whole grid.
-__device__ __forceinline__ uint8_t adj6(uint8_t v, uint8_t xm, uint8_t xp, uint8_t ym, uint8_t yp, uint8_t zm,
-                                        uint8_t zp) {
-  uint32_t t = ((v & 0xAAu) >> 1) | ((xp & 0x55u) << 1);
-  t |= ((v & 0x55u) << 1) | ((xm & 0xAAu) >> 1);
-  t |= ((v & 0xCCu) >> 2) | ((yp & 0x33u) << 2);
-  t |= ((v & 0x33u) << 2) | ((ym & 0xCCu) >> 2);
-  t |= ((v & 0xF0u) >> 4) | ((zp & 0x0Fu) << 4);
-  t |= ((v & 0x0Fu) << 4) | ((zm & 0xF0u) >> 4);
-  return (uint8_t)t;
-}
-
-// GM_REF erosion select: base pass (cells inside data_res with D != 0 and
-// X != 0xff are cleared when the centre 2c+1 is eroded, GMorpho.cu:4360-4370,
-// 4644-4646), then cells whose byte differs from a 6-neighbour
-// (Grid.cu:1499-1570) take 0xff & ~eroded (GMorpho.cu:5353-5360).
-__device__ __forceinline__ uint8_t base_ero(const uint8_t* X, const uint8_t* D, const uint8_t* Eb, int64_t c,
-                                            bool inside) {
-  const uint8_t d = D[c];
-  return (inside && d != 0 && X[c] != 0xff && Eb[c]) ? (uint8_t)0 : d;
-}
-
 // ---------------------------------------------------------------------
-// the same cell-level kernels, four consecutive cells (one u32) per thread
-// block (64, 4): x quads along threadIdx.x, y along threadIdx.y, z = blockIdx.z
+// cell-level kernels; cell grids of this section are boxes of rx * ry * rz
+// cells (Dims), z = blockIdx.z
 // ---------------------------------------------------------------------
 
-// cell grids of this section are boxes of rx * ry * rz cells (Dims)
 struct Dims { int x, y, z; };
 __device__ __forceinline__ int64_t cidx(int x, int y, int z, Dims d) { return idx3(x, y, z, d.x, d.y); }
-__device__ __forceinline__ uint32_t ld4(const uint8_t* g, int x4, int y, int z, Dims d) {
-  return *reinterpret_cast<const uint32_t*>(g + cidx(x4, y, z, d));
-}
-__device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
-
-__global__ void __launch_bounds__(256) k_dil_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
-                                                     uint8_t* __restrict__ D, Dims g, DataRes dr, CBox roi) {
-  const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
-  const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= g.x || y >= g.y || !cbox_meets(roi, x4, x4 + 3, y, y, z, z)) return;
-  // full flags of the base-pass byte for x in [x4, x4+4], (y, y+1) x (z, z+1)
-  uint32_t full[2][2];
-  uint32_t center = 0, dfc = 0;
-#pragma unroll
-  for (int dz = 0; dz < 2; dz++)
-#pragma unroll
-    for (int dy = 0; dy < 2; dy++) {
-      const int yy = y + dy, zz = z + dz;
-      uint32_t f = 0;
-      if (yy < g.y && zz < g.z) {
-        const uint32_t xw = ld4(X, x4, yy, zz, g), dw = ld4(Df, x4, yy, zz, g);
-        const bool iyz = yy < dr.v[1] && zz < dr.v[2];
-#pragma unroll
-        for (int i = 0; i < 5; i++) {
-          const int xx = x4 + i;
-          if (xx >= g.x) break;
-          const uint32_t xb = i < 4 ? byte_of(xw, i) : X[cidx(xx, yy, zz, g)];
-          const uint32_t db = i < 4 ? byte_of(dw, i) : Df[cidx(xx, yy, zz, g)];
-          const bool inside = iyz && xx < dr.v[0];
-          const uint32_t d0 = (inside && xb != 0xffu && (db & 1u)) ? 0xffu : xb;
-          f |= (uint32_t)(d0 == 0xffu) << i;
-          if (dz == 0 && dy == 0 && i < 4) { center |= d0 << (8 * i); }
-        }
-        if (dz == 0 && dy == 0) dfc = dw;
-      }
-      full[dz][dy] = f;
-    }
-  uint32_t out = 0;
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int x = x4 + i;
-    bool tag = false;
-    if (x <= g.x - 2 && y <= g.y - 2 && z <= g.z - 2) {
-      const uint32_t m = 3u << i;
-      const int n = __popc(full[0][0] & m) + __popc(full[0][1] & m) + __popc(full[1][0] & m) + __popc(full[1][1] & m);
-      tag = n != 0 && n != 8;
-    }
-    out |= (tag ? byte_of(dfc, i) : byte_of(center, i)) << (8 * i);
-  }
-  *reinterpret_cast<uint32_t*>(D + cidx(x4, y, z, g)) = out;
-}
 
 // Dilation flags from a resident squared lattice distance field E of the
 // input grid (u16 per fine voxel: the value the dilation's z pass computes,
@@ -1328,94 +1239,219 @@ __global__ void __launch_bounds__(256) k_dil_threshold(const uint16_t* __restric
   *reinterpret_cast<uint32_t*>(out + cidx(x4, y, z, g)) = out4;
 }
 
-__global__ void __launch_bounds__(256) k_contour4(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, Dims g,
-                                                  int exact, CBox roi) {
-  const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
-  const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= g.x || y >= g.y || !cbox_meets(roi, x4, x4 + 3, y, y, z, z)) return;
-  const uint32_t v4 = ld4(D, x4, y, z, g);
-  const uint32_t xm = x4 > 0 ? D[cidx(x4 - 1, y, z, g)] : 0u;
-  const uint32_t xp = x4 + 4 < g.x ? D[cidx(x4 + 4, y, z, g)] : 0u;
-  const uint32_t ym4 = y > 0 ? ld4(D, x4, y - 1, z, g) : 0u, yp4 = y < g.y - 1 ? ld4(D, x4, y + 1, z, g) : 0u;
-  const uint32_t zm4 = z > 0 ? ld4(D, x4, y, z - 1, g) : 0u, zp4 = z < g.z - 1 ? ld4(D, x4, y, z + 1, g) : 0u;
-  uint32_t out = 0;
-  const bool yz_in = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int x = x4 + i;
-    const uint32_t v = byte_of(v4, i);
-    const uint32_t l = i == 0 ? xm : byte_of(v4, i - 1), r = i == 3 ? xp : byte_of(v4, i + 1);
-    uint32_t o = 0;
-    if (exact || (yz_in && x >= 1 && x <= g.x - 2 && v != 0xffu))
-      o = adj6((uint8_t)v, (uint8_t)l, (uint8_t)r, (uint8_t)byte_of(ym4, i), (uint8_t)byte_of(yp4, i),
-               (uint8_t)byte_of(zm4, i), (uint8_t)byte_of(zp4, i)) & ~v & 0xffu;
-    out |= o << (8 * i);
-  }
-  *reinterpret_cast<uint32_t*>(S + cidx(x4, y, z, g)) = out;
-}
 
 __device__ __forceinline__ uint32_t c0_of(uint32_t x, uint32_t d, uint32_t eb, bool inside) {
   return (inside && d != 0u && x != 0xffu && eb) ? 0u : d;
 }
 
-__global__ void __launch_bounds__(256) k_ero_select4(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
-                                                     const uint8_t* __restrict__ Eb, const uint8_t* __restrict__ Ef,
-                                                     uint8_t* __restrict__ C, Dims g, DataRes dr, int exact, CBox roi) {
-  const int x4 = 4 * (blockIdx.x * 64 + threadIdx.x);
-  const int y = blockIdx.y * 4 + threadIdx.y, z = blockIdx.z;
-  if (x4 >= g.x || y >= g.y || !cbox_meets(roi, x4, x4 + 3, y, y, z, z)) return;
-  const uint32_t d4 = ld4(D, x4, y, z, g), ef4 = ld4(Ef, x4, y, z, g);
-  if (exact) {
-    *reinterpret_cast<uint32_t*>(C + cidx(x4, y, z, g)) = d4 & ~ef4;
-    return;
-  }
-  const uint32_t x4v = ld4(X, x4, y, z, g), eb4 = ld4(Eb, x4, y, z, g);
-  const bool iyz = y < dr.v[1] && z < dr.v[2];
-  // C0 along the row at x4-1 .. x4+4
-  uint32_t row[6];
-#pragma unroll
-  for (int i = 0; i < 6; i++) {
-    const int xx = x4 - 1 + i;
-    if (xx < 0 || xx >= g.x) { row[i] = 0u; continue; }
-    uint32_t xb, db, eb;
-    if (i >= 1 && i <= 4) { xb = byte_of(x4v, i - 1); db = byte_of(d4, i - 1); eb = byte_of(eb4, i - 1); }
-    else { const int64_t c = cidx(xx, y, z, g); xb = X[c]; db = D[c]; eb = Eb[c]; }
-    row[i] = c0_of(xb, db, eb, iyz && xx < dr.v[0]);
-  }
-  // C0 of the four y/z neighbour rows
-  uint32_t nb[4] = {0u, 0u, 0u, 0u};
-  const int ny[4] = {y - 1, y + 1, y, y};
-  const int nz[4] = {z, z, z - 1, z + 1};
-  const bool interior_yz = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
-  if (interior_yz) {
-#pragma unroll
-    for (int n = 0; n < 4; n++) {
-      const uint32_t xw = ld4(X, x4, ny[n], nz[n], g), dw = ld4(D, x4, ny[n], nz[n], g),
-                     ew = ld4(Eb, x4, ny[n], nz[n], g);
-      const bool in_yz = ny[n] < dr.v[1] && nz[n] < dr.v[2];
-      uint32_t w = 0;
-#pragma unroll
-      for (int i = 0; i < 4; i++)
-        w |= c0_of(byte_of(xw, i), byte_of(dw, i), byte_of(ew, i), in_yz && x4 + i < dr.v[0]) << (8 * i);
-      nb[n] = w;
-    }
-  }
-  uint32_t out = 0;
-#pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const int x = x4 + i;
-    const uint32_t c0 = row[i + 1];
-    bool tag = false;
-    if (interior_yz && x >= 1 && x <= g.x - 2) {
-      tag = row[i] != c0 || row[i + 2] != c0 || byte_of(nb[0], i) != c0 || byte_of(nb[1], i) != c0 ||
-            byte_of(nb[2], i) != c0 || byte_of(nb[3], i) != c0;
-    }
-    out |= (tag ? (0xffu & ~byte_of(ef4, i)) : c0) << (8 * i);
-  }
-  *reinterpret_cast<uint32_t*>(C + cidx(x4, y, z, g)) = out;
-}
 
 static dim3 quad_grid(Dims g) { return dim3((g.x / 4 + 63) / 64, (g.y + 3) / 4, g.z); }
+
+// ---------------------------------------------------------------------
+// The same cell-level kernels on 16 consecutive cells per thread (one
+// 16-byte load per row), four cells per 32-bit word at a time: the
+// per-byte rules become byte masks (__vcmp*4) and shifts that stay within
+// bytes.  Block (32, 8): x along threadIdx.x, y along threadIdx.y.
+// ---------------------------------------------------------------------
+
+__device__ __forceinline__ uint4 ld16(const uint8_t* g, int x16, int y, int z, Dims d) {
+  return *reinterpret_cast<const uint4*>(g + cidx(x16, y, z, d));
+}
+__device__ __forceinline__ uint32_t w_of(const uint4& q, int j) {
+  return j == 0 ? q.x : (j == 1 ? q.y : (j == 2 ? q.z : q.w));
+}
+// 0xff in byte i where cell x0 + i satisfies lo <= x < hi
+__device__ __forceinline__ uint32_t xrange_mask(int x0, int lo, int hi) {
+  uint32_t m = 0;
+#pragma unroll
+  for (int i = 0; i < 4; i++) m |= (x0 + i >= lo && x0 + i < hi) ? (0xffu << (8 * i)) : 0u;
+  return m;
+}
+// the word of cells x0 + 1 .. x0 + 4 (x0 - 1 .. x0 + 2) from the word of
+// x0 .. x0 + 3 and the byte after (before) it
+__device__ __forceinline__ uint32_t next_cells(uint32_t w, uint32_t after) { return (w >> 8) | (after << 24); }
+__device__ __forceinline__ uint32_t prev_cells(uint32_t w, uint32_t before) { return (w << 8) | before; }
+
+// Contour of the dilation: fine voxels outside D that are 6-adjacent to D.
+// GM_REF: only for cells in [1, res-2]^3 whose byte is not 0xff
+// (TagVoxelsContourByErosion, Grid.cu:1230-1327); GM_EXACT: whole grid.
+__global__ void __launch_bounds__(256) k_contour16(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, Dims g,
+                                                   int exact, CBox roi) {
+  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
+  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
+  const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
+  const uint4 v = ld16(D, x16, y, z, g);
+  const uint32_t before = x16 > 0 ? D[cidx(x16 - 1, y, z, g)] : 0u;
+  const uint32_t after = x16 + 16 < g.x ? D[cidx(x16 + 16, y, z, g)] : 0u;
+  const uint4 ym = y > 0 ? ld16(D, x16, y - 1, z, g) : z4, yp = y < g.y - 1 ? ld16(D, x16, y + 1, z, g) : z4;
+  const uint4 zm = z > 0 ? ld16(D, x16, y, z - 1, g) : z4, zp = z < g.z - 1 ? ld16(D, x16, y, z + 1, g) : z4;
+  const bool yz_in = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
+  uint32_t o[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t vw = w_of(v, j);
+    const uint32_t l = prev_cells(vw, j > 0 ? w_of(v, j - 1) >> 24 : before);
+    const uint32_t r = next_cells(vw, j < 3 ? w_of(v, j + 1) & 0xffu : after);
+    // 6-neighbours of each fine voxel (bit x + 2y + 4z of a byte)
+    uint32_t t = ((vw & 0xAAAAAAAAu) >> 1) | ((r & 0x55555555u) << 1);
+    t |= ((vw & 0x55555555u) << 1) | ((l & 0xAAAAAAAAu) >> 1);
+    t |= ((vw & 0xCCCCCCCCu) >> 2) | ((w_of(yp, j) & 0x33333333u) << 2);
+    t |= ((vw & 0x33333333u) << 2) | ((w_of(ym, j) & 0xCCCCCCCCu) >> 2);
+    t |= ((vw & 0xF0F0F0F0u) >> 4) | ((w_of(zp, j) & 0x0F0F0F0Fu) << 4);
+    t |= ((vw & 0x0F0F0F0Fu) << 4) | ((w_of(zm, j) & 0xF0F0F0F0u) >> 4);
+    uint32_t m = 0xffffffffu;
+    if (!exact) m = yz_in ? (__vcmpne4(vw, 0xffffffffu) & xrange_mask(x16 + 4 * j, 1, g.x - 1)) : 0u;
+    o[j] = t & ~vw & m;
+  }
+  *reinterpret_cast<uint4*>(S + cidx(x16, y, z, g)) = make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+// GM_REF dilation select: base pass (cells inside data_res that are not
+// full take 0xff when their child-0 corner is dilated, GMorpho.cu:2848-2927)
+// then the tight contour (forward 2x2x2 block mixes full and non-full,
+// Grid.cu:1589-1607) takes the fine per-voxel byte (GMorpho.cu:2930-3056).
+//
+// base-pass bytes of the dilation (GM_REF) of one row of 16 cells and the
+// full flags (0xff per full byte) of the cells x16 + 1 .. x16 + 16
+__device__ __forceinline__ void base_dil_row(const uint8_t* X, const uint8_t* Df, int x16, int yy, int zz, Dims g,
+                                             const DataRes& dr, uint32_t d0[4], uint32_t f[4], uint32_t fr[4],
+                                             uint32_t dfw[4]) {
+  if (yy >= g.y || zz >= g.z) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) { d0[j] = 0u; f[j] = 0u; fr[j] = 0u; dfw[j] = 0u; }
+    return;
+  }
+  const bool iyz = yy < dr.v[1] && zz < dr.v[2];
+  const uint4 xq = ld16(X, x16, yy, zz, g), dq = ld16(Df, x16, yy, zz, g);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t xw = w_of(xq, j), dw = w_of(dq, j);
+    const uint32_t in = iyz ? xrange_mask(x16 + 4 * j, 0, dr.v[0]) : 0u;
+    const uint32_t cond = in & __vcmpne4(xw, 0xffffffffu) & ((dw & 0x01010101u) * 0xffu);
+    d0[j] = xw | cond;
+    f[j] = __vcmpeq4(d0[j], 0xffffffffu);
+    dfw[j] = dw;
+  }
+  // full flag of cell x16 + 16
+  uint32_t fa = 0u;
+  if (x16 + 16 < g.x) {
+    const int64_t c = cidx(x16 + 16, yy, zz, g);
+    const uint32_t xb = X[c], db = Df[c];
+    const bool inside = iyz && x16 + 16 < dr.v[0];
+    const uint32_t d = (inside && xb != 0xffu && (db & 1u)) ? 0xffu : xb;
+    fa = d == 0xffu ? 0xffu : 0u;
+  }
+#pragma unroll
+  for (int j = 0; j < 4; j++) fr[j] = next_cells(f[j], j < 3 ? f[j + 1] & 0xffu : fa);
+}
+
+__global__ void __launch_bounds__(256) k_dil_select16(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
+                                                      uint8_t* __restrict__ D, Dims g, DataRes dr, CBox roi) {
+  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
+  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
+  uint32_t any[4] = {0u, 0u, 0u, 0u}, all[4] = {~0u, ~0u, ~0u, ~0u}, d0c[4], dfc[4];
+#pragma unroll
+  for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++) {
+      uint32_t d0[4], f[4], fr[4], dfw[4];
+      base_dil_row(X, Df, x16, y + dy, z + dz, g, dr, d0, f, fr, dfw);
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        any[j] |= f[j] | fr[j];
+        all[j] &= f[j] & fr[j];
+        if (dz == 0 && dy == 0) { d0c[j] = d0[j]; dfc[j] = dfw[j]; }
+      }
+    }
+  // the forward 2x2x2 block mixes full and non-full bytes (cells <= dims - 2)
+  const bool yz_ok = y <= g.y - 2 && z <= g.z - 2;
+  uint32_t o[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t tag = yz_ok ? (any[j] & ~all[j] & xrange_mask(x16 + 4 * j, 0, g.x - 1)) : 0u;
+    o[j] = (tag & dfc[j]) | (~tag & d0c[j]);
+  }
+  *reinterpret_cast<uint4*>(D + cidx(x16, y, z, g)) = make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+// GM_REF erosion select: base pass (cells inside data_res with D != 0 and
+// X != 0xff are cleared when the centre 2c+1 is eroded, GMorpho.cu:4360-4370,
+// 4644-4646), then cells whose byte differs from a 6-neighbour
+// (Grid.cu:1499-1570) take 0xff & ~eroded (GMorpho.cu:5353-5360).
+//
+// C0 = base erosion of 16 cells of one row: 0 where the cell is inside the
+// data, D != 0, X != 0xff and its lattice point 2c+1 is eroded; D otherwise
+__device__ __forceinline__ void base_ero_row(const uint8_t* X, const uint8_t* D, const uint8_t* Eb, int x16, int yy,
+                                             int zz, Dims g, const DataRes& dr, uint32_t c0[4]) {
+  const bool iyz = yy < dr.v[1] && zz < dr.v[2];
+  const uint4 xq = ld16(X, x16, yy, zz, g), dq = ld16(D, x16, yy, zz, g), eq = ld16(Eb, x16, yy, zz, g);
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t dw = w_of(dq, j);
+    const uint32_t in = iyz ? xrange_mask(x16 + 4 * j, 0, dr.v[0]) : 0u;
+    const uint32_t cond = in & __vcmpne4(dw, 0u) & __vcmpne4(w_of(xq, j), 0xffffffffu) & __vcmpne4(w_of(eq, j), 0u);
+    c0[j] = dw & ~cond;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_ero_select16(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
+                                                      const uint8_t* __restrict__ Eb, const uint8_t* __restrict__ Ef,
+                                                      uint8_t* __restrict__ C, Dims g, DataRes dr, int exact,
+                                                      CBox roi) {
+  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
+  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
+  const uint4 ef = ld16(Ef, x16, y, z, g);
+  if (exact) {
+    const uint4 d = ld16(D, x16, y, z, g);
+    *reinterpret_cast<uint4*>(C + cidx(x16, y, z, g)) =
+        make_uint4(d.x & ~ef.x, d.y & ~ef.y, d.z & ~ef.z, d.w & ~ef.w);
+    return;
+  }
+  uint32_t c0[4];
+  base_ero_row(X, D, Eb, x16, y, z, g, dr, c0);
+  // C0 of the cells x16 - 1 and x16 + 16
+  const bool iyz = y < dr.v[1] && z < dr.v[2];
+  uint32_t before = 0u, after = 0u;
+  if (x16 > 0) {
+    const int64_t c = cidx(x16 - 1, y, z, g);
+    before = c0_of(X[c], D[c], Eb[c], iyz && x16 - 1 < dr.v[0]);
+  }
+  if (x16 + 16 < g.x) {
+    const int64_t c = cidx(x16 + 16, y, z, g);
+    after = c0_of(X[c], D[c], Eb[c], iyz && x16 + 16 < dr.v[0]);
+  }
+  const bool interior_yz = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
+  uint32_t diff[4] = {0u, 0u, 0u, 0u};
+  if (interior_yz) {
+    const int ny[4] = {y - 1, y + 1, y, y};
+    const int nz[4] = {z, z, z - 1, z + 1};
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      uint32_t cn[4];
+      base_ero_row(X, D, Eb, x16, ny[n], nz[n], g, dr, cn);
+#pragma unroll
+      for (int j = 0; j < 4; j++) diff[j] |= __vcmpne4(c0[j], cn[j]);
+    }
+  }
+  uint32_t o[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const uint32_t l = prev_cells(c0[j], j > 0 ? c0[j - 1] >> 24 : before);
+    const uint32_t r = next_cells(c0[j], j < 3 ? c0[j + 1] & 0xffu : after);
+    const uint32_t tag = interior_yz ? ((diff[j] | __vcmpne4(c0[j], l) | __vcmpne4(c0[j], r)) &
+                                        xrange_mask(x16 + 4 * j, 1, g.x - 1))
+                                     : 0u;
+    o[j] = (tag & ~w_of(ef, j)) | (~tag & c0[j]);
+  }
+  *reinterpret_cast<uint4*>(C + cidx(x16, y, z, g)) = make_uint4(o[0], o[1], o[2], o[3]);
+}
+
+static dim3 grid16(Dims g) { return dim3((g.x / 16 + 31) / 32, (g.y + 7) / 8, g.z); }
+
+
 
 // max clamped radius over the fine radius grid
 __global__ void k_rmax(const int8_t* __restrict__ R, int64_t n, int* __restrict__ out) {
@@ -1584,7 +1620,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     }
   }
   if (!exact) {
-    GM_LAUNCH(kc, "k_dil_select", st, k_dil_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, Df, D, g, dr, R_D));
+    GM_LAUNCH(kc, "k_dil_select", st, k_dil_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, Df, D, g, dr, R_D));
   }
   // ---- occupancy map of D (erosion outputs are needed on D only) ----
   {
@@ -1592,7 +1628,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     GM_LAUNCH(kc, "k_occ_map8", st, k_occ_map8<<<(nb + 7) / 8, 256, 0, st>>>(D, rx, ry, mdx, mdy, nb, dmap));
   }
   // ---- contour ----
-  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact ? 1 : 0, R_S));
+  GM_LAUNCH(kc, "k_contour", st, k_contour16<<<grid16(g), dim3(32, 8), 0, st>>>(D, S, g, exact ? 1 : 0, R_S));
   // ---- erosion ----
   {
     const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
@@ -1657,7 +1693,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       }
     }
     GM_LAUNCH(kc, "k_ero_select", st,
-              k_ero_select4<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0,
+              k_ero_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0,
                                                                           F));
   }
   if (a.S_out) {
@@ -1706,7 +1742,7 @@ cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounte
 
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc) {
   const Dims g{res, res, res};
-  GM_LAUNCH(kc, "k_contour", st, k_contour4<<<quad_grid(g), dim3(64, 4), 0, st>>>(D, S, g, exact, CBox{{0, 0, 0}, {res, res, res}}));
+  GM_LAUNCH(kc, "k_contour", st, k_contour16<<<grid16(g), dim3(32, 8), 0, st>>>(D, S, g, exact, CBox{{0, 0, 0}, {res, res, res}}));
   return cudaGetLastError();
 }
 
