@@ -517,6 +517,7 @@ gm_status gm_mesh_box(gm_ctx* ctx, const gm_box_desc* box, const uint8_t* d_clos
   if (s != GM_OK) return s;
   if (!d_closing || !out || bilateral_iters < 0)
     return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh_box: NULL buffer or negative iteration count");
+  if (!aligned16(d_closing)) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh_box: the grid must be 16-byte aligned");
   if (win) {
     if (win->global_res < 1) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh_box: global_res must be positive");
     for (int a = 0; a < 3; a++)
@@ -595,6 +596,7 @@ gm_status gm_mesh(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_closin
   if (s != GM_OK) return s;
   if (!d_closing || !out || bilateral_iters < 0)
     return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh: NULL buffer or negative iteration count");
+  if (!aligned16(d_closing)) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_mesh: the grid must be 16-byte aligned");
   if ((s = set_device(ctx)) != GM_OK) return s;
   if ((s = mesh_impl(ctx, desc, d_closing, bilateral_iters, (cudaStream_t)stream)) != GM_OK) return s;
   out->vertices = ctx->mesh.V;
@@ -749,7 +751,7 @@ gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items
     gm_status s = check_desc(ctx, &items[i].desc);
     if (s != GM_OK) return s;
     if (!items[i].d_input || !items[i].d_closing || !aligned16(items[i].d_input) ||
-        (items[i].d_scale && !aligned16(items[i].d_scale)))
+        !aligned16(items[i].d_closing) || (items[i].d_scale && !aligned16(items[i].d_scale)))
       return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: item " + std::to_string(i));
   }
   if (n == 0) return GM_OK;

@@ -140,8 +140,8 @@ struct MeshBuffers {
   float* N2 = nullptr;      // unused (kept for ABI-stable layout of the struct)
   float4* N4a = nullptr;    // v_cap, bilateral ping-pong (16-byte normals)
   float4* N4b = nullptr;    // v_cap
-  uint2* nbr = nullptr;     // 3 * t_cap: the two other vertices of each corner
-  float2* wpos = nullptr;   // 3 * t_cap: their position terms |pa-pb|^2 / sigma_p^2
+  uint4* ent = nullptr;     // 3 * t_cap: the two other vertices of each corner and their position
+                            // terms |pa-pb|^2 / sigma_p^2 (float bits)
   uint32_t* T = nullptr;    // 3 * t_cap
   uint32_t* adj = nullptr;  // 3 * t_cap (vertex -> corner list)
   uint32_t* rowptr = nullptr;  // v_cap + 1

@@ -37,7 +37,9 @@ __device__ __forceinline__ int nv_owned(int em) { return (em & 1) + ((em >> 3) &
 
 constexpr int kBrick = 16;               // cells per brick edge
 constexpr int kTileE = kBrick + 2;       // tile edge (halo 2 for neighbour cells)
-constexpr int kTileCells = kTileE * kTileE * kTileE;
+constexpr int kTileP = 32;               // tile row pitch (bytes): rows are one 16-byte and one 2-byte store
+constexpr int kTileCells = kTileP * kTileE * kTileE;
+__device__ __forceinline__ int tix(int x, int y, int z) { return x + kTileP * (y + kTileE * z); }
 constexpr int kCellsPerBrick = kBrick * kBrick * kBrick;
 constexpr int kMcThreads = 256;
 constexpr int kCellsPerThread = kCellsPerBrick / kMcThreads;
@@ -52,26 +54,35 @@ __device__ __forceinline__ void brick_origin(int b, int& ox, int& oy, int& oz) {
 struct GDims { int x, y, z; };
 __device__ __forceinline__ int64_t gidx(int x, int y, int z, GDims d) { return idx3(x, y, z, d.x, d.y); }
 
-__device__ void load_tile(const uint8_t* __restrict__ C, GDims d, int ox, int oy, int oz, uint8_t* tile) {
-  for (int i = threadIdx.x; i < kTileCells; i += blockDim.x) {
-    const int lx = i % kTileE, ly = (i / kTileE) % kTileE, lz = i / (kTileE * kTileE);
-    const int x = ox + lx, y = oy + ly, z = oz + lz;
-    tile[i] = (x < d.x && y < d.y && z < d.z) ? C[gidx(x, y, z, d)] : (uint8_t)0;
-  }
-}
-
-// Loads the tile and tells (block-uniformly) whether it can hold a mixed
-// cube: a tile whose bytes are all 0x00 or all 0xff has none.
+// Loads the tile (cells o .. o + 17 per axis, zero outside the grid) and
+// tells (block-uniformly) whether it can hold a mixed cube: a tile whose
+// bytes are all 0x00 or all 0xff has none.  One row (18 cells along x) is
+// a 16-byte and a 2-byte load: bricks start at multiples of 16 cells and
+// grid edges are multiples of 16, so a row is either inside the grid up to
+// cell o + 15 or outside, and so are cells o + 16, o + 17.
 __device__ bool load_tile_mixed(const uint8_t* __restrict__ C, GDims d, int ox, int oy, int oz, uint8_t* tile) {
   int seen0 = 0, seen1 = 0, part = 0;
-  for (int i = threadIdx.x; i < kTileCells; i += blockDim.x) {
-    const int lx = i % kTileE, ly = (i / kTileE) % kTileE, lz = i / (kTileE * kTileE);
-    const int x = ox + lx, y = oy + ly, z = oz + lz;
-    const uint8_t v = (x < d.x && y < d.y && z < d.z) ? C[gidx(x, y, z, d)] : (uint8_t)0;
-    tile[i] = v;
-    seen0 |= v == 0x00;
-    seen1 |= v == 0xff;
-    part |= v != 0x00 && v != 0xff;
+  for (int row = threadIdx.x; row < kTileE * kTileE; row += blockDim.x) {
+    const int ly = row % kTileE, lz = row / kTileE;
+    const int y = oy + ly, z = oz + lz;
+    uint4 q = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t h = 0u;
+    if (y < d.y && z < d.z && ox < d.x) {
+      q = *reinterpret_cast<const uint4*>(C + gidx(ox, y, z, d));
+      if (ox + kBrick < d.x) h = *reinterpret_cast<const uint16_t*>(C + gidx(ox + kBrick, y, z, d));
+    }
+    uint8_t* trow = tile + kTileP * row;
+    *reinterpret_cast<uint4*>(trow) = q;
+    *reinterpret_cast<uint16_t*>(trow + kBrick) = (uint16_t)h;
+    // the two halo bytes, repeated to fill a word (repeats change no test)
+    const uint32_t w[5] = {q.x, q.y, q.z, q.w, h | (h << 16)};
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      const uint32_t z4 = __vcmpeq4(w[k], 0u), f4 = __vcmpeq4(w[k], 0xffffffffu);
+      seen0 |= z4 != 0u;
+      seen1 |= f4 != 0u;
+      part |= (~(z4 | f4)) != 0u;
+    }
   }
   const int mixed = __syncthreads_or(part | (seen0 & seen1));
   if (mixed) return true;
@@ -90,7 +101,7 @@ __device__ __forceinline__ void cube_values(const uint8_t* tile, int lx, int ly,
     for (int j = 0; j < 3; j++)
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        const uint8_t cell = tile[(lx + (i >> 1)) + kTileE * (ly + (j >> 1)) + kTileE * kTileE * (lz + (k >> 1))];
+        const uint8_t cell = tile[tix(lx + (i >> 1), ly + (j >> 1), lz + (k >> 1))];
         const uint32_t bit = (cell >> ((i & 1) + 2 * (j & 1) + 4 * (k & 1))) & 1u;
         b27 |= bit << (i + 3 * j + 9 * k);
       }
@@ -118,7 +129,7 @@ __device__ __forceinline__ bool cell_uniform(const uint8_t* tile, int lx, int ly
   uint32_t o = 0, a = 0xffu;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    const uint32_t v = tile[(lx + (k & 1)) + kTileE * (ly + ((k >> 1) & 1)) + kTileE * kTileE * (lz + (k >> 2))];
+    const uint32_t v = tile[tix(lx + (k & 1), ly + ((k >> 1) & 1), lz + (k >> 2))];
     o |= v;
     a &= v;
   }
@@ -286,7 +297,7 @@ __device__ uint32_t block_prefix_inplace(uint32_t* cnt, int n) {
 
 __global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                           uint32_t* __restrict__ brick_tot) {
-  __shared__ uint8_t tile[kTileCells];
+  __shared__ __align__(16) uint8_t tile[kTileCells];
   __shared__ uint16_t list[kCellsPerBrick];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
@@ -317,35 +328,69 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restri
   }
 }
 
-// exclusive scan of the brick totals, in place; totals at index nb.
-__global__ void __launch_bounds__(1024) k_scan_bricks(uint32_t* __restrict__ bt, int nb) {
-  __shared__ uint32_t part[4][1024];
-  const int t = threadIdx.x;
-  const int per = (nb + 1023) / 1024;
-  const int b0 = t * per, b1 = min(nb, b0 + per);
-  uint32_t s[4] = {0, 0, 0, 0};
-  for (int b = b0; b < b1; b++)
-    for (int c = 0; c < 4; c++) s[c] += bt[4 * b + c];
-  for (int c = 0; c < 4; c++) part[c][t] = s[c];
-  __syncthreads();
-  // Hillis-Steele over 1024 partial sums
-  for (int o = 1; o < 1024; o <<= 1) {
-    uint32_t v[4];
-    for (int c = 0; c < 4; c++) v[c] = t >= o ? part[c][t - o] : 0;
-    __syncthreads();
-    for (int c = 0; c < 4; c++) part[c][t] += v[c];
-    __syncthreads();
+// Exclusive scan of the four brick counters, in place, totals at index nb:
+// chunks of 1024 bricks, one block each.  k_brick_sums leaves each chunk's
+// sums after the counters (index nb + 1 + chunk); k_scan_bricks adds the
+// sums of the chunks before its own and scans its chunk (16-byte loads).
+constexpr int kBrickChunk = 1024;
+
+__device__ __forceinline__ uint4 add4(uint4 a, uint4 b) { return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ uint4 shfl_up4(uint4 v, int o) {
+  return make_uint4(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o),
+                    __shfl_up_sync(0xffffffffu, v.z, o), __shfl_up_sync(0xffffffffu, v.w, o));
+}
+__device__ __forceinline__ uint4 shfl4(uint4 v, int src) {
+  return make_uint4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                    __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+}
+// inclusive scan over the block (1024 threads); *total = the block's sum
+__device__ __forceinline__ uint4 block_incl_scan4(uint4 v, uint4* total) {
+  __shared__ uint4 warp_tot[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint4 t = shfl_up4(v, o);
+    if (lane >= o) v = add4(v, t);
   }
-  uint32_t run[4];
-  for (int c = 0; c < 4; c++) run[c] = part[c][t] - s[c];
-  for (int b = b0; b < b1; b++)
-    for (int c = 0; c < 4; c++) {
-      const uint32_t v = bt[4 * b + c];
-      bt[4 * b + c] = run[c];
-      run[c] += v;
+  if (lane == 31) warp_tot[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    uint4 w = warp_tot[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint4 t = shfl_up4(w, o);
+      if (lane >= o) w = add4(w, t);
     }
-  if (t == 1023)
-    for (int c = 0; c < 4; c++) bt[4 * nb + c] = part[c][1023];
+    warp_tot[lane] = w;
+  }
+  __syncthreads();
+  if (wid > 0) v = add4(v, warp_tot[wid - 1]);
+  *total = warp_tot[31];
+  return v;
+}
+
+__global__ void __launch_bounds__(kBrickChunk) k_brick_sums(uint32_t* __restrict__ bt, int nb) {
+  const int b = blockIdx.x * kBrickChunk + threadIdx.x;
+  const uint4 v = b < nb ? reinterpret_cast<const uint4*>(bt)[b] : make_uint4(0u, 0u, 0u, 0u);
+  uint4 tot;
+  block_incl_scan4(v, &tot);
+  if (threadIdx.x == 0) reinterpret_cast<uint4*>(bt)[nb + 1 + blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kBrickChunk) k_scan_bricks(uint32_t* __restrict__ bt, int nb) {
+  // sums of the chunks before this one (at most kBrickChunk chunks)
+  const int t = threadIdx.x;
+  uint4 prev = t < (int)blockIdx.x ? reinterpret_cast<const uint4*>(bt)[nb + 1 + t] : make_uint4(0u, 0u, 0u, 0u);
+  uint4 off;
+  block_incl_scan4(prev, &off);
+  __syncthreads();  // the scan's shared totals are reused below
+  const int b = blockIdx.x * kBrickChunk + t;
+  const uint4 v = b < nb ? reinterpret_cast<const uint4*>(bt)[b] : make_uint4(0u, 0u, 0u, 0u);
+  uint4 tot;
+  const uint4 incl = block_incl_scan4(v, &tot);
+  const uint4 excl = make_uint4(incl.x - v.x, incl.y - v.y, incl.z - v.z, incl.w - v.w);
+  if (b < nb) reinterpret_cast<uint4*>(bt)[b] = add4(off, excl);
+  if (t == 0 && blockIdx.x == gridDim.x - 1) reinterpret_cast<uint4*>(bt)[nb] = add4(off, tot);
 }
 
 // Float expressions of findIntersection (MarchingCubesMesher.cu:98-100) with
@@ -365,7 +410,7 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
                                                           uint32_t* __restrict__ cell_voff,
                                                           float* __restrict__ V, float bx, float by, float bz,
                                                           float cs, float iso) {
-  __shared__ uint8_t tile[kTileCells];
+  __shared__ __align__(16) uint8_t tile[kTileCells];
   __shared__ uint16_t list[kCellsPerBrick];
   __shared__ uint32_t offs[kCellsPerBrick];
   int ox, oy, oz;
@@ -488,11 +533,11 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
                                                               const uint32_t* __restrict__ cell_voff,
                                                               uint32_t* __restrict__ T, uint32_t nt_total,
                                                               uint32_t* __restrict__ fix, int fix_cap) {
-  extern __shared__ uint32_t mc_smem[];
-  uint32_t* info = mc_smem;                                   // [17^3]
-  uint32_t* offs = info + kInfoE * kInfoE * kInfoE;           // [4096]
-  uint16_t* list = reinterpret_cast<uint16_t*>(offs + kCellsPerBrick);  // [4096]
-  uint8_t* tile = reinterpret_cast<uint8_t*>(list + kCellsPerBrick);    // [18^3]
+  extern __shared__ uint4 mc_smem[];
+  uint8_t* tile = reinterpret_cast<uint8_t*>(mc_smem);                          // [18 * 18 rows of kTileP]
+  uint32_t* info = reinterpret_cast<uint32_t*>(tile + kTileCells);              // [17^3]
+  uint32_t* offs = info + kInfoE * kInfoE * kInfoE;                             // [4096]
+  uint16_t* list = reinterpret_cast<uint16_t*>(offs + kCellsPerBrick);          // [4096]
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
   if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) return;
@@ -836,7 +881,7 @@ __device__ __forceinline__ float dist2(float3 a, float3 b) {
 // |pa - pb|^2 / sigma_p^2 (GMorpho.cu:6561-6569).
 __global__ void k_adj_prep(const float* __restrict__ V, const uint32_t* __restrict__ T,
                            const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
-                           float sp2, uint2* __restrict__ nbr, float2* __restrict__ wpos) {
+                           float sp2, uint4* __restrict__ ent) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
     const float3 pa = ld3(V, (uint32_t)v);
     for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
@@ -844,8 +889,8 @@ __global__ void k_adj_prep(const float* __restrict__ V, const uint32_t* __restri
       const uint32_t t = corner / 3, role = corner - 3 * t;
       const uint32_t ib = T[3 * (size_t)t + (role == 0 ? 1 : 0)];
       const uint32_t ic = T[3 * (size_t)t + (role == 2 ? 1 : 2)];
-      nbr[i] = make_uint2(ib, ic);
-      wpos[i] = make_float2(__fdiv_rn(dist2(pa, ld3(V, ib)), sp2), __fdiv_rn(dist2(pa, ld3(V, ic)), sp2));
+      ent[i] = make_uint4(ib, ic, __float_as_uint(__fdiv_rn(dist2(pa, ld3(V, ib)), sp2)),
+                          __float_as_uint(__fdiv_rn(dist2(pa, ld3(V, ic)), sp2)));
     }
   }
 }
@@ -857,10 +902,11 @@ __device__ __forceinline__ float dist2n(float4 a, float4 b) {
 
 // One bilateral normal iteration (BilateralMeshFiltering{,Normalize},
 // GMorpho.cu:6539-6620): each incident triangle adds w1 n_b + w2 n_c,
-// accumulated per vertex in triangle order.
+// accumulated per vertex in triangle order.  An entry holds the triangle's
+// two other vertices and their position terms (one 16-byte load).
 __global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __restrict__ rowptr,
-                            const uint2* __restrict__ nbr, const float2* __restrict__ wpos, int64_t nv, float sn2,
-                            int zero_isolated, float4* __restrict__ Nout, float* __restrict__ N3) {
+                            const uint4* __restrict__ ent, int64_t nv, float sn2, int zero_isolated,
+                            float4* __restrict__ Nout, float* __restrict__ N3) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
     if (zero_isolated && rowptr[v] == rowptr[v + 1]) {
       Nout[v] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -870,13 +916,12 @@ __global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __re
     float3 acc = make_float3(0.f, 0.f, 0.f);
     const float4 na = Nin[v];
     for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
-      const uint2 bc = nbr[i];
-      const float2 wp = wpos[i];
-      const float4 nb = Nin[bc.x], nc = Nin[bc.y];
+      const uint4 e = ent[i];
+      const float4 nb = Nin[e.x], nc = Nin[e.y];
       // the reference library is built with -use_fast_math (GMorpho/cuda.prf:47),
       // so its exp and division here are the fast forms
-      const float w1 = __expf(-__fadd_rn(wp.x, __fdividef(dist2n(na, nb), sn2)));
-      const float w2 = __expf(-__fadd_rn(wp.y, __fdividef(dist2n(na, nc), sn2)));
+      const float w1 = __expf(-__fadd_rn(__uint_as_float(e.z), __fdividef(dist2n(na, nb), sn2)));
+      const float w2 = __expf(-__fadd_rn(__uint_as_float(e.w), __fdividef(dist2n(na, nc), sn2)));
       acc.x = __fadd_rn(acc.x, __fadd_rn(__fmul_rn(w1, nb.x), __fmul_rn(w2, nc.x)));
       acc.y = __fadd_rn(acc.y, __fadd_rn(__fmul_rn(w1, nb.y), __fmul_rn(w2, nc.y)));
       acc.z = __fadd_rn(acc.z, __fadd_rn(__fmul_rn(w1, nb.z), __fmul_rn(w2, nc.z)));
@@ -898,7 +943,7 @@ static int gs_blocks(int64_t n, int threads, int sms) {
 
 void MeshBuffers::release() {
   cudaFree(V); cudaFree(N); cudaFree(N2); cudaFree(N4a); cudaFree(N4b); cudaFree(T); cudaFree(adj);
-  cudaFree(nbr); cudaFree(wpos); cudaFree(rowptr); cudaFree(cursor); cudaFree(cell_voff); cudaFree(brick_tot);
+  cudaFree(ent); cudaFree(rowptr); cudaFree(cursor); cudaFree(cell_voff); cudaFree(brick_tot);
   cudaFree(fix);
   *this = MeshBuffers();
 }
@@ -940,7 +985,8 @@ static cudaError_t ensure_grid_buffers(MeshBuffers& b, int64_t cells, int nb) {
   if (nb + 1 > b.bricks_cap) {
     if (b.brick_tot) cudaFree(b.brick_tot);
     b.brick_tot = nullptr;
-    e = cudaMalloc(&b.brick_tot, sizeof(uint32_t) * 4 * (size_t)(nb + 1));
+    // counters and totals (nb + 1), then the chunk sums of the scan
+    e = cudaMalloc(&b.brick_tot, sizeof(uint32_t) * 4 * ((size_t)nb + 1 + (nb + kBrickChunk - 1) / kBrickChunk));
     if (e != cudaSuccess) return e;
     b.bricks_cap = nb + 1;
   }
@@ -977,16 +1023,14 @@ static cudaError_t ensure_vertex_buffers(MeshBuffers& b, int64_t nv) {
 static cudaError_t ensure_triangle_buffers(MeshBuffers& b, int64_t nt) {
   cudaError_t e;
   if (b.t_cap < nt || b.T == nullptr) {
-    cudaFree(b.T); cudaFree(b.adj); cudaFree(b.nbr); cudaFree(b.wpos);
+    cudaFree(b.T); cudaFree(b.adj); cudaFree(b.ent);
     b.T = b.adj = nullptr;
-    b.nbr = nullptr;
-    b.wpos = nullptr;
+    b.ent = nullptr;
     b.t_cap = 0;
     const int64_t c = nt + nt / 4 + 1024;
     if ((e = cudaMalloc(&b.T, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.adj, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.nbr, sizeof(uint2) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.wpos, sizeof(float2) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.ent, sizeof(uint4) * 3 * (size_t)c)) != cudaSuccess) return e;
     b.t_cap = c;
   }
   return cudaSuccess;
@@ -1010,7 +1054,12 @@ cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st
   cudaError_t e = ensure_grid_buffers(b, cells, nb);
   if (e != cudaSuccess) return e;
   GM_LAUNCH(kc, "k_mc_count", st, k_mc_count<<<nb, kMcThreads, 0, st>>>(a.C, gd, window_of(a), b.brick_tot));
-  GM_LAUNCH(kc, "k_scan_bricks", st, k_scan_bricks<<<1, 1024, 0, st>>>(b.brick_tot, nb));
+  {
+    const int nchunks = (nb + kBrickChunk - 1) / kBrickChunk;
+    if (nchunks > kBrickChunk) return cudaErrorInvalidValue;
+    GM_LAUNCH(kc, "k_brick_sums", st, k_brick_sums<<<nchunks, kBrickChunk, 0, st>>>(b.brick_tot, nb));
+    GM_LAUNCH(kc, "k_scan_bricks", st, k_scan_bricks<<<nchunks, kBrickChunk, 0, st>>>(b.brick_tot, nb));
+  }
   return cudaMemcpyAsync(h_tot4, b.brick_tot + 4 * (size_t)nb, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
 }
 
@@ -1094,14 +1143,14 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
                                                                       iters == 0 ? b.N : nullptr));
   if (iters > 0) {
     GM_LAUNCH(kc, "k_adj_prep", st,
-              k_adj_prep<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, 1.f, b.nbr, b.wpos));
+              k_adj_prep<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, 1.f, b.ent));
   }
   float4* nin = b.N4a;
   float4* nout = b.N4b;
   for (int it = 0; it < iters; it++) {
     const float sn = it < 2 ? 1e10f : 0.2f;  // GMorpho.cu:6959-6969
     GM_LAUNCH(kc, "k_bilateral", st,
-              k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.rowptr, b.nbr, b.wpos, nv, sn * sn, zi, nout,
+              k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.rowptr, b.ent, nv, sn * sn, zi, nout,
                                                                    it == iters - 1 ? b.N : nullptr));
     float4* t = nin; nin = nout; nout = t;
   }

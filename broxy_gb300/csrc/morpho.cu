@@ -856,7 +856,7 @@ __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, i
 }
 
 template <int G, typename TIn, int FIN>
-__global__ void __launch_bounds__(256) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
+__global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
                                                   int sub, int halo, uint32_t cap, RField R,
                                                   int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
