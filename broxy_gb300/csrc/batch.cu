@@ -52,6 +52,9 @@ struct BatchState {
   unsigned* d_ext = nullptr;  // occupied extent, 3 per instance
   unsigned* h_ext = nullptr;  // pinned
   int ext_cap = 0;
+  void* d_filter = nullptr;   // table of the grouped normal filtering (mesh_filter_table_bytes)
+  void* h_filter = nullptr;   // pinned
+  int filter_cap = 0;
   cudaEvent_t fork = nullptr;
   cudaStream_t cap_st = nullptr;  // capture / replay stream (the caller's may be the legacy stream)
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -77,6 +80,8 @@ void batch_release(void* p) {
   cudaFree(b->d_rmax);
   if (b->h_ext) cudaFreeHost(b->h_ext);
   cudaFree(b->d_ext);
+  if (b->h_filter) cudaFreeHost(b->h_filter);
+  cudaFree(b->d_filter);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->cap_st) cudaStreamDestroy(b->cap_st);
   if (b->ev_in) cudaEventDestroy(b->ev_in);
@@ -363,6 +368,7 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     a.cell_size = it[i].desc.cell_size;
     a.isovalue = 0.95f;
     a.bilateral_iters = bilateral;
+    a.defer_filter = bilateral > 0;  // filtered below, all grids per launch
     a.num_sms = sms;
     // the closing is empty beyond the extent: mesh only its cells (the
     // whole grid's border rule, identical mesh)
@@ -388,6 +394,27 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
   for (int l = 0; l < L; l++) {
     cudaEventRecord(b->lanes[l].done, b->lanes[l].st);
     cudaStreamWaitEvent(st, b->lanes[l].done, 0);
+  }
+  if (bilateral > 0) {
+    // normal filtering of all the meshes, one launch per iteration (the
+    // host table is free again: the previous call's copy of it preceded this
+    // call's closings on st, which the lane synchronisation above waited for)
+    if (b->filter_cap < n) {
+      if (b->h_filter) cudaFreeHost(b->h_filter);
+      cudaFree(b->d_filter);
+      b->h_filter = nullptr;
+      b->d_filter = nullptr;
+      b->filter_cap = 0;
+      if ((e = cudaMallocHost(&b->h_filter, mesh_filter_table_bytes(n))) != cudaSuccess) return e;
+      if ((e = cudaMalloc(&b->d_filter, mesh_filter_table_bytes(n))) != cudaSuccess) return e;
+      b->filter_cap = n;
+    }
+    std::vector<MeshBuffers*> mp(n);
+    std::vector<int> zi(n, 0);
+    for (int i = 0; i < n; i++) mp[i] = &b->meshes[i];
+    if ((e = mesh_filter_group(mp.data(), b->nv.data(), zi.data(), n, bilateral, b->d_filter, b->h_filter, sms, st,
+                               kc)) != cudaSuccess)
+      return e;
   }
   return cudaGetLastError();
 }

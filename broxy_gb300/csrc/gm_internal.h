@@ -130,6 +130,9 @@ struct MeshArgs {
   int emit_lo[3] = {0, 0, 0}, emit_hi[3] = {0, 0, 0};
   int zero_isolated = 0;  // (0,0,0) normal for vertices no triangle uses
   cudaEvent_t geometry_done = nullptr;  // recorded once vertices and triangles are final (before normals)
+  // mesh_emit stops after the vertex normals and the bilateral entries:
+  // the caller runs the filtering (mesh_filter_group, several meshes at once)
+  bool defer_filter = false;
 };
 
 // Device-side mesh buffers, grown on demand by the caller of launch_mesh.
@@ -170,6 +173,13 @@ cudaError_t mesh_reserve(MeshBuffers& b, int res, int64_t nv, int64_t nt);
 // Phase 2: emission into b (capacities must be >= counts).
 cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt, cudaStream_t st,
                       KernelCounter* kc);
+// The bilateral filtering of several meshes emitted with defer_filter, one
+// launch per iteration over all their vertices; `table` is device memory of
+// mesh_filter_table_bytes(n) (the call writes it from `h_table`, pinned host
+// memory of the same size).  Results equal mesh_emit's own filtering.
+size_t mesh_filter_table_bytes(int n);
+cudaError_t mesh_filter_group(MeshBuffers* const* meshes, const int64_t* nv, const int* zero_isolated, int n,
+                              int iters, void* table, void* h_table, int sms, cudaStream_t st, KernelCounter* kc);
 
 // ---------------------------------------------------------------- scale field
 cudaError_t launch_scale_brush(int8_t* R, int n, const float* bbox_min, float cell_size, const float* pos,

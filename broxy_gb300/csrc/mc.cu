@@ -932,6 +932,55 @@ __global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __re
   }
 }
 
+// The same iteration over the vertices of several meshes at once (one
+// launch per iteration for a batch): vertex g of the concatenation belongs
+// to the mesh m with start[m] <= g < start[m + 1].
+struct BilMesh {
+  const float4* Na;       // normals of even iterations' inputs (N4a)
+  float4* Nb;             // and odd (N4b)
+  const uint32_t* rowptr;
+  const uint4* ent;
+  float* N3;              // final normals (last iteration)
+  int zero_isolated;
+};
+
+__global__ void k_bilateral_group(const BilMesh* __restrict__ meshes, const int64_t* __restrict__ start, int n,
+                                  int odd, int last, float sn2) {
+  const int64_t total = start[n];
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = n - 1;  // last m with start[m] <= g
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (start[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    const BilMesh& M = meshes[lo];
+    const int64_t v = g - start[lo];
+    const float4* Nin = odd ? M.Nb : M.Na;
+    float4* Nout = odd ? const_cast<float4*>(M.Na) : M.Nb;
+    float* N3 = last ? M.N3 : nullptr;
+    const uint32_t* rowptr = M.rowptr;
+    if (M.zero_isolated && rowptr[v] == rowptr[v + 1]) {
+      Nout[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
+      continue;
+    }
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    const float4 na = Nin[v];
+    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
+      const uint4 e = M.ent[i];
+      const float4 nb = Nin[e.x], nc = Nin[e.y];
+      const float w1 = __expf(-__fadd_rn(__uint_as_float(e.z), __fdividef(dist2n(na, nb), sn2)));
+      const float w2 = __expf(-__fadd_rn(__uint_as_float(e.w), __fdividef(dist2n(na, nc), sn2)));
+      acc.x = __fadd_rn(acc.x, __fadd_rn(__fmul_rn(w1, nb.x), __fmul_rn(w2, nc.x)));
+      acc.y = __fadd_rn(acc.y, __fadd_rn(__fmul_rn(w1, nb.y), __fmul_rn(w2, nc.y)));
+      acc.z = __fadd_rn(acc.z, __fadd_rn(__fmul_rn(w1, nb.z), __fmul_rn(w2, nc.z)));
+    }
+    const float3 nn = normalize3(acc);
+    Nout[v] = make_float4(nn.x, nn.y, nn.z, 0.f);
+    if (N3) { N3[3 * v] = nn.x; N3[3 * v + 1] = nn.y; N3[3 * v + 2] = nn.z; }
+  }
+}
+
 // ------------------------------------------------------------------ host
 
 static int gs_blocks(int64_t n, int threads, int sms) {
@@ -1145,6 +1194,7 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
     GM_LAUNCH(kc, "k_adj_prep", st,
               k_adj_prep<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, 1.f, b.ent));
   }
+  if (a.defer_filter) return cudaGetLastError();
   float4* nin = b.N4a;
   float4* nout = b.N4b;
   for (int it = 0; it < iters; it++) {
@@ -1153,6 +1203,36 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
               k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.rowptr, b.ent, nv, sn * sn, zi, nout,
                                                                    it == iters - 1 ? b.N : nullptr));
     float4* t = nin; nin = nout; nout = t;
+  }
+  return cudaGetLastError();
+}
+
+size_t mesh_filter_table_bytes(int n) {
+  return ((sizeof(BilMesh) * (size_t)n + 15) / 16) * 16 + sizeof(int64_t) * ((size_t)n + 1);
+}
+
+cudaError_t mesh_filter_group(MeshBuffers* const* meshes, const int64_t* nv, const int* zero_isolated, int n,
+                              int iters, void* table, void* h_table, int sms, cudaStream_t st, KernelCounter* kc) {
+  if (iters <= 0 || n <= 0) return cudaSuccess;
+  BilMesh* hm = static_cast<BilMesh*>(h_table);
+  int64_t* hs = reinterpret_cast<int64_t*>(static_cast<uint8_t*>(h_table) + ((sizeof(BilMesh) * (size_t)n + 15) / 16) * 16);
+  hs[0] = 0;
+  for (int i = 0; i < n; i++) {
+    const MeshBuffers& b = *meshes[i];
+    hm[i] = BilMesh{b.N4a, b.N4b, b.rowptr, b.ent, b.N, zero_isolated[i]};
+    hs[i + 1] = hs[i] + nv[i];
+  }
+  const int64_t total = hs[n];
+  cudaError_t e = cudaMemcpyAsync(table, h_table, mesh_filter_table_bytes(n), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess || total == 0) return e;
+  const BilMesh* dm = static_cast<const BilMesh*>(table);
+  const int64_t* ds = reinterpret_cast<const int64_t*>(static_cast<const uint8_t*>(table) +
+                                                       ((sizeof(BilMesh) * (size_t)n + 15) / 16) * 16);
+  for (int it = 0; it < iters; it++) {
+    const float sn = it < 2 ? 1e10f : 0.2f;  // GMorpho.cu:6959-6969
+    GM_LAUNCH(kc, "k_bilateral", st,
+              k_bilateral_group<<<gs_blocks(total, 256, sms), 256, 0, st>>>(dm, ds, n, it & 1, it == iters - 1,
+                                                                            sn * sn));
   }
   return cudaGetLastError();
 }

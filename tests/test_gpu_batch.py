@@ -1,7 +1,8 @@
 """Batched closing + meshing of uneven grids: every instance must equal a
 separate gm_close + gm_mesh of it, bit for bit (closing bytes, triangle
-indices, vertices), with the lane count forced and autotuned, and on the
-replay of the captured CUDA graph."""
+indices, vertices, filtered normals — the batch filters all its meshes in
+one launch per iteration), with the lane count forced and autotuned, and on
+the replay of the captured CUDA graph."""
 import numpy as np
 import pytest
 
@@ -31,8 +32,8 @@ def test_batch_equals_separate_calls(gm_ctx, lanes):
     for rep in range(2):  # the second pass replays the captured graph
         meshes = gm_ctx.batch_close_mesh(items, bilateral_iters=2, lanes=lanes)
         torch.cuda.synchronize()
-        got = [(items[i][4].cpu().numpy(), meshes[i][0].cpu().numpy(), meshes[i][2].cpu().numpy())
-               for i in range(len(items))]
+        got = [(items[i][4].cpu().numpy(), meshes[i][0].cpu().numpy(), meshes[i][2].cpu().numpy(),
+                meshes[i][1].cpu().numpy()) for i in range(len(items))]
         for i, it in enumerate(inst):
             ref = gm_ctx.close(descs[i], it["X"], None, it["radius"])
             V, N, T = gm_ctx.mesh(descs[i], ref, 2)
@@ -40,6 +41,7 @@ def test_batch_equals_separate_calls(gm_ctx, lanes):
             assert np.array_equal(got[i][0], ref.cpu().numpy())
             assert np.array_equal(got[i][2], T.cpu().numpy())
             assert np.array_equal(got[i][1], V.cpu().numpy())
+            assert np.array_equal(got[i][3], N.cpu().numpy(), equal_nan=True)
     if lanes == 0:
         assert gm_ctx.batch_lanes in (1, 2, 4, 8, 16)
 
@@ -79,14 +81,15 @@ def test_batch_occupied_extent(gm_ctx, mode, se):
         Rd = torch.as_tensor(R).cuda() if R is not None else None
         descs.append(d)
         items.append((d, Xd, Rd, r, torch.empty_like(Xd)))
-    meshes = gm_ctx.batch_close_mesh(items, mode=mode, se=se, bilateral_iters=2, lanes=2)
+    meshes = gm_ctx.batch_close_mesh(items, mode=mode, se=se, bilateral_iters=3, lanes=2)
     torch.cuda.synchronize()
-    got = [(items[i][4].cpu().numpy(), meshes[i][0].cpu().numpy(), meshes[i][2].cpu().numpy())
-           for i in range(len(items))]
+    got = [(items[i][4].cpu().numpy(), meshes[i][0].cpu().numpy(), meshes[i][2].cpu().numpy(),
+            meshes[i][1].cpu().numpy()) for i in range(len(items))]
     for i, (d, Xd, Rd, r, _) in enumerate(items):
         ref = gm_ctx.close(d, Xd, Rd, r, mode, se)
-        V, N, T = gm_ctx.mesh(d, ref, 2)
+        V, N, T = gm_ctx.mesh(d, ref, 3)
         torch.cuda.synchronize()
         assert np.array_equal(got[i][0], ref.cpu().numpy())
         assert np.array_equal(got[i][2], T.cpu().numpy())
         assert np.array_equal(got[i][1], V.cpu().numpy())
+        assert np.array_equal(got[i][3], N.cpu().numpy(), equal_nan=True)
