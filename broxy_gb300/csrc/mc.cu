@@ -878,10 +878,12 @@ __device__ __forceinline__ float dist2(float3 a, float3 b) {
 
 // Per corner (vertex a of triangle t): the other two vertices b, c in the
 // reference's order and the iteration-invariant position terms
-// |pa - pb|^2 / sigma_p^2 (GMorpho.cu:6561-6569).
+// |pa - pb|^2 / sigma_p^2 (GMorpho.cu:6561-6569).  sigma_p is 1
+// (GMorpho.cu:6959-6969), so the term is the squared distance itself (an
+// IEEE division by 1 is exact).
 __global__ void k_adj_prep(const float* __restrict__ V, const uint32_t* __restrict__ T,
                            const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
-                           float sp2, uint4* __restrict__ ent) {
+                           uint4* __restrict__ ent) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
     const float3 pa = ld3(V, (uint32_t)v);
     for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
@@ -889,8 +891,7 @@ __global__ void k_adj_prep(const float* __restrict__ V, const uint32_t* __restri
       const uint32_t t = corner / 3, role = corner - 3 * t;
       const uint32_t ib = T[3 * (size_t)t + (role == 0 ? 1 : 0)];
       const uint32_t ic = T[3 * (size_t)t + (role == 2 ? 1 : 2)];
-      ent[i] = make_uint4(ib, ic, __float_as_uint(__fdiv_rn(dist2(pa, ld3(V, ib)), sp2)),
-                          __float_as_uint(__fdiv_rn(dist2(pa, ld3(V, ic)), sp2)));
+      ent[i] = make_uint4(ib, ic, __float_as_uint(dist2(pa, ld3(V, ib))), __float_as_uint(dist2(pa, ld3(V, ic))));
     }
   }
 }
@@ -1192,7 +1193,7 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
                                                                       iters == 0 ? b.N : nullptr));
   if (iters > 0) {
     GM_LAUNCH(kc, "k_adj_prep", st,
-              k_adj_prep<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, 1.f, b.ent));
+              k_adj_prep<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, b.ent));
   }
   if (a.defer_filter) return cudaGetLastError();
   float4* nin = b.N4a;

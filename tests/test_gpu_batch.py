@@ -93,3 +93,25 @@ def test_batch_occupied_extent(gm_ctx, mode, se):
         assert np.array_equal(got[i][2], T.cpu().numpy())
         assert np.array_equal(got[i][1], V.cpu().numpy())
         assert np.array_equal(got[i][3], N.cpu().numpy(), equal_nan=True)
+
+
+def test_batch_normals_of_large_meshes(gm_ctx):
+    """Ten larger grids (over half a million vertices in all) filtered
+    together, one launch per iteration: every mesh's normals equal its own
+    gm_mesh filtering, bit for bit."""
+    import torch
+    inst = synth.batch_instances(seed=4200, count=10, lo=200, hi=300, device="cuda")
+    items = []
+    for it in inst:
+        d = api.make_desc(it["res"], it["data_res"], cell_size=1.0 / it["res"])
+        items.append((d, it["X"].contiguous(), None, it["radius"], torch.empty_like(it["X"])))
+    meshes = gm_ctx.batch_close_mesh(items, bilateral_iters=5, lanes=3)
+    torch.cuda.synchronize()
+    got = [(m[0].cpu().numpy(), m[1].cpu().numpy(), m[2].cpu().numpy()) for m in meshes]
+    assert sum(len(g[0]) for g in got) > 3 * 192 * 1024
+    for (d, X, R, r, out), (Vb, Nb, Tb) in zip(items, got):
+        V, N, T = gm_ctx.mesh(d, out, 5)
+        torch.cuda.synchronize()
+        assert np.array_equal(Vb, V.cpu().numpy())
+        assert np.array_equal(Tb, T.cpu().numpy())
+        assert np.array_equal(Nb, N.cpu().numpy(), equal_nan=True)
