@@ -1451,6 +1451,79 @@ __global__ void __launch_bounds__(256) k_ero_select16(const uint8_t* __restrict_
 
 static dim3 grid16(Dims g) { return dim3((g.x / 16 + 31) / 32, (g.y + 7) / 8, g.z); }
 
+// GM_REF erosion select in two steps, so that the centre erosion Ef is
+// computed only where it is read.  k_ero_tag16 writes the base erosion C0
+// into C (final for untagged cells), the refinement tags (0xff per tagged
+// cell) into T and marks the 8^3-cell blocks holding a tagged cell in tmap
+// (zeroed by the caller); once Ef is known on those blocks, k_ero_fix16
+// writes 0xff & ~Ef on the tagged cells.  The bytes equal k_ero_select16's.
+__global__ void __launch_bounds__(256) k_ero_tag16(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
+                                                   const uint8_t* __restrict__ Eb, uint8_t* __restrict__ C,
+                                                   uint8_t* __restrict__ T, uint8_t* __restrict__ tmap, int mdx,
+                                                   int mdy, Dims g, DataRes dr, CBox roi) {
+  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
+  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
+  uint32_t c0[4];
+  base_ero_row(X, D, Eb, x16, y, z, g, dr, c0);
+  const bool iyz = y < dr.v[1] && z < dr.v[2];
+  uint32_t before = 0u, after = 0u;
+  if (x16 > 0) {
+    const int64_t c = cidx(x16 - 1, y, z, g);
+    before = c0_of(X[c], D[c], Eb[c], iyz && x16 - 1 < dr.v[0]);
+  }
+  if (x16 + 16 < g.x) {
+    const int64_t c = cidx(x16 + 16, y, z, g);
+    after = c0_of(X[c], D[c], Eb[c], iyz && x16 + 16 < dr.v[0]);
+  }
+  const bool interior_yz = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
+  uint32_t tag[4] = {0u, 0u, 0u, 0u};
+  if (interior_yz) {
+    uint32_t diff[4] = {0u, 0u, 0u, 0u};
+    const int ny[4] = {y - 1, y + 1, y, y};
+    const int nz[4] = {z, z, z - 1, z + 1};
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      uint32_t cn[4];
+      base_ero_row(X, D, Eb, x16, ny[n], nz[n], g, dr, cn);
+#pragma unroll
+      for (int j = 0; j < 4; j++) diff[j] |= __vcmpne4(c0[j], cn[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const uint32_t l = prev_cells(c0[j], j > 0 ? c0[j - 1] >> 24 : before);
+      const uint32_t r = next_cells(c0[j], j < 3 ? c0[j + 1] & 0xffu : after);
+      tag[j] = (diff[j] | __vcmpne4(c0[j], l) | __vcmpne4(c0[j], r)) & xrange_mask(x16 + 4 * j, 1, g.x - 1);
+    }
+  }
+  const int64_t o = cidx(x16, y, z, g);
+  *reinterpret_cast<uint4*>(C + o) = make_uint4(c0[0], c0[1], c0[2], c0[3]);
+  *reinterpret_cast<uint4*>(T + o) = make_uint4(tag[0], tag[1], tag[2], tag[3]);
+  // cells x16 .. x16 + 7 and x16 + 8 .. x16 + 15 lie in two 8^3 blocks
+  const int64_t mb = idx3(x16 >> 3, y >> 3, z >> 3, mdx, mdy);
+  if (tag[0] | tag[1]) tmap[mb] = 1;
+  if (tag[2] | tag[3]) tmap[mb + 1] = 1;
+}
+
+__global__ void __launch_bounds__(256) k_ero_fix16(const uint8_t* __restrict__ T, const uint8_t* __restrict__ Ef,
+                                                   uint8_t* __restrict__ C, Dims g, CBox roi) {
+  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
+  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
+  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
+  const int64_t o = cidx(x16, y, z, g);
+  const uint4 t = *reinterpret_cast<const uint4*>(T + o);
+  if ((t.x | t.y | t.z | t.w) == 0u) return;
+  const uint4 e = *reinterpret_cast<const uint4*>(Ef + o);
+  uint4 c = *reinterpret_cast<const uint4*>(C + o);
+  c.x = (t.x & ~e.x) | (~t.x & c.x);
+  c.y = (t.y & ~e.y) | (~t.y & c.y);
+  c.z = (t.z & ~e.z) | (~t.z & c.z);
+  c.w = (t.w & ~e.w) | (~t.w & c.w);
+  *reinterpret_cast<uint4*>(C + o) = c;
+}
+
+
+
 
 
 // max clamped radius over the fine radius grid
@@ -1506,9 +1579,9 @@ static CBox cbox_grow(const CBox& b, int g, int axes, const int dims[3]) {
 size_t close_workspace_bytes_box(int rx, int ry, int rz) {
   const size_t Nx = 2 * (size_t)rx, Ny = 2 * (size_t)ry, Nz = 2 * (size_t)rz, V = Nx * Ny * Nz;
   const size_t cells = (size_t)rx * ry * rz;
-  // buf16 x2, buf8, HL1 (rx, Ny, Nz), HL2 (rx, ry, Nz), Df, Eb, Ef, S, D, radius map + alignment slack
-  return 2 * V * 2 + V + (size_t)rx * Ny * Nz * 2 + (size_t)rx * ry * Nz * 2 + 5 * cells + V / 4096 + cells / 512 +
-         16 * 256;
+  // buf16 x2, buf8, HL1, HL2, Df, Eb, Ef, S, D, radius map, D and tag block maps + alignment slack
+  return 2 * V * 2 + V + (size_t)rx * Ny * Nz * 2 + (size_t)rx * ry * Nz * 2 + 5 * cells + V / 4096 + 2 * (cells / 512) +
+         17 * 256;
 }
 
 size_t close_workspace_bytes(int res) { return close_workspace_bytes_box(res, res, res); }
@@ -1541,6 +1614,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   uint8_t* rmap = carve(p, V / 4096);
   const int mdx = rx / 8, mdy = ry / 8, mdz = rz / 8;
   uint8_t* dmap = carve(p, (size_t)mdx * mdy * mdz);
+  uint8_t* tmap = carve(p, (size_t)mdx * mdy * mdz);  // 8^3-cell blocks holding refinement-tagged cells
   const int rmax = a.rmax;
   DataRes dr{{a.data_res[0], a.data_res[1], a.data_res[2]}};
   const bool exact = a.mode == 1;
@@ -1629,6 +1703,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   }
   // ---- contour ----
   GM_LAUNCH(kc, "k_contour", st, k_contour16<<<grid16(g), dim3(32, 8), 0, st>>>(D, S, g, exact ? 1 : 0, R_S));
+  // (S holds the refinement tags after the erosion's x pass in GM_REF)
+  if (a.S_out) cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
   // ---- erosion ----
   {
     const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
@@ -1658,21 +1734,37 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                                               B_ero_x));
     }
     if (K <= 32767) {
-      // ero z needs its outputs on D grown by one cell (the refinement tags
-      // cells next to D), ero y its outputs there and within the z window
-      // (ehalo fine voxels) of it
-      const int gz = (ehalo + 1) / 2 + 1;
-      launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
-                                         kc, "k_pass_ero_y", nullptr, 0,
-                                         NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1 + gz, B_ero_y});
-      launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                         "k_pass_ero_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1, R_Ef});
-      if (!exact) {
+      const int gz = (ehalo + 1) / 2 + 1;  // cells covering the z window (ehalo fine voxels) of a z pass
+      if (exact) {
+        // ero z needs its outputs on D grown by one cell, ero y its outputs
+        // there and within the z window of it
+        launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
+                                           kc, "k_pass_ero_y", nullptr, 0,
+                                           NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1 + gz, B_ero_y});
+        launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
+                                           "k_pass_ero_z", nullptr, 0,
+                                           NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1, R_Ef});
+      } else {
         // erob z needs its flags on D only, erob y within its z window
         launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_y", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 1, 0, 0, gz, B_erob_y});
+                                           "k_pass_erob_y", nullptr, 0,
+                                           NeedMap{dmap, mdx, mdy, mdz, 0, 1, 0, 0, gz, B_erob_y});
         launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_z", nullptr, 0, NeedMap{dmap, mdx, mdy, mdz, 0, 0, 0, 0, 0, R_Eb});
+                                           "k_pass_erob_z", nullptr, 0,
+                                           NeedMap{dmap, mdx, mdy, mdz, 0, 0, 0, 0, 0, R_Eb});
+        // base erosion and refinement tags (the contour S is read by nobody
+        // any more: it holds the tags), then the centre erosion only on the
+        // blocks of tagged cells (ero y within the z window of them)
+        cudaMemsetAsync(tmap, 0, (size_t)mdx * mdy * mdz, st);
+        GM_LAUNCH(kc, "k_ero_tag", st,
+                  k_ero_tag16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, a.C_out, S, tmap, mdx, mdy, g, dr, F));
+        launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
+                                           kc, "k_pass_ero_y", nullptr, 0,
+                                           NeedMap{tmap, mdx, mdy, mdz, 1, 1, 0, 0, gz, B_ero_y});
+        launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
+                                           "k_pass_ero_z", nullptr, 0,
+                                           NeedMap{tmap, mdx, mdy, mdz, 1, 1, 0, 0, 0, R_Ef});
+        GM_LAUNCH(kc, "k_ero_fix", st, k_ero_fix16<<<grid16(g), dim3(32, 8), 0, st>>>(S, Ef, a.C_out, g, F));
       }
     } else {
       const int span = kTileOut + 2 * ehalo;
@@ -1692,12 +1784,9 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                                 HL2, Eb, rx, ry, rz, ehalo, K));
       }
     }
-    GM_LAUNCH(kc, "k_ero_select", st,
-              k_ero_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0,
-                                                                          F));
-  }
-  if (a.S_out) {
-    cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
+    if (exact || K > 32767)
+      GM_LAUNCH(kc, "k_ero_select", st,
+                k_ero_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0, F));
   }
   return cudaGetLastError();
 }
