@@ -10,34 +10,47 @@
 
 namespace gm {
 
-__global__ void k_scale_brush(int8_t* __restrict__ R, int n, float bx, float by, float bz, float cell, float px,
-                              float py, float pz, float v, float h, float target, int mode, int x0, int y0, int z0,
-                              int x1, int y1, int z1) {
+// One warp per fine row (y, z) of the brush box, lanes along x (coalesced
+// bytes).  A row is skipped when its squared distance with ux = 0 already
+// fails the test: rounding is monotone and every term is non-negative, so
+// fma(uz, uz, fma(uy, uy, ux*ux)) >= fma(uz, uz, fma(uy, uy, 0)) for every
+// x, and the per-voxel test below could not pass either.
+__global__ void __launch_bounds__(256) k_scale_brush(int8_t* __restrict__ R, int n, float bx, float by, float bz,
+                                                     float cell, float px, float py, float pz, float v, float h,
+                                                     float target, int mode, int x0, int y0, int z0, int x1, int y1,
+                                                     int z1) {
   const int wx = x1 - x0 + 1, wy = y1 - y0 + 1, wz = z1 - z0 + 1;
-  const int64_t total = (int64_t)wx * wy * wz;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int x = x0 + (int)(i % wx), y = y0 + (int)((i / wx) % wy), z = z0 + (int)(i / ((int64_t)wx * wy));
-    const float ux = __fsub_rn(__fmaf_rn(cell, (float)x, bx), px);
+  const int lane = threadIdx.x & 31;
+  const int64_t rows = (int64_t)wy * wz;
+  const float reach = __fadd_rn(v, h);
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < rows;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int y = y0 + (int)(r % wy), z = z0 + (int)(r / wy);
     const float uy = __fsub_rn(__fmaf_rn(cell, (float)y, by), py);
     const float uz = __fsub_rn(__fmaf_rn(cell, (float)z, bz), pz);
-    const float d = __fsqrt_rn(__fmaf_rn(uz, uz, __fmaf_rn(uy, uy, __fmul_rn(ux, ux))));
-    if (!(d < __fadd_rn(v, h))) continue;
-    float w;
-    if (d < v) {
-      w = 1.f;
-    } else {
-      const float a = __fdiv_rn(__fsub_rn(d, v), h);
-      const float b = __fsub_rn(1.f, __fmul_rn(a, a));
-      w = __fmul_rn(b, b);
+    if (!(__fsqrt_rn(__fmaf_rn(uz, uz, __fmaf_rn(uy, uy, 0.f))) < reach)) continue;  // warp-uniform
+    const int64_t row = fine_index(0, y, z, n);
+    for (int x = x0 + lane; x < x0 + wx; x += 32) {
+      const float ux = __fsub_rn(__fmaf_rn(cell, (float)x, bx), px);
+      const float d = __fsqrt_rn(__fmaf_rn(uz, uz, __fmaf_rn(uy, uy, __fmul_rn(ux, ux))));
+      if (!(d < reach)) continue;
+      float w;
+      if (d < v) {
+        w = 1.f;
+      } else {
+        const float a = __fdiv_rn(__fsub_rn(d, v), h);
+        const float b = __fsub_rn(1.f, __fmul_rn(a, a));
+        w = __fmul_rn(b, b);
+      }
+      const int64_t idx = row + x;
+      const float prev = (float)R[idx];
+      float dist = __fadd_rn(__fmul_rn(prev, __fsub_rn(1.f, w)), __fmul_rn(w, target));
+      dist = floorf(dist);
+      dist = fmaxf(fminf(dist, 127.f), 0.f);
+      if (mode == 1) R[idx] = (int8_t)floorf(fmaxf(dist, prev));
+      else if (mode == 2) R[idx] = (int8_t)floorf(fminf(dist, prev));
+      else if (mode == 3) R[idx] = (int8_t)dist;
     }
-    const int64_t idx = fine_index(x, y, z, n);
-    const float prev = (float)R[idx];
-    float dist = __fadd_rn(__fmul_rn(prev, __fsub_rn(1.f, w)), __fmul_rn(w, target));
-    dist = floorf(dist);
-    dist = fmaxf(fminf(dist, 127.f), 0.f);
-    if (mode == 1) R[idx] = (int8_t)floorf(fmaxf(dist, prev));
-    else if (mode == 2) R[idx] = (int8_t)floorf(fminf(dist, prev));
-    else if (mode == 3) R[idx] = (int8_t)dist;
   }
 }
 
@@ -61,10 +74,10 @@ cudaError_t launch_scale_brush(int8_t* R, int n, const float* bbox_min, float ce
     if (hi[a] > n - 1) hi[a] = n - 1;
   }
   if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) return cudaSuccess;
-  const int64_t total = (int64_t)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
-  int blocks = (int)((total + 255) / 256);
+  const int64_t rows = (int64_t)(hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+  int64_t blocks = (rows + 7) / 8;  // a warp per row
   if (blocks > 152 * 32) blocks = 152 * 32;
-  GM_LAUNCH(kc, "k_scale_brush", st, k_scale_brush<<<blocks, 256, 0, st>>>(R, n, bbox_min[0], bbox_min[1], bbox_min[2], cell_size, pos[0], pos[1],
+  GM_LAUNCH(kc, "k_scale_brush", st, k_scale_brush<<<(unsigned)blocks, 256, 0, st>>>(R, n, bbox_min[0], bbox_min[1], bbox_min[2], cell_size, pos[0], pos[1],
                                         pos[2], v, h, target, mode, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]));
   return cudaGetLastError();
 }
