@@ -59,6 +59,32 @@ def test_close_uniform_cube(gm_ctx, res, seed, r, mode):
     assert np.array_equal(Cg, Co)
 
 
+@pytest.mark.parametrize("mode", [L.GM_REF, L.GM_EXACT])
+def test_close_large_radius(gm_ctx, mode):
+    """Radii of 92 and more: the erosion's saturation 4 (r - 1)^2 no longer
+    fits the packed 16-bit taps, and the wide-value passes run instead."""
+    res = 32
+    X = synth.random_grid(res, 31, density=0.2, blobs=3)
+    D, S, Cg = _run(gm_ctx, res, X, uniform=100, mode=mode)
+    Do, So, Co = _oracle(res, X, None, 100, mode, 0)
+    assert np.array_equal(D, Do)
+    assert np.array_equal(S, So)
+    assert np.array_equal(Cg, Co)
+
+
+@pytest.mark.parametrize("mode", [L.GM_REF, L.GM_EXACT])
+def test_close_large_variable_radius(gm_ctx, mode):
+    res = 32
+    X = synth.random_grid(res, 32, density=0.2, blobs=3)
+    rng = np.random.default_rng(33)
+    scale = rng.integers(60, 111, size=(2 * res) ** 3).astype(np.int8)
+    D, S, Cg = _run(gm_ctx, res, X, scale=scale, mode=mode)
+    Do, So, Co = _oracle(res, X, scale, 0, mode, 0)
+    assert np.array_equal(D, Do)
+    assert np.array_equal(S, So)
+    assert np.array_equal(Cg, Co)
+
+
 @pytest.mark.parametrize("res,seed", [(16, 21), (32, 22), (64, 23)])
 @pytest.mark.parametrize("mode", [L.GM_REF, L.GM_EXACT])
 def test_close_variable_radius(gm_ctx, res, seed, mode):
