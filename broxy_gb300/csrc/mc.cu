@@ -822,17 +822,6 @@ __global__ void k_adj_fill(const uint32_t* __restrict__ T, int64_t nt, const uin
   }
 }
 
-__global__ void k_adj_sort(const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj, int64_t nv) {
-  for (int64_t v = 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t b = rowptr[v], e = rowptr[v + 1];
-    for (uint32_t i = b + 1; i < e; i++) {
-      const uint32_t key = adj[i];
-      uint32_t j = i;
-      while (j > b && adj[j - 1] > key) { adj[j] = adj[j - 1]; j--; }
-      adj[j] = key;
-    }
-  }
-}
 
 __device__ __forceinline__ float3 ld3(const float* p, uint32_t i) {
   return make_float3(p[3 * (size_t)i], p[3 * (size_t)i + 1], p[3 * (size_t)i + 2]);
@@ -843,62 +832,116 @@ __device__ __forceinline__ float3 normalize3(float3 n) {
   return make_float3(__fdiv_rn(n.x, l), __fdiv_rn(n.y, l), __fdiv_rn(n.z, l));
 }
 
-// Area-weighted normals (ComputeMeshNormals, GMorpho.cu:6498-6524) summed per
-// vertex in triangle order, then normalised (GMorpho.cu:6526-6537).
-__global__ void k_vertex_normals(const float* __restrict__ V, const uint32_t* __restrict__ T,
-                                 const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
-                                 int zero_isolated, float4* __restrict__ N4, float* __restrict__ N3) {
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
-    if (zero_isolated && rowptr[v] == rowptr[v + 1]) {
-      N4[v] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
-      continue;
-    }
-    float3 acc = make_float3(0.f, 0.f, 0.f);
-    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
-      const uint32_t t = adj[i] / 3;
-      const float3 p0 = ld3(V, T[3 * (size_t)t]), p1 = ld3(V, T[3 * (size_t)t + 1]), p2 = ld3(V, T[3 * (size_t)t + 2]);
-      const float3 a = make_float3(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
-      const float3 b = make_float3(__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z));
-      const float nx = __fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y));
-      const float ny = __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z));
-      const float nz = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
-      acc = make_float3(__fadd_rn(acc.x, nx), __fadd_rn(acc.y, ny), __fadd_rn(acc.z, nz));
-    }
-    const float3 n = normalize3(acc);
-    N4[v] = make_float4(n.x, n.y, n.z, 0.f);
-    if (N3) { N3[3 * v] = n.x; N3[3 * v + 1] = n.y; N3[3 * v + 2] = n.z; }
-  }
-}
 
 __device__ __forceinline__ float dist2(float3 a, float3 b) {
   const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-// Per corner (vertex a of triangle t): the other two vertices b, c in the
-// reference's order and the iteration-invariant position terms
-// |pa - pb|^2 / sigma_p^2 (GMorpho.cu:6561-6569).  sigma_p is 1
-// (GMorpho.cu:6959-6969), so the term is the squared distance itself (an
-// IEEE division by 1 is exact).
-__global__ void k_adj_prep(const float* __restrict__ V, const uint32_t* __restrict__ T,
-                           const uint32_t* __restrict__ rowptr, const uint32_t* __restrict__ adj, int64_t nv,
-                           uint4* __restrict__ ent) {
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
-    const float3 pa = ld3(V, (uint32_t)v);
-    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
-      const uint32_t corner = adj[i];
-      const uint32_t t = corner / 3, role = corner - 3 * t;
-      const uint32_t ib = T[3 * (size_t)t + (role == 0 ? 1 : 0)];
-      const uint32_t ic = T[3 * (size_t)t + (role == 2 ? 1 : 2)];
-      ent[i] = make_uint4(ib, ic, __float_as_uint(dist2(pa, ld3(V, ib))), __float_as_uint(dist2(pa, ld3(V, ic))));
-    }
-  }
-}
 
 __device__ __forceinline__ float dist2n(float4 a, float4 b) {
   const float dx = __fsub_rn(a.x, b.x), dy = __fsub_rn(a.y, b.y), dz = __fsub_rn(a.z, b.z);
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// The per-vertex steps after the incident-triangle lists are filled, in
+// one kernel: the list sorted into triangle order (in registers, a bitonic
+// network over 8 or 16 slots; vertex 0's row is already in order, longer
+// lists are sorted in place); the area-weighted normal (ComputeMeshNormals,
+// GMorpho.cu:6498-6524) summed in that order and normalised
+// (GMorpho.cu:6526-6537); and, when the normals are filtered, each corner's
+// filter record: the other two vertices b, c in the reference's order and
+// the iteration-invariant position terms |pa - pb|^2 / sigma_p^2
+// (GMorpho.cu:6561-6569) — sigma_p is 1 (GMorpho.cu:6959-6969), so the term
+// is the squared distance itself (an IEEE division by 1 is exact).  Every
+// incident triangle's vertices and positions are loaded once for both.
+template <int M>
+__device__ __forceinline__ void bitonic_sort(uint32_t (&k)[M]) {
+#pragma unroll
+  for (int s = 2; s <= M; s <<= 1)
+#pragma unroll
+    for (int j = s >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (int i = 0; i < M; i++) {
+        const int l = i ^ j;
+        if (l > i) {
+          const uint32_t a = k[i], b = k[l];
+          const bool up = (i & s) == 0;
+          k[i] = up ? min(a, b) : max(a, b);
+          k[l] = up ? max(a, b) : min(a, b);
+        }
+      }
+}
+
+// one incident corner: its triangle's normal term, and its filter record
+__device__ __forceinline__ void adj_corner(const float* __restrict__ V, const uint32_t* __restrict__ T,
+                                           uint32_t corner, const float3& pa, float3& acc, uint4* rec) {
+  const uint32_t t = corner / 3, role = corner - 3 * t;
+  const uint32_t i0 = T[3 * (size_t)t], i1 = T[3 * (size_t)t + 1], i2 = T[3 * (size_t)t + 2];
+  const float3 p0 = ld3(V, i0), p1 = ld3(V, i1), p2 = ld3(V, i2);
+  const float3 a = make_float3(__fsub_rn(p1.x, p0.x), __fsub_rn(p1.y, p0.y), __fsub_rn(p1.z, p0.z));
+  const float3 b = make_float3(__fsub_rn(p2.x, p0.x), __fsub_rn(p2.y, p0.y), __fsub_rn(p2.z, p0.z));
+  const float nx = __fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y));
+  const float ny = __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z));
+  const float nz = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
+  acc = make_float3(__fadd_rn(acc.x, nx), __fadd_rn(acc.y, ny), __fadd_rn(acc.z, nz));
+  if (rec) {
+    // the other two vertices in the reference's order: (1, 2), (0, 2), (0, 1)
+    const uint32_t ib = role == 0 ? i1 : i0, ic = role == 2 ? i1 : i2;
+    const float3 pb = role == 0 ? p1 : p0, pc = role == 2 ? p1 : p2;
+    *rec = make_uint4(ib, ic, __float_as_uint(dist2(pa, pb)), __float_as_uint(dist2(pa, pc)));
+  }
+}
+
+__global__ void k_adj_finish(const float* __restrict__ V, const uint32_t* __restrict__ T,
+                             const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj, int64_t nv,
+                             int zero_isolated, float4* __restrict__ N4, float* __restrict__ N3,
+                             uint4* __restrict__ ent) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t b = rowptr[v], e = rowptr[v + 1], n = e - b;
+    if (zero_isolated && n == 0) {
+      N4[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
+      continue;
+    }
+    const float3 pa = ld3(V, (uint32_t)v);
+    float3 acc = make_float3(0.f, 0.f, 0.f);
+    if (v != 0 && n <= 8) {
+      uint32_t key[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) key[k] = (uint32_t)k < n ? adj[b + k] : 0xffffffffu;
+      bitonic_sort<8>(key);
+#pragma unroll
+      for (int k = 0; k < 8; k++)
+        if ((uint32_t)k < n) {
+          adj[b + k] = key[k];
+          adj_corner(V, T, key[k], pa, acc, ent ? ent + b + k : nullptr);
+        }
+    } else if (v != 0 && n <= 16) {
+      uint32_t key[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) key[k] = (uint32_t)k < n ? adj[b + k] : 0xffffffffu;
+      bitonic_sort<16>(key);
+#pragma unroll
+      for (int k = 0; k < 16; k++)
+        if ((uint32_t)k < n) {
+          adj[b + k] = key[k];
+          adj_corner(V, T, key[k], pa, acc, ent ? ent + b + k : nullptr);
+        }
+    } else {
+      if (v != 0)
+        for (uint32_t i = b + 1; i < e; i++) {  // in place (vertex 0's row is already in order)
+          const uint32_t key = adj[i];
+          uint32_t j = i;
+          while (j > b && adj[j - 1] > key) { adj[j] = adj[j - 1]; j--; }
+          adj[j] = key;
+        }
+      for (uint32_t i = b; i < e; i++) adj_corner(V, T, adj[i], pa, acc, ent ? ent + i : nullptr);
+    }
+    const float3 nn = normalize3(acc);
+    N4[v] = make_float4(nn.x, nn.y, nn.z, 0.f);
+    if (N3) { N3[3 * v] = nn.x; N3[3 * v + 1] = nn.y; N3[3 * v + 2] = nn.z; }
+  }
 }
 
 // One bilateral normal iteration (BilateralMeshFiltering{,Normalize},
@@ -1185,16 +1228,12 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   cudaMemsetAsync(b.cursor, 0, sizeof(uint32_t) * (size_t)(nv + 1), st);
   GM_LAUNCH(kc, "k_adj_fill", st, k_adj_fill<<<gs_blocks(3 * nt, 256, sms), 256, 0, st>>>(b.T, nt, b.rowptr, b.cursor, b.adj));
   GM_LAUNCH(kc, "k_row0_fill", st, k_row0_fill<<<nchunks0, 256, 0, st>>>(b.T, 3 * nt, offs0, b.rowptr, b.adj));
-  GM_LAUNCH(kc, "k_adj_sort", st, k_adj_sort<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.rowptr, b.adj, nv));
   const int iters = a.bilateral_iters;
   const int zi = a.zero_isolated;
-  GM_LAUNCH(kc, "k_vertex_normals", st,
-            k_vertex_normals<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, zi, b.N4a,
-                                                                      iters == 0 ? b.N : nullptr));
-  if (iters > 0) {
-    GM_LAUNCH(kc, "k_adj_prep", st,
-              k_adj_prep<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, b.ent));
-  }
+  GM_LAUNCH(kc, "k_adj_finish", st,
+            k_adj_finish<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, zi, b.N4a,
+                                                                  iters == 0 ? b.N : nullptr,
+                                                                  iters > 0 ? b.ent : nullptr));
   if (a.defer_filter) return cudaGetLastError();
   float4* nin = b.N4a;
   float4* nout = b.N4b;
