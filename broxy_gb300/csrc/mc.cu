@@ -893,7 +893,7 @@ __device__ __forceinline__ void adj_corner(const float* __restrict__ V, const ui
   }
 }
 
-__global__ void k_adj_finish(const float* __restrict__ V, const uint32_t* __restrict__ T,
+__global__ void __launch_bounds__(256, 3) k_adj_finish(const float* __restrict__ V, const uint32_t* __restrict__ T,
                              const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj, int64_t nv,
                              int zero_isolated, float4* __restrict__ N4, float* __restrict__ N3,
                              uint4* __restrict__ ent) {
