@@ -38,10 +38,10 @@ def _edits(res, n=12, seed=7):
     return out
 
 
-def _run(slots, edits, res=128):
+def _run(slots, edits, res=128, mode=L.GM_REF):
     import torch
     desc, X, R = _setup(res)
-    srv = api.Server(desc, X, R, slots=slots, max_crop_res=96, rmax=8, mode=L.GM_REF)
+    srv = api.Server(desc, X, R, slots=slots, max_crop_res=96, rmax=8, mode=mode)
     results = []
     for c, scale, support, mode in edits:
         srv.submit(c, scale, support, 0.0, mode)
@@ -60,6 +60,19 @@ def test_local_reclosing_equals_full_closing(gm_ctx):
     crops = {r["crop_res"] for r in results}
     assert len(crops) >= 2 and any(c & (c - 1) for c in crops)  # several sizes, not only powers of two
     full = gm_ctx.close(desc, X, R, 0, L.GM_REF, L.GM_SE_SPHERE)
+    torch.cuda.synchronize()
+    assert torch.equal(C, full)
+    srv.destroy()
+
+
+def test_local_reclosing_exact_mode(gm_ctx):
+    """The pure ball closing (GM_EXACT) served the same way: its dilation is
+    the threshold of the resident distance field too."""
+    import torch
+    edits = _edits(128, n=8, seed=17)
+    desc, X, R, C, results, srv = _run(2, edits, mode=L.GM_EXACT)
+    assert all(r["status"] == L.GM_OK for r in results)
+    full = gm_ctx.close(desc, X, R, 0, L.GM_EXACT, L.GM_SE_SPHERE)
     torch.cuda.synchronize()
     assert torch.equal(C, full)
     srv.destroy()
