@@ -110,6 +110,11 @@ struct gm_ctx {
   // host-buffer updates: a copy stream and its events
   cudaStream_t copy_st = nullptr;
   cudaEvent_t ev_copy = nullptr, ev_geom = nullptr;
+  // the radius field's upload in z slabs: one event per slab copied and per
+  // slab bound read back, the bounds in pinned memory
+  static constexpr int kSlabs = 4;
+  cudaEvent_t ev_slab[kSlabs] = {}, ev_max[kSlabs] = {};
+  int* h_slab = nullptr;
   // last mesh
   gm::MeshBuffers mesh;
   int64_t nv = 0, nt = 0;
@@ -215,6 +220,11 @@ gm_status gm_ctx_destroy(gm_ctx* ctx) {
   if (ctx->copy_st) cudaStreamDestroy(ctx->copy_st);
   if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
   if (ctx->ev_geom) cudaEventDestroy(ctx->ev_geom);
+  for (int k = 0; k < gm_ctx::kSlabs; k++) {
+    if (ctx->ev_slab[k]) cudaEventDestroy(ctx->ev_slab[k]);
+    if (ctx->ev_max[k]) cudaEventDestroy(ctx->ev_max[k]);
+  }
+  if (ctx->h_slab) cudaFreeHost(ctx->h_slab);
   ctx->mesh.release();
   gm::batch_release(ctx->batch);
   ctx->kc.release();
@@ -348,12 +358,15 @@ gm_status gm_pyramid_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t*
 
 static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
                             int32_t uniform_radius, int mode, int se, uint8_t* d_closing, uint8_t* d_dilation,
-                            uint8_t* d_contour, cudaStream_t st, bool xpass_done = false) {
+                            uint8_t* d_contour, cudaStream_t st, bool xpass_done = false, bool ypass_done = false,
+                            int rmax_known = 0) {
   gm_status s;
   const int res = desc->res;
   const int64_t fine = (int64_t)8 * res * res * res;
   int rmax;
-  if (d_scale) {
+  if (d_scale && rmax_known > 0) {
+    rmax = rmax_known;  // ctx->rmap and the bound built by the caller (the slab upload of gm_update)
+  } else if (d_scale) {
     // the radius bound and the per-tile radius map in one pass over the field
     if ((s = ensure(ctx, (void**)&ctx->rmap, ctx->rmap_bytes, (size_t)fine / 4096 + 16, "radius map")) != GM_OK)
       return s;
@@ -385,6 +398,7 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   a.num_sms = ctx->num_sms;
   a.rmap_in = d_scale ? ctx->rmap : nullptr;
   a.xpass_done = xpass_done;
+  a.ypass_done = ypass_done;
   GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close");
   return GM_OK;
 }
@@ -631,6 +645,24 @@ static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_
   if ((s = ensure(ctx, (void**)&ctx->d_X, ctx->X_bytes, cells, "input grid")) != GM_OK) return s;
   if ((s = ensure(ctx, (void**)&ctx->d_C, ctx->C_bytes, cells, "closing grid")) != GM_OK) return s;
   if (h_scale && (s = ensure(ctx, (void**)&ctx->d_R, ctx->R_bytes, 8 * cells, "scale grid")) != GM_OK) return s;
+  // uniform radius in fine voxels: floor(global_scale / (cell_size / 2))
+  // (GMorpho/ScaleField.cu:143-146 with cell_size_sf = cell_size / 2)
+  const float gate = std::floor(2.f * global_scale / desc->cell_size);
+  const int uniform = (int)std::floor(global_scale / (0.5f * desc->cell_size));
+  const bool morph = gate > 1.f;
+  // The radius field arrives in z slabs (sphere closings): each slab's
+  // radius map, and the dilation's y pass over a slab once the bounds of the
+  // slabs within 128 fine voxels of it are known, run while later slabs are
+  // still being copied.
+  const int slab_cells = res / gm_ctx::kSlabs;
+  const bool slabs = h_scale && morph && !asym && slab_cells % 8 == 0;
+  if (slabs && !ctx->h_slab) {
+    GM_CHECK_CUDA(ctx, cudaMallocHost(&ctx->h_slab, gm_ctx::kSlabs * sizeof(int)), "slab bounds");
+    for (int k = 0; k < gm_ctx::kSlabs; k++) {
+      GM_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_slab[k], cudaEventDisableTiming), "slab event");
+      GM_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_max[k], cudaEventDisableTiming), "slab event");
+    }
+  }
   // the radius field's upload waits only for the work already on the stream
   // (earlier uses of the buffer), then runs beside the grid's upload and x pass
   // (the grid is issued first: copies of one direction are served in order)
@@ -638,15 +670,20 @@ static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_
   GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_X, h_input, cells, cudaMemcpyHostToDevice, st), "gm_update H2D");
   if (h_scale) {
     GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_st, ctx->ev_copy, 0), "gm_update");
-    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_R, h_scale, 8 * cells, cudaMemcpyHostToDevice, ctx->copy_st),
-                  "gm_update H2D");
+    if (slabs) {
+      const size_t slab_bytes = 8 * cells / gm_ctx::kSlabs;
+      for (int k = 0; k < gm_ctx::kSlabs; k++) {
+        GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_R + k * slab_bytes, h_scale + k * slab_bytes, slab_bytes,
+                                           cudaMemcpyHostToDevice, ctx->copy_st),
+                      "gm_update H2D");
+        GM_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev_slab[k], ctx->copy_st), "gm_update");
+      }
+    } else {
+      GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_R, h_scale, 8 * cells, cudaMemcpyHostToDevice, ctx->copy_st),
+                    "gm_update H2D");
+    }
     GM_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev_copy, ctx->copy_st), "gm_update");
   }
-  // uniform radius in fine voxels: floor(global_scale / (cell_size / 2))
-  // (GMorpho/ScaleField.cu:143-146 with cell_size_sf = cell_size / 2)
-  const float gate = std::floor(2.f * global_scale / desc->cell_size);
-  const int uniform = (int)std::floor(global_scale / (0.5f * desc->cell_size));
-  const bool morph = gate > 1.f;
   bool xpass = false;
   if (morph) {
     if ((s = ensure(ctx, (void**)&ctx->ws, ctx->ws_bytes, gm::close_workspace_bytes(res), "closing workspace")) !=
@@ -660,13 +697,50 @@ static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_
     xpass = true;
   }
   const int8_t* d_scale = nullptr;
+  int rmax_known = 0;
+  if (slabs) {
+    const int N = 2 * res, mb = N / 16;
+    const int slab_fine = 2 * slab_cells;
+    const size_t slab_bytes = (size_t)N * N * slab_fine;
+    const size_t slab_blocks = (size_t)mb * mb * (slab_fine / 16);
+    const int reach = (128 + slab_fine - 1) / slab_fine;  // slabs within 128 fine voxels
+    if ((s = ensure(ctx, (void**)&ctx->rmap, ctx->rmap_bytes, 8 * cells / 4096 + 16, "radius map")) != GM_OK) return s;
+    gm::CloseArgs a;
+    a.res = res;
+    a.X = ctx->d_X;
+    a.workspace = ctx->ws;
+    a.se = 0;
+    a.rmap_in = ctx->rmap;
+    int next = 0;  // next slab whose y pass is due
+    for (int k = 0; k < gm_ctx::kSlabs; k++) {
+      GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_slab[k], 0), "gm_update");
+      GM_CHECK_CUDA(ctx, gm::launch_radius_map_dense(ctx->d_R + k * slab_bytes, N, N, slab_fine,
+                                                     ctx->rmap + k * slab_blocks, ctx->d_int + k, st, &ctx->kc),
+                    "radius bound");
+      GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->h_slab + k, ctx->d_int + k, sizeof(int), cudaMemcpyDeviceToHost, st),
+                    "radius bound");
+      GM_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev_max[k], st), "radius bound");
+      // y passes whose neighbouring bounds are all known now
+      const int upto = k == gm_ctx::kSlabs - 1 ? gm_ctx::kSlabs : k + 1 - reach;
+      if (next < upto) GM_CHECK_CUDA(ctx, cudaEventSynchronize(ctx->ev_max[k]), "radius bound");
+      for (; next < upto; next++) {
+        int rb = 2;
+        for (int j = std::max(0, next - reach); j <= std::min(gm_ctx::kSlabs - 1, next + reach); j++)
+          rb = std::max(rb, ctx->h_slab[j]);
+        GM_CHECK_CUDA(ctx, gm::launch_close_ypass(a, next * slab_cells, (next + 1) * slab_cells, rb, st, &ctx->kc),
+                      "gm_update y pass");
+      }
+    }
+    for (int k = 0; k < gm_ctx::kSlabs; k++) rmax_known = std::max(rmax_known, ctx->h_slab[k]);
+    rmax_known = std::max(rmax_known, 2);
+  }
   if (h_scale) {
     GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_copy, 0), "gm_update");
     d_scale = ctx->d_R;
   }
   if (morph) {
     s = close_impl(ctx, desc, ctx->d_X, d_scale, uniform, mode, asym ? GM_SE_CUBE : GM_SE_SPHERE, ctx->d_C, nullptr,
-                   nullptr, st, xpass);
+                   nullptr, st, xpass, slabs, rmax_known);
     if (s != GM_OK) return s;
   } else {
     GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_C, ctx->d_X, cells, cudaMemcpyDeviceToDevice, st), "gm_update copy");

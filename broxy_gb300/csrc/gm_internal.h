@@ -54,6 +54,7 @@ struct CloseArgs {
   int64_t r_sy = 0, r_sz = 0;  // its y / z strides in bytes when it is a view into a larger field (0: dense)
   const uint8_t* rmap_in = nullptr;  // its 16^3-block radius map when already built (launch_radius_map_dense)
   bool xpass_done = false;  // the dilation's x pass already ran (launch_close_xpass) into the workspace
+  bool ypass_done = false;  // and its y pass (launch_close_ypass over slabs covering the grid; sphere only)
   // Cells [roi_lo, roi_hi) where the caller needs the closing (roi_hi[0] == 0:
   // everywhere).  Work that cannot reach them is skipped, and the closing and
   // the optional D / S outputs hold no meaningful values outside them.
@@ -82,6 +83,15 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
 // saturation of the largest radius, so that it can run before the radius
 // field is on the device; launch_close then skips it (xpass_done).
 cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounter* kc);
+// The sphere dilation's y pass on the cells z0 <= z < z1 alone, after the x
+// pass, with a radius bound r_bound for that part only: the largest clamped
+// radius within 128 fine voxels (along z) of it.  Its values are read only
+// by outputs within r + 1 <= 128 fine voxels, whose thresholds (r + 1)^2 the
+// part's saturation (r_bound + 1)^2 covers; the tile windows come from
+// a.rmap_in, which must hold that part's blocks.  Slabs covering the grid
+// make the y pass of launch_close (ypass_done), so that it can run while
+// the radius field is still arriving.
+cudaError_t launch_close_ypass(const CloseArgs& a, int z0, int z1, int r_bound, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
 // The squared lattice distance field of a cubic grid: per fine voxel p (u16,
 // x-fastest, (2 res)^3), the smallest squared distance from lattice point p

@@ -796,6 +796,10 @@ struct NeedMap {
   int x_shift, t_shift;
   int gx, ga, gt;
   CBox roi;             // tiles whose own cells miss it are skipped as well
+  // launch over third-axis block rows third0 .. third0 + third_n - 1 only
+  // (third_n == 0: all); a skipped tile writes saturation values, so a part of
+  // a pass that must leave the rest of its output alone is launched this way
+  int third0 = 0, third_n = 0;
 };
 
 __device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int nout) {
@@ -803,7 +807,8 @@ __device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int no
   const int cx0 = x0 >> nm.x_shift, cx1 = (x0 + kDpxCols - 1) >> nm.x_shift;
   const int oa = o0, ob = min(o0 + kDpxOut, nout) - 1;
   const int ca0 = sub ? oa : oa >> 1, ca1 = sub ? ob : ob >> 1;
-  const int ct0 = (2 * (int)blockIdx.z) >> nm.t_shift, ct1 = (2 * (int)blockIdx.z + 1) >> nm.t_shift;
+  const int bz = (int)blockIdx.z + nm.third0;
+  const int ct0 = (2 * bz) >> nm.t_shift, ct1 = (2 * bz + 1) >> nm.t_shift;
   // (a, t) are (y, z) for the y pass and (z, y) for the z pass
   {
     const int ya = axis == 1 ? ca0 : ct0, yb = axis == 1 ? ca1 : ct1;
@@ -834,13 +839,13 @@ __device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int no
 // and its two third-axis coordinates widened by `rext` (the y pass feeds z
 // outputs up to a halo away).  Block-uniform.
 __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, int nx, int n3, int axis, int nout,
-                           int o0, int rext) {
+                           int o0, int rext, int bz) {
   __shared__ int rt_s;
   if (threadIdx.x == 0) rt_s = 0;
   __syncthreads();
   const int xa = (blockIdx.x * kDpxCols) >> 4, xb = (min(blockIdx.x * kDpxCols + kDpxCols, nx) - 1) >> 4;
   const int aa = o0 >> 4, ab = (min(o0 + kDpxOut, nout) - 1) >> 4;
-  const int ta = max(2 * (int)blockIdx.z - rext, 0) >> 4, tb = min(2 * (int)blockIdx.z + 1 + rext, n3 - 1) >> 4;
+  const int ta = max(2 * bz - rext, 0) >> 4, tb = min(2 * bz + 1 + rext, n3 - 1) >> 4;
   const int cx = xb - xa + 1, ca = ab - aa + 1, ct = tb - ta + 1;
   int m = 0;
   for (int i = threadIdx.x; i < cx * ca * ct; i += blockDim.x) {
@@ -868,7 +873,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   const int na = axis == 1 ? ny : nz;
   const int n3 = axis == 1 ? nz : ny;
   const int nout = sub ? na / 2 : na;
-  const int third = 2 * blockIdx.z + tpar;
+  const int third = 2 * ((int)blockIdx.z + need.third0) + tpar;
   const int64_t sa = axis == 1 ? (int64_t)nx : (int64_t)nx * ny;
   const int64_t s3 = axis == 1 ? (int64_t)nx * ny : (int64_t)nx;
   const int o0 = blockIdx.y * kDpxOut;
@@ -880,7 +885,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   // that reads this tile has r(p) <= rt, so terms >= (rt+1)^2 never decide.
   int halo_e = halo;
   if (rmap != nullptr && step == 1) {
-    const int rt = tile_radius(rmap, nx >> 4, ny >> 4, nx, n3, axis, nout, o0, rext);
+    const int rt = tile_radius(rmap, nx >> 4, ny >> 4, nx, n3, axis, nout, o0, rext, (int)blockIdx.z + need.third0);
     const uint32_t ct = G == KERN_CUBE ? (uint32_t)(rt + 1) : (uint32_t)((rt + 1) * (rt + 1));
     cap = ct < cap ? ct : cap;
     halo_e = rt + 2 < halo ? rt + 2 : halo;
@@ -1102,7 +1107,7 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   const int na = axis == 1 ? ny : nz;
   const int n3 = axis == 1 ? nz : ny;
   const int nout = sub ? na / 2 : na;
-  dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, (n3 + 1) / 2);
+  dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, need.third_n > 0 ? need.third_n : (n3 + 1) / 2);
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
                                                           uniform_r, rx, ry, rmap, rext, need));
@@ -1663,6 +1668,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     if (!a.xpass_done && launch_dil_pass_x(a.X, buf8, rx, ry, rz, dcap, B_dil_x, st, kc) != cudaSuccess)
       return cudaGetLastError();
     uint8_t* dst = exact ? D : Df;
+    if (a.ypass_done && a.se != 0) return cudaErrorInvalidValue;
     if (dil_cap <= 32767) {
       if (a.se == 1) {
         launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
@@ -1670,8 +1676,9 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
         launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
                                            rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
       } else {
-        launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
-                                         ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
+        if (!a.ypass_done)
+          launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
+                                           ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
         launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
                                           rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
       }
@@ -1827,6 +1834,30 @@ cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounte
   // saturation of the largest clamped radius (127): exact distances up to
   // 129, so any radius bound found later is covered
   return launch_dil_pass_x(a.X, buf8, rx, ry, rz, 129, CBox{{0, 0, 0}, {rx, ry, rz}}, st, kc);
+}
+
+cudaError_t launch_close_ypass(const CloseArgs& a, int z0, int z1, int r_bound, cudaStream_t st, KernelCounter* kc) {
+  const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
+  const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
+  const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
+  if (rx % 16 != 0 || ry % 16 != 0 || rz % 16 != 0 || rx <= 0 || ry <= 0 || rz <= 0 || a.se != 0 ||
+      a.rmap_in == nullptr || z0 < 0 || z1 > rz || z0 >= z1)
+    return cudaErrorInvalidValue;
+  const int Nx = 2 * rx, Ny = 2 * ry, Nz = 2 * rz;
+  const size_t V = (size_t)Nx * Ny * Nz;
+  uint8_t* p = a.workspace;
+  uint16_t* buf16a = reinterpret_cast<uint16_t*>(carve(p, V * 2));  // same places as in launch_close
+  carve(p, V * 2);
+  uint8_t* buf8 = carve(p, V);
+  const int rb = clamp_radius(r_bound);
+  const int dil_r = rb + 1, dil_halo = dil_r + 1;
+  const uint32_t dil_cap = (uint32_t)(dil_r * dil_r);
+  const RField RNONE{nullptr, 0, 0};
+  launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx, ry, st,
+                                   kc, "k_pass_dil_y", a.rmap_in, dil_halo,
+                                   NeedMap{nullptr, 0, 0, 0, 1, 1, 0, 0, 0,
+                                           CBox{{0, 0, 0}, {1 << 30, 1 << 30, 1 << 30}}, z0, z1 - z0});
+  return cudaGetLastError();
 }
 
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc) {

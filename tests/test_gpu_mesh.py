@@ -195,6 +195,33 @@ def test_update_to_host_equals_update_and_download(gm_ctx, with_field):
     assert np.array_equal(T2, T)
 
 
+@pytest.mark.parametrize("res", [128, 256])
+def test_update_slab_upload_equals_close_and_mesh(gm_ctx, res):
+    """gm_update takes the radius field in four z slabs and runs the
+    dilation's y pass of a slab with the radius bound of the slabs within 128
+    fine voxels of it: with radii that differ strongly from slab to slab, the
+    mesh equals gm_close + gm_mesh of the same inputs (one bound for all)."""
+    import torch
+    N = 2 * res
+    X = synth.blob_grid(res, 150, count=60, device="cuda").cpu().numpy()
+    rng = np.random.default_rng(151)
+    R = np.empty((N, N, N), np.int8)  # z, y, x
+    for k, top in enumerate([30, 3, 70, 5]):
+        z0, z1 = k * N // 4, (k + 1) * N // 4
+        R[z0:z1] = rng.integers(0, top + 1, size=(z1 - z0, N, N), dtype=np.int8)
+    R = R.reshape(-1)
+    desc = api.make_desc(res, cell_size=1.0 / res)
+    nv, nt = gm_ctx.update(desc, X, R, 4.0 / res)
+    V, Nn, T = gm_ctx.mesh_download(nv, nt)
+    C = gm_ctx.close(desc, torch.as_tensor(X).cuda(), torch.as_tensor(R).cuda(), 0)
+    V2, N2, T2 = gm_ctx.mesh(desc, C, 20)
+    torch.cuda.synchronize()
+    assert nt > 1000
+    assert np.array_equal(T, T2.view(torch.int32).cpu().numpy().view(np.uint32))
+    assert np.array_equal(V, V2.cpu().numpy())
+    assert np.array_equal(Nn, N2.cpu().numpy(), equal_nan=True)
+
+
 def test_update_gate_skips_morphology(gm_ctx):
     # floor(2 * gs / cell) <= 1 leaves the input unchanged (GMorpho.cu:7783)
     res = 16
