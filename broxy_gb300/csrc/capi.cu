@@ -359,7 +359,7 @@ gm_status gm_pyramid_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t*
 static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
                             int32_t uniform_radius, int mode, int se, uint8_t* d_closing, uint8_t* d_dilation,
                             uint8_t* d_contour, cudaStream_t st, bool xpass_done = false, bool ypass_done = false,
-                            int rmax_known = 0) {
+                            int rmax_known = 0, bool zpass_done = false) {
   gm_status s;
   const int res = desc->res;
   const int64_t fine = (int64_t)8 * res * res * res;
@@ -399,6 +399,7 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   a.rmap_in = d_scale ? ctx->rmap : nullptr;
   a.xpass_done = xpass_done;
   a.ypass_done = ypass_done;
+  a.zpass_done = zpass_done;
   GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close");
   return GM_OK;
 }
@@ -698,6 +699,7 @@ static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_
   }
   const int8_t* d_scale = nullptr;
   int rmax_known = 0;
+  bool zpass = false;
   if (slabs) {
     const int N = 2 * res, mb = N / 16;
     const int slab_fine = 2 * slab_cells;
@@ -711,7 +713,11 @@ static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_
     a.workspace = ctx->ws;
     a.se = 0;
     a.rmap_in = ctx->rmap;
-    int next = 0;  // next slab whose y pass is due
+    const bool zslabs = slab_cells % 32 == 0;  // whole z-pass output tiles per slab
+    a.mode = mode;
+    a.R = ctx->d_R;
+    int bound[gm_ctx::kSlabs];
+    int next = 0, znext = 0;  // next slabs whose y / z pass is due
     for (int k = 0; k < gm_ctx::kSlabs; k++) {
       GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_slab[k], 0), "gm_update");
       GM_CHECK_CUDA(ctx, gm::launch_radius_map_dense(ctx->d_R + k * slab_bytes, N, N, slab_fine,
@@ -727,10 +733,18 @@ static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_
         int rb = 2;
         for (int j = std::max(0, next - reach); j <= std::min(gm_ctx::kSlabs - 1, next + reach); j++)
           rb = std::max(rb, ctx->h_slab[j]);
+        bound[next] = rb;
         GM_CHECK_CUDA(ctx, gm::launch_close_ypass(a, next * slab_cells, (next + 1) * slab_cells, rb, st, &ctx->kc),
                       "gm_update y pass");
+        // z passes whose window's y passes are all issued now
+        const int zupto = next == gm_ctx::kSlabs - 1 ? gm_ctx::kSlabs : next + 1 - reach;
+        for (; zslabs && znext < zupto; znext++)
+          GM_CHECK_CUDA(ctx, gm::launch_close_zpass(a, znext * slab_cells, (znext + 1) * slab_cells, bound[znext],
+                                                    st, &ctx->kc),
+                        "gm_update z pass");
       }
     }
+    zpass = zslabs;
     for (int k = 0; k < gm_ctx::kSlabs; k++) rmax_known = std::max(rmax_known, ctx->h_slab[k]);
     rmax_known = std::max(rmax_known, 2);
   }
@@ -740,7 +754,7 @@ static gm_status update_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_
   }
   if (morph) {
     s = close_impl(ctx, desc, ctx->d_X, d_scale, uniform, mode, asym ? GM_SE_CUBE : GM_SE_SPHERE, ctx->d_C, nullptr,
-                   nullptr, st, xpass, slabs, rmax_known);
+                   nullptr, st, xpass, slabs, rmax_known, zpass);
     if (s != GM_OK) return s;
   } else {
     GM_CHECK_CUDA(ctx, cudaMemcpyAsync(ctx->d_C, ctx->d_X, cells, cudaMemcpyDeviceToDevice, st), "gm_update copy");

@@ -46,15 +46,16 @@ int64_t profile_json(KernelCounter& kc, char* buf, int64_t cap);
   } while (0)
 
 struct CloseArgs {
-  int res;            // base resolution of a cubic grid (a multiple of 16)
+  int res = 0;        // base resolution of a cubic grid (a multiple of 16)
   int dims[3] = {0, 0, 0};  // box grid rx, ry, rz (multiples of 16) when dims[0] > 0; res is then unused
-  int data_res[3];    // cells with data (GMorpho/Voxelizer.cu:453-454)
-  const uint8_t* X;   // input packed grid, res^3
-  const int8_t* R;    // fine radius grid (2res)^3, or nullptr for uniform_r
+  int data_res[3] = {0, 0, 0};  // cells with data (GMorpho/Voxelizer.cu:453-454)
+  const uint8_t* X = nullptr;   // input packed grid, res^3
+  const int8_t* R = nullptr;    // fine radius grid (2res)^3, or nullptr for uniform_r
   int64_t r_sy = 0, r_sz = 0;  // its y / z strides in bytes when it is a view into a larger field (0: dense)
   const uint8_t* rmap_in = nullptr;  // its 16^3-block radius map when already built (launch_radius_map_dense)
   bool xpass_done = false;  // the dilation's x pass already ran (launch_close_xpass) into the workspace
   bool ypass_done = false;  // and its y pass (launch_close_ypass over slabs covering the grid; sphere only)
+  bool zpass_done = false;  // and its z pass (launch_close_zpass over slabs covering the grid; sphere only)
   // Cells [roi_lo, roi_hi) where the caller needs the closing (roi_hi[0] == 0:
   // everywhere).  Work that cannot reach them is skipped, and the closing and
   // the optional D / S outputs hold no meaningful values outside them.
@@ -65,15 +66,15 @@ struct CloseArgs {
   // instead of three passes.
   const uint16_t* edt = nullptr;
   int64_t e_sy = 0, e_sz = 0;
-  int uniform_r;      // radius when R == nullptr
-  int rmax;           // upper bound of the clamped radius over the grid
-  int mode;           // 0 = GM_REF, 1 = GM_EXACT
-  int se;             // 0 = sphere dilation, 1 = cube dilation
-  uint8_t* C_out;     // closing, res^3
-  uint8_t* D_out;     // optional dilation, res^3
-  uint8_t* S_out;     // optional dilation contour, res^3
-  uint8_t* workspace; // close_workspace_bytes(res)
-  int num_sms;
+  int uniform_r = 0;            // radius when R == nullptr
+  int rmax = 2;                 // upper bound of the clamped radius over the grid
+  int mode = 0;                 // 0 = GM_REF, 1 = GM_EXACT
+  int se = 0;                   // 0 = sphere dilation, 1 = cube dilation
+  uint8_t* C_out = nullptr;     // closing, res^3
+  uint8_t* D_out = nullptr;     // optional dilation, res^3
+  uint8_t* S_out = nullptr;     // optional dilation contour, res^3
+  uint8_t* workspace = nullptr; // close_workspace_bytes(res)
+  int num_sms = 0;
 };
 
 size_t close_workspace_bytes(int res);
@@ -92,6 +93,13 @@ cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounte
 // make the y pass of launch_close (ypass_done), so that it can run while
 // the radius field is still arriving.
 cudaError_t launch_close_ypass(const CloseArgs& a, int z0, int z1, int r_bound, cudaStream_t st, KernelCounter* kc);
+// Its z pass (threshold and packing into the dilation) on the cells
+// z0 <= z < z1 (multiples of 32: whole output tiles), once the y pass has
+// run on the cells within 128 fine voxels of them and their radii are on
+// the device; r_bound as for launch_close_ypass (every output tile's own
+// radius bound is at most it, so windows and saturation are those of the
+// whole-grid pass).
+cudaError_t launch_close_zpass(const CloseArgs& a, int z0, int z1, int r_bound, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
 // The squared lattice distance field of a cubic grid: per fine voxel p (u16,
 // x-fastest, (2 res)^3), the smallest squared distance from lattice point p

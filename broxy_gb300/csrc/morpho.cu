@@ -796,10 +796,11 @@ struct NeedMap {
   int x_shift, t_shift;
   int gx, ga, gt;
   CBox roi;             // tiles whose own cells miss it are skipped as well
-  // launch over third-axis block rows third0 .. third0 + third_n - 1 only
-  // (third_n == 0: all); a skipped tile writes saturation values, so a part of
-  // a pass that must leave the rest of its output alone is launched this way
-  int third0 = 0, third_n = 0;
+  // launch over third-axis block rows third0 .. third0 + third_n - 1 and
+  // output tiles out0 .. out0 + out_n - 1 only (0: all); a skipped tile
+  // writes saturation values, so a part of a pass that must leave the rest
+  // of its output alone is launched this way
+  int third0 = 0, third_n = 0, out0 = 0, out_n = 0;
 };
 
 __device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int nout) {
@@ -876,7 +877,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   const int third = 2 * ((int)blockIdx.z + need.third0) + tpar;
   const int64_t sa = axis == 1 ? (int64_t)nx : (int64_t)nx * ny;
   const int64_t s3 = axis == 1 ? (int64_t)nx * ny : (int64_t)nx;
-  const int o0 = blockIdx.y * kDpxOut;
+  const int o0 = ((int)blockIdx.y + need.out0) * kDpxOut;
   const int step = sub ? 2 : 1;
   const int lo = (sub ? 2 * o0 + 1 : o0) - halo;
   const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
@@ -1107,7 +1108,8 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   const int na = axis == 1 ? ny : nz;
   const int n3 = axis == 1 ? nz : ny;
   const int nout = sub ? na / 2 : na;
-  dim3 g((nx + kDpxCols - 1) / kDpxCols, (nout + kDpxOut - 1) / kDpxOut, need.third_n > 0 ? need.third_n : (n3 + 1) / 2);
+  dim3 g((nx + kDpxCols - 1) / kDpxCols, need.out_n > 0 ? need.out_n : (nout + kDpxOut - 1) / kDpxOut,
+         need.third_n > 0 ? need.third_n : (n3 + 1) / 2);
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
                                                           uniform_r, rx, ry, rmap, rext, need));
@@ -1597,6 +1599,34 @@ static inline uint8_t* carve(uint8_t*& p, size_t bytes) {
   return r;
 }
 
+// The closing's workspace, carved the same way by every entry point that
+// works in it (launch_close and the parts that run before it).
+struct CloseWs {
+  uint16_t *buf16a, *buf16b, *HL1, *HL2;
+  uint8_t *buf8, *Df, *Eb, *Ef, *S, *D, *rmap, *dmap, *tmap;
+};
+
+static CloseWs close_ws(const CloseArgs& a, int rx, int ry, int rz) {
+  const size_t Nx = 2 * (size_t)rx, Ny = 2 * (size_t)ry, Nz = 2 * (size_t)rz, V = Nx * Ny * Nz;
+  const size_t cells = (size_t)rx * ry * rz, blocks8 = cells / 512;
+  uint8_t* p = a.workspace;
+  CloseWs w;
+  w.buf16a = reinterpret_cast<uint16_t*>(carve(p, V * 2));
+  w.buf16b = reinterpret_cast<uint16_t*>(carve(p, V * 2));
+  w.buf8 = carve(p, V);
+  w.HL1 = reinterpret_cast<uint16_t*>(carve(p, (size_t)rx * Ny * Nz * 2));
+  w.HL2 = reinterpret_cast<uint16_t*>(carve(p, (size_t)rx * ry * Nz * 2));
+  w.Df = carve(p, cells);
+  w.Eb = carve(p, cells);
+  w.Ef = carve(p, cells);
+  w.S = carve(p, cells);
+  w.D = a.D_out != nullptr ? a.D_out : carve(p, cells);
+  w.rmap = carve(p, V / 4096);
+  w.dmap = carve(p, blocks8);
+  w.tmap = carve(p, blocks8);
+  return w;
+}
+
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc) {
   const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
   const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
@@ -1605,21 +1635,21 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const Dims g{rx, ry, rz};
   const int Nx = 2 * rx, Ny = 2 * ry, Nz = 2 * rz;
   const size_t V = (size_t)Nx * Ny * Nz, cells = (size_t)rx * ry * rz;
-  uint8_t* p = a.workspace;
-  uint16_t* buf16a = reinterpret_cast<uint16_t*>(carve(p, V * 2));
-  uint16_t* buf16b = reinterpret_cast<uint16_t*>(carve(p, V * 2));
-  uint8_t* buf8 = carve(p, V);
-  uint16_t* HL1 = reinterpret_cast<uint16_t*>(carve(p, (size_t)rx * Ny * Nz * 2));
-  uint16_t* HL2 = reinterpret_cast<uint16_t*>(carve(p, (size_t)rx * ry * Nz * 2));
-  uint8_t* Df = carve(p, cells);
-  uint8_t* Eb = carve(p, cells);
-  uint8_t* Ef = carve(p, cells);
-  uint8_t* S = carve(p, cells);
-  uint8_t* D = a.D_out != nullptr ? a.D_out : carve(p, cells);
-  uint8_t* rmap = carve(p, V / 4096);
+  const CloseWs w = close_ws(a, rx, ry, rz);
+  uint16_t* buf16a = w.buf16a;
+  uint16_t* buf16b = w.buf16b;
+  uint8_t* buf8 = w.buf8;
+  uint16_t* HL1 = w.HL1;
+  uint16_t* HL2 = w.HL2;
+  uint8_t* Df = w.Df;
+  uint8_t* Eb = w.Eb;
+  uint8_t* Ef = w.Ef;
+  uint8_t* S = w.S;
+  uint8_t* D = w.D;
+  uint8_t* rmap = w.rmap;
   const int mdx = rx / 8, mdy = ry / 8, mdz = rz / 8;
-  uint8_t* dmap = carve(p, (size_t)mdx * mdy * mdz);
-  uint8_t* tmap = carve(p, (size_t)mdx * mdy * mdz);  // 8^3-cell blocks holding refinement-tagged cells
+  uint8_t* dmap = w.dmap;
+  uint8_t* tmap = w.tmap;  // 8^3-cell blocks holding refinement-tagged cells
   const int rmax = a.rmax;
   DataRes dr{{a.data_res[0], a.data_res[1], a.data_res[2]}};
   const bool exact = a.mode == 1;
@@ -1668,7 +1698,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     if (!a.xpass_done && launch_dil_pass_x(a.X, buf8, rx, ry, rz, dcap, B_dil_x, st, kc) != cudaSuccess)
       return cudaGetLastError();
     uint8_t* dst = exact ? D : Df;
-    if (a.ypass_done && a.se != 0) return cudaErrorInvalidValue;
+    if ((a.ypass_done || a.zpass_done) && a.se != 0) return cudaErrorInvalidValue;
     if (dil_cap <= 32767) {
       if (a.se == 1) {
         launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
@@ -1679,8 +1709,10 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
         if (!a.ypass_done)
           launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
                                            ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
-        launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
-                                          rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
+        if (!a.zpass_done)
+          launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF,
+                                            a.uniform_r, rx, ry, st, kc, "k_pass_dil_z", tile_map, 0,
+                                            roi_only(R_Df, 1, 1));
       }
     } else {
       const int span = kTileOut + 2 * dil_halo;
@@ -1826,11 +1858,7 @@ cudaError_t launch_close_xpass(const CloseArgs& a, cudaStream_t st, KernelCounte
   const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
   const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
   if (rx % 16 != 0 || ry % 16 != 0 || rz % 16 != 0 || rx <= 0 || ry <= 0 || rz <= 0) return cudaErrorInvalidValue;
-  const size_t V = (size_t)8 * rx * ry * rz;
-  uint8_t* p = a.workspace;
-  carve(p, V * 2);
-  carve(p, V * 2);
-  uint8_t* buf8 = carve(p, V);  // same place as in launch_close
+  uint8_t* buf8 = close_ws(a, rx, ry, rz).buf8;
   // saturation of the largest clamped radius (127): exact distances up to
   // 129, so any radius bound found later is covered
   return launch_dil_pass_x(a.X, buf8, rx, ry, rz, 129, CBox{{0, 0, 0}, {rx, ry, rz}}, st, kc);
@@ -1844,11 +1872,9 @@ cudaError_t launch_close_ypass(const CloseArgs& a, int z0, int z1, int r_bound, 
       a.rmap_in == nullptr || z0 < 0 || z1 > rz || z0 >= z1)
     return cudaErrorInvalidValue;
   const int Nx = 2 * rx, Ny = 2 * ry, Nz = 2 * rz;
-  const size_t V = (size_t)Nx * Ny * Nz;
-  uint8_t* p = a.workspace;
-  uint16_t* buf16a = reinterpret_cast<uint16_t*>(carve(p, V * 2));  // same places as in launch_close
-  carve(p, V * 2);
-  uint8_t* buf8 = carve(p, V);
+  const CloseWs w = close_ws(a, rx, ry, rz);
+  uint16_t* buf16a = w.buf16a;
+  uint8_t* buf8 = w.buf8;
   const int rb = clamp_radius(r_bound);
   const int dil_r = rb + 1, dil_halo = dil_r + 1;
   const uint32_t dil_cap = (uint32_t)(dil_r * dil_r);
@@ -1857,6 +1883,29 @@ cudaError_t launch_close_ypass(const CloseArgs& a, int z0, int z1, int r_bound, 
                                    kc, "k_pass_dil_y", a.rmap_in, dil_halo,
                                    NeedMap{nullptr, 0, 0, 0, 1, 1, 0, 0, 0,
                                            CBox{{0, 0, 0}, {1 << 30, 1 << 30, 1 << 30}}, z0, z1 - z0});
+  return cudaGetLastError();
+}
+
+cudaError_t launch_close_zpass(const CloseArgs& a, int z0, int z1, int r_bound, cudaStream_t st, KernelCounter* kc) {
+  const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
+  const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
+  const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
+  // whole output tiles (32 cells along z) only
+  if (rx % 16 != 0 || ry % 16 != 0 || rz % 16 != 0 || rx <= 0 || ry <= 0 || rz <= 0 || a.se != 0 ||
+      a.rmap_in == nullptr || a.R == nullptr || z0 < 0 || z1 > rz || z0 >= z1 || z0 % 32 != 0 || z1 % 32 != 0)
+    return cudaErrorInvalidValue;
+  const int Nx = 2 * rx, Ny = 2 * ry, Nz = 2 * rz;
+  const CloseWs w = close_ws(a, rx, ry, rz);
+  uint8_t* dst = a.mode == 1 ? w.D : w.Df;
+  const int rb = clamp_radius(r_bound);
+  const int dil_r = rb + 1, dil_halo = dil_r + 1;
+  const uint32_t dil_cap = (uint32_t)(dil_r * dil_r);
+  const RField RF{a.R, a.r_sy > 0 ? a.r_sy : (int64_t)Nx, a.r_sz > 0 ? a.r_sz : (int64_t)Nx * Ny};
+  launch_dpx<KERN_LAT, uint16_t, 1>(w.buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r, rx,
+                                    ry, st, kc, "k_pass_dil_z", a.rmap_in, 0,
+                                    NeedMap{nullptr, 0, 0, 0, 1, 1, 0, 0, 0,
+                                            CBox{{0, 0, 0}, {1 << 30, 1 << 30, 1 << 30}}, 0, 0, z0 / 32,
+                                            (z1 - z0) / 32});
   return cudaGetLastError();
 }
 

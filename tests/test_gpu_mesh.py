@@ -195,12 +195,13 @@ def test_update_to_host_equals_update_and_download(gm_ctx, with_field):
     assert np.array_equal(T2, T)
 
 
-@pytest.mark.parametrize("res", [128, 256])
-def test_update_slab_upload_equals_close_and_mesh(gm_ctx, res):
+@pytest.mark.parametrize("res,mode", [(128, L.GM_REF), (256, L.GM_REF), (256, L.GM_EXACT)])
+def test_update_slab_upload_equals_close_and_mesh(gm_ctx, res, mode):
     """gm_update takes the radius field in four z slabs and runs the
-    dilation's y pass of a slab with the radius bound of the slabs within 128
-    fine voxels of it: with radii that differ strongly from slab to slab, the
-    mesh equals gm_close + gm_mesh of the same inputs (one bound for all)."""
+    dilation's y and z passes of a slab with the radius bound of the slabs
+    within 128 fine voxels of it: with radii that differ strongly from slab
+    to slab, the mesh equals gm_close + gm_mesh of the same inputs (one bound
+    for all)."""
     import torch
     N = 2 * res
     X = synth.blob_grid(res, 150, count=60, device="cuda").cpu().numpy()
@@ -211,9 +212,9 @@ def test_update_slab_upload_equals_close_and_mesh(gm_ctx, res):
         R[z0:z1] = rng.integers(0, top + 1, size=(z1 - z0, N, N), dtype=np.int8)
     R = R.reshape(-1)
     desc = api.make_desc(res, cell_size=1.0 / res)
-    nv, nt = gm_ctx.update(desc, X, R, 4.0 / res)
+    nv, nt = gm_ctx.update(desc, X, R, 4.0 / res, mode=mode)
     V, Nn, T = gm_ctx.mesh_download(nv, nt)
-    C = gm_ctx.close(desc, torch.as_tensor(X).cuda(), torch.as_tensor(R).cuda(), 0)
+    C = gm_ctx.close(desc, torch.as_tensor(X).cuda(), torch.as_tensor(R).cuda(), 0, mode)
     V2, N2, T2 = gm_ctx.mesh(desc, C, 20)
     torch.cuda.synchronize()
     assert nt > 1000
