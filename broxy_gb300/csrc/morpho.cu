@@ -900,7 +900,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   uint32_t* tile = tileu + tpar * span * 32;
   const bool colok = x < nx && third < n3;
   int finite = 0;
-  constexpr bool kTileMin = G == KERN_CEN2 || G == KERN_LAT2;
+  constexpr bool kTileMin = G == KERN_CEN2 || G == KERN_LAT2 || (G == KERN_LAT && FIN == 1);
   uint32_t vmin = 0xffffffffu;  // smallest loaded value (both lanes)
   for (int s = skip + grp; s < span - skip; s += 4) {
     const int a = lo + s;
@@ -920,10 +920,11 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   // Every tile value is >= tmin, so a tap whose kernel value reaches
   // cap - tmin cannot bring an output below the saturation value cap: the
   // window of this tile ends at the last tap below it (kernels grow with
-  // |delta|).  Erosion passes only: their inputs carry the per-site offset
+  // |delta|).  Erosion passes: their inputs carry the per-site offset
   // K - 4 (r - 1)^2, so tiles whose sites all have small radii need short
-  // windows; dilation tiles next to a surface hold zeros (and use their
-  // radius bound instead).
+  // windows; the final dilation pass: tiles whose inputs are all far from
+  // the input stop early.  (The first dilation pass, whose tiles next to a
+  // surface hold zeros, is faster without it.)
   uint32_t tmin = 0;
   int halo_t = step == 1 ? halo_e : halo;
   if (kTileMin) {
