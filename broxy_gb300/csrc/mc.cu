@@ -959,8 +959,11 @@ __global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __re
     }
     float3 acc = make_float3(0.f, 0.f, 0.f);
     const float4 na = Nin[v];
-    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
-      const uint4 e = ent[i];
+    const uint32_t i0 = rowptr[v], i1 = rowptr[v + 1];
+    uint4 en = i0 < i1 ? ent[i0] : make_uint4(0u, 0u, 0u, 0u);  // the next record, loaded one entry ahead
+    for (uint32_t i = i0; i < i1; i++) {
+      const uint4 e = en;
+      if (i + 1 < i1) en = ent[i + 1];
       const float4 nb = Nin[e.x], nc = Nin[e.y];
       // the reference library is built with -use_fast_math (GMorpho/cuda.prf:47),
       // so its exp and division here are the fast forms
