@@ -34,6 +34,8 @@ namespace gm {
 struct BatchLane {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
+  cudaStream_t em = nullptr;       // mesh emission of the lane's grids (beside its later closings)
+  cudaEvent_t em_done = nullptr;
   uint8_t* ws = nullptr;
   size_t ws_bytes = 0;
   uint8_t *Xc = nullptr, *Cc = nullptr;  // crop buffers (radius fields are read in place)
@@ -44,6 +46,7 @@ struct BatchState {
   std::vector<BatchLane> lanes;
   std::vector<MeshBuffers> meshes;
   std::vector<int64_t> nv, nt;
+  std::vector<cudaEvent_t> ev_count;  // per grid: its mesh counts are on the host
   uint32_t* h_tot = nullptr;  // pinned, 4 per instance
   int h_tot_cap = 0;
   int* d_rmax = nullptr;      // one int per instance
@@ -70,11 +73,14 @@ void batch_release(void* p) {
   for (BatchLane& l : b->lanes) {
     if (l.st) cudaStreamDestroy(l.st);
     if (l.done) cudaEventDestroy(l.done);
+    if (l.em) cudaStreamDestroy(l.em);
+    if (l.em_done) cudaEventDestroy(l.em_done);
     cudaFree(l.ws);
     cudaFree(l.Xc);
     cudaFree(l.Cc);
   }
   for (MeshBuffers& m : b->meshes) m.release();
+  for (cudaEvent_t ev : b->ev_count) cudaEventDestroy(ev);
   if (b->h_tot) cudaFreeHost(b->h_tot);
   if (b->h_rmax) cudaFreeHost(b->h_rmax);
   cudaFree(b->d_rmax);
@@ -119,6 +125,10 @@ static cudaError_t ensure_lanes(BatchState* b, int L) {
     if (e != cudaSuccess) return e;
     e = cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming);
     if (e != cudaSuccess) return e;
+    e = cudaStreamCreateWithFlags(&l.em, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreateWithFlags(&l.em_done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
     b->lanes.push_back(l);
   }
   cudaError_t e = cudaSuccess;
@@ -146,9 +156,12 @@ static std::vector<int> assign(int n, const std::vector<int>& ext, int L) {
 }
 
 // The closing phase: fork from `st`, every lane runs its instances, join.
+// With `ma`, each closing is followed on its lane by the mesh counts of the
+// grid (totals to the pinned b->h_tot) and the grid's event, so that its
+// emission can start while the lane goes on closing other grids.
 static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* it, const int* rmax,
                                     const std::vector<int>& ext, int mode, int se, int L, const std::vector<int>& lane,
-                                    int sms, cudaStream_t st, KernelCounter* kc) {
+                                    int sms, cudaStream_t st, KernelCounter* kc, const MeshArgs* ma = nullptr) {
   cudaError_t e = cudaEventRecord(b->fork, st);
   if (e != cudaSuccess) return e;
   for (int l = 0; l < L; l++)
@@ -181,6 +194,16 @@ static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* i
     a.num_sms = sms;
     if ((e = launch_close(a, ln.st, kc)) != cudaSuccess) return e;
     if (crop && (e = launch_embed(ln.Cc, E, it[i].d_closing, res, ln.st, kc)) != cudaSuccess) return e;
+    if (ma) {
+      if ((e = mesh_count_launch(ma[i], b->meshes[i], ln.st, kc, b->h_tot + 4 * i)) != cudaSuccess) return e;
+      // an external event node when captured: the host waits on it after the replay
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if ((e = cudaStreamIsCapturing(ln.st, &cs)) != cudaSuccess) return e;
+      if ((e = cudaEventRecordWithFlags(b->ev_count[i], ln.st,
+                                        cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                            : cudaEventRecordDefault)) != cudaSuccess)
+        return e;
+    }
   }
   for (int l = 0; l < L; l++) {
     if ((e = cudaEventRecord(b->lanes[l].done, b->lanes[l].st)) != cudaSuccess) return e;
@@ -315,8 +338,52 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     b->tuned[tune_sig] = L;
   }
   const std::vector<int> lane = assign(n, ext, L);
-  // closing phase: replay the captured graph when the batch is unchanged
-  const uint64_t sig = signature(n, it, ext, mode, se, L);
+  // mesh arguments, count buffers, pinned totals and per-grid events, all
+  // allocated before the closing phase (which may be captured)
+  std::vector<MeshArgs> ma;
+  if (meshes) {
+    if ((int)b->meshes.size() < n) b->meshes.resize(n);
+    b->nv.assign(n, 0);
+    b->nt.assign(n, 0);
+    if (b->h_tot_cap < n) {
+      if (b->h_tot) cudaFreeHost(b->h_tot);
+      b->h_tot = nullptr;
+      if ((e = cudaMallocHost(&b->h_tot, sizeof(uint32_t) * 4 * n)) != cudaSuccess) return e;
+      b->h_tot_cap = n;
+    }
+    while ((int)b->ev_count.size() < n) {
+      cudaEvent_t ev;
+      if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+      b->ev_count.push_back(ev);
+    }
+    ma.resize(n);
+    for (int i = 0; i < n; i++) {
+      MeshArgs& a = ma[i];
+      a.res = it[i].desc.res;
+      a.C = it[i].d_closing;
+      for (int k = 0; k < 3; k++) a.bbox_min[k] = it[i].desc.bbox_min[k];
+      a.cell_size = it[i].desc.cell_size;
+      a.isovalue = 0.95f;
+      a.bilateral_iters = bilateral;
+      a.defer_filter = bilateral > 0;  // filtered below, all grids per launch
+      a.num_sms = sms;
+      // the closing is empty beyond the extent: mesh only its cells (the
+      // whole grid's border rule, identical mesh)
+      a.gres = a.res;
+      for (int k = 0; k < 3; k++) {
+        a.tag_lo[k] = a.emit_lo[k] = 0;
+        a.tag_hi[k] = a.emit_hi[k] = ext[i];
+      }
+      if ((e = mesh_prepare_grid(a, b->meshes[i])) != cudaSuccess) return e;
+    }
+  }
+  // closing phase (with the mesh counts): replay the captured graph when the
+  // batch is unchanged
+  uint64_t sig = signature(n, it, ext, mode, se, L);
+  if (meshes) {
+    sig = mix(sig, (uint64_t)(uintptr_t)b->h_tot);
+    for (int i = 0; i < n; i++) sig = mix(sig, (uint64_t)(uintptr_t)b->meshes[i].brick_tot);
+  }
   const bool graphable = all_uniform && !(kc && kc->profiling);
   if (graphable) {
     if (!b->graph || b->graph_sig != sig) {
@@ -327,7 +394,8 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
       cudaGraph_t g = nullptr;
       KernelCounter cap;  // counts the kernels the graph holds
       if ((e = cudaStreamBeginCapture(b->cap_st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-      const cudaError_t ec = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, b->cap_st, &cap);
+      const cudaError_t ec = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, b->cap_st, &cap,
+                                              meshes ? ma.data() : nullptr);
       e = cudaStreamEndCapture(b->cap_st, &g);
       if (ec != cudaSuccess) return ec;
       if (e != cudaSuccess) return e;
@@ -344,47 +412,20 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     if ((e = cudaStreamWaitEvent(st, b->ev_out, 0)) != cudaSuccess) return e;
     if (kc) kc->launches += b->graph_kernels;
   } else {
-    if ((e = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, st, kc)) != cudaSuccess) return e;
+    if ((e = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, st, kc,
+                              meshes ? ma.data() : nullptr)) != cudaSuccess)
+      return e;
   }
   if (!meshes) return cudaGetLastError();
-  // meshing: counts on the lanes, one synchronisation, emission on the lanes
-  if ((int)b->meshes.size() < n) b->meshes.resize(n);
-  b->nv.assign(n, 0);
-  b->nt.assign(n, 0);
-  if (b->h_tot_cap < n) {
-    if (b->h_tot) cudaFreeHost(b->h_tot);
-    b->h_tot = nullptr;
-    if ((e = cudaMallocHost(&b->h_tot, sizeof(uint32_t) * 4 * n)) != cudaSuccess) return e;
-    b->h_tot_cap = n;
-  }
-  if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return e;
-  for (int l = 0; l < L; l++) cudaStreamWaitEvent(b->lanes[l].st, b->fork, 0);
-  std::vector<MeshArgs> ma(n);
+  // meshing: each grid's emission, on its lane's emission stream, once its
+  // counts are on the host (the closings of later grids go on meanwhile)
   for (int i = 0; i < n; i++) {
-    MeshArgs& a = ma[i];
-    a.res = it[i].desc.res;
-    a.C = it[i].d_closing;
-    for (int k = 0; k < 3; k++) a.bbox_min[k] = it[i].desc.bbox_min[k];
-    a.cell_size = it[i].desc.cell_size;
-    a.isovalue = 0.95f;
-    a.bilateral_iters = bilateral;
-    a.defer_filter = bilateral > 0;  // filtered below, all grids per launch
-    a.num_sms = sms;
-    // the closing is empty beyond the extent: mesh only its cells (the
-    // whole grid's border rule, identical mesh)
-    a.gres = a.res;
-    for (int k = 0; k < 3; k++) {
-      a.tag_lo[k] = a.emit_lo[k] = 0;
-      a.tag_hi[k] = a.emit_hi[k] = ext[i];
-    }
-    if ((e = mesh_count_launch(a, b->meshes[i], b->lanes[lane[i]].st, kc, b->h_tot + 4 * i)) != cudaSuccess) return e;
-  }
-  for (int l = 0; l < L; l++)
-    if ((e = cudaStreamSynchronize(b->lanes[l].st)) != cudaSuccess) return e;
-  for (int i = 0; i < n; i++) {
+    if ((e = cudaEventSynchronize(b->ev_count[i])) != cudaSuccess) return e;
     if ((e = mesh_count_finish(b->meshes[i], b->h_tot + 4 * i, &b->nv[i], &b->nt[i])) != cudaSuccess) return e;
     if (b->nv[i] > 0xfffffff0LL || b->nt[i] > 0x7ffffff0LL) return cudaErrorInvalidValue;
-    if ((e = mesh_emit(ma[i], b->meshes[i], b->nv[i], b->nt[i], b->lanes[lane[i]].st, kc)) != cudaSuccess) return e;
+    cudaStream_t em = b->lanes[lane[i]].em;
+    if ((e = cudaStreamWaitEvent(em, b->ev_count[i], 0)) != cudaSuccess) return e;
+    if ((e = mesh_emit(ma[i], b->meshes[i], b->nv[i], b->nt[i], em, kc)) != cudaSuccess) return e;
     meshes[i].vertices = b->meshes[i].V;
     meshes[i].normals = b->meshes[i].N;
     meshes[i].triangles = b->meshes[i].T;
@@ -392,13 +433,14 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     meshes[i].num_triangles = b->nt[i];
   }
   for (int l = 0; l < L; l++) {
-    cudaEventRecord(b->lanes[l].done, b->lanes[l].st);
-    cudaStreamWaitEvent(st, b->lanes[l].done, 0);
+    cudaEventRecord(b->lanes[l].em_done, b->lanes[l].em);
+    cudaStreamWaitEvent(st, b->lanes[l].em_done, 0);
   }
   if (bilateral > 0) {
     // normal filtering of all the meshes, one launch per iteration (the
     // host table is free again: the previous call's copy of it preceded this
-    // call's closings on st, which the lane synchronisation above waited for)
+    // call's closings on st, which the waits for the grids' counts above
+    // followed)
     if (b->filter_cap < n) {
       if (b->h_filter) cudaFreeHost(b->h_filter);
       cudaFree(b->d_filter);

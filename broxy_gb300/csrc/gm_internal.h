@@ -185,6 +185,9 @@ cudaError_t mesh_count(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, Kerne
 cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st, KernelCounter* kc,
                               uint32_t* h_tot4);
 cudaError_t mesh_count_finish(MeshBuffers& b, const uint32_t* tot, int64_t* nv, int64_t* nt);
+// The buffers mesh_count_launch needs, allocated now (so that the count can
+// be captured in a CUDA graph, where nothing may be allocated).
+cudaError_t mesh_prepare_grid(const MeshArgs& a, MeshBuffers& b);
 // Allocate up front for meshes of a cubic grid of edge res with up to nv
 // vertices and nt triangles (later meshes only grow the buffers further).
 cudaError_t mesh_reserve(MeshBuffers& b, int res, int64_t nv, int64_t nt);

@@ -1159,6 +1159,12 @@ cudaError_t mesh_count_launch(const MeshArgs& a, MeshBuffers& b, cudaStream_t st
   return cudaMemcpyAsync(h_tot4, b.brick_tot + 4 * (size_t)nb, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
 }
 
+cudaError_t mesh_prepare_grid(const MeshArgs& a, MeshBuffers& b) {
+  int d[3];
+  grid_dims(a, d);
+  return ensure_grid_buffers(b, (int64_t)d[0] * d[1] * d[2], brick_count(d));
+}
+
 cudaError_t mesh_count_finish(MeshBuffers& b, const uint32_t* tot, int64_t* nv, int64_t* nt) {
   *nv = tot[1];
   *nt = tot[2];
