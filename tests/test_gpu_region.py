@@ -95,20 +95,22 @@ def _swap_xz_bytes(C, dims):
 
 
 @pytest.mark.parametrize("mode", [L.GM_REF, L.GM_EXACT])
-def test_long_rows_equal_transposed_box(gm_ctx, mode):
-    """Rows of 2048 fine voxels (two 32-bit words per lane in the x pass)
-    against the same grid with x and z exchanged (short rows): the closing
-    commutes with the exchange."""
+@pytest.mark.parametrize("rx", [1024, 2048])
+def test_long_rows_equal_transposed_box(gm_ctx, mode, rx):
+    """Rows of 2048 fine voxels (two 32-bit words per lane in the x passes)
+    and of 4096 (the block-per-row x passes) against the same grid with x and
+    z exchanged (short rows): the closing commutes with the exchange."""
     import torch
-    long_dims, short_dims = (1024, 32, 32), (32, 32, 1024)
+    long_dims, short_dims = (rx, 32, 32), (32, 32, rx)
     g = torch.Generator().manual_seed(9500)
     X = torch.zeros(long_dims[2], long_dims[1], long_dims[0], dtype=torch.uint8)
     # random blocks and sparse voxels away from the y / z borders
-    X[6:26, 6:26, :] = torch.where(torch.rand(20, 20, 1024, generator=g) < 0.08,
-                                   torch.randint(0, 256, (20, 20, 1024), generator=g, dtype=torch.uint8),
-                                   torch.zeros(20, 20, 1024, dtype=torch.uint8))
+    X[6:26, 6:26, :] = torch.where(torch.rand(20, 20, rx, generator=g) < 0.08,
+                                   torch.randint(0, 256, (20, 20, rx), generator=g, dtype=torch.uint8),
+                                   torch.zeros(20, 20, rx, dtype=torch.uint8))
     X[10:20, 12:18, 100:180] = 0xFF
     X[8:24, 8:24, 700:705] = 0xFF
+    X[9:22, 7:25, rx - 40:rx - 30] = 0xFF
     X = X.view(-1).cuda()
     Xt = _swap_xz_bytes(X, long_dims)
     C_long = gm_ctx.close_box(api.make_box(long_dims), X, None, 5, mode, L.GM_SE_SPHERE)
