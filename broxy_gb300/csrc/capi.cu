@@ -112,7 +112,7 @@ struct gm_ctx {
   cudaEvent_t ev_copy = nullptr, ev_geom = nullptr;
   // the radius field's upload in z slabs: one event per slab copied and per
   // slab bound read back, the bounds in pinned memory
-  static constexpr int kSlabs = 4;
+  static constexpr int kSlabs = 8;
   cudaEvent_t ev_slab[kSlabs] = {}, ev_max[kSlabs] = {};
   int* h_slab = nullptr;
   // last mesh
