@@ -471,7 +471,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--res", type=int, default=RES)
-    ap.add_argument("--cpu-res", type=int, default=64, help="base cells per axis of the CPU crop")
+    ap.add_argument("--cpu-res", type=int, default=256, help="base cells per axis of the CPU crop")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-grid batching comparison")
