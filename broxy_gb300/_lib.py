@@ -121,6 +121,17 @@ PROTOTYPES = {
     "gm_erode_bvh": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int32, _P, _P]),
     "gm_layout_zwords_to_packed": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "gm_layout_packed_to_zwords": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
+    "gm_close_rotcube": (C.c_int, [_P, C.POINTER(GridDesc), _P, _P, C.c_int32, _P, C.c_int32, C.c_int, _P, _P, _P,
+                                   _P]),
+    "gm_frame_field_create": (C.c_int, [_P, _P, _P, C.c_int32, C.POINTER(_P)]),
+    "gm_frame_field_destroy": (C.c_int, [_P]),
+    "gm_frame_field_add_point": (C.c_int, [_P, _P, _P]),
+    "gm_frame_field_update_point": (C.c_int, [_P, C.c_int32, _P]),
+    "gm_frame_field_num_points": (C.c_int32, [_P]),
+    "gm_frame_field_get_point": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "gm_frame_field_generate": (C.c_int, [_P, C.POINTER(C.c_int32), _P]),
+    "gm_frame_field_quats": (C.c_int, [_P, C.POINTER(_P), C.POINTER(C.c_int32)]),
+    "gm_rotation_to_twist": (C.c_int, [_P, _P, _P, _P]),
 }
 
 _lib = None

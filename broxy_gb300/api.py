@@ -113,6 +113,20 @@ class Context:
         self._check(st)
         return out
 
+    # f2: GMorpho::Update with a frame field
+    def close_rotcube(self, desc, X, quats, quat_res, R=None, uniform_radius=4, mode=L.GM_REF, out=None, D=None,
+                      S=None):
+        """Rotated-cube dilation under the quaternion field `quats` (device,
+        (quat_res^3, 4) float32 x y z w, e.g. FrameField.quats()) then the
+        sphere erosion."""
+        import torch
+        if out is None:
+            out = torch.empty_like(X)
+        self._check(self.lib.gm_close_rotcube(self.ctx, C.byref(desc), _ptr(X), _ptr(R), int(uniform_radius),
+                                              _ptr(quats), int(quat_res), mode, _ptr(out), _ptr(D), _ptr(S),
+                                              _stream()))
+        return out
+
     # a8
     def contour(self, desc, grid, mode=L.GM_REF, inplace=False):
         import torch
@@ -326,6 +340,77 @@ class BVH:
             self.destroy()
         except Exception:
             pass
+
+
+class FrameField:
+    """FrameField with the BiHarmonicSystem method (gm_frame_field_*): a
+    quaternion per node of a res^3 lattice over the box, interpolating up to
+    20 hard-constrained rotations."""
+
+    def __init__(self, ctx, bbox_min, bbox_max, res):
+        self.ctx = ctx
+        self.res = int(res)
+        h = C.c_void_p()
+        lo = (C.c_float * 3)(*[float(v) for v in bbox_min])
+        hi = (C.c_float * 3)(*[float(v) for v in bbox_max])
+        ctx._check(ctx.lib.gm_frame_field_create(ctx.ctx, lo, hi, self.res, C.byref(h)))
+        self.h = h
+
+    def add_point(self, position, twist):
+        p = (C.c_float * 3)(*[float(v) for v in position])
+        t = (C.c_float * 3)(*[float(v) for v in twist])
+        self.ctx._check(self.ctx.lib.gm_frame_field_add_point(self.h, p, t))
+
+    def update_point(self, i, twist):
+        t = (C.c_float * 3)(*[float(v) for v in twist])
+        self.ctx._check(self.ctx.lib.gm_frame_field_update_point(self.h, int(i), t))
+
+    def num_points(self):
+        return int(self.ctx.lib.gm_frame_field_num_points(self.h))
+
+    def point(self, i):
+        g = (C.c_float * 3)()
+        t = (C.c_float * 3)()
+        self.ctx._check(self.ctx.lib.gm_frame_field_get_point(self.h, int(i), g, t))
+        return tuple(g), tuple(t)
+
+    def generate(self):
+        """Solve the field; returns the solver's iteration count."""
+        it = C.c_int32()
+        self.ctx._check(self.ctx.lib.gm_frame_field_generate(self.h, C.byref(it), _stream()))
+        return it.value
+
+    def quats(self):
+        """Zero-copy (res^3, 4) float32 device array, valid until the next
+        generate or destroy."""
+        import torch
+        p = C.c_void_p()
+        r = C.c_int32()
+        self.ctx._check(self.ctx.lib.gm_frame_field_quats(self.h, C.byref(p), C.byref(r)))
+        n = r.value ** 3
+        return torch.as_tensor(DevicePtrArray(p.value, (n, 4), "<f4"), device="cuda")
+
+    def destroy(self):
+        if self.h:
+            self.ctx.lib.gm_frame_field_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def rotation_to_twist(e_x, e_y, e_z):
+    """FrameField::RotationToTwistCayley (gm_rotation_to_twist)."""
+    lib = L.load()
+    a = [(C.c_float * 3)(*[float(v) for v in e]) for e in (e_x, e_y, e_z)]
+    out = (C.c_float * 3)()
+    st = lib.gm_rotation_to_twist(a[0], a[1], a[2], out)
+    if st != L.GM_OK:
+        raise L.GMError(st, "gm_rotation_to_twist")
+    return tuple(out)
 
 
 class Server:

@@ -23,8 +23,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
-SOURCES = ["morpho.cu", "mc.cu", "pyramid.cu", "scalefield.cu", "voxelize.cu", "capi.cu", "close_noalloc.cu", "bvh.cu", "batch.cu", "serve.cu", "crop.cu"]
+SOURCES = ["morpho.cu", "mc.cu", "pyramid.cu", "scalefield.cu", "voxelize.cu", "capi.cu", "close_noalloc.cu", "bvh.cu", "batch.cu", "serve.cu", "crop.cu", "rotcube.cu", "framefield.cu"]
 HOST_SOURCES = ["gmorpho_classes.cpp", "meshio.cpp"]
+# The rotated-cube predicates evaluate the reference's float expressions
+# without fused multiply-adds, as the CPU oracle does.
+FILE_FLAGS = {"rotcube.cu": ["-fmad=false"]}
 
 
 def nvcc():
@@ -72,7 +75,8 @@ def build(verbose=False, force=False, ptxas_v=False):
         o = os.path.join(OBJDIR, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            cmd = [nv] + ARCH + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_v else []) + ["-c", s, "-o", o]
+            cmd = [nv] + ARCH + NVCC_FLAGS + FILE_FLAGS.get(src, []) + (["-Xptxas", "-v"] if ptxas_v else []) + [
+                "-c", s, "-o", o]
             jobs.append(cmd)
     out = []
     if jobs:

@@ -5,11 +5,13 @@
 // launches.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/gmorpho_gb300.h"
 #include "gm_common.cuh"
@@ -359,7 +361,7 @@ gm_status gm_pyramid_build(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t*
 static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
                             int32_t uniform_radius, int mode, int se, uint8_t* d_closing, uint8_t* d_dilation,
                             uint8_t* d_contour, cudaStream_t st, bool xpass_done = false, bool ypass_done = false,
-                            int rmax_known = 0, bool zpass_done = false) {
+                            int rmax_known = 0, bool zpass_done = false, const gm::RotCubeArgs* rotcube = nullptr) {
   gm_status s;
   const int res = desc->res;
   const int64_t fine = (int64_t)8 * res * res * res;
@@ -400,6 +402,18 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   a.xpass_done = xpass_done;
   a.ypass_done = ypass_done;
   a.zpass_done = zpass_done;
+  if (rotcube) {
+    // the rotated-cube dilation into the closing's D, its scratch in the
+    // part of the workspace that the erosion writes first
+    gm::RotCubeArgs r = *rotcube;
+    size_t have = 0;
+    r.D = gm::close_ws_dilation(a);
+    r.scratch = gm::close_ws_scratch(a, &have);
+    r.num_sms = ctx->num_sms;
+    if (have < gm::rotcube_scratch_bytes(res)) return fail(ctx, GM_ERR_CUDA, "gm_close_rotcube: workspace too small");
+    GM_CHECK_CUDA(ctx, gm::launch_rotcube_dilation(r, st, &ctx->kc), "gm_close_rotcube");
+    a.dilation_done = true;
+  }
   GM_CHECK_CUDA(ctx, gm::launch_close(a, st, &ctx->kc), "gm_close");
   return GM_OK;
 }
@@ -418,6 +432,33 @@ gm_status gm_close(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input
   if ((s = set_device(ctx)) != GM_OK) return s;
   return close_impl(ctx, desc, d_input, d_scale, uniform_radius, (int)mode, (int)se, d_closing, d_dilation, d_contour,
                     (cudaStream_t)stream);
+}
+
+gm_status gm_close_rotcube(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
+                           int32_t uniform_radius, const float* d_quats, int32_t quat_res, gm_mode mode,
+                           uint8_t* d_closing, uint8_t* d_dilation, uint8_t* d_contour, void* stream) {
+  if (!ctx) return GM_ERR_INVALID_ARGUMENT;
+  gm_status s = check_desc(ctx, desc);
+  if (s != GM_OK) return s;
+  if (!d_input || !d_closing || !d_quats)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_rotcube: NULL input, quaternion field or output");
+  if (!aligned16(d_input) || (d_scale && !aligned16(d_scale)) || !aligned16(d_quats))
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_rotcube: device buffers must be 16-byte aligned");
+  if (quat_res < 1 || quat_res > 1024)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_rotcube: quat_res must lie in [1, 1024]");
+  if (mode != GM_REF && mode != GM_EXACT) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_close_rotcube: unknown mode");
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  gm::RotCubeArgs r;
+  r.res = desc->res;
+  for (int i = 0; i < 3; i++) r.data_res[i] = desc->data_res[i];
+  r.X = d_input;
+  r.R = d_scale;
+  r.uniform_r = uniform_radius;
+  r.Q = d_quats;
+  r.qres = quat_res;
+  r.mode = (int)mode;
+  return close_impl(ctx, desc, d_input, d_scale, uniform_radius, (int)mode, GM_SE_CUBE, d_closing, d_dilation,
+                    d_contour, (cudaStream_t)stream, false, false, 0, false, &r);
 }
 
 gm_status gm_contour(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_grid, uint8_t* d_out, gm_mode mode,
@@ -975,6 +1016,199 @@ gm_status gm_layout_packed_to_zwords(gm_ctx* ctx, int32_t res, const uint8_t* d_
   if (s != GM_OK) return s;
   GM_CHECK_CUDA(ctx, gm::launch_layout(res, d_zwords, const_cast<uint8_t*>(d_grid), 1, (cudaStream_t)stream, &ctx->kc),
                 "layout");
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ frame field
+
+}  // extern "C"
+
+struct gm_frame_field {
+  gm_ctx* ctx = nullptr;
+  int res = 0;
+  float bbox_min[3] = {0, 0, 0}, bbox_max[3] = {0, 0, 0};
+  float cell_size = 0.f;
+  struct Point {
+    float grid[3];   // floored lattice position
+    float twist[3];  // rotation vector (axis * angle)
+  };
+  std::vector<Point> points;
+  gm::FrameFieldGpu gpu;
+  bool generated = false;
+};
+
+namespace {
+
+constexpr int kMaxHardConstraints = 20;  // max_hc_number_ (GMorpho/FrameField.h, FrameField::FrameField)
+
+// The constraint quaternion (sin(theta/2) v, cos(theta/2)) of a twist:
+// theta = |twist| in float, v = twist scaled by 1.f / theta (left as is when
+// theta is 0), sine and cosine in double (FrameFieldSparseBiharmonic.cu:
+// 487-503; Common/Vec3.h:203-216).
+void twist_quat(const float* tw, float* q) {
+  const float theta = (float)std::sqrt((double)(tw[0] * tw[0] + tw[1] * tw[1] + tw[2] * tw[2]));
+  float v[3] = {tw[0], tw[1], tw[2]};
+  if (theta != 0.0f) {
+    const float inv = 1.0f / theta;
+    for (int i = 0; i < 3; i++) v[i] *= inv;
+  }
+  const double s = std::sin(0.5 * (double)theta), c = std::cos(0.5 * (double)theta);
+  for (int i = 0; i < 3; i++) q[i] = (float)(s * (double)v[i]);
+  q[3] = (float)c;
+}
+
+}  // namespace
+
+extern "C" {
+
+gm_status gm_frame_field_create(gm_ctx* ctx, const float* bbox_min, const float* bbox_max, int32_t res,
+                                gm_frame_field** out) {
+  if (!ctx || !bbox_min || !bbox_max || !out) return GM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (res < 2 || res > 256) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_frame_field_create: res must lie in [2, 256]");
+  gm_status s;
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  gm_frame_field* f = new gm_frame_field();
+  f->ctx = ctx;
+  f->res = res;
+  for (int i = 0; i < 3; i++) f->bbox_min[i] = bbox_min[i], f->bbox_max[i] = bbox_max[i];
+  // InitSparseBiharmonicSystem (FrameFieldSparseBiharmonic.cu:28-38)
+  f->cell_size = std::max(std::fabs(bbox_max[0] - bbox_min[0]),
+                          std::max(std::fabs(bbox_max[1] - bbox_min[1]), std::fabs(bbox_max[2] - bbox_min[2]))) /
+                 (float)res;
+  cudaError_t e = gm::frame_field_alloc(f->gpu, res);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    gm::frame_field_free(f->gpu);
+    delete f;
+    return fail(ctx, e == cudaErrorMemoryAllocation ? GM_ERR_OUT_OF_MEMORY : GM_ERR_CUDA,
+                std::string("gm_frame_field_create: ") + cudaGetErrorString(e));
+  }
+  *out = f;
+  return GM_OK;
+}
+
+gm_status gm_frame_field_destroy(gm_frame_field* ff) {
+  if (!ff) return GM_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ff->ctx->device);
+  gm::frame_field_free(ff->gpu);
+  delete ff;
+  return GM_OK;
+}
+
+gm_status gm_frame_field_add_point(gm_frame_field* ff, const float* position, const float* twist) {
+  if (!ff || !position || !twist) return GM_ERR_INVALID_ARGUMENT;
+  if ((int)ff->points.size() >= kMaxHardConstraints)
+    return fail(ff->ctx, GM_ERR_CAPACITY, "gm_frame_field_add_point: at most 20 hard constraints");
+  // AddHardConstrainedPoint (FrameField.cu:64-77): lattice position
+  // floor((position - bbox_min) * (1 / cell_size))
+  gm_frame_field::Point pt;
+  const float inv = 1.f / ff->cell_size;
+  for (int i = 0; i < 3; i++) {
+    pt.grid[i] = std::floor((position[i] - ff->bbox_min[i]) * inv);
+    pt.twist[i] = twist[i];
+    if (!(pt.grid[i] >= 0.f && pt.grid[i] < (float)ff->res))
+      return fail(ff->ctx, GM_ERR_INVALID_ARGUMENT, "gm_frame_field_add_point: position outside the field's box");
+  }
+  ff->points.push_back(pt);
+  return GM_OK;
+}
+
+gm_status gm_frame_field_update_point(gm_frame_field* ff, int32_t i, const float* twist) {
+  if (!ff || !twist) return GM_ERR_INVALID_ARGUMENT;
+  if (i < 0 || i >= (int32_t)ff->points.size())
+    return fail(ff->ctx, GM_ERR_INVALID_ARGUMENT, "gm_frame_field_update_point: no such point");
+  for (int k = 0; k < 3; k++) ff->points[i].twist[k] = twist[k];
+  return GM_OK;
+}
+
+int32_t gm_frame_field_num_points(const gm_frame_field* ff) { return ff ? (int32_t)ff->points.size() : -1; }
+
+gm_status gm_frame_field_get_point(const gm_frame_field* ff, int32_t i, float* grid_position, float* twist) {
+  if (!ff || i < 0 || i >= (int32_t)ff->points.size()) return GM_ERR_INVALID_ARGUMENT;
+  for (int k = 0; k < 3; k++) {
+    if (grid_position) grid_position[k] = ff->points[i].grid[k];
+    if (twist) twist[k] = ff->points[i].twist[k];
+  }
+  return GM_OK;
+}
+
+gm_status gm_frame_field_generate(gm_frame_field* ff, int32_t* iterations, void* stream) {
+  if (!ff) return GM_ERR_INVALID_ARGUMENT;
+  gm_ctx* ctx = ff->ctx;
+  gm_status s;
+  if ((s = set_device(ctx)) != GM_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (iterations) *iterations = 0;
+  if (ff->points.empty()) {
+    // InitQuats writes (0, 1, 0, 0) whatever it is given
+    // (FrameFieldSparseBiharmonic.cu:649-671)
+    GM_CHECK_CUDA(ctx, gm::frame_field_fill(ff->gpu, 0.f, 1.f, 0.f, 0.f, st, &ctx->kc), "gm_frame_field_generate");
+  } else {
+    const int n = (int)ff->points.size();
+    std::vector<int64_t> nodes(n);
+    std::vector<float> rhs(4 * (size_t)n);
+    const int64_t r = ff->res;
+    for (int c = 0; c < n; c++) {
+      const auto& pt = ff->points[c];
+      nodes[c] = (int64_t)pt.grid[0] + r * (int64_t)pt.grid[1] + r * r * (int64_t)pt.grid[2];
+      twist_quat(pt.twist, &rhs[4 * (size_t)c]);
+    }
+    int it = 0;
+    GM_CHECK_CUDA(ctx, gm::frame_field_solve(ff->gpu, nodes.data(), rhs.data(), n, 1e-10, 400000, &it, st, &ctx->kc),
+                  "gm_frame_field_generate");
+    if (iterations) *iterations = it;
+  }
+  ff->generated = true;
+  return GM_OK;
+}
+
+gm_status gm_frame_field_quats(const gm_frame_field* ff, const float** d_quats, int32_t* res) {
+  if (!ff || !d_quats) return GM_ERR_INVALID_ARGUMENT;
+  if (!ff->generated) return fail(ff->ctx, GM_ERR_NOT_READY, "gm_frame_field_quats: generate first");
+  *d_quats = reinterpret_cast<const float*>(ff->gpu.quats);
+  if (res) *res = ff->res;
+  return GM_OK;
+}
+
+// RotationToTwistCayley (FrameField.cu:228-252): the Cayley transform
+// C = (R - I)(R + I)^-1 of the rotation with columns e_x, e_y, e_z gives the
+// axis (-C12, C02, -C01), normalised; the angle is
+// acos(clamp((trace - 1) / 2)).  In double; R + I singular (half turns)
+// is rejected.
+gm_status gm_rotation_to_twist(const float* e_x, const float* e_y, const float* e_z, float* twist) {
+  if (!e_x || !e_y || !e_z || !twist) return GM_ERR_INVALID_ARGUMENT;
+  double R[3][3];
+  for (int i = 0; i < 3; i++) R[i][0] = e_x[i], R[i][1] = e_y[i], R[i][2] = e_z[i];
+  double P[3][3], M[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      P[i][j] = R[i][j] + (i == j ? 1.0 : 0.0);
+      M[i][j] = R[i][j] - (i == j ? 1.0 : 0.0);
+    }
+  // inverse of P by its adjugate
+  double A[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      const int i1 = (j + 1) % 3, i2 = (j + 2) % 3, j1 = (i + 1) % 3, j2 = (i + 2) % 3;
+      A[i][j] = P[i1][j1] * P[i2][j2] - P[i1][j2] * P[i2][j1];
+    }
+  const double det = P[0][0] * A[0][0] + P[0][1] * A[1][0] + P[0][2] * A[2][0];
+  if (!(std::fabs(det) > 1e-12)) return GM_ERR_INVALID_ARGUMENT;
+  double C[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double t = 0;
+      for (int k = 0; k < 3; k++) t += M[i][k] * A[k][j];
+      C[i][j] = t / det;
+    }
+  double ax[3] = {-C[1][2], C[0][2], -C[0][1]};
+  const double len = std::sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+  if (len != 0.0)
+    for (double& a : ax) a /= len;
+  const double cth = (R[0][0] + R[1][1] + R[2][2] - 1.0) / 2.0;
+  const double theta = std::acos(std::min(std::max(cth, -1.0), 1.0));
+  for (int i = 0; i < 3; i++) twist[i] = (float)(theta * ax[i]);
   return GM_OK;
 }
 

@@ -56,6 +56,9 @@ struct CloseArgs {
   bool xpass_done = false;  // the dilation's x pass already ran (launch_close_xpass) into the workspace
   bool ypass_done = false;  // and its y pass (launch_close_ypass over slabs covering the grid; sphere only)
   bool zpass_done = false;  // and its z pass (launch_close_zpass over slabs covering the grid; sphere only)
+  // The dilation is already in the closing's D (D_out, or the workspace's D:
+  // close_ws_dilation); launch_close runs the erosion half only.
+  bool dilation_done = false;
   // Cells [roi_lo, roi_hi) where the caller needs the closing (roi_hi[0] == 0:
   // everywhere).  Work that cannot reach them is skipped, and the closing and
   // the optional D / S outputs hold no meaningful values outside them.
@@ -101,6 +104,52 @@ cudaError_t launch_close_ypass(const CloseArgs& a, int z0, int z1, int r_bound, 
 // whole-grid pass).
 cudaError_t launch_close_zpass(const CloseArgs& a, int z0, int z1, int r_bound, cudaStream_t st, KernelCounter* kc);
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc);
+// Where launch_close keeps the dilation D (a.D_out, or its workspace slot),
+// and a scratch region of the workspace that launch_close overwrites only
+// after it has started (free for work that runs before it on its stream).
+uint8_t* close_ws_dilation(const CloseArgs& a);
+uint8_t* close_ws_scratch(const CloseArgs& a, size_t* bytes);
+
+// ---- rotated-cube dilation under a frame field (rotcube.cu) ----
+constexpr int kRotCubeMaxLevels = 12;  // res <= 2048
+struct RotCubeArgs {
+  int res = 0;                  // power of two
+  int data_res[3] = {0, 0, 0};
+  const uint8_t* X = nullptr;   // input grid
+  const int8_t* R = nullptr;    // fine radius grid, or nullptr for uniform_r
+  int uniform_r = 0;
+  const float* Q = nullptr;     // quaternions (x, y, z, w) of a qres^3 lattice, x-fastest, 16-byte aligned
+  int qres = 0;
+  int mode = 0;                 // 0 = GM_REF (base pass + conservative contour), 1 = GM_EXACT (every fine voxel)
+  uint8_t* D = nullptr;         // dilation out, res^3
+  uint8_t* scratch = nullptr;   // rotcube_scratch_bytes(res)
+  int num_sms = 0;
+};
+size_t rotcube_scratch_bytes(int res);
+
+// ---- frame field: the biharmonic quaternion system (framefield.cu) ----
+struct FrameFieldGpu {
+  int res = 0;
+  float4* quats = nullptr;  // res^3 (x, y, z, w)
+  double* vecs = nullptr;   // x, r, p, y, Ap: 4 doubles per node each
+  double *x = nullptr, *r = nullptr, *p = nullptr, *y = nullptr, *Ap = nullptr;
+  double* part = nullptr;   // block partial sums
+  double* sc = nullptr;     // CG scalars
+  double* h_sc = nullptr;   // pinned copy of the scalars
+  uint8_t* S = nullptr;     // screened (hard-constrained) nodes
+  cudaGraphExec_t graph = nullptr;
+};
+cudaError_t frame_field_alloc(FrameFieldGpu& f, int res);
+void frame_field_free(FrameFieldGpu& f);
+cudaError_t frame_field_fill(FrameFieldGpu& f, float qx, float qy, float qz, float qw, cudaStream_t st,
+                             KernelCounter* kc);
+// Solves (L^T L + S) q_k = b_k for the four components; nodes[c] / rhs4[4c..]
+// are the constrained nodes (x + res*y + res^2*z) and their quaternions, in
+// the order given (the last one on a node wins).  Stops when every
+// component's residual is <= tol * |b_k| or after max_iters iterations.
+cudaError_t frame_field_solve(FrameFieldGpu& f, const int64_t* nodes, const float* rhs4, int npts, double tol,
+                              int max_iters, int* iters_out, cudaStream_t st, KernelCounter* kc);
+cudaError_t launch_rotcube_dilation(const RotCubeArgs& a, cudaStream_t st, KernelCounter* kc);
 // The squared lattice distance field of a cubic grid: per fine voxel p (u16,
 // x-fastest, (2 res)^3), the smallest squared distance from lattice point p
 // to an occupied fine voxel box, saturated at (rmax + 1)^2 — what the sphere

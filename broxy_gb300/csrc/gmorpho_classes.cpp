@@ -6,7 +6,9 @@
 // Exception (GMorpho/GMorpho.cu:50-56) carrying the library message.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <limits>
 #include <cstring>
 #include <fstream>
 #include <mutex>
@@ -278,6 +280,103 @@ void ScaleField::UpdateGrid() {
   if (s != GM_OK) throw Exception(message(ctx, s, "ScaleField::UpdateGrid"));
 }
 
+// ------------------------------------------------------------------ FrameField
+
+FrameField::~FrameField() {
+  if (ff_) gm_frame_field_destroy(ff_);
+}
+
+void FrameField::Init(const Vec3f& bbox_min, const Vec3f& bbox_max, const Vec3i& res, OptimMethod optim_method) {
+  if (optim_method != BiHarmonicSystem) throw Exception("unsupported: LocalOptimization");
+  gm_ctx* ctx = shared_ctx();
+  if (ff_) gm_frame_field_destroy(ff_);
+  ff_ = nullptr;
+  hc_points_.clear();
+  const float lo[3] = {bbox_min[0], bbox_min[1], bbox_min[2]}, hi[3] = {bbox_max[0], bbox_max[1], bbox_max[2]};
+  const int s = gm_frame_field_create(ctx, lo, hi, res[0], &ff_);
+  if (s != GM_OK) throw Exception(message(ctx, s, "FrameField::Init"));
+  bbox_min_ = bbox_min;
+  bbox_max_ = bbox_max;
+  res_ = res;
+  cell_size_ = std::max(std::fabs(bbox_max[0] - bbox_min[0]),
+                        std::max(std::fabs(bbox_max[1] - bbox_min[1]), std::fabs(bbox_max[2] - bbox_min[2]))) /
+               res[0];
+}
+
+Vec3f FrameField::RotationToTwistCayley(const Vec3f& e_x, const Vec3f& e_y, const Vec3f& e_z) {
+  float t[3];
+  const int s = gm_rotation_to_twist(&e_x[0], &e_y[0], &e_z[0], t);
+  if (s != GM_OK) throw Exception("RotationToTwistCayley: half turn (R + I singular)");
+  return Vec3f(t[0], t[1], t[2]);
+}
+
+void FrameField::AddHardConstrainedPoint(const Vec3f& position, const Vec3f& e_x, const Vec3f& e_y,
+                                         const Vec3f& e_z) {
+  AddHardConstrainedPoint(position, RotationToTwistCayley(e_x, e_y, e_z));
+}
+
+void FrameField::AddHardConstrainedPoint(const Vec3f& position, const Vec3f& twist) {
+  if (!ff_) throw Exception("Init must come first");
+  const int s = gm_frame_field_add_point(ff_, &position[0], &twist[0]);
+  if (s == GM_ERR_CAPACITY) return;  // past 20 points the reference ignores the call
+  if (s != GM_OK) throw Exception(message(shared_ctx(), s, "FrameField::AddHardConstrainedPoint"));
+  float g[3], t[3];
+  gm_frame_field_get_point(ff_, (int32_t)hc_points_.size(), g, t);
+  hc_points_.push_back(FramePoint(Vec3f(g[0], g[1], g[2]), Vec3f(t[0], t[1], t[2])));
+}
+
+void FrameField::UpdateHardConstrainedPoint(int i, const Vec3f& e_x, const Vec3f& e_y, const Vec3f& e_z) {
+  UpdateHardConstrainedPoint(i, RotationToTwistCayley(e_x, e_y, e_z));
+}
+
+void FrameField::UpdateHardConstrainedPoint(int i, const Vec3f& twist) {
+  if (!ff_ || i < 0 || i >= (int)hc_points_.size()) return;
+  gm_frame_field_update_point(ff_, i, &twist[0]);
+  hc_points_[i].set_twist(twist);
+}
+
+Vec3f FrameField::GetHardConstrainedPointTwist(int i) {
+  if (i >= 0 && i < (int)hc_points_.size()) return hc_points_[i].twist();
+  return Vec3f(0, 0, 0);
+}
+
+int FrameField::GetHardConstrainedPointId(const Vec3f& position) {
+  return GetHardConstrainedPointId(position, cell_size_);
+}
+
+// nearest hard-constrained node within eps_tolerance (FrameField.cu:103-126)
+int FrameField::GetHardConstrainedPointId(const Vec3f& position, float eps_tolerance) {
+  int best = -1;
+  float best_d = std::numeric_limits<float>::max();
+  for (int i = 0; i < (int)hc_points_.size(); i++) {
+    float d2 = 0.f;
+    for (int k = 0; k < 3; k++) {
+      const float c = cell_size_ * hc_points_[i].position()[k] + bbox_min_[k];
+      d2 += (position[k] - c) * (position[k] - c);
+    }
+    const float d = std::sqrt(d2);
+    if (d < eps_tolerance && d < best_d) {
+      best_d = d;
+      best = i;
+    }
+  }
+  return best;
+}
+
+const float* FrameField::quats_pong() const {
+  if (!ff_) throw Exception("Init must come first");
+  const float* q = nullptr;
+  const int s = gm_frame_field_quats(ff_, &q, nullptr);
+  if (s != GM_OK) throw Exception(message(shared_ctx(), s, "FrameField::quats_pong"));
+  return q;
+}
+
+void FrameField::Generate(bool, bool) {
+  if (!ff_) throw Exception("Init must come first");
+  const int s = gm_frame_field_generate(ff_, nullptr, nullptr);
+  if (s != GM_OK) throw Exception(message(shared_ctx(), s, "FrameField::Generate"));
+}
+
 // ------------------------------------------------------------------ Voxelizer
 
 Voxelizer::~Voxelizer() {}
@@ -350,18 +449,33 @@ void GMorpho::close(const ScaleField* sf, int uniform_radius, int se) {
         "gm_close");
 }
 
-void GMorpho::Update(Mesh& mesh, const ScaleField& sf, const FrameField&) {
-  if (use_frame_field_) throw Exception("unsupported: frame-field (rotated cube) dilation");
-  // gate of GMorpho.cu:7783: morphology only when floor(2 gs / cell) > 1
-  if (std::floor(2.f * sf.global_scale() / cell_size()) > 1.f)
-    close(&sf, 0, use_asymmetric_closing_ ? GM_SE_CUBE : GM_SE_SPHERE);
-  else
+void GMorpho::close_rotcube(const ScaleField& sf, const FrameField& ff) {
+  if (!ctx_) throw Exception("Load must come first");
+  gm_grid_desc d = desc_of(input_grid_);
+  const float* q = ff.quats_pong();
+  check(gm_close_rotcube(ctx_, &d, input_grid_.grid_gpu().voxels, reinterpret_cast<const int8_t*>(sf.scale_grid()), 0,
+                         q, ff.res()[0], (gm_mode)mode_, closing_grid_.grid_gpu().voxels,
+                         dilation_grid_.grid_gpu().voxels, nullptr, nullptr),
+        "gm_close_rotcube");
+}
+
+void GMorpho::Update(Mesh& mesh, const ScaleField& sf, const FrameField& ff) {
+  // gate of GMorpho.cu:7783: morphology only when floor(2 gs / cell) > 1;
+  // the frame field matters with the asymmetric closing only (:7785-7791)
+  if (std::floor(2.f * sf.global_scale() / cell_size()) > 1.f) {
+    if (use_asymmetric_closing_ && use_frame_field_)
+      close_rotcube(sf, ff);
+    else
+      close(&sf, 0, use_asymmetric_closing_ ? GM_SE_CUBE : GM_SE_SPHERE);
+  } else {
     closing_grid_.CopyVoxelsFrom(input_grid_);
+  }
   ExtractClosingMesh(mesh, use_asymmetric_closing_ ? 200 : 20);
 }
 
 void GMorpho::DilateBySphereMipmap(const ScaleField& sf) { close(&sf, 0, GM_SE_SPHERE); }
 void GMorpho::DilateByCubeMipmap(const ScaleField& sf) { close(&sf, 0, GM_SE_CUBE); }
+void GMorpho::DilateByRotCubeMipmap(const ScaleField& sf, const FrameField& ff) { close_rotcube(sf, ff); }
 // The closing runs both halves in one call; the erosion of the last
 // dilation is already in closing_grid().
 void GMorpho::ErodeBySphereMipmap(const ScaleField&) {}

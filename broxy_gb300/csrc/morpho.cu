@@ -1628,6 +1628,24 @@ static CloseWs close_ws(const CloseArgs& a, int rx, int ry, int rz) {
   return w;
 }
 
+uint8_t* close_ws_dilation(const CloseArgs& a) {
+  const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
+  const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
+  const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
+  return close_ws(a, rx, ry, rz).D;
+}
+
+// buf16a and buf16b: first written by the dilation's passes or, when the
+// dilation is done, by the erosion's x pass
+uint8_t* close_ws_scratch(const CloseArgs& a, size_t* bytes) {
+  const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
+  const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
+  const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
+  const CloseWs w = close_ws(a, rx, ry, rz);
+  if (bytes) *bytes = (size_t)(reinterpret_cast<uint8_t*>(w.buf8) - reinterpret_cast<uint8_t*>(w.buf16a));
+  return reinterpret_cast<uint8_t*>(w.buf16a);
+}
+
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc) {
   const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
   const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
@@ -1676,65 +1694,67 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const CBox B_ero_y = cbox_grow(R_Ef, win, 4, dims), B_erob_y = cbox_grow(R_Eb, win, 4, dims);
   const CBox B_ero_x = cbox_grow(R_Eb, win, 6, dims);
 
-  // ---- dilation ----
-  const int dil_r = rmax + 1;  // "Safety Measure" radius + 1 (GMorpho.cu:2864)
-  const int dcap = (a.se == 1 ? rmax + 2 : dil_r + 1) < 255 ? (a.se == 1 ? rmax + 2 : dil_r + 1) : 255;
-  const uint32_t dil_cap = a.se == 1 ? (uint32_t)(rmax + 1) : (uint32_t)(dil_r * dil_r);
-  const int dil_halo = dil_r + 1;
-  const uint8_t* tile_map = nullptr;  // per-tile radius bounds of the dilation passes
-  if (a.edt != nullptr) {
-    // resident distance field: the dilation is its per-voxel threshold
-    if (a.se != 0) return cudaErrorInvalidValue;
-  } else if (a.R != nullptr && a.rmap_in != nullptr) {
-    tile_map = a.rmap_in;  // built by the caller together with the radius bound
-  } else if (a.R != nullptr) {
-    if (launch_radius_map(RF, Nx, Ny, Nz, rmap, nullptr, st, kc) != cudaSuccess) return cudaGetLastError();
-    tile_map = rmap;
-  }
-  if (a.edt != nullptr) {
-    GM_LAUNCH(kc, "k_dil_threshold", st,
-              k_dil_threshold<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.edt, a.e_sy, a.e_sz, RF, a.uniform_r, g,
-                                                                    exact ? D : Df, R_Df));
-  } else {
-    if (!a.xpass_done && launch_dil_pass_x(a.X, buf8, rx, ry, rz, dcap, B_dil_x, st, kc) != cudaSuccess)
-      return cudaGetLastError();
-    uint8_t* dst = exact ? D : Df;
-    if ((a.ypass_done || a.zpass_done) && a.se != 0) return cudaErrorInvalidValue;
-    if (dil_cap <= 32767) {
-      if (a.se == 1) {
-        launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
-                                          ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
-        launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
-                                           rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
-      } else {
-        if (!a.ypass_done)
-          launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
-                                           ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
-        if (!a.zpass_done)
-          launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF,
-                                            a.uniform_r, rx, ry, st, kc, "k_pass_dil_z", tile_map, 0,
-                                            roi_only(R_Df, 1, 1));
-      }
-    } else {
-      const int span = kTileOut + 2 * dil_halo;
-      dim3 gy(cdiv(Nx, 32), cdiv(Ny, kTileOut), Nz);
-      if (a.se == 1)
-        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CUBE, uint8_t><<<gy, dim3(32, kRows), span * 32 * 2, st>>>(
-                                             buf8, buf16a, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap));
-      else
-        GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT, uint8_t><<<gy, dim3(32, kRows), span * 32 * 2, st>>>(
-                                             buf8, buf16a, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap));
-      dim3 gz(cdiv(Nx, 32), cdiv(Nz, kTileOut), Ny / 2);
-      if (a.se == 1)
-        GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CUBE, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                           buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
-      else
-        GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
-                                           buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
+  // ---- dilation ---- (skipped when the caller has put it in D already)
+  if (!a.dilation_done) {
+    const int dil_r = rmax + 1;  // "Safety Measure" radius + 1 (GMorpho.cu:2864)
+    const int dcap = (a.se == 1 ? rmax + 2 : dil_r + 1) < 255 ? (a.se == 1 ? rmax + 2 : dil_r + 1) : 255;
+    const uint32_t dil_cap = a.se == 1 ? (uint32_t)(rmax + 1) : (uint32_t)(dil_r * dil_r);
+    const int dil_halo = dil_r + 1;
+    const uint8_t* tile_map = nullptr;  // per-tile radius bounds of the dilation passes
+    if (a.edt != nullptr) {
+      // resident distance field: the dilation is its per-voxel threshold
+      if (a.se != 0) return cudaErrorInvalidValue;
+    } else if (a.R != nullptr && a.rmap_in != nullptr) {
+      tile_map = a.rmap_in;  // built by the caller together with the radius bound
+    } else if (a.R != nullptr) {
+      if (launch_radius_map(RF, Nx, Ny, Nz, rmap, nullptr, st, kc) != cudaSuccess) return cudaGetLastError();
+      tile_map = rmap;
     }
-  }
-  if (!exact) {
-    GM_LAUNCH(kc, "k_dil_select", st, k_dil_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, Df, D, g, dr, R_D));
+    if (a.edt != nullptr) {
+      GM_LAUNCH(kc, "k_dil_threshold", st,
+                k_dil_threshold<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.edt, a.e_sy, a.e_sz, RF, a.uniform_r, g,
+                                                                      exact ? D : Df, R_Df));
+    } else {
+      if (!a.xpass_done && launch_dil_pass_x(a.X, buf8, rx, ry, rz, dcap, B_dil_x, st, kc) != cudaSuccess)
+        return cudaGetLastError();
+      uint8_t* dst = exact ? D : Df;
+      if ((a.ypass_done || a.zpass_done) && a.se != 0) return cudaErrorInvalidValue;
+      if (dil_cap <= 32767) {
+        if (a.se == 1) {
+          launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
+                                            ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
+          launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
+                                             rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
+        } else {
+          if (!a.ypass_done)
+            launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
+                                             ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
+          if (!a.zpass_done)
+            launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF,
+                                              a.uniform_r, rx, ry, st, kc, "k_pass_dil_z", tile_map, 0,
+                                              roi_only(R_Df, 1, 1));
+        }
+      } else {
+        const int span = kTileOut + 2 * dil_halo;
+        dim3 gy(cdiv(Nx, 32), cdiv(Ny, kTileOut), Nz);
+        if (a.se == 1)
+          GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_CUBE, uint8_t><<<gy, dim3(32, kRows), span * 32 * 2, st>>>(
+                                               buf8, buf16a, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap));
+        else
+          GM_LAUNCH(kc, "k_axis_pass", st, k_axis_pass<KERN_LAT, uint8_t><<<gy, dim3(32, kRows), span * 32 * 2, st>>>(
+                                               buf8, buf16a, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap));
+        dim3 gz(cdiv(Nx, 32), cdiv(Nz, kTileOut), Ny / 2);
+        if (a.se == 1)
+          GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_CUBE, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
+                                             buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
+        else
+          GM_LAUNCH(kc, "k_final_z", st, k_final_z<KERN_LAT, FIN_DIL><<<gz, dim3(32, 8), 2 * span * 32 * 2, st>>>(
+                                             buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
+      }
+    }
+    if (!exact) {
+      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, Df, D, g, dr, R_D));
+    }
   }
   // ---- occupancy map of D (erosion outputs are needed on D only) ----
   {

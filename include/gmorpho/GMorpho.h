@@ -52,6 +52,8 @@ class GMorpho {
   void Update(Mesh& mesh, const ScaleField& scale_field, const FrameField& frame_field);
   void DilateBySphereMipmap(const ScaleField& scale_field);
   void DilateByCubeMipmap(const ScaleField& scale_field);
+  // the rotated-cube dilation and the sphere erosion in one call (closing_grid())
+  void DilateByRotCubeMipmap(const ScaleField& scale_field, const FrameField& frame_field);
   void ErodeBySphereMipmap(const ScaleField& scale_field);
   void ErodeAllocation() {}
   void ExtractClosingMeshAllocation() {}
@@ -70,6 +72,7 @@ class GMorpho {
 
  private:
   void close(const ScaleField* sf, int uniform_radius, int se);
+  void close_rotcube(const ScaleField& sf, const FrameField& ff);
   void check(int status, const char* what);
 
   Voxelizer voxelizer_;

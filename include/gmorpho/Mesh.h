@@ -18,6 +18,7 @@ struct Vec3 {
 };
 typedef Vec3<float> Vec3f;
 typedef Vec3<unsigned int> Vec3ui;
+typedef Vec3<int> Vec3i;
 
 class Mesh {
  public:

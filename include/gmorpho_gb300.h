@@ -150,6 +150,55 @@ gm_status gm_close_noalloc(const gm_grid_desc* desc, const uint8_t* d_input, con
                            int32_t uniform_radius, gm_mode mode, gm_se se, uint8_t* d_closing,
                            uint8_t* d_dilation, uint8_t* d_contour, void* stream);
 
+/* ---------------------------------------------------------------- frame field */
+/* FrameField with the BiHarmonicSystem method (GMorpho/FrameField.h,
+ * FrameField.cu, FrameFieldSparseBiharmonic.cu): a quaternion per node of a
+ * res^3 lattice over [bbox_min, bbox_max] (cell size = largest extent / res),
+ * interpolating up to 20 hard-constrained rotations.  The context must
+ * outlive the field. */
+typedef struct gm_frame_field gm_frame_field;
+gm_status gm_frame_field_create(gm_ctx* ctx, const float* bbox_min, const float* bbox_max, int32_t res,
+                                gm_frame_field** out);
+gm_status gm_frame_field_destroy(gm_frame_field* ff);
+/* AddHardConstrainedPoint(position, twist) (FrameField.cu:64-77): the node
+ * floor((position - bbox_min) / cell_size) takes the rotation of rotation
+ * vector `twist` (axis * angle).  GM_ERR_CAPACITY past 20 points (the
+ * reference ignores them silently); GM_ERR_INVALID_ARGUMENT for a node
+ * outside the lattice (the reference writes out of bounds). */
+gm_status gm_frame_field_add_point(gm_frame_field* ff, const float* position, const float* twist);
+gm_status gm_frame_field_update_point(gm_frame_field* ff, int32_t i, const float* twist);
+int32_t gm_frame_field_num_points(const gm_frame_field* ff);
+gm_status gm_frame_field_get_point(const gm_frame_field* ff, int32_t i, float* grid_position, float* twist);
+/* Generate (FrameField.cu:556-575): without points every node is
+ * (0, 1, 0, 0); otherwise, per component k, (L^T L + S) q_k = b_k with L the
+ * degree-normalised 6-neighbour Laplacian (float entries as the reference
+ * builds them), S the indicator of constrained nodes and b_k their
+ * quaternions (sin(theta/2) axis, cos(theta/2)).  The reference factors the
+ * system in float (sparse Cholesky); here conjugate gradients in double
+ * until every residual is below 1e-10 |b_k|.  *iterations (may be NULL): the
+ * iterations run.  Synchronises the stream. */
+gm_status gm_frame_field_generate(gm_frame_field* ff, int32_t* iterations, void* stream);
+/* The device quaternions ((x, y, z, w) floats per node, x-fastest; the
+ * reference's quats_pong), valid until the next generate or destroy. */
+gm_status gm_frame_field_quats(const gm_frame_field* ff, const float** d_quats, int32_t* res);
+/* FrameField::RotationToTwistCayley (FrameField.cu:228-252) in double;
+ * GM_ERR_INVALID_ARGUMENT for half turns (R + I singular). */
+gm_status gm_rotation_to_twist(const float* e_x, const float* e_y, const float* e_z, float* twist);
+
+/* GMorpho::Update with use_frame_field (GMorpho/GMorpho.cu:7785-7803):
+ * DilateByRotCubeMipmap (GMorpho.cu:3058-3230, 1712-1837, 2464-2602), the
+ * dilation by cubes of half size r(p) rotated by the quaternion field
+ * interpolated at p, then ErodeBySphereMipmap as in gm_close.  d_quats:
+ * (x, y, z, w) floats per node of a quat_res^3 lattice, x-fastest, 16-byte
+ * aligned (FrameField::quats_pong, e.g. gm_frame_field_quats).  GM_REF: the
+ * reference's base pass over cells inside data_res and its conservative
+ * contour refinement; GM_EXACT: the per-voxel predicate everywhere.  The
+ * reference reads one node past the field on its top faces; those reads
+ * are clamped to the last node here. */
+gm_status gm_close_rotcube(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,
+                           int32_t uniform_radius, const float* d_quats, int32_t quat_res, gm_mode mode,
+                           uint8_t* d_closing, uint8_t* d_dilation, uint8_t* d_contour, void* stream);
+
 /* Grid::TransformToContour (GMorpho/Grid.cu:2381-2408, 1230-1327): fine
  * voxels outside the grid's set that are 6-adjacent to it; GM_REF keeps the
  * reference's restriction to cells in [1, res-2]^3 whose byte is not 0xff,

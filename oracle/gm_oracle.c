@@ -298,6 +298,93 @@ static int fine_radius(const int8_t *scale, int n, int x, int y, int z) {
   return clamp_radius(scale[fine_index(x, y, z, n)]);
 }
 
+/* The erosion half of the closing from the dilation D: contour S of D,
+ * closing_grid_.CopyVoxelsFrom (dilation_grid_) and ErodeBySphereMipmap
+ * (GMorpho.cu:7800-7803).  pyr and tag are scratch. */
+static void erode_from(const uint8_t *X, const int8_t *scale, int res,
+                       const int *data_res, int mode, const uint8_t *D,
+                       uint8_t *S, uint8_t *C, uint64_t *pyr, uint8_t *tag) {
+  const int N = 2 * res;
+  const int64_t nc = (int64_t)res * res * res;
+  if (mode == 0) {
+    /* TransformToContour (Grid.cu:2381-2408) */
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++)
+          S[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = contour_byte(D, res, x, y, z);
+    gmo_pyramid_build(S, scale, res, pyr);
+    memcpy(C, D, nc); /* closing_grid_.CopyVoxelsFrom (dilation_grid_) (GMorpho.cu:7800) */
+    /* ErodeBySphereTexMipmapBaseILP2 (GMorpho.cu:4349-4647): a cell with
+     * D != 0 and X != 0xff is cleared when its centre 2c+1 is eroded. */
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < data_res[2]; z++)
+      for (int y = 0; y < data_res[1]; y++)
+        for (int x = 0; x < data_res[0]; x++) {
+          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
+          if (D[c] == 0x00 || X[c] == 0xff) continue;
+          if (gmo_erode_query2(pyr, res, 2 * (2 * x + 1), 2 * (2 * y + 1), 2 * (2 * z + 1))) C[c] = 0;
+        }
+    /* ComputeContourBase + ErodeBySphereTexMipmapPersistentWarpILP
+     * (Grid.cu:1975-2071, GMorpho.cu:5041-5375): tagged cells become
+     * 0xff & ~eroded, not masked by D (GMorpho.cu:5353-5360). */
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++)
+          tag[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = (uint8_t)tag_base(C, res, x, y, z);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++) {
+          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
+          if (!tag[c]) continue;
+          uint8_t eroded = 0;
+          for (int k = 0; k < 8; k++) {
+            int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
+            if (gmo_erode_query2(pyr, res, 2 * fx + 1, 2 * fy + 1, 2 * fz + 1)) eroded |= (uint8_t)(1 << k);
+          }
+          C[c] = (uint8_t)(0xff & ~eroded);
+        }
+  } else {
+    /* contour over the whole grid: voxels outside D, 6-adjacent to D */
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++) {
+          uint8_t b = 0;
+          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
+          for (int k = 0; k < 8; k++) {
+            int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
+            if ((D[c] >> k) & 1) continue;
+            int adj = 0;
+            if (fx > 0 && grid_bit(D, res, fx - 1, fy, fz)) adj = 1;
+            if (fx < N - 1 && grid_bit(D, res, fx + 1, fy, fz)) adj = 1;
+            if (fy > 0 && grid_bit(D, res, fx, fy - 1, fz)) adj = 1;
+            if (fy < N - 1 && grid_bit(D, res, fx, fy + 1, fz)) adj = 1;
+            if (fz > 0 && grid_bit(D, res, fx, fy, fz - 1)) adj = 1;
+            if (fz < N - 1 && grid_bit(D, res, fx, fy, fz + 1)) adj = 1;
+            if (adj) b |= (uint8_t)(1 << k);
+          }
+          S[c] = b;
+        }
+    gmo_pyramid_build(S, scale, res, pyr);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++) {
+          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
+          uint8_t b = D[c];
+          for (int k = 0; k < 8; k++) {
+            if (!((b >> k) & 1)) continue;
+            int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
+            if (gmo_erode_query2(pyr, res, 2 * fx + 1, 2 * fy + 1, 2 * fz + 1)) b &= (uint8_t)~(1 << k);
+          }
+          C[c] = b;
+        }
+  }
+}
+
 int gmo_close(const uint8_t *X, const int8_t *scale, int res,
               const int *data_res, int mode, int se, uint8_t *Dout,
               uint8_t *Sout, uint8_t *Cout) {
@@ -347,45 +434,6 @@ int gmo_close(const uint8_t *X, const int8_t *scale, int res,
           }
           D[c] = b;
         }
-    /* TransformToContour (Grid.cu:2381-2408) */
-#pragma omp parallel for schedule(static)
-    for (int z = 0; z < res; z++)
-      for (int y = 0; y < res; y++)
-        for (int x = 0; x < res; x++)
-          S[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = contour_byte(D, res, x, y, z);
-    gmo_pyramid_build(S, scale, res, pyr);
-    memcpy(C, D, nc); /* closing_grid_.CopyVoxelsFrom (dilation_grid_) (GMorpho.cu:7800) */
-    /* ErodeBySphereTexMipmapBaseILP2 (GMorpho.cu:4349-4647): a cell with
-     * D != 0 and X != 0xff is cleared when its centre 2c+1 is eroded. */
-#pragma omp parallel for schedule(dynamic, 1)
-    for (int z = 0; z < data_res[2]; z++)
-      for (int y = 0; y < data_res[1]; y++)
-        for (int x = 0; x < data_res[0]; x++) {
-          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
-          if (D[c] == 0x00 || X[c] == 0xff) continue;
-          if (gmo_erode_query2(pyr, res, 2 * (2 * x + 1), 2 * (2 * y + 1), 2 * (2 * z + 1))) C[c] = 0;
-        }
-    /* ComputeContourBase + ErodeBySphereTexMipmapPersistentWarpILP
-     * (Grid.cu:1975-2071, GMorpho.cu:5041-5375): tagged cells become
-     * 0xff & ~eroded, not masked by D (GMorpho.cu:5353-5360). */
-#pragma omp parallel for schedule(static)
-    for (int z = 0; z < res; z++)
-      for (int y = 0; y < res; y++)
-        for (int x = 0; x < res; x++)
-          tag[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = (uint8_t)tag_base(C, res, x, y, z);
-#pragma omp parallel for schedule(dynamic, 1)
-    for (int z = 0; z < res; z++)
-      for (int y = 0; y < res; y++)
-        for (int x = 0; x < res; x++) {
-          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
-          if (!tag[c]) continue;
-          uint8_t eroded = 0;
-          for (int k = 0; k < 8; k++) {
-            int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
-            if (gmo_erode_query2(pyr, res, 2 * fx + 1, 2 * fy + 1, 2 * fz + 1)) eroded |= (uint8_t)(1 << k);
-          }
-          C[c] = (uint8_t)(0xff & ~eroded);
-        }
   } else {
     /* GM_EXACT: the reference's fine predicates at every fine voxel. */
 #pragma omp parallel for schedule(dynamic, 1)
@@ -400,42 +448,8 @@ int gmo_close(const uint8_t *X, const int8_t *scale, int res,
           }
           D[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = b;
         }
-    /* contour over the whole grid: voxels outside D, 6-adjacent to D */
-#pragma omp parallel for schedule(static)
-    for (int z = 0; z < res; z++)
-      for (int y = 0; y < res; y++)
-        for (int x = 0; x < res; x++) {
-          uint8_t b = 0;
-          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
-          for (int k = 0; k < 8; k++) {
-            int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
-            if ((D[c] >> k) & 1) continue;
-            int adj = 0;
-            if (fx > 0 && grid_bit(D, res, fx - 1, fy, fz)) adj = 1;
-            if (fx < N - 1 && grid_bit(D, res, fx + 1, fy, fz)) adj = 1;
-            if (fy > 0 && grid_bit(D, res, fx, fy - 1, fz)) adj = 1;
-            if (fy < N - 1 && grid_bit(D, res, fx, fy + 1, fz)) adj = 1;
-            if (fz > 0 && grid_bit(D, res, fx, fy, fz - 1)) adj = 1;
-            if (fz < N - 1 && grid_bit(D, res, fx, fy, fz + 1)) adj = 1;
-            if (adj) b |= (uint8_t)(1 << k);
-          }
-          S[c] = b;
-        }
-    gmo_pyramid_build(S, scale, res, pyr);
-#pragma omp parallel for schedule(dynamic, 1)
-    for (int z = 0; z < res; z++)
-      for (int y = 0; y < res; y++)
-        for (int x = 0; x < res; x++) {
-          int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
-          uint8_t b = D[c];
-          for (int k = 0; k < 8; k++) {
-            if (!((b >> k) & 1)) continue;
-            int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
-            if (gmo_erode_query2(pyr, res, 2 * fx + 1, 2 * fy + 1, 2 * fz + 1)) b &= (uint8_t)~(1 << k);
-          }
-          C[c] = b;
-        }
   }
+  erode_from(X, scale, res, data_res, mode, D, S, C, pyr, tag);
   if (Dout) memcpy(Dout, D, nc);
   if (Sout) memcpy(Sout, S, nc);
   if (Cout) memcpy(Cout, C, nc);
@@ -483,6 +497,235 @@ int gmo_close_exact_brute(const uint8_t *X, const int8_t *scale, int res, int se
         Cout[c] |= (uint8_t)(1 << ((fx & 1) | ((fy & 1) << 1) | ((fz & 1) << 2)));
       }
   free(D); free(S);
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* f2 — rotated-cube dilation under a quaternion field                 */
+/* ------------------------------------------------------------------ */
+/* The float expressions are evaluated as the reference writes them
+ * (left-to-right sums; this file is compiled with -ffp-contract=off, so
+ * no multiply-add is fused); the CUDA kernels evaluate the same operations
+ * with explicit rounding and give the same booleans. */
+
+typedef struct { float x, y, z, w; } quat_t;
+
+/* Field node i.  On its top faces the reference reads one node past the
+ * field (InterpolateQuaternionField, GMorpho.cu:1658-1667: x wraps to the
+ * next row, y to the next slice, z past the allocation); reads past the
+ * last node are clamped to it here. */
+static quat_t q_node(const float *Q, int64_t n, int64_t i) {
+  if (i > n - 1) i = n - 1;
+  quat_t q = {Q[4 * i], Q[4 * i + 1], Q[4 * i + 2], Q[4 * i + 3]};
+  return q;
+}
+
+/* (1 - t) a + t b: interpolate_cube_group with an empty group
+ * (cuda_math.h:424-430, called with group size 0 at GMorpho.cu:1733, 2515) */
+static quat_t q_lerp(quat_t a, quat_t b, float t) {
+  const float s = 1.f - t;
+  quat_t r = {s * a.x + t * b.x, s * a.y + t * b.y, s * a.z + t * b.z, s * a.w + t * b.w};
+  return r;
+}
+
+/* Hamilton product a b, terms in the order of cuda_math.h:386-393 */
+static quat_t q_mul(quat_t a, quat_t b) {
+  quat_t r;
+  r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+  r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+  r.y = a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x;
+  r.z = a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w;
+  return r;
+}
+
+/* InterpolateQuaternionField (GMorpho.cu:1631-1710) at lattice point
+ * (ix, iy, iz) of a grid of `res` points per axis, then
+ * quat = normalize (conj (quat)) and the rotated axes rotate (quat, e_k) =
+ * conj(quat) (e_k, 0) quat (GMorpho.cu:1735-1745, 2517-2527;
+ * cuda_math.h:396-401).  axes = b_x, b_y, b_z. */
+void gmo_rotcube_frame(const float *Q, int qres, int ix, int iy, int iz, int res, float *axes) {
+  const float fx = (float)qres * ((float)ix / (float)res);
+  const float fy = (float)qres * ((float)iy / (float)res);
+  const float fz = (float)qres * ((float)iz / (float)res);
+  const int jx = (int)fx, jy = (int)fy, jz = (int)fz;
+  const int64_t sy = qres, sz = (int64_t)qres * qres, n = sz * qres;
+  const int64_t b = jx + sy * jy + sz * jz;
+  const float tx = fx - (float)jx, ty = fy - (float)jy, tz = fz - (float)jz;
+  const quat_t q00 = q_lerp(q_node(Q, n, b), q_node(Q, n, b + 1), tx);
+  const quat_t q01 = q_lerp(q_node(Q, n, b + sz), q_node(Q, n, b + 1 + sz), tx);
+  const quat_t q10 = q_lerp(q_node(Q, n, b + sy), q_node(Q, n, b + 1 + sy), tx);
+  const quat_t q11 = q_lerp(q_node(Q, n, b + sy + sz), q_node(Q, n, b + 1 + sy + sz), tx);
+  quat_t q = q_lerp(q_lerp(q00, q10, ty), q_lerp(q01, q11, ty), tz);
+  q.x = -q.x;
+  q.y = -q.y;
+  q.z = -q.z;
+  const float len = sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  q.x = q.x / len;
+  q.y = q.y / len;
+  q.z = q.z / len;
+  q.w = q.w / len;
+  const quat_t qc = {-q.x, -q.y, -q.z, q.w};
+  for (int a = 0; a < 3; a++) {
+    const quat_t u = {a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f, 0.f};
+    const quat_t r = q_mul(qc, q_mul(u, q));
+    axes[3 * a] = r.x;
+    axes[3 * a + 1] = r.y;
+    axes[3 * a + 2] = r.z;
+  }
+}
+
+typedef struct {
+  float c[3];            /* structuring element centre, fine units */
+  float bx[3], by[3], bz[3];
+  float se;              /* half size (the radius) */
+} rc_query_t;
+
+/* HasRotCubeSEOverlap (GMorpho.cu:241-302, 334-349): separating-axis test
+ * of the rotated cube against the node box of centre n and half size hs,
+ * t = centre - n; false as soon as one of the 15 axes separates. */
+static int rc_overlap(const rc_query_t *q, float nx, float ny, float nz, float hs) {
+  const float tx = q->c[0] - nx, ty = q->c[1] - ny, tz = q->c[2] - nz;
+  const float *bx = q->bx, *by = q->by, *bz = q->bz;
+  const float se = q->se;
+  if (fabsf(tx) > hs + se * (fabsf(bx[0]) + fabsf(by[0]) + fabsf(bz[0]))) return 0;
+  if (fabsf(ty) > hs + se * (fabsf(bx[1]) + fabsf(by[1]) + fabsf(bz[1]))) return 0;
+  if (fabsf(tz) > hs + se * (fabsf(bx[2]) + fabsf(by[2]) + fabsf(bz[2]))) return 0;
+  if (fabsf(tx * bx[0] + ty * bx[1] + tz * bx[2]) > hs * (fabsf(bx[0]) + fabsf(bx[1]) + fabsf(bx[2])) + se) return 0;
+  if (fabsf(tx * by[0] + ty * by[1] + tz * by[2]) > hs * (fabsf(by[0]) + fabsf(by[1]) + fabsf(by[2])) + se) return 0;
+  if (fabsf(tx * bz[0] + ty * bz[1] + tz * bz[2]) > hs * (fabsf(bz[0]) + fabsf(bz[1]) + fabsf(bz[2])) + se) return 0;
+  if (fabsf(tz * bx[1] - ty * bx[2]) > hs * (fabsf(bx[2]) + fabsf(bx[1])) + se * (fabsf(bz[0]) + fabsf(by[0]))) return 0;
+  if (fabsf(tz * by[1] - ty * by[2]) > hs * (fabsf(by[2]) + fabsf(by[1])) + se * (fabsf(bz[0]) + fabsf(bx[0]))) return 0;
+  if (fabsf(tz * bz[1] - ty * bz[2]) > hs * (fabsf(bz[2]) + fabsf(bz[1])) + se * (fabsf(by[0]) + fabsf(bx[0]))) return 0;
+  if (fabsf(tx * bx[2] - tz * bx[0]) > hs * (fabsf(bx[2]) + fabsf(bx[0])) + se * (fabsf(bz[1]) + fabsf(by[1]))) return 0;
+  if (fabsf(tx * by[2] - tz * by[0]) > hs * (fabsf(by[2]) + fabsf(by[0])) + se * (fabsf(bz[1]) + fabsf(bx[1]))) return 0;
+  if (fabsf(tx * bz[2] - tz * bz[0]) > hs * (fabsf(bz[2]) + fabsf(bz[0])) + se * (fabsf(by[1]) + fabsf(bx[1]))) return 0;
+  if (fabsf(ty * bx[0] - tx * bx[1]) > hs * (fabsf(bx[1]) + fabsf(bx[0])) + se * (fabsf(bz[2]) + fabsf(by[2]))) return 0;
+  if (fabsf(ty * by[0] - tx * by[1]) > hs * (fabsf(by[1]) + fabsf(by[0])) + se * (fabsf(bz[2]) + fabsf(bx[2]))) return 0;
+  if (fabsf(ty * bz[0] - tx * bz[1]) > hs * (fabsf(bz[1]) + fabsf(bz[0])) + se * (fabsf(by[2]) + fabsf(bx[2]))) return 0;
+  return 1;
+}
+
+/* Traversal of DilateByRotCubeByTexMipmap{Base,} (GMorpho.cu:1747-1831,
+ * 2529-2583): true iff some occupied fine voxel is reached through nodes
+ * that all overlap the rotated cube. */
+static int rc_run(const uint64_t *pyr, int res, const rc_query_t *q) {
+  const int L = ilog2i(res), maxd = L + 1, max_res = 1 << maxd;
+  node_t stack[8 * 24];
+  int sp = 0;
+  stack[sp++] = (node_t){0, 0, 0, 0};
+  while (sp > 0) {
+    const node_t nd = stack[--sp];
+    const int level = L - nd.d, nl = res >> level;
+    const uint64_t tex = pyr[level_offset(res, level) + (int64_t)nd.x + (int64_t)nl * nd.y +
+                             (int64_t)nl * nl * nd.z];
+    const int occ = (int)(tex >> 56);
+    const float ncs = (float)(max_res >> (nd.d + 1));
+    for (int k = 0; k < 8; k++) {
+      if (!(occ & (1 << k))) continue;
+      const int bx = 2 * nd.x + (k & 1), by = 2 * nd.y + ((k >> 1) & 1), bz = 2 * nd.z + (k >> 2);
+      if (!rc_overlap(q, ncs * ((float)bx + 0.5f), ncs * ((float)by + 0.5f), ncs * ((float)bz + 0.5f), 0.5f * ncs))
+        continue;
+      if (nd.d + 1 == maxd) return 1;
+      stack[sp++] = (node_t){nd.d + 1, bx, by, bz};
+    }
+  }
+  return 0;
+}
+
+int gmo_rotcube_query(const uint64_t *pyr, int res, const float *Q, int qres, int px, int py, int pz,
+                      int frame_res, int cx, int cy, int cz, int radius) {
+  rc_query_t q;
+  float ax[9];
+  gmo_rotcube_frame(Q, qres, px, py, pz, frame_res, ax);
+  for (int i = 0; i < 3; i++) {
+    q.bx[i] = ax[i];
+    q.by[i] = ax[3 + i];
+    q.bz[i] = ax[6 + i];
+  }
+  q.c[0] = (float)cx;
+  q.c[1] = (float)cy;
+  q.c[2] = (float)cz;
+  q.se = (float)radius;
+  return rc_run(pyr, res, &q);
+}
+
+/* TagVoxelsContourBaseConservative (GMorpho/Grid.cu:1464-1498): c in
+ * [1, res-2]^3 whose byte differs from one of its eight diagonal
+ * neighbours c + (+-1, +-1, +-1) (the loop keeps only offsets with all
+ * three components non-zero). */
+static int tag_conservative(const uint8_t *g, int res, int x, int y, int z) {
+  if (x < 1 || y < 1 || z < 1 || x > res - 2 || y > res - 2 || z > res - 2) return 0;
+  const int64_t s1 = res, s2 = (int64_t)res * res;
+  const int64_t c = x + s1 * y + s2 * z;
+  for (int k = 0; k < 8; k++) {
+    const int64_t o = ((k & 1) ? 1 : -1) + s1 * (((k >> 1) & 1) ? 1 : -1) + s2 * ((k >> 2) ? 1 : -1);
+    if (g[c + o] != g[c]) return 1;
+  }
+  return 0;
+}
+
+/* the eight fine voxels of cell (x, y, z), each with its own frame
+ * (frame grid 2 res) and radius (GMorpho.cu:2492-2527) */
+static uint8_t rc_cell_fine(const uint64_t *pyr, int res, const float *Q, int qres, int x, int y, int z) {
+  const uint64_t tex = pyr[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z];
+  uint8_t b = 0;
+  for (int k = 0; k < 8; k++) {
+    const int fx = 2 * x + (k & 1), fy = 2 * y + ((k >> 1) & 1), fz = 2 * z + (k >> 2);
+    const int r = (int)((tex >> (7 * k)) & 0x7f);
+    if (gmo_rotcube_query(pyr, res, Q, qres, fx, fy, fz, 2 * res, fx, fy, fz, r)) b |= (uint8_t)(1 << k);
+  }
+  return b;
+}
+
+int gmo_close_rotcube(const uint8_t *X, const int8_t *scale, int res, const int *data_res, const float *Q, int qres,
+                      int mode, uint8_t *Dout, uint8_t *Sout, uint8_t *Cout) {
+  const int64_t nc = (int64_t)res * res * res;
+  uint64_t *pyr = (uint64_t *)malloc(sizeof(uint64_t) * gmo_pyramid_size(res));
+  uint8_t *D = (uint8_t *)malloc(nc), *S = (uint8_t *)malloc(nc), *C = (uint8_t *)malloc(nc);
+  uint8_t *tag = (uint8_t *)malloc(nc);
+  if (!pyr || !D || !S || !C || !tag) return -1;
+  gmo_pyramid_build(X, scale, res, pyr);
+  memcpy(D, X, nc);
+  if (mode == 0) {
+    /* DilateByRotCubeByTexMipmapBase (GMorpho.cu:1712-1837): cells inside
+     * data_res that are not full, frame at the cell (frame grid res),
+     * centre 2c, radius of child 0 */
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < data_res[2]; z++)
+      for (int y = 0; y < data_res[1]; y++)
+        for (int x = 0; x < data_res[0]; x++) {
+          const int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
+          if (X[c] == 0xff) continue;
+          const int r = (int)(pyr[c] & 0x7f);
+          if (gmo_rotcube_query(pyr, res, Q, qres, x, y, z, res, 2 * x, 2 * y, 2 * z, r)) D[c] = 0xff;
+        }
+    /* ComputeContourBaseConservative + DilateByRotCubeByTexMipmap
+     * (GMorpho.cu:3183-3224, 2464-2602): tagged cells are overwritten */
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++)
+          tag[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = (uint8_t)tag_conservative(D, res, x, y, z);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++) {
+          const int64_t c = (int64_t)x + (int64_t)res * y + (int64_t)res * res * z;
+          if (tag[c]) D[c] = rc_cell_fine(pyr, res, Q, qres, x, y, z);
+        }
+  } else {
+    /* GM_EXACT: the fine predicate at every fine voxel */
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < res; z++)
+      for (int y = 0; y < res; y++)
+        for (int x = 0; x < res; x++)
+          D[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = rc_cell_fine(pyr, res, Q, qres, x, y, z);
+  }
+  erode_from(X, scale, res, data_res, mode, D, S, C, pyr, tag);
+  if (Dout) memcpy(Dout, D, nc);
+  if (Sout) memcpy(Sout, S, nc);
+  if (Cout) memcpy(Cout, C, nc);
+  free(pyr); free(D); free(S); free(C); free(tag);
   return 0;
 }
 

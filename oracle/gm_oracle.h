@@ -74,6 +74,26 @@ int gmo_close(const uint8_t *X, const int8_t *scale, int res,
 int gmo_close_exact_brute(const uint8_t *X, const int8_t *scale, int res,
                           int se, uint8_t *C);
 
+/* f2 — rotated-cube dilation under a quaternion field Q: (x, y, z, w)
+ * floats per node of a qres^3 lattice, x-fastest (FrameField::quats_pong).
+ * gmo_rotcube_frame: the rotated axes b_x, b_y, b_z (9 floats) at lattice
+ * point i of a grid of `res` points per axis (InterpolateQuaternionField
+ * and normalize (conj (quat)), GMorpho.cu:1631-1710, 1735-1745).
+ * gmo_rotcube_query: the traversal of DilateByRotCubeByTexMipmap{Base,}
+ * with the frame at point p of a frame_res grid, centre c (fine units) and
+ * half size `radius`.
+ * gmo_close_rotcube: DilateByRotCubeMipmap then the sphere erosion
+ * (GMorpho.cu:3058-3230, 7785-7803); mode 0 GM_REF, 1 GM_EXACT (the fine
+ * predicate at every fine voxel).  Outputs may be NULL; returns 0. */
+void gmo_rotcube_frame(const float *Q, int qres, int ix, int iy, int iz,
+                       int res, float *axes);
+int gmo_rotcube_query(const uint64_t *pyr, int res, const float *Q, int qres,
+                      int px, int py, int pz, int frame_res, int cx, int cy,
+                      int cz, int radius);
+int gmo_close_rotcube(const uint8_t *X, const int8_t *scale, int res,
+                      const int *data_res, const float *Q, int qres, int mode,
+                      uint8_t *D, uint8_t *S, uint8_t *C);
+
 /* a12..a15 — contour marching cubes in the reference's emission order.
  * First call with V == NULL to get the counts.  Returns 0 on success,
  * -1 if the capacities are too small. */

@@ -60,6 +60,9 @@ def lib():
                                       C.c_int]
         L.gmo_grid_attributes.argtypes = [_f32p, C.c_int64, C.c_int, C.c_float, _f32p, _f32p, _f32p, _i32p]
         L.gmo_voxelize.argtypes = [_f32p, C.c_int64, _u32p, C.c_int64, C.c_int, _f32p, C.c_float, _u8p]
+        L.gmo_rotcube_frame.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _f32p]
+        L.gmo_rotcube_query.argtypes = [_u64p, C.c_int, _f32p, C.c_int] + [C.c_int] * 8
+        L.gmo_close_rotcube.argtypes = [_u8p, _i8p, C.c_int, _i32p, _f32p, C.c_int, C.c_int, _u8p, _u8p, _u8p]
         L.gmo_morton3.restype = C.c_uint32
         L.gmo_morton3.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
         _lib = L
@@ -99,6 +102,32 @@ def close(X, res, data_res, scale, mode=0, se=0):
                          _p(Cg, _u8p))
     assert rc == 0
     return D, S, Cg
+
+
+def close_rotcube(X, res, data_res, scale, quats, qres, mode=0):
+    """Rotated-cube dilation under the quaternion field `quats` ((qres^3, 4)
+    float32, x y z w) then the sphere erosion; returns (D, S, C)."""
+    X = _c(X, np.uint8).reshape(-1)
+    scale = _c(scale, np.int8).reshape(-1)
+    Q = _c(quats, np.float32).reshape(-1)
+    assert Q.size == 4 * qres ** 3
+    D = np.zeros(res ** 3, np.uint8)
+    S = np.zeros(res ** 3, np.uint8)
+    Cg = np.zeros(res ** 3, np.uint8)
+    dr = np.asarray(data_res, dtype=np.int32)
+    rc = lib().gmo_close_rotcube(_p(X, _u8p), _p(scale, _i8p), res, _p(dr, _i32p), _p(Q, _f32p), qres, mode,
+                                 _p(D, _u8p), _p(S, _u8p), _p(Cg, _u8p))
+    assert rc == 0
+    return D, S, Cg
+
+
+def rotcube_frame(quats, qres, i, res):
+    """The rotated axes (3, 3) = b_x, b_y, b_z at lattice point i of a grid
+    of `res` points per axis."""
+    Q = _c(quats, np.float32).reshape(-1)
+    out = np.zeros(9, np.float32)
+    lib().gmo_rotcube_frame(_p(Q, _f32p), qres, int(i[0]), int(i[1]), int(i[2]), res, _p(out, _f32p))
+    return out.reshape(3, 3)
 
 
 def close_exact_brute(X, res, scale, se=0):

@@ -1,6 +1,7 @@
 // Exercises the reference-style C++ classes over libgmorpho_gb300, the way
 // the reference viewer drives them (BroxyViewer.cpp:108-232): load a mesh,
-// set a global scale, Update, brush the scale field, Update again.
+// set a global scale, Update, brush the scale field, Update again, then the
+// asymmetric closing with and without a frame field.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -52,12 +53,31 @@ int main(int argc, char** argv) {
       const float l = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
       if (l == l && !(std::fabs(l - 1.f) < 1e-3f)) return 4;
     }
+    // frame field over the grid's box at res / 16 (BroxyViewer.cpp:141-157),
+    // first without constraints, then with one (BroxyViewer.cpp:700-713)
+    const int fres = (int)gm.res()[0] / 16;
+    ff.Init(gm.bbox_min(), gm.bbox_max(), Vec3i(fres, fres, fres), FrameField::BiHarmonicSystem);
+    ff.Generate(false, false);
     gm.set_use_frame_field(true);
-    try {
-      gm.Update(out, sf, ff);
+    Mesh rot0, rot1;
+    gm.Update(rot0, sf, ff);
+    ff.AddHardConstrainedPoint(input.P()[0], Vec3f(0.f, 0.f, 0.6f));
+    // the point is kept at its lattice node, within sqrt(3) cells of it
+    if (ff.GetNumberOfHardConstrainedPoints() != 1 ||
+        ff.GetHardConstrainedPointId(input.P()[0], 2.f * ff.cell_size()) != 0)
       return 5;
-    } catch (const GMorpho::Exception&) {
+    ff.Generate(false, true);
+    gm.Update(rot1, sf, ff);
+    printf("%zu %zu\n", rot0.T().size(), rot1.T().size());
+    try {
+      FrameField lo;
+      lo.Init(gm.bbox_min(), gm.bbox_max(), Vec3i(4, 4, 4), FrameField::LocalOptimization);
+      return 6;
+    } catch (const FrameField::Exception&) {
     }
+  } catch (const FrameField::Exception& e) {
+    fprintf(stderr, "%s\n", e.msg().c_str());
+    return 1;
   } catch (const GMorpho::Exception& e) {
     fprintf(stderr, "%s\n", e.msg().c_str());
     return 1;

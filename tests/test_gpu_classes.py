@@ -38,9 +38,10 @@ def test_cpp_classes_drive_the_pipeline(tmp_path):
     write_off(off_in, V, F)
     r = subprocess.run([exe, off_in, off_out], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    nv, t1, t2, t3 = (int(x) for x in r.stdout.split())
+    nv, t1, t2, t3, r0, r1 = (int(x) for x in r.stdout.split())
     assert nv > 0 and t1 > 0 and t2 > 0 and t3 > 0
     assert t2 != t1  # the brush changed the radius field and the mesh
+    assert r0 > 0 and r1 > 0  # frame-field closings (axis-aligned, then with a constraint)
 
 
 def test_contour_matches_oracle(gm_ctx):
