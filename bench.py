@@ -281,6 +281,11 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
             result["batch"] = run_batch(args, ctx)
         except Exception as exc:  # reported, never hides the headline line
             result["batch"] = {"error": repr(exc)[:300]}
+    if rank == 0 and not args.no_frame_field:
+        try:
+            result["frame_field"] = run_frame_field(args, ctx, X, R, res)
+        except Exception as exc:
+            result["frame_field"] = {"error": repr(exc)[:300]}
     if rank == 0 and not args.no_serve:
         import torch
         torch.cuda.empty_cache()
@@ -336,6 +341,47 @@ def run_batch(args, ctx):
             "edge_min": min(edges), "edge_max": max(edges), "fine_voxels": int(vox), "triangles": int(t_batch),
             "radius": "U{1..24}", "closing": "GM_REF sphere, 20 bilateral iterations",
             "batched_gvoxel_s": round(vox / (batch_ms * 1e-3) / 1e9, 3)}
+
+
+def run_frame_field(args, ctx, X, R, res):
+    """Frame-field workload on the same grid and radius field: a frame field
+    of (res/16)^3 nodes over the grid's box with 4 seeded hard constraints
+    (FrameField::Generate, biharmonic system), then the rotated-cube closing
+    (GMorpho::Update with use_frame_field) and its mesh with the 200
+    bilateral iterations of the asymmetric closing."""
+    import torch
+    from broxy_gb300 import api
+    qres = max(2, res // 16)
+    rng = np.random.default_rng(6000)
+    ff = api.FrameField(ctx, (0, 0, 0), (1, 1, 1), qres)
+    for _ in range(4):
+        ff.add_point(rng.uniform(0.1, 0.9, 3), rng.normal(size=3) * 0.6)
+    t0 = time.perf_counter()
+    iters = ff.generate()
+    gen_ms = (time.perf_counter() - t0) * 1e3
+    Q = ff.quats()
+    desc = api.make_desc(res, cell_size=1.0 / res)
+    out = torch.empty_like(X)
+    st = torch.cuda.current_stream()
+    ctx.close_rotcube(desc, X, Q, qres, R, 0, api.L.GM_REF, out=out)
+    ctx.mesh(desc, out, 200)
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    reps = 3
+    close_ms = mesh_ms = 0.0
+    for _ in range(reps):
+        e0.record(st)
+        ctx.close_rotcube(desc, X, Q, qres, R, 0, api.L.GM_REF, out=out)
+        e1.record(st)
+        _, _, T = ctx.mesh(desc, out, 200)
+        e2.record(st)
+        torch.cuda.synchronize()
+        close_ms += e0.elapsed_time(e1) / reps
+        mesh_ms += e1.elapsed_time(e2) / reps
+    ff.destroy()
+    vox = (2 * res) ** 3
+    return {"field_nodes": qres ** 3, "constraints": 4, "generate_ms": round(gen_ms, 2), "cg_iterations": iters,
+            "closing_ms": round(close_ms, 3), "closing_gvoxel_s": round(vox / (close_ms * 1e-3) / 1e9, 3),
+            "mesh_ms_200_bilateral": round(mesh_ms, 3), "triangles": int(T.shape[0])}
 
 
 def run_serve(args):
@@ -476,6 +522,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-grid batching comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the edit-server measurement")
+    ap.add_argument("--no-frame-field", action="store_true", help="skip the frame-field closing measurement")
     ap.add_argument("--serve-res", type=int, default=1024, help="base cells of the resident grid (1024 = 2048^3)")
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-edits", type=int, default=200)
