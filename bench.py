@@ -377,11 +377,19 @@ def run_frame_field(args, ctx, X, R, res):
         torch.cuda.synchronize()
         close_ms += e0.elapsed_time(e1) / reps
         mesh_ms += e1.elapsed_time(e2) / reps
+    # one more closing with per-kernel events (not part of the timings above)
+    ctx.profile(True)
+    ctx.profile_reset()
+    ctx.close_rotcube(desc, X, Q, qres, R, 0, api.L.GM_REF, out=out)
+    torch.cuda.synchronize()
+    prof = ctx.profile_read()
+    ctx.profile(False)
     ff.destroy()
     vox = (2 * res) ** 3
     return {"field_nodes": qres ** 3, "constraints": 4, "generate_ms": round(gen_ms, 2), "cg_iterations": iters,
             "closing_ms": round(close_ms, 3), "closing_gvoxel_s": round(vox / (close_ms * 1e-3) / 1e9, 3),
-            "mesh_ms_200_bilateral": round(mesh_ms, 3), "triangles": int(T.shape[0])}
+            "mesh_ms_200_bilateral": round(mesh_ms, 3), "triangles": int(T.shape[0]),
+            "kernels_ms": {k: round(v["ms"], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])[:8]}}
 
 
 def run_serve(args):

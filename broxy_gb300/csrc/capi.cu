@@ -409,6 +409,9 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
     size_t have = 0;
     r.D = gm::close_ws_dilation(a);
     r.scratch = gm::close_ws_scratch(a, &have);
+    r.E = gm::close_ws_field(a);
+    r.edt_workspace = ctx->ws;
+    r.rmax = rmax;
     r.num_sms = ctx->num_sms;
     if (have < gm::rotcube_scratch_bytes(res)) return fail(ctx, GM_ERR_CUDA, "gm_close_rotcube: workspace too small");
     GM_CHECK_CUDA(ctx, gm::launch_rotcube_dilation(r, st, &ctx->kc), "gm_close_rotcube");

@@ -109,6 +109,9 @@ cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cud
 // after it has started (free for work that runs before it on its stream).
 uint8_t* close_ws_dilation(const CloseArgs& a);
 uint8_t* close_ws_scratch(const CloseArgs& a, size_t* bytes);
+// the workspace's second u16 fine field (2 (2 rx)(2 ry)(2 rz) bytes), which
+// launch_edt leaves alone
+uint16_t* close_ws_field(const CloseArgs& a);
 
 // ---- rotated-cube dilation under a frame field (rotcube.cu) ----
 constexpr int kRotCubeMaxLevels = 12;  // res <= 2048
@@ -123,6 +126,13 @@ struct RotCubeArgs {
   int mode = 0;                 // 0 = GM_REF (base pass + conservative contour), 1 = GM_EXACT (every fine voxel)
   uint8_t* D = nullptr;         // dilation out, res^3
   uint8_t* scratch = nullptr;   // rotcube_scratch_bytes(res)
+  // Distance shortcuts (optional): E receives the input grid's squared
+  // lattice distance field ((2 res)^3 u16) built by launch_edt in
+  // edt_workspace (close_workspace_bytes(res); E and scratch must lie
+  // outside the parts launch_edt uses).  rmax: the largest clamped radius.
+  uint16_t* E = nullptr;
+  uint8_t* edt_workspace = nullptr;
+  int rmax = 0;
   int num_sms = 0;
 };
 size_t rotcube_scratch_bytes(int res);

@@ -1635,15 +1635,22 @@ uint8_t* close_ws_dilation(const CloseArgs& a) {
   return close_ws(a, rx, ry, rz).D;
 }
 
-// buf16a and buf16b: first written by the dilation's passes or, when the
-// dilation is done, by the erosion's x pass
+// buf16a: first written by the dilation's passes or, when the dilation is
+// done, by the erosion's x pass
 uint8_t* close_ws_scratch(const CloseArgs& a, size_t* bytes) {
   const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
   const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
   const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
   const CloseWs w = close_ws(a, rx, ry, rz);
-  if (bytes) *bytes = (size_t)(reinterpret_cast<uint8_t*>(w.buf8) - reinterpret_cast<uint8_t*>(w.buf16a));
+  if (bytes) *bytes = (size_t)(reinterpret_cast<uint8_t*>(w.buf16b) - reinterpret_cast<uint8_t*>(w.buf16a));
   return reinterpret_cast<uint8_t*>(w.buf16a);
+}
+
+uint16_t* close_ws_field(const CloseArgs& a) {
+  const int rx = a.dims[0] > 0 ? a.dims[0] : a.res;
+  const int ry = a.dims[0] > 0 ? a.dims[1] : a.res;
+  const int rz = a.dims[0] > 0 ? a.dims[2] : a.res;
+  return close_ws(a, rx, ry, rz).buf16b;
 }
 
 cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc) {

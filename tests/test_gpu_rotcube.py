@@ -88,6 +88,22 @@ def test_rotcube_ref_variable_radius(gm_ctx, res, qres):
         assert np.array_equal(g, w), name
 
 
+@pytest.mark.parametrize("uniform", [12, 24, None])
+def test_rotcube_large_radius(gm_ctx, uniform):
+    """Sparse voxels and one block with radii up to 24: the dilation covers
+    most of the grid, so most queries are decided by the distance shortcuts
+    and the rest by the warp search; D, S, C still equal the oracle's."""
+    res, qres = 64, 4
+    X = _grid(res, 9400 + (uniform or 0), density=0.0005, blocks=1)
+    Q = _field(qres, 9500)
+    sc = None if uniform else _scale(res, 9600, 2, 25)
+    got = _run(gm_ctx, res, X, Q, qres, scale=sc, uniform=uniform or 0)
+    want = _oracle(res, X, Q, qres, sc, uniform or 0, 0)
+    for g, w, name in zip(got, want, "DSC"):
+        assert np.array_equal(g, w), name
+    assert 0.1 < (want[0] == 0xFF).mean() < 0.99
+
+
 def test_rotcube_exact(gm_ctx):
     res, qres = 32, 3
     X = _grid(res, 8500)
