@@ -123,7 +123,7 @@ KERNEL_BYTES_PER_VOXEL = {
 # one ncu capture of each kernel, scaled to the 1024^3 workload by the
 # units processed (see profiles/).
 TRAFFIC = {
-    "k_bilateral": 599_000_000,     # 137.3 MB at 1.10M vertices / 2.19M triangles, x4.366
+    "k_bilateral": 338_000_000,     # 77.5 MB at 1.10M vertices / 2.19M triangles, x4.366
     "k_pass_dil_z": 3_354_000_000,  # 419.3 MB at 512^3 fine voxels, x8
 }
 
@@ -224,9 +224,10 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
     def kernel_roof(name, rec):
         per_launch_ms = rec["ms"] / rec["launches"]
         if name == "k_bilateral":
-            # per iteration: normal in + out and row pointer per vertex (16 + 16 + 4 B), the two
-            # neighbour ids and position weights per corner (8 + 8 B)
-            nbytes, model = 36 * nv + 48 * nt, "36 B/vertex + 48 B/triangle per iteration"
+            # per iteration: normal in + out, row pointer and record count per vertex
+            # (16 + 16 + 4 + 2 B), one 8-byte record per (vertex, neighbour) pair: three per
+            # triangle on a closed mesh (each edge shared by two triangles, read from both ends)
+            nbytes, model = 38 * nv + 24 * nt, "38 B/vertex + 24 B/triangle per iteration"
         elif name in KERNEL_BYTES_PER_VOXEL:
             nbytes, model = KERNEL_BYTES_PER_VOXEL[name] * V, "%.4f B/fine voxel" % KERNEL_BYTES_PER_VOXEL[name]
         else:

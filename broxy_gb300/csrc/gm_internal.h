@@ -220,8 +220,11 @@ struct MeshBuffers {
   float* N2 = nullptr;      // unused (kept for ABI-stable layout of the struct)
   float4* N4a = nullptr;    // v_cap, bilateral ping-pong (16-byte normals)
   float4* N4b = nullptr;    // v_cap
-  uint4* ent = nullptr;     // 3 * t_cap: the two other vertices of each corner and their position
-                            // terms |pa-pb|^2 / sigma_p^2 (float bits)
+  uint2* ent = nullptr;     // 6 * t_cap: filter records as built, vertex v's from 2 rowptr[v] (a
+                            // neighbour and its position term |pa-pb|^2, float bits; the sign bit
+                            // set when two incident triangles share the neighbour)
+  uint2* rec = nullptr;     // 6 * t_cap: the same records packed, vertex v's at [roff[v], roff[v+1])
+  uint32_t* roff = nullptr; // v_cap + 1
   uint32_t* T = nullptr;    // 3 * t_cap
   uint32_t* adj = nullptr;  // 3 * t_cap (vertex -> corner list)
   uint32_t* rowptr = nullptr;  // v_cap + 1

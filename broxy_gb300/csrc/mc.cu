@@ -875,7 +875,7 @@ __device__ __forceinline__ void bitonic_sort(uint32_t (&k)[M]) {
 
 // one incident corner: its triangle's normal term, and its filter record
 __device__ __forceinline__ void adj_corner(const float* __restrict__ V, const uint32_t* __restrict__ T,
-                                           uint32_t corner, const float3& pa, float3& acc, uint4* rec) {
+                                           uint32_t corner, const float3& pa, float3& acc, uint64_t* pair) {
   const uint32_t t = corner / 3, role = corner - 3 * t;
   const uint32_t i0 = T[3 * (size_t)t], i1 = T[3 * (size_t)t + 1], i2 = T[3 * (size_t)t + 2];
   const float3 p0 = ld3(V, i0), p1 = ld3(V, i1), p2 = ld3(V, i2);
@@ -885,50 +885,85 @@ __device__ __forceinline__ void adj_corner(const float* __restrict__ V, const ui
   const float ny = __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z));
   const float nz = __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x));
   acc = make_float3(__fadd_rn(acc.x, nx), __fadd_rn(acc.y, ny), __fadd_rn(acc.z, nz));
-  if (rec) {
-    // the other two vertices in the reference's order: (1, 2), (0, 2), (0, 1)
+  if (pair) {
+    // the other two vertices (reference order (1, 2), (0, 2), (0, 1)) as
+    // (vertex << 32 | position term bits)
     const uint32_t ib = role == 0 ? i1 : i0, ic = role == 2 ? i1 : i2;
     const float3 pb = role == 0 ? p1 : p0, pc = role == 2 ? p1 : p2;
-    *rec = make_uint4(ib, ic, __float_as_uint(dist2(pa, pb)), __float_as_uint(dist2(pa, pc)));
+    pair[0] = ((uint64_t)ib << 32) | __float_as_uint(dist2(pa, pb));
+    pair[1] = ((uint64_t)ic << 32) | __float_as_uint(dist2(pa, pc));
   }
+}
+
+template <int M>
+__device__ __forceinline__ void bitonic_sort64(uint64_t (&k)[M]) {
+#pragma unroll
+  for (int s = 2; s <= M; s <<= 1)
+#pragma unroll
+    for (int j = s >> 1; j > 0; j >>= 1)
+#pragma unroll
+      for (int i = 0; i < M; i++) {
+        const int l = i ^ j;
+        if (l > i) {
+          const uint64_t a = k[i], b = k[l];
+          const bool up = (i & s) == 0;
+          k[i] = up ? (a < b ? a : b) : (a < b ? b : a);
+          k[l] = up ? (a < b ? b : a) : (a < b ? a : b);
+        }
+      }
+}
+
+// The filter records of a vertex from its neighbour pairs sorted by
+// (vertex, term): one record per neighbour, or per two occurrences of it
+// (an edge shared by two incident triangles), the sign bit marking a
+// double.  Returns the number of records written.
+__device__ __forceinline__ uint32_t put_records(const uint64_t* kv, int m, uint2* rec) {
+  uint32_t w = 0;
+  int run = 0;
+  for (int i = 0; i < m; i++) {
+    if (kv[i] == ~0ull) break;
+    run = (i > 0 && (kv[i] >> 32) == (kv[i - 1] >> 32)) ? run + 1 : 0;
+    if (run & 1) continue;
+    const bool dbl = i + 1 < m && kv[i + 1] != ~0ull && (kv[i + 1] >> 32) == (kv[i] >> 32);
+    rec[w++] = make_uint2((uint32_t)(kv[i] >> 32), (uint32_t)kv[i] | (dbl ? 0x80000000u : 0u));
+  }
+  return w;
 }
 
 __global__ void __launch_bounds__(256, 3) k_adj_finish(const float* __restrict__ V, const uint32_t* __restrict__ T,
                              const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj, int64_t nv,
                              int zero_isolated, float4* __restrict__ N4, float* __restrict__ N3,
-                             uint4* __restrict__ ent) {
+                             uint2* __restrict__ ent, uint32_t* __restrict__ ncnt) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t b = rowptr[v], e = rowptr[v + 1], n = e - b;
     if (zero_isolated && n == 0) {
       N4[v] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
+      if (ent) ncnt[v] = 0;
       continue;
     }
     const float3 pa = ld3(V, (uint32_t)v);
     float3 acc = make_float3(0.f, 0.f, 0.f);
     if (v != 0 && n <= 8) {
       uint32_t key[8];
+      uint64_t kv[16];
 #pragma unroll
       for (int k = 0; k < 8; k++) key[k] = (uint32_t)k < n ? adj[b + k] : 0xffffffffu;
       bitonic_sort<8>(key);
 #pragma unroll
-      for (int k = 0; k < 8; k++)
+      for (int k = 0; k < 8; k++) {
+        kv[2 * k] = kv[2 * k + 1] = ~0ull;
         if ((uint32_t)k < n) {
           adj[b + k] = key[k];
-          adj_corner(V, T, key[k], pa, acc, ent ? ent + b + k : nullptr);
+          adj_corner(V, T, key[k], pa, acc, ent ? kv + 2 * k : nullptr);
         }
-    } else if (v != 0 && n <= 16) {
-      uint32_t key[16];
-#pragma unroll
-      for (int k = 0; k < 16; k++) key[k] = (uint32_t)k < n ? adj[b + k] : 0xffffffffu;
-      bitonic_sort<16>(key);
-#pragma unroll
-      for (int k = 0; k < 16; k++)
-        if ((uint32_t)k < n) {
-          adj[b + k] = key[k];
-          adj_corner(V, T, key[k], pa, acc, ent ? ent + b + k : nullptr);
-        }
+      }
+      if (ent) {
+        bitonic_sort64<16>(kv);
+        ncnt[v] = put_records(kv, 16, ent + 2 * (size_t)b);
+      }
     } else {
+      // rare (more than 8 incident triangles): sorted in memory
       if (v != 0)
         for (uint32_t i = b + 1; i < e; i++) {  // in place (vertex 0's row is already in order)
           const uint32_t key = adj[i];
@@ -936,7 +971,32 @@ __global__ void __launch_bounds__(256, 3) k_adj_finish(const float* __restrict__
           while (j > b && adj[j - 1] > key) { adj[j] = adj[j - 1]; j--; }
           adj[j] = key;
         }
-      for (uint32_t i = b; i < e; i++) adj_corner(V, T, adj[i], pa, acc, ent ? ent + i : nullptr);
+      // the pairs in the record slots, sorted there, then merged in place
+      uint64_t* kv = ent ? reinterpret_cast<uint64_t*>(ent + 2 * (size_t)b) : nullptr;
+      for (uint32_t i = b; i < e; i++) adj_corner(V, T, adj[i], pa, acc, kv ? kv + 2 * (i - b) : nullptr);
+      if (kv) {
+        const uint32_t m = 2 * n;
+        for (uint32_t i = 1; i < m; i++) {
+          const uint64_t x = kv[i];
+          uint32_t j = i;
+          while (j > 0 && kv[j - 1] > x) { kv[j] = kv[j - 1]; j--; }
+          kv[j] = x;
+        }
+        // merged records never overtake the pairs still to be read
+        uint32_t w = 0;
+        int run = 0;
+        uint32_t prev = 0;
+        for (uint32_t i = 0; i < m; i++) {
+          const uint64_t x = kv[i];
+          const uint32_t id = (uint32_t)(x >> 32);
+          run = (i > 0 && id == prev) ? run + 1 : 0;
+          prev = id;
+          if (run & 1) continue;
+          const bool dbl = i + 1 < m && (uint32_t)(kv[i + 1] >> 32) == id;
+          ent[2 * (size_t)b + w++] = make_uint2(id, (uint32_t)x | (dbl ? 0x80000000u : 0u));
+        }
+        ncnt[v] = w;
+      }
     }
     const float3 nn = normalize3(acc);
     N4[v] = make_float4(nn.x, nn.y, nn.z, 0.f);
@@ -944,38 +1004,56 @@ __global__ void __launch_bounds__(256, 3) k_adj_finish(const float* __restrict__
   }
 }
 
+// Packs each vertex's records (built from 2 rowptr[v], roff from the scan
+// of their counts) so that the iterations read them contiguously.
+__global__ void k_rec_pack(const uint2* __restrict__ ent, const uint32_t* __restrict__ rowptr,
+                           const uint32_t* __restrict__ roff, int64_t nv, uint2* __restrict__ rec) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const uint2* src = ent + 2 * (size_t)rowptr[v];
+    const uint32_t r0 = roff[v], n = roff[v + 1] - r0;
+    for (uint32_t i = 0; i < n; i++) rec[r0 + i] = src[i];
+  }
+}
+
 // One bilateral normal iteration (BilateralMeshFiltering{,Normalize},
-// GMorpho.cu:6539-6620): each incident triangle adds w1 n_b + w2 n_c,
-// accumulated per vertex in triangle order.  An entry holds the triangle's
-// two other vertices and their position terms (one 16-byte load).
-__global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __restrict__ rowptr,
-                            const uint4* __restrict__ ent, int64_t nv, float sn2, int zero_isolated,
+// GMorpho.cu:6539-6620): each incident triangle adds w1 n_b + w2 n_c.  A
+// neighbour shared by two incident triangles appears twice in that sum with
+// the same weight; its record (8 bytes: vertex, position term) carries the
+// doubling in the sign bit, so that each neighbour is read once.  The sum
+// runs over the neighbours in vertex order (deterministic).
+__device__ __forceinline__ float3 bilateral_sum(const float4* __restrict__ Nin, const uint2* __restrict__ rec,
+                                                uint32_t n, float4 na, float sn2) {
+  float3 acc = make_float3(0.f, 0.f, 0.f);
+  uint2 en = n ? rec[0] : make_uint2(0u, 0u);  // the next record, loaded one ahead
+  for (uint32_t i = 0; i < n; i++) {
+    const uint2 e = en;
+    if (i + 1 < n) en = rec[i + 1];
+    const float4 nb = Nin[e.x];
+    // the reference library is built with -use_fast_math (GMorpho/cuda.prf:47),
+    // so its exp and division here are the fast forms
+    float w = __expf(-__fadd_rn(__uint_as_float(e.y & 0x7fffffffu), __fdividef(dist2n(na, nb), sn2)));
+    if (e.y >> 31) w = __fadd_rn(w, w);
+    acc.x = __fadd_rn(acc.x, __fmul_rn(w, nb.x));
+    acc.y = __fadd_rn(acc.y, __fmul_rn(w, nb.y));
+    acc.z = __fadd_rn(acc.z, __fmul_rn(w, nb.z));
+  }
+  return acc;
+}
+
+__global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __restrict__ roff,
+                            const uint2* __restrict__ rec, int64_t nv, float sn2, int zero_isolated,
                             float4* __restrict__ Nout, float* __restrict__ N3) {
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
-    if (zero_isolated && rowptr[v] == rowptr[v + 1]) {
+    const uint32_t r0 = roff[v], n = roff[v + 1] - r0;
+    if (zero_isolated && n == 0) {
       Nout[v] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
       continue;
     }
-    float3 acc = make_float3(0.f, 0.f, 0.f);
-    const float4 na = Nin[v];
-    const uint32_t i0 = rowptr[v], i1 = rowptr[v + 1];
-    uint4 en = i0 < i1 ? ent[i0] : make_uint4(0u, 0u, 0u, 0u);  // the next record, loaded one entry ahead
-    for (uint32_t i = i0; i < i1; i++) {
-      const uint4 e = en;
-      if (i + 1 < i1) en = ent[i + 1];
-      const float4 nb = Nin[e.x], nc = Nin[e.y];
-      // the reference library is built with -use_fast_math (GMorpho/cuda.prf:47),
-      // so its exp and division here are the fast forms
-      const float w1 = __expf(-__fadd_rn(__uint_as_float(e.z), __fdividef(dist2n(na, nb), sn2)));
-      const float w2 = __expf(-__fadd_rn(__uint_as_float(e.w), __fdividef(dist2n(na, nc), sn2)));
-      acc.x = __fadd_rn(acc.x, __fadd_rn(__fmul_rn(w1, nb.x), __fmul_rn(w2, nc.x)));
-      acc.y = __fadd_rn(acc.y, __fadd_rn(__fmul_rn(w1, nb.y), __fmul_rn(w2, nc.y)));
-      acc.z = __fadd_rn(acc.z, __fadd_rn(__fmul_rn(w1, nb.z), __fmul_rn(w2, nc.z)));
-    }
-    const float3 n = normalize3(acc);
-    Nout[v] = make_float4(n.x, n.y, n.z, 0.f);
-    if (N3) { N3[3 * v] = n.x; N3[3 * v + 1] = n.y; N3[3 * v + 2] = n.z; }
+    const float3 acc = bilateral_sum(Nin, rec + r0, n, Nin[v], sn2);
+    const float3 nn = normalize3(acc);
+    Nout[v] = make_float4(nn.x, nn.y, nn.z, 0.f);
+    if (N3) { N3[3 * v] = nn.x; N3[3 * v + 1] = nn.y; N3[3 * v + 2] = nn.z; }
   }
 }
 
@@ -985,8 +1063,8 @@ __global__ void k_bilateral(const float4* __restrict__ Nin, const uint32_t* __re
 struct BilMesh {
   const float4* Na;       // normals of even iterations' inputs (N4a)
   float4* Nb;             // and odd (N4b)
-  const uint32_t* rowptr;
-  const uint4* ent;
+  const uint32_t* roff;
+  const uint2* rec;
   float* N3;              // final normals (last iteration)
   int zero_isolated;
 };
@@ -1005,23 +1083,13 @@ __global__ void k_bilateral_group(const BilMesh* __restrict__ meshes, const int6
     const float4* Nin = odd ? M.Nb : M.Na;
     float4* Nout = odd ? const_cast<float4*>(M.Na) : M.Nb;
     float* N3 = last ? M.N3 : nullptr;
-    const uint32_t* rowptr = M.rowptr;
-    if (M.zero_isolated && rowptr[v] == rowptr[v + 1]) {
+    const uint32_t r0 = M.roff[v], nrec = M.roff[v + 1] - r0;
+    if (M.zero_isolated && nrec == 0) {
       Nout[v] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (N3) { N3[3 * v] = 0.f; N3[3 * v + 1] = 0.f; N3[3 * v + 2] = 0.f; }
       continue;
     }
-    float3 acc = make_float3(0.f, 0.f, 0.f);
-    const float4 na = Nin[v];
-    for (uint32_t i = rowptr[v]; i < rowptr[v + 1]; i++) {
-      const uint4 e = M.ent[i];
-      const float4 nb = Nin[e.x], nc = Nin[e.y];
-      const float w1 = __expf(-__fadd_rn(__uint_as_float(e.z), __fdividef(dist2n(na, nb), sn2)));
-      const float w2 = __expf(-__fadd_rn(__uint_as_float(e.w), __fdividef(dist2n(na, nc), sn2)));
-      acc.x = __fadd_rn(acc.x, __fadd_rn(__fmul_rn(w1, nb.x), __fmul_rn(w2, nc.x)));
-      acc.y = __fadd_rn(acc.y, __fadd_rn(__fmul_rn(w1, nb.y), __fmul_rn(w2, nc.y)));
-      acc.z = __fadd_rn(acc.z, __fadd_rn(__fmul_rn(w1, nb.z), __fmul_rn(w2, nc.z)));
-    }
+    const float3 acc = bilateral_sum(Nin, M.rec + r0, nrec, Nin[v], sn2);
     const float3 nn = normalize3(acc);
     Nout[v] = make_float4(nn.x, nn.y, nn.z, 0.f);
     if (N3) { N3[3 * v] = nn.x; N3[3 * v + 1] = nn.y; N3[3 * v + 2] = nn.z; }
@@ -1039,7 +1107,7 @@ static int gs_blocks(int64_t n, int threads, int sms) {
 
 void MeshBuffers::release() {
   cudaFree(V); cudaFree(N); cudaFree(N2); cudaFree(N4a); cudaFree(N4b); cudaFree(T); cudaFree(adj);
-  cudaFree(ent); cudaFree(rowptr); cudaFree(cursor); cudaFree(cell_voff); cudaFree(brick_tot);
+  cudaFree(ent); cudaFree(rec); cudaFree(roff); cudaFree(rowptr); cudaFree(cursor); cudaFree(cell_voff); cudaFree(brick_tot);
   cudaFree(fix);
   *this = MeshBuffers();
 }
@@ -1100,9 +1168,11 @@ static cudaError_t ensure_vertex_buffers(MeshBuffers& b, int64_t nv) {
   cudaError_t e;
   if (b.v_cap < nv || b.V == nullptr) {
     cudaFree(b.V); cudaFree(b.N); cudaFree(b.N4a); cudaFree(b.N4b); cudaFree(b.rowptr); cudaFree(b.cursor);
+    cudaFree(b.roff);
     b.V = b.N = nullptr;
     b.N4a = b.N4b = nullptr;
     b.rowptr = b.cursor = nullptr;
+    b.roff = nullptr;
     b.v_cap = 0;
     const int64_t c = nv + nv / 4 + 1024;
     if ((e = cudaMalloc(&b.V, sizeof(float) * 3 * (size_t)c)) != cudaSuccess) return e;
@@ -1111,6 +1181,7 @@ static cudaError_t ensure_vertex_buffers(MeshBuffers& b, int64_t nv) {
     if ((e = cudaMalloc(&b.N4b, sizeof(float4) * (size_t)c)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.rowptr, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.cursor, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.roff, sizeof(uint32_t) * ((size_t)c + 1))) != cudaSuccess) return e;
     b.v_cap = c;
   }
   return cudaSuccess;
@@ -1119,14 +1190,15 @@ static cudaError_t ensure_vertex_buffers(MeshBuffers& b, int64_t nv) {
 static cudaError_t ensure_triangle_buffers(MeshBuffers& b, int64_t nt) {
   cudaError_t e;
   if (b.t_cap < nt || b.T == nullptr) {
-    cudaFree(b.T); cudaFree(b.adj); cudaFree(b.ent);
+    cudaFree(b.T); cudaFree(b.adj); cudaFree(b.ent); cudaFree(b.rec);
     b.T = b.adj = nullptr;
-    b.ent = nullptr;
+    b.ent = b.rec = nullptr;
     b.t_cap = 0;
     const int64_t c = nt + nt / 4 + 1024;
     if ((e = cudaMalloc(&b.T, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
     if ((e = cudaMalloc(&b.adj, sizeof(uint32_t) * 3 * (size_t)c)) != cudaSuccess) return e;
-    if ((e = cudaMalloc(&b.ent, sizeof(uint4) * 3 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.ent, sizeof(uint2) * 6 * (size_t)c)) != cudaSuccess) return e;
+    if ((e = cudaMalloc(&b.rec, sizeof(uint2) * 6 * (size_t)c)) != cudaSuccess) return e;
     b.t_cap = c;
   }
   return cudaSuccess;
@@ -1242,14 +1314,22 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   GM_LAUNCH(kc, "k_adj_finish", st,
             k_adj_finish<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.V, b.T, b.rowptr, b.adj, nv, zi, b.N4a,
                                                                   iters == 0 ? b.N : nullptr,
-                                                                  iters > 0 ? b.ent : nullptr));
+                                                                  iters > 0 ? b.ent : nullptr, b.cursor));
+  if (iters > 0) {
+    // the records packed: counts (in cursor) scanned into roff
+    GM_LAUNCH(kc, "k_scan_sums", st, k_scan_sums<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums));
+    GM_LAUNCH(kc, "k_scan_small", st, k_scan_small<<<1, 1024, 0, st>>>(sums, nchunks));
+    GM_LAUNCH(kc, "k_scan_apply", st, k_scan_apply<<<nchunks, 256, 0, st>>>(b.cursor, nv, sums, b.roff));
+    GM_LAUNCH(kc, "k_rec_pack", st,
+              k_rec_pack<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(b.ent, b.rowptr, b.roff, nv, b.rec));
+  }
   if (a.defer_filter) return cudaGetLastError();
   float4* nin = b.N4a;
   float4* nout = b.N4b;
   for (int it = 0; it < iters; it++) {
     const float sn = it < 2 ? 1e10f : 0.2f;  // GMorpho.cu:6959-6969
     GM_LAUNCH(kc, "k_bilateral", st,
-              k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.rowptr, b.ent, nv, sn * sn, zi, nout,
+              k_bilateral<<<gs_blocks(nv, 256, sms), 256, 0, st>>>(nin, b.roff, b.rec, nv, sn * sn, zi, nout,
                                                                    it == iters - 1 ? b.N : nullptr));
     float4* t = nin; nin = nout; nout = t;
   }
@@ -1268,7 +1348,7 @@ cudaError_t mesh_filter_group(MeshBuffers* const* meshes, const int64_t* nv, con
   hs[0] = 0;
   for (int i = 0; i < n; i++) {
     const MeshBuffers& b = *meshes[i];
-    hm[i] = BilMesh{b.N4a, b.N4b, b.rowptr, b.ent, b.N, zero_isolated[i]};
+    hm[i] = BilMesh{b.N4a, b.N4b, b.roff, b.rec, b.N, zero_isolated[i]};
     hs[i + 1] = hs[i] + nv[i];
   }
   const int64_t total = hs[n];
