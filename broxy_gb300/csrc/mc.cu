@@ -277,24 +277,6 @@ __device__ int brick_candidates(const uint8_t* tile, const McWin& w, int ox, int
   return (int)total;
 }
 
-// exclusive prefix sums of cnt[0..n) in place (list order), per-thread
-// contiguous chunks; returns the total
-__device__ uint32_t block_prefix_inplace(uint32_t* cnt, int n) {
-  const int per = (n + kMcThreads - 1) / kMcThreads;
-  const int b0 = threadIdx.x * per, b1 = min(n, b0 + per);
-  uint32_t sum = 0;
-  for (int j = b0; j < b1; j++) sum += cnt[j];
-  uint32_t total;
-  uint32_t run = block_scan1(sum, total);
-  for (int j = b0; j < b1; j++) {
-    const uint32_t c = cnt[j];
-    cnt[j] = run;
-    run += c;
-  }
-  __syncthreads();
-  return total;
-}
-
 __global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                           uint32_t* __restrict__ brick_tot) {
   __shared__ __align__(16) uint8_t tile[kTileCells];
@@ -412,32 +394,32 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __res
                                                           float cs, float iso) {
   __shared__ __align__(16) uint8_t tile[kTileCells];
   __shared__ uint16_t list[kCellsPerBrick];
-  __shared__ uint32_t offs[kCellsPerBrick];
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
   if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) return;
   const int nc = brick_candidates(tile, w, ox, oy, oz, list);
-  // vertices per candidate, then their offsets in Morton order
-  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
-    int lx, ly, lz;
-    local_coords(list[j], lx, ly, lz);
-    int vals[8];
-    cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, true);
-    offs[j] = m ? cell_counts(vals, m).verts : 0u;
-  }
-  __syncthreads();
-  block_prefix_inplace(offs, nc);
+  // the candidates in rounds of one per thread: a block scan of the round's
+  // vertex counts gives each its first vertex, in list (Morton) order
   const uint32_t base = brick_off[4 * blockIdx.x + 1];
-  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
-    int lx, ly, lz;
-    local_coords(list[j], lx, ly, lz);
+  uint32_t run = 0;
+  for (int j0 = 0; j0 < nc; j0 += kMcThreads) {
+    const int j = j0 + (int)threadIdx.x;
+    int lx = 0, ly = 0, lz = 0, m = 0;
     int vals[8];
-    cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, true);
+    uint32_t nvert = 0;
+    if (j < nc) {
+      local_coords(list[j], lx, ly, lz);
+      cube_values(tile, lx, ly, lz, vals);
+      m = mixed_mask(vals, true);
+      if (m) nvert = cell_counts(vals, m).verts;
+    }
+    uint32_t round_total;
+    const uint32_t pre = block_scan1(nvert, round_total);
+    const uint32_t first = base + run + pre;
+    run += round_total;
     if (!m) continue;
     const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    uint32_t vo = base + offs[j];
+    uint32_t vo = first;
     cell_voff[gidx(gx, gy, gz, gd)] = vo;
     for (int s = 0; s < 8; s++) {
       if (!((m >> s) & 1)) continue;
@@ -513,8 +495,8 @@ __device__ __forceinline__ uint32_t info_of(const int vals[8], int m) {
 }
 
 // dynamic shared memory of k_mc_triangles
-constexpr size_t kTriSmem = sizeof(uint32_t) * (kInfoE * kInfoE * kInfoE + kCellsPerBrick) +
-                            sizeof(uint16_t) * kCellsPerBrick + kTileCells;
+constexpr size_t kTriSmem = sizeof(uint32_t) * kInfoE * kInfoE * kInfoE + sizeof(uint16_t) * kCellsPerBrick +
+                            kTileCells;
 
 // Vertex offset of cube k of the cell whose summary is `info` (absent: -1),
 // with its edge-0 / edge-3 ownership.
@@ -536,22 +518,19 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
   extern __shared__ uint4 mc_smem[];
   uint8_t* tile = reinterpret_cast<uint8_t*>(mc_smem);                          // [18 * 18 rows of kTileP]
   uint32_t* info = reinterpret_cast<uint32_t*>(tile + kTileCells);              // [17^3]
-  uint32_t* offs = info + kInfoE * kInfoE * kInfoE;                             // [4096]
-  uint16_t* list = reinterpret_cast<uint16_t*>(offs + kCellsPerBrick);          // [4096]
+  uint16_t* list = reinterpret_cast<uint16_t*>(info + kInfoE * kInfoE * kInfoE);  // [4096]
   int ox, oy, oz;
   brick_origin(blockIdx.x, ox, oy, oz);
   if (!brick_live(w, ox, oy, oz) || !load_tile_mixed(C, gd, ox, oy, oz, tile)) return;
   for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) info[i] = 0u;
   const int nc = brick_candidates(tile, w, ox, oy, oz, list);
-  // summaries of the own candidates, and their triangle counts
+  // summaries of the own candidates
   for (int j = threadIdx.x; j < nc; j += blockDim.x) {
     int lx, ly, lz;
     local_coords(list[j], lx, ly, lz);
     int vals[8];
     cube_values(tile, lx, ly, lz, vals);
-    const int m = mixed_mask(vals, true);
-    info[lx + kInfoE * (ly + kInfoE * lz)] = info_of(vals, m);
-    offs[j] = (m && win_emit(w, ox + lx, oy + ly, oz + lz)) ? cell_counts(vals, m).tris : 0u;
+    info[lx + kInfoE * (ly + kInfoE * lz)] = info_of(vals, mixed_mask(vals, true));
   }
   // the neighbour layer (cells 16 along some axis)
   for (int i = threadIdx.x; i < kInfoE * kInfoE * kInfoE; i += blockDim.x) {
@@ -560,19 +539,32 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
     info[i] = cell_info(tile, lx, ly, lz, win_tag(w, ox + lx, oy + ly, oz + lz));
   }
   __syncthreads();
-  block_prefix_inplace(offs, nc);
+  // the candidates in rounds of one per thread: a block scan of the round's
+  // triangle counts gives each its first triangle, in list (Morton) order
   const uint32_t tbase = brick_off[4 * blockIdx.x + 2];
-  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
-    int lx, ly, lz;
-    local_coords(list[j], lx, ly, lz);
-    const uint32_t myinfo = info[lx + kInfoE * (ly + kInfoE * lz)];
-    const int m = (int)(myinfo & 0xffu);
-    if (!m) continue;
-    uint32_t to = tbase + offs[j];
-    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    if (!win_emit(w, gx, gy, gz)) continue;
+  uint32_t run = 0;
+  for (int j0 = 0; j0 < nc; j0 += kMcThreads) {
+    const int j = j0 + (int)threadIdx.x;
+    int lx = 0, ly = 0, lz = 0, m = 0;
     int vals[8];
-    cube_values(tile, lx, ly, lz, vals);
+    bool emit = false;
+    uint32_t ntri = 0;
+    if (j < nc) {
+      local_coords(list[j], lx, ly, lz);
+      m = (int)(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu);
+      emit = m != 0 && win_emit(w, ox + lx, oy + ly, oz + lz);
+      if (emit) {
+        cube_values(tile, lx, ly, lz, vals);
+        ntri = cell_counts(vals, m).tris;
+      }
+    }
+    uint32_t round_total;
+    const uint32_t pre = block_scan1(ntri, round_total);
+    const uint32_t first = tbase + run + pre;
+    run += round_total;
+    if (!emit) continue;
+    uint32_t to = first;
+    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
     uint32_t vo = cell_voff[gidx(gx, gy, gz, gd)];
     for (int s = 0; s < 8; s++) {
       if (!((m >> s) & 1)) continue;
