@@ -365,23 +365,6 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   gm_status s;
   const int res = desc->res;
   const int64_t fine = (int64_t)8 * res * res * res;
-  int rmax;
-  if (d_scale && rmax_known > 0) {
-    rmax = rmax_known;  // ctx->rmap and the bound built by the caller (the slab upload of gm_update)
-  } else if (d_scale) {
-    // the radius bound and the per-tile radius map in one pass over the field
-    if ((s = ensure(ctx, (void**)&ctx->rmap, ctx->rmap_bytes, (size_t)fine / 4096 + 16, "radius map")) != GM_OK)
-      return s;
-    GM_CHECK_CUDA(ctx, gm::launch_radius_map_dense(d_scale, 2 * res, 2 * res, 2 * res, ctx->rmap, ctx->d_int, st,
-                                                   &ctx->kc),
-                  "radius bound");
-    int h = 0;
-    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_int, sizeof(int), cudaMemcpyDeviceToHost, st), "radius bound");
-    GM_CHECK_CUDA(ctx, cudaStreamSynchronize(st), "radius bound");
-    rmax = h < 2 ? 2 : h;
-  } else {
-    rmax = gm::clamp_radius(uniform_radius);
-  }
   if ((s = ensure(ctx, (void**)&ctx->ws, ctx->ws_bytes, gm::close_workspace_bytes(res), "closing workspace")) != GM_OK)
     return s;
   gm::CloseArgs a;
@@ -390,7 +373,6 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   a.X = d_input;
   a.R = d_scale;
   a.uniform_r = uniform_radius;
-  a.rmax = rmax;
   a.mode = mode;
   a.se = se;
   a.C_out = d_closing;
@@ -402,6 +384,45 @@ static gm_status close_impl(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t
   a.xpass_done = xpass_done;
   a.ypass_done = ypass_done;
   a.zpass_done = zpass_done;
+  int rmax;
+  if (d_scale && rmax_known > 0) {
+    rmax = rmax_known;  // ctx->rmap and the bound built by the caller (the slab upload of gm_update)
+  } else if (d_scale) {
+    // the radius bound and the per-tile radius map in one pass over the
+    // field, on a side stream; the sphere dilation's x pass (it reads only
+    // the grid, saturated for any radius) runs meanwhile on `st`
+    if ((s = ensure(ctx, (void**)&ctx->rmap, ctx->rmap_bytes, (size_t)fine / 4096 + 16, "radius map")) != GM_OK)
+      return s;
+    a.rmap_in = ctx->rmap;
+    if (!ctx->copy_st) {
+      GM_CHECK_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_st, cudaStreamNonBlocking), "copy stream");
+      GM_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming), "copy event");
+      GM_CHECK_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_geom, cudaEventDisableTiming), "geometry event");
+    }
+    const bool overlap = se == 0 && !xpass_done && !rotcube;
+    cudaStream_t rs = overlap ? ctx->copy_st : st;
+    if (overlap) {
+      GM_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev_copy, st), "radius bound");
+      GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(rs, ctx->ev_copy, 0), "radius bound");
+    }
+    GM_CHECK_CUDA(ctx, gm::launch_radius_map_dense(d_scale, 2 * res, 2 * res, 2 * res, ctx->rmap, ctx->d_int, rs,
+                                                   &ctx->kc),
+                  "radius bound");
+    if (overlap) {
+      // (queued before the read-back below, which blocks the host)
+      GM_CHECK_CUDA(ctx, cudaEventRecord(ctx->ev_copy, rs), "radius bound");
+      GM_CHECK_CUDA(ctx, gm::launch_close_xpass(a, st, &ctx->kc), "gm_close");
+      a.xpass_done = true;
+      GM_CHECK_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_copy, 0), "radius bound");
+    }
+    int h = 0;
+    GM_CHECK_CUDA(ctx, cudaMemcpyAsync(&h, ctx->d_int, sizeof(int), cudaMemcpyDeviceToHost, rs), "radius bound");
+    GM_CHECK_CUDA(ctx, cudaStreamSynchronize(rs), "radius bound");
+    rmax = h < 2 ? 2 : h;
+  } else {
+    rmax = gm::clamp_radius(uniform_radius);
+  }
+  a.rmax = rmax;
   if (rotcube) {
     // the rotated-cube dilation into the closing's D, its scratch in the
     // part of the workspace that the erosion writes first
