@@ -104,6 +104,26 @@ def test_rotcube_large_radius(gm_ctx, uniform):
     assert 0.1 < (want[0] == 0xFF).mean() < 0.99
 
 
+@pytest.mark.parametrize("res,uniform", [(16, 3), (64, 75)])
+def test_rotcube_smallest_grid_and_huge_radius(gm_ctx, res, uniform):
+    """res 16 (four pyramid levels); and radius 75 around one corner block:
+    the distance field saturates below the miss bound (3 x 76^2), so every
+    query beyond the radius is searched."""
+    qres = 2
+    if uniform > 64:
+        X = np.zeros((res, res, res), np.uint8)
+        X[2:5, 3:6, 2:4] = 0xFF
+        X = X.reshape(-1)
+    else:
+        X = _grid(res, 9700 + res, density=0.002, blocks=1)
+    Q = _field(qres, 9800)
+    got = _run(gm_ctx, res, X, Q, qres, uniform=uniform)
+    want = _oracle(res, X, Q, qres, None, uniform, 0)
+    for g, w, name in zip(got, want, "DSC"):
+        assert np.array_equal(g, w), name
+    assert 0 < (want[0] == 0xFF).mean() < 1
+
+
 def test_rotcube_exact(gm_ctx):
     res, qres = 32, 3
     X = _grid(res, 8500)
