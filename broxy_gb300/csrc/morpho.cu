@@ -1660,7 +1660,7 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   if (rx % 16 != 0 || ry % 16 != 0 || rz % 16 != 0 || rx <= 0 || ry <= 0 || rz <= 0) return cudaErrorInvalidValue;
   const Dims g{rx, ry, rz};
   const int Nx = 2 * rx, Ny = 2 * ry, Nz = 2 * rz;
-  const size_t V = (size_t)Nx * Ny * Nz, cells = (size_t)rx * ry * rz;
+  const size_t cells = (size_t)rx * ry * rz;
   const CloseWs w = close_ws(a, rx, ry, rz);
   uint16_t* buf16a = w.buf16a;
   uint16_t* buf16b = w.buf16b;
