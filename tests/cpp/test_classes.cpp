@@ -2,8 +2,11 @@
 // the reference viewer drives them (BroxyViewer.cpp:108-232): load a mesh,
 // set a global scale, Update, brush the scale field, Update again, then the
 // asymmetric closing with and without a frame field.
+#include <cuda_runtime.h>
+
 #include <cmath>
 #include <cstdio>
+#include <string>
 #include <cstdlib>
 #include <vector>
 
@@ -13,7 +16,7 @@ using namespace MorphoGraphics;
 
 int main(int argc, char** argv) {
   if (argc < 3) {
-    fprintf(stderr, "usage: %s in.off out.off\n", argv[0]);
+    fprintf(stderr, "usage: %s in.off out.off [dump_dir]\n", argv[0]);
     return 2;
   }
   Mesh input;
@@ -69,6 +72,31 @@ int main(int argc, char** argv) {
     ff.Generate(false, true);
     gm.Update(rot1, sf, ff);
     printf("%zu %zu\n", rot0.T().size(), rot1.T().size());
+    // the frame-field closing's inputs and result, for a parity check
+    // against the CPU oracle (argv[3]: a directory)
+    if (argc > 3) {
+      const std::string dir = argv[3];
+      const size_t cells = (size_t)gm.res()[0] * gm.res()[1] * gm.res()[2];
+      auto dump = [&](const std::string& name, const void* dev, size_t bytes) {
+        std::vector<unsigned char> h(bytes);
+        if (cudaMemcpy(h.data(), dev, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) return false;
+        FILE* f = fopen((dir + "/" + name).c_str(), "wb");
+        if (!f) return false;
+        fwrite(h.data(), 1, bytes, f);
+        fclose(f);
+        return true;
+      };
+      const size_t fr = (size_t)ff.res()[0] * ff.res()[1] * ff.res()[2];
+      if (!dump("input.bin", gm.input_grid().grid_gpu().voxels, cells) ||
+          !dump("closing.bin", gm.closing_grid().grid_gpu().voxels, cells) ||
+          !dump("scale.bin", sf.scale_grid(), 8 * cells) || !dump("quats.bin", ff.quats_pong(), 16 * fr))
+        return 7;
+      FILE* f = fopen((dir + "/meta.txt").c_str(), "w");
+      if (!f) return 7;
+      fprintf(f, "%u %u %u %u %d\n", gm.res()[0], gm.input_grid().data_res()[0], gm.input_grid().data_res()[1],
+              gm.input_grid().data_res()[2], ff.res()[0]);
+      fclose(f);
+    }
     try {
       FrameField lo;
       lo.Init(gm.bbox_min(), gm.bbox_max(), Vec3i(4, 4, 4), FrameField::LocalOptimization);

@@ -29,19 +29,28 @@ def test_cpp_classes_drive_the_pipeline(tmp_path):
     build()
     exe = str(tmp_path / "test_classes")
     libdir = os.path.dirname(L.LIB_PATH)
-    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"),
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I/usr/local/cuda/include",
                     os.path.join(ROOT, "tests", "cpp", "test_classes.cpp"), "-o", exe,
                     "-L", libdir, "-lgmorpho_gb300", "-Wl,-rpath," + libdir,
                     "-L/usr/local/cuda/lib64", "-lcudart"], check=True)
     V, F = synth.spheres_mesh(seed=1000, count=8, level=2)
     off_in, off_out = str(tmp_path / "in.off"), str(tmp_path / "out.off")
     write_off(off_in, V, F)
-    r = subprocess.run([exe, off_in, off_out], capture_output=True, text=True)
+    r = subprocess.run([exe, off_in, off_out, str(tmp_path)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     nv, t1, t2, t3, r0, r1 = (int(x) for x in r.stdout.split())
     assert nv > 0 and t1 > 0 and t2 > 0 and t3 > 0
     assert t2 != t1  # the brush changed the radius field and the mesh
     assert r0 > 0 and r1 > 0  # frame-field closings (axis-aligned, then with a constraint)
+    # the frame-field closing of the class path against the CPU oracle
+    from oracle import oracle as O
+    res, dx, dy, dz, qres = (int(v) for v in open(tmp_path / "meta.txt").read().split())
+    X = np.fromfile(tmp_path / "input.bin", np.uint8)
+    Cg = np.fromfile(tmp_path / "closing.bin", np.uint8)
+    R = np.fromfile(tmp_path / "scale.bin", np.int8)
+    Q = np.fromfile(tmp_path / "quats.bin", np.float32).reshape(-1, 4)
+    _, _, Co = O.close_rotcube(X, res, [dx, dy, dz], R, Q, qres, 0)
+    assert np.array_equal(Cg, Co)
 
 
 def test_contour_matches_oracle(gm_ctx):

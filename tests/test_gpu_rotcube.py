@@ -211,6 +211,27 @@ def test_frame_field_matches_oracle(gm_ctx, qres, npts):
     ff.destroy()
 
 
+def test_frame_field_same_node_last_wins(gm_ctx):
+    """Two constraints on one lattice node: S is set once and b takes the
+    later point's quaternion (FrameFieldSparseBiharmonic.cu:353-364,
+    481-507), on a box that is not the unit cube."""
+    import torch
+    lo, hi, qres = (-2.0, 1.0, 0.5), (2.0, 3.0, 4.0), 10
+    pts = [((0.1, 2.0, 2.0), (0.3, 0.0, 0.0)), ((1.5, 1.2, 3.5), (0.0, 0.8, 0.0)),
+           ((0.15, 2.05, 2.02), (0.0, 0.0, -1.1))]
+    g0 = F.lattice_position(pts[0][0], lo, hi, qres)
+    assert g0 == F.lattice_position(pts[2][0], lo, hi, qres)
+    ff = api.FrameField(gm_ctx, lo, hi, qres)
+    for pos, tw in pts:
+        ff.add_point(pos, tw)
+    ff.generate()
+    got = ff.quats().cpu().numpy()
+    torch.cuda.synchronize()
+    want = F.generate(qres, lo, hi, pts)
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+    ff.destroy()
+
+
 def test_frame_field_defaults_and_limits(gm_ctx):
     ff = api.FrameField(gm_ctx, (-1, -1, -1), (1, 1, 1), 6)
     with pytest.raises(L.GMError):
