@@ -119,6 +119,18 @@ KERNEL_BYTES_PER_VOXEL = {
 }
 
 
+# What limits each kernel, from its ncu capture (profiles/): the min-plus
+# passes are bound by the integer ALU pipe of their packed DPX taps, not by
+# HBM, so their HBM fraction is low by construction.
+LIMITER = {
+    "k_pass_dil_z": "integer ALU pipe (packed DPX min-plus taps, up to 2 (r + 2) per output); DRAM traffic = algorithmic",
+    "k_pass_dil_y": "integer ALU pipe (packed DPX min-plus taps)",
+    "k_pass_ero_y": "integer ALU pipe (packed DPX min-plus taps)",
+    "k_pass_ero_z": "integer ALU pipe (packed DPX min-plus taps)",
+    "k_bilateral": "HBM (gathers of neighbour normals and records)",
+}
+
+
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # one ncu capture of each kernel, scaled to the 1024^3 workload by the
 # units processed (see profiles/).
@@ -241,7 +253,7 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
         ach = nbytes / (per_launch_ms * 1e-3) / 1e9
         return {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": TRAFFIC.get(name) if res == RES else None,
-                "algorithmic_bytes_per_launch": int(nbytes), "bytes_model": model,
+                "algorithmic_bytes_per_launch": int(nbytes), "bytes_model": model, "limiter": LIMITER.get(name),
                 "per_launch_ms": round(per_launch_ms, 4)}
 
     if top[0] is not None:
