@@ -19,6 +19,21 @@
 
 namespace gm {
 
+cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> set;  // (kernel, device) -> limit set
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& have = set[{kernel, dev}];
+  if (have >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) have = bytes;
+  return e;
+}
+
 cudaEvent_t KernelCounter::start(cudaStream_t st) {
   cudaEvent_t e;
   if (!pool.empty()) {

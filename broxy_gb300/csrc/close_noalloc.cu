@@ -15,8 +15,6 @@
 // loads the library holds this array until the process exits.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "../../include/gmorpho_gb300.h"
 #include "gm_common.cuh"
 #include "gm_internal.h"
@@ -24,36 +22,32 @@
 namespace {
 
 constexpr size_t kStaticScratchBytes = (size_t)16 << 20;
-constexpr size_t kRmaxSlotBytes = 256;  // radius-bound reduction result, then the closing workspace
+// Layout of the array: the radius bound (one int), the 16^3-block radius
+// map of a radius field, then the closing workspace.
+constexpr size_t kRmaxSlotBytes = 256;
 
 __device__ __align__(256) uint8_t g_close_scratch[kStaticScratchBytes];
 
-// The array's name is only a host-side stand-in: host code must use the
-// device address obtained from cudaGetSymbolAddress, looked up once per
-// device with that device current.
-std::mutex g_setup_mu;
-constexpr int kMaxDevices = 64;
-uint8_t* g_scratch_addr[kMaxDevices] = {};
-int g_num_sms[kMaxDevices] = {};
+size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+size_t rmap_slot_bytes(int res) { return round256((size_t)8 * res * res * res / 4096 + 16); }
 
+// The array's name is only a host-side stand-in: host code must use the
+// device address that cudaGetSymbolAddress gives for the current device and
+// context.  It is looked up on every call (the lookup allocates nothing), so
+// that a device reset or another context made current on the same device
+// never leaves a stale address behind.
 cudaError_t scratch_for_current_device(uint8_t** out, int* sms) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (g_scratch_addr[dev] == nullptr) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_close_scratch);
-    if (e != cudaSuccess) return e;
-    int n = 0;
-    e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = static_cast<uint8_t*>(p);
-    g_num_sms[dev] = n;
-  }
-  *out = g_scratch_addr[dev];
-  *sms = g_num_sms[dev];
+  void* p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_close_scratch);
+  if (e != cudaSuccess) return e;
+  int n = 0;
+  e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  *out = static_cast<uint8_t*>(p);
+  *sms = n;
   return cudaSuccess;
 }
 
@@ -72,7 +66,8 @@ extern "C" gm_status gm_close_noalloc(const gm_grid_desc* desc, const uint8_t* d
     return GM_ERR_INVALID_ARGUMENT;
   if ((mode != GM_REF && mode != GM_EXACT) || (se != GM_SE_SPHERE && se != GM_SE_CUBE)) return GM_ERR_INVALID_ARGUMENT;
   const int res = desc->res;
-  if (kRmaxSlotBytes + gm::close_workspace_bytes(res) > kStaticScratchBytes) return GM_ERR_CAPACITY;
+  const size_t ws_offset = kRmaxSlotBytes + rmap_slot_bytes(res);
+  if (ws_offset + gm::close_workspace_bytes(res) > kStaticScratchBytes) return GM_ERR_CAPACITY;
 
   cudaStream_t st = (cudaStream_t)stream;
   uint8_t* scratch = nullptr;
@@ -81,17 +76,23 @@ extern "C" gm_status gm_close_noalloc(const gm_grid_desc* desc, const uint8_t* d
     cudaGetLastError();
     return GM_ERR_CUDA;
   }
+  gm::CloseArgs a;
   int rmax = gm::clamp_radius(uniform_radius);
   if (d_scale) {
-    int* d_rmax = reinterpret_cast<int*>(scratch);  // cleared by launch_rmax before use
-    const int64_t fine = (int64_t)8 * res * res * res;
-    if (gm::launch_rmax(d_scale, fine, d_rmax, sms, st, nullptr) != cudaSuccess) return GM_ERR_CUDA;
+    // One pass over the field gives the tile radius map that the dilation
+    // reads and the radius bound; the host needs the bound to size the
+    // passes, so this waits for the stream (no stream capture is possible
+    // with a radius field).
+    int* d_rmax = reinterpret_cast<int*>(scratch);  // cleared by the map's launch
+    uint8_t* d_rmap = scratch + kRmaxSlotBytes;
+    if (gm::launch_radius_map_dense(d_scale, 2 * res, 2 * res, 2 * res, d_rmap, d_rmax, st, nullptr) != cudaSuccess)
+      return GM_ERR_CUDA;
     int h = 0;
     if (cudaMemcpyAsync(&h, d_rmax, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return GM_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return GM_ERR_CUDA;
-    rmax = h;
+    rmax = h < 2 ? 2 : h;
+    a.rmap_in = d_rmap;
   }
-  gm::CloseArgs a;
   a.res = res;
   for (int i = 0; i < 3; i++) a.data_res[i] = desc->data_res[i];
   a.X = d_input;
@@ -103,7 +104,7 @@ extern "C" gm_status gm_close_noalloc(const gm_grid_desc* desc, const uint8_t* d
   a.C_out = d_closing;
   a.D_out = d_dilation;
   a.S_out = d_contour;
-  a.workspace = scratch + kRmaxSlotBytes;  // every field is written before it is read
+  a.workspace = scratch + ws_offset;  // every field is written before it is read
   a.num_sms = sms;
   return gm::launch_close(a, st, nullptr) == cudaSuccess ? GM_OK : GM_ERR_CUDA;
 }

@@ -33,6 +33,12 @@ struct KernelCounter {
   void release();  // destroys the event pool
 };
 
+// Raises `kernel`'s dynamic shared memory limit to at least `bytes` on the
+// current device.  The attribute is per device, so the record of what was
+// set is kept per (kernel, device); safe to call from several host threads.
+// Needed only above the default 48 KB.
+cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes);
+
 // JSON {"name": {"launches": n, "ms": t}, ...} of the counter's totals;
 // returns the bytes needed (with the terminating zero), copies when cap allows
 int64_t profile_json(KernelCounter& kc, char* buf, int64_t cap);

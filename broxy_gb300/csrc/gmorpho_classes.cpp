@@ -433,6 +433,7 @@ void GMorpho::Load(const float* P, const float* N, int nv, const unsigned int* T
   dilation_grid_.CopyVoxelsFrom(input_grid_);
   closing_grid_.Init(g.bbox_min(), g.bbox_max(), g.res(), g.data_res(), g.cell_size());
   closing_grid_.CopyVoxelsFrom(dilation_grid_);
+  bbox_ = BoundingBox(g.bbox_min(), g.bbox_max());
   if (!ctx_) {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -491,6 +492,14 @@ void GMorpho::DilateBySphereMipmap(float se_size) {
   close(nullptr, (int)std::floor(2.f * se_size / cell_size()), GM_SE_SPHERE);
 }
 void GMorpho::ErodeBySphereMipmap(float) {}
+
+void GMorpho::ErodeByBVH(float se_size) {
+  if (!ctx_) throw Exception("Load must come first");
+  gm_grid_desc d = desc_of(input_grid_);
+  check(gm_erode_bvh(ctx_, &d, input_grid_.grid_gpu().voxels, dilation_grid_.grid_gpu().voxels,
+                     (int32_t)std::floor(2.f * se_size / cell_size()), closing_grid_.grid_gpu().voxels, nullptr),
+        "gm_erode_bvh");
+}
 
 void GMorpho::ExtractClosingMesh() { ExtractClosingMesh(morpho_mesh_, 20); }
 

@@ -1271,11 +1271,7 @@ cudaError_t mesh_emit(const MeshArgs& a, MeshBuffers& b, int64_t nv, int64_t nt,
   cudaMemsetAsync(b.fix, 0, sizeof(uint32_t), st);
   GM_LAUNCH(kc, "k_mc_vertices", st, k_mc_vertices<<<nb, kMcThreads, 0, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.V, a.bbox_min[0], a.bbox_min[1],
                                            a.bbox_min[2], cs, a.isovalue));
-  static bool tri_smem_set = false;  // > 48 KB of dynamic shared memory
-  if (!tri_smem_set) {
-    cudaFuncSetAttribute(k_mc_triangles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTriSmem);
-    tri_smem_set = true;
-  }
+  ensure_dynamic_smem(reinterpret_cast<const void*>(k_mc_triangles), kTriSmem);
   GM_LAUNCH(kc, "k_mc_triangles", st, k_mc_triangles<<<nb, kMcThreads, kTriSmem, st>>>(a.C, gd, w, b.brick_tot, b.cell_voff, b.T, (uint32_t)nt, b.fix,
                                             b.fix_cap));
   GM_LAUNCH(kc, "k_mc_fix91", st, k_mc_fix91<<<1, 256, 0, st>>>(b.fix, b.fix_cap, b.T));

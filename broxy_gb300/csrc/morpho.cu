@@ -1101,11 +1101,7 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
                        KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0,
                        NeedMap need = NeedMap{nullptr, 0, 0, 0, 0, 0, 0, 0, 0, CBox{{0, 0, 0}, {1 << 30, 1 << 30, 1 << 30}}}) {
   const size_t smem = dpx_smem_bytes(sub, halo);
-  static size_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    cudaFuncSetAttribute(k_pass_dpx<G, TIn, FIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = smem;
-  }
+  ensure_dynamic_smem(reinterpret_cast<const void*>(k_pass_dpx<G, TIn, FIN>), smem);
   const int na = axis == 1 ? ny : nz;
   const int n3 = axis == 1 ? nz : ny;
   const int nout = sub ? na / 2 : na;
@@ -1781,21 +1777,13 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     const size_t smem = sizeof(uint32_t) * (4 * (size_t)W + 4 * (size_t)Nx + 4 * (size_t)rx + 8 * (size_t)Nx);
     if (W <= 64) {
       const size_t smem_w = kEroXWarps * ero_x_w_warp_bytes(rx);
-      static size_t ero_xw_configured = 0;
-      if (smem_w > 48 * 1024 && smem_w > ero_xw_configured) {
-        cudaFuncSetAttribute(k_ero_pass_x_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w);
-        ero_xw_configured = smem_w;
-      }
+      ensure_dynamic_smem(reinterpret_cast<const void*>(k_ero_pass_x_w), smem_w);
       const unsigned blocks = (unsigned)(((int64_t)ry * rz + kEroXWarps - 1) / kEroXWarps);
       GM_LAUNCH(kc, "k_ero_pass_x", st,
                 k_ero_pass_x_w<<<blocks, 32 * kEroXWarps, smem_w, st>>>(S, RF, a.uniform_r, rx, ry, rz, ehalo, K,
                                                                         buf16a, HL1, B_ero_x));
     } else {
-      static size_t ero_x_configured = 0;
-      if (smem > 48 * 1024 && smem > ero_x_configured) {
-        cudaFuncSetAttribute(k_ero_pass_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        ero_x_configured = smem;
-      }
+      ensure_dynamic_smem(reinterpret_cast<const void*>(k_ero_pass_x), smem);
       GM_LAUNCH(kc, "k_ero_pass_x", st,
                 k_ero_pass_x<<<dim3(ry, rz), 256, smem, st>>>(S, RF, a.uniform_r, rx, ry, ehalo, K, buf16a, HL1,
                                                               B_ero_x));

@@ -4,6 +4,7 @@
 #pragma once
 #include <string>
 
+#include "BoundingVolume.h"
 #include "FrameField.h"
 #include "Grid.h"
 #include "Mesh.h"
@@ -25,9 +26,13 @@ class GMorpho {
     std::string msg_;
   };
 
+  typedef MorphoGraphics::AxisAlignedBoundingBox BoundingBox;
+
   GMorpho();
   virtual ~GMorpho();
 
+  // the grid's box after Load (GMorpho.h:63)
+  const BoundingBox& bbox() const { return bbox_; }
   const Vec3f& bbox_min() const { return input_grid_.bbox_min(); }
   const Vec3f& bbox_max() const { return input_grid_.bbox_max(); }
   const Vec3ui& res() const { return input_grid_.res(); }
@@ -40,8 +45,10 @@ class GMorpho {
   bool use_frame_field() { return use_frame_field_; }
   void set_bilateral_filtering(bool v) { bilateral_filtering_ = v; }
   Mesh get_morpho_mesh() { return morpho_mesh_; }
-  // The reference exposes its 4V-byte splat map here; this library does not
-  // build one (it keeps one vertex offset per cell instead).
+  // The reference exposes its internal 4V-byte splat map here (scratch of
+  // its mesh extraction, GMorpho.cu:6787-6834, read by nothing outside
+  // GMorpho); this library does not build one (it keeps one vertex offset
+  // per cell instead), so there is no such buffer: nullptr.
   unsigned int* grid_2x2x2_uint() { return nullptr; }
   // GM_REF (default) reproduces the reference grids; GM_EXACT = 1 gives the
   // pure ball closing.
@@ -64,6 +71,9 @@ class GMorpho {
   void ErodeBySphereMipmap(float se_size);
   void ExtractClosingMesh();
   void ExtractClosingMesh(Mesh& mesh, int num_bilateral_iters = 20);
+  // erosion of the last dilation by a BVH over its contour, uniform radius
+  // floor(2 se_size / cell_size) (GMorpho.cu:9308-9401), into closing_grid()
+  void ErodeByBVH(float se_size);
 
   // device grids of the last update (packed 2x2x2 bytes)
   const Grid& input_grid() const { return input_grid_; }
@@ -76,6 +86,7 @@ class GMorpho {
   void check(int status, const char* what);
 
   Voxelizer voxelizer_;
+  BoundingBox bbox_;
   float se_size_ = 0.f;
   bool use_asymmetric_closing_ = false;
   bool use_frame_field_ = false;

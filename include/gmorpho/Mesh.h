@@ -3,6 +3,7 @@
 // uses: positions, normals, triangles.
 #pragma once
 #include <cstdio>
+#include <ostream>
 #include <string>
 #include <vector>
 
@@ -16,6 +17,26 @@ struct Vec3 {
   T& operator[](int i) { return v[i]; }
   const T& operator[](int i) const { return v[i]; }
 };
+template <typename T>
+inline Vec3<T> operator*(T s, const Vec3<T>& a) {
+  return Vec3<T>(s * a[0], s * a[1], s * a[2]);
+}
+template <typename T>
+inline Vec3<T> operator*(const Vec3<T>& a, T s) {
+  return s * a;
+}
+template <typename T>
+inline Vec3<T> operator+(const Vec3<T>& a, const Vec3<T>& b) {
+  return Vec3<T>(a[0] + b[0], a[1] + b[1], a[2] + b[2]);
+}
+template <typename T>
+inline Vec3<T> operator-(const Vec3<T>& a, const Vec3<T>& b) {
+  return Vec3<T>(a[0] - b[0], a[1] - b[1], a[2] - b[2]);
+}
+template <typename T>
+inline std::ostream& operator<<(std::ostream& os, const Vec3<T>& a) {
+  return os << a[0] << " " << a[1] << " " << a[2];
+}
 typedef Vec3<float> Vec3f;
 typedef Vec3<unsigned int> Vec3ui;
 typedef Vec3<int> Vec3i;

@@ -141,9 +141,13 @@ gm_status gm_close(gm_ctx* ctx, const gm_grid_desc* desc, const uint8_t* d_input
  * Allocates nothing: its scratch is a fixed 16 MiB array held by the library
  * on every GPU that loads it (until exit), so res <= 64 (128^3 fine voxels);
  * larger grids return GM_ERR_CAPACITY.  Inputs and outputs are the caller's,
- * as for gm_close, on the current device.  The first call on a device looks
- * up that array's device address (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the one array: calls that
+ * as for gm_close, on the current device.  Every call looks up that array's
+ * device address for the current device and context (cudaGetSymbolAddress,
+ * which allocates nothing), so a device reset or a context switch between
+ * calls is safe.  With a radius field (d_scale != NULL) the call reads the
+ * field's radius bound back to the host and so waits for `stream` to drain
+ * up to that point; with a uniform radius it only enqueues work.  All calls
+ * share the one array and each leaves its contents behind: calls that
  * overlap on the GPU (other streams, other threads) race on it.  No context,
  * no kernel counter, no error message beyond the status. */
 gm_status gm_close_noalloc(const gm_grid_desc* desc, const uint8_t* d_input, const int8_t* d_scale,

@@ -68,3 +68,36 @@ def test_contour_matches_oracle(gm_ctx):
         torch.cuda.synchronize()
         assert np.array_equal(out.cpu().numpy(), S)
         assert np.array_equal(inplace.cpu().numpy(), S)
+
+
+def test_viewer_calls_compile_and_run(tmp_path, gm_ctx):
+    """The reference viewer's own call forms (gmorpho.bbox().min(),
+    2u * gmorpho.res(), Vec3i from res / 16, streaming a Vec3i, the closing
+    toggles and base scale steps) compile against include/gmorpho/ and run;
+    GMorpho::ErodeByBVH equals the C ABI's gm_erode_bvh on the same grids."""
+    import torch
+    from __graft_entry__ import build
+    from broxy_gb300 import api
+    build()
+    exe = str(tmp_path / "test_viewer_calls")
+    libdir = os.path.dirname(L.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I/usr/local/cuda/include",
+                    os.path.join(ROOT, "tests", "cpp", "test_viewer_calls.cpp"), "-o", exe,
+                    "-L", libdir, "-lgmorpho_gb300", "-Wl,-rpath," + libdir,
+                    "-L/usr/local/cuda/lib64", "-lcudart"], check=True)
+    V, F = synth.spheres_mesh(seed=1001, count=8, level=2)
+    off_in = str(tmp_path / "in.off")
+    write_off(off_in, V, F)
+    r = subprocess.run([exe, off_in, str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    last = r.stdout.strip().splitlines()[-1].split()
+    t_asym, t_sym, t_up, t_down, res, radius, no_map, dx, dy, dz = (int(v) for v in last)
+    assert min(t_asym, t_sym, t_up, t_down) > 0 and no_map == 1
+    assert t_down == t_sym or t_up != t_sym  # the scale steps changed the closing
+    X = np.fromfile(tmp_path / "input.bin", np.uint8)
+    D = np.fromfile(tmp_path / "dilation.bin", np.uint8)
+    Cb = np.fromfile(tmp_path / "bvh_closing.bin", np.uint8)
+    desc = api.make_desc(res, data_res=(dx, dy, dz))
+    Cg = gm_ctx.erode_bvh(desc, torch.as_tensor(X).cuda(), torch.as_tensor(D).cuda(), radius)
+    torch.cuda.synchronize()
+    assert np.array_equal(Cg.cpu().numpy(), Cb)

@@ -77,6 +77,28 @@ def test_normals_match_oracle(gm_ctx, iters):
     np.testing.assert_allclose(N, No, atol=NORMAL_ATOL, rtol=0)
 
 
+def test_normals_are_deterministic(gm_ctx):
+    """Normals and bilateral filtering sum in a fixed order (per-vertex
+    gathers, not the reference's float atomics, GMorpho.cu:6498-6620): two
+    runs on the same grid, and a run in another context, give the same bits."""
+    from broxy_gb300 import api
+    res = 64
+    X = synth.random_grid(res, 131)
+    _, _, Cg = O.close(X, res, [res] * 3, O.scale_grid(res, uniform=4), 0, 0)
+    runs = [_mesh(gm_ctx, res, Cg, 20) for _ in range(2)]
+    other = api.Context(0)
+    try:
+        runs.append(_mesh(other, res, Cg, 20))
+    finally:
+        other.close_ctx()
+    V0, N0, T0, _ = runs[0]
+    assert len(T0) > 1000
+    for V, N, T, _ in runs[1:]:
+        assert np.array_equal(T, T0)
+        assert V.tobytes() == V0.tobytes()
+        assert N.tobytes() == N0.tobytes()
+
+
 @pytest.mark.parametrize("iters", [0, 20])
 def test_border_solid_matches_oracle(gm_ctx, iters):
     # A solid cut by the grid border: cubes of border cells are never
