@@ -301,9 +301,17 @@ static int fine_radius(const int8_t *scale, int n, int x, int y, int z) {
 /* The erosion half of the closing from the dilation D: contour S of D,
  * closing_grid_.CopyVoxelsFrom (dilation_grid_) and ErodeBySphereMipmap
  * (GMorpho.cu:7800-7803).  pyr and tag are scratch. */
+static int64_t count_nonzero(const uint8_t *a, int64_t n) {
+  int64_t k = 0;
+#pragma omp parallel for reduction(+ : k) schedule(static)
+  for (int64_t i = 0; i < n; i++) k += a[i] != 0;
+  return k;
+}
+
 static void erode_from(const uint8_t *X, const int8_t *scale, int res,
                        const int *data_res, int mode, const uint8_t *D,
-                       uint8_t *S, uint8_t *C, uint64_t *pyr, uint8_t *tag) {
+                       uint8_t *S, uint8_t *C, uint64_t *pyr, uint8_t *tag,
+                       int64_t *erosion_list) {
   const int N = 2 * res;
   const int64_t nc = (int64_t)res * res * res;
   if (mode == 0) {
@@ -333,6 +341,7 @@ static void erode_from(const uint8_t *X, const int8_t *scale, int res,
       for (int y = 0; y < res; y++)
         for (int x = 0; x < res; x++)
           tag[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = (uint8_t)tag_base(C, res, x, y, z);
+    if (erosion_list) *erosion_list = count_nonzero(tag, nc);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int z = 0; z < res; z++)
       for (int y = 0; y < res; y++)
@@ -385,9 +394,9 @@ static void erode_from(const uint8_t *X, const int8_t *scale, int res,
   }
 }
 
-int gmo_close(const uint8_t *X, const int8_t *scale, int res,
-              const int *data_res, int mode, int se, uint8_t *Dout,
-              uint8_t *Sout, uint8_t *Cout) {
+int gmo_close_lists(const uint8_t *X, const int8_t *scale, int res,
+                    const int *data_res, int mode, int se, uint8_t *Dout,
+                    uint8_t *Sout, uint8_t *Cout, int64_t *lists) {
   const int N = 2 * res;
   const int64_t nc = (int64_t)res * res * res;
   const int64_t npyr = gmo_pyramid_size(res);
@@ -420,6 +429,7 @@ int gmo_close(const uint8_t *X, const int8_t *scale, int res,
       for (int y = 0; y < res; y++)
         for (int x = 0; x < res; x++)
           tag[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = (uint8_t)tag_tight(D, res, x, y, z);
+    if (lists) lists[0] = count_nonzero(tag, nc);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int z = 0; z < res; z++)
       for (int y = 0; y < res; y++)
@@ -449,12 +459,18 @@ int gmo_close(const uint8_t *X, const int8_t *scale, int res,
           D[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = b;
         }
   }
-  erode_from(X, scale, res, data_res, mode, D, S, C, pyr, tag);
+  erode_from(X, scale, res, data_res, mode, D, S, C, pyr, tag, lists ? &lists[1] : NULL);
   if (Dout) memcpy(Dout, D, nc);
   if (Sout) memcpy(Sout, S, nc);
   if (Cout) memcpy(Cout, C, nc);
   free(pyr); free(D); free(S); free(C); free(tag);
   return 0;
+}
+
+int gmo_close(const uint8_t *X, const int8_t *scale, int res,
+              const int *data_res, int mode, int se, uint8_t *Dout,
+              uint8_t *Sout, uint8_t *Cout) {
+  return gmo_close_lists(X, scale, res, data_res, mode, se, Dout, Sout, Cout, NULL);
 }
 
 int gmo_close_exact_brute(const uint8_t *X, const int8_t *scale, int res, int se,
@@ -721,7 +737,7 @@ int gmo_close_rotcube(const uint8_t *X, const int8_t *scale, int res, const int 
         for (int x = 0; x < res; x++)
           D[(int64_t)x + (int64_t)res * y + (int64_t)res * res * z] = rc_cell_fine(pyr, res, Q, qres, x, y, z);
   }
-  erode_from(X, scale, res, data_res, mode, D, S, C, pyr, tag);
+  erode_from(X, scale, res, data_res, mode, D, S, C, pyr, tag, NULL);
   if (Dout) memcpy(Dout, D, nc);
   if (Sout) memcpy(Sout, S, nc);
   if (Cout) memcpy(Cout, C, nc);

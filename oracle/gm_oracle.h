@@ -69,6 +69,15 @@ int gmo_close(const uint8_t *X, const int8_t *scale, int res,
               const int *data_res, int mode, int se,
               uint8_t *D, uint8_t *S, uint8_t *C);
 
+/* gmo_close, also giving the sizes of the reference's two refinement
+ * lists in GM_REF: lists[0] = cells tagged by ComputeContourBaseTight on
+ * the base dilation (the fine dilation's work list, GMorpho.cu:3573-3590),
+ * lists[1] = cells tagged by ComputeContourBase on the base erosion (the
+ * persistent erosion kernel's work list, GMorpho.cu:6661-6688). */
+int gmo_close_lists(const uint8_t *X, const int8_t *scale, int res,
+                    const int *data_res, int mode, int se,
+                    uint8_t *D, uint8_t *S, uint8_t *C, int64_t *lists);
+
 /* Pure brute-force ball closing (no pyramid, no two-level structure):
  * the GM_EXACT definition evaluated by exhaustive search.  Small grids only. */
 int gmo_close_exact_brute(const uint8_t *X, const int8_t *scale, int res,

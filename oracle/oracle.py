@@ -52,6 +52,7 @@ def lib():
         L.gmo_dilate_query_brute.argtypes = [_u8p, _i8p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.gmo_erode_query2_brute.argtypes = [_u8p, _i8p, C.c_int, C.c_int, C.c_int, C.c_int]
         L.gmo_close.argtypes = [_u8p, _i8p, C.c_int, _i32p, C.c_int, C.c_int, _u8p, _u8p, _u8p]
+        L.gmo_close_lists.argtypes = [_u8p, _i8p, C.c_int, _i32p, C.c_int, C.c_int, _u8p, _u8p, _u8p, _i64p]
         L.gmo_close_exact_brute.argtypes = [_u8p, _i8p, C.c_int, C.c_int, _u8p]
         L.gmo_mc.argtypes = [_u8p, C.c_int, _f32p, C.c_float, C.c_float, _f32p, C.c_int64, _u32p, C.c_int64,
                              _i64p, _i64p]
@@ -102,6 +103,23 @@ def close(X, res, data_res, scale, mode=0, se=0):
                          _p(Cg, _u8p))
     assert rc == 0
     return D, S, Cg
+
+
+def close_lists(X, res, data_res, scale, se=0):
+    """GM_REF closing; returns (D, S, C, (tight dilation list size, base
+    erosion list size)): the work lists of the reference's refinement
+    kernels."""
+    X = _c(X, np.uint8).reshape(-1)
+    scale = _c(scale, np.int8).reshape(-1)
+    D = np.zeros(res ** 3, np.uint8)
+    S = np.zeros(res ** 3, np.uint8)
+    Cg = np.zeros(res ** 3, np.uint8)
+    lists = np.zeros(2, np.int64)
+    dr = np.asarray(data_res, dtype=np.int32)
+    rc = lib().gmo_close_lists(_p(X, _u8p), _p(scale, _i8p), res, _p(dr, _i32p), 0, se, _p(D, _u8p), _p(S, _u8p),
+                               _p(Cg, _u8p), _p(lists, _i64p))
+    assert rc == 0
+    return D, S, Cg, (int(lists[0]), int(lists[1]))
 
 
 def close_rotcube(X, res, data_res, scale, quats, qres, mode=0):
