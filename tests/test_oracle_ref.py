@@ -1,0 +1,149 @@
+"""The reference GMorpho itself, compiled from its own CUDA sources for this
+GPU (oracle/_ref/libgmref.so, recipe oracle/refbuild/build_ref.py), run
+through GMorpho::Update on seeded inputs: its grids must equal the CPU
+oracle's byte for byte, and so must this library's.  This pins the oracle
+(and through it every other parity test) to the reference's own outputs.
+
+The reference runs in a child process (oracle/refbuild/run_ref.py), built
+with the adaptations listed in oracle/refbuild/build_ref.py.  Every input is
+checked with the oracle before the reference runs, so that
+the reference kernels stay inside their buffers and barriers:
+  * the persistent erosion kernel's first pass reads 1600 entries of its
+    cell list (100 blocks x 128 threads / 8, GMorpho.cu:5061-5065,
+    6674-6688), so the list must hold at least 1600 cells; a multiple of 4
+    cells also gives every warp the same number of passes;
+  * the fine dilation kernel returns threads past its list before a block
+    barrier (GMorpho.cu:2940-2942, 3044-3051): a list of a multiple of 16
+    cells fills every launched block or none;
+  * the marching-cubes buffers are fixed (MAX_NUM_MCM_CELLS, MAX_V_SIZE,
+    MAX_T_SIZE, GMorpho.h:39-41): 8 x contour cells <= 1.6M, vertices <= 1M,
+    triangles <= 2M, and the contour is not empty.
+Grids are at most 128^3 fine voxels, so the reference's 64-entry traversal
+stacks cannot overflow (7 pushes per level below the root, 7 levels).
+
+Meshes: identical triangle arrays except the slot after a case-91 cube,
+which the reference's extra triangle and the next cube's first triangle
+write concurrently (MarchingCubesMesher.cu:1487-1497): those rows may hold
+either; vertices within 1e-6 relative; normals within 2e-3 (the reference
+sums them with float atomics).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from broxy_gb300 import _lib as L
+from broxy_gb300 import api, synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+# (name, input kind, res, uniform radius (0: radius field), radius field span, se, data_res, seed)
+CASES = [
+    ("random32_r4_sphere", "random", 32, 4, 0, 0, [32, 32, 32], 101),
+    ("random32_field_sphere", "random", 32, 0, 6, 0, [32, 32, 32], 212),
+    ("blob64_r6_sphere", "blob", 64, 6, 0, 0, [64, 64, 64], 355),
+    ("blob64_field_sphere", "blob", 64, 0, 10, 0, [64, 64, 64], 439),
+    ("random32_r3_cube", "random", 32, 3, 0, 1, [32, 32, 32], 520),
+    ("blob64_r5_datares", "blob", 64, 5, 0, 0, [60, 52, 64], 624),
+    ("blob64_field_cube", "blob", 64, 0, 8, 1, [64, 64, 64], 762),
+]
+
+
+def _reference_library():
+    from oracle.refbuild import build_ref
+    if not build_ref.available():
+        pytest.skip("reference sources not staged (oracle/_ref/src): built only where the reference is present")
+    return build_ref.build()
+
+
+def _run_reference(tmp_path, X, R, res, data_res, se, cap_v, cap_t):
+    """The reference's Update on one input, in a child process (a fault of
+    the reference code would otherwise end the test session)."""
+    import subprocess
+    import sys
+    _reference_library()
+    inp, out = str(tmp_path / "ref_in.npz"), str(tmp_path / "ref_out.npz")
+    np.savez(inp, X=X, R=R, res=res, data_res=np.asarray(data_res, np.int32), se=se, cap_v=cap_v, cap_t=cap_t)
+    script = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "refbuild",
+                          "run_ref.py")
+    p = subprocess.run([sys.executable, script, inp, out], capture_output=True, text=True, timeout=600)
+    assert os.path.exists(out), p.stdout[-2000:] + p.stderr[-2000:]
+    r = np.load(out)
+    assert int(r["rc"]) == 0, str(r["err"]) + "\n" + p.stdout[-3000:]
+    return r
+
+
+def _mcm_cells(Cg, res):
+    d = synth.unpack_dense(Cg, res)
+    N = 2 * res
+    s = sum(d[z:N - 1 + z, y:N - 1 + y, x:N - 1 + x].astype(np.int32)
+            for z in (0, 1) for y in (0, 1) for x in (0, 1))
+    mixed = (s > 0) & (s < 8)
+    m = np.zeros((res, res, res), bool)
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                sub = mixed[dz::2, dy::2, dx::2][:res, :res, :res]
+                m[:sub.shape[0], :sub.shape[1], :sub.shape[2]] |= sub
+    return int(m[1:res - 1, 1:res - 1, 1:res - 1].sum())
+
+
+def _cases_91(Cg, res):
+    """Number of fine cubes of case 91 (the case whose triangle table holds
+    one more triangle than its count)."""
+    d = synth.unpack_dense(Cg, res).astype(np.int32)
+    N = 2 * res
+    corner = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    v = sum(d[z:N - 1 + z, y:N - 1 + y, x:N - 1 + x] << k for k, (x, y, z) in enumerate(corner))
+    return int((v == 91).sum())
+
+
+def _inputs(kind, res, uniform, span, seed):
+    X = synth.random_grid(res, seed) if kind == "random" else synth.blob_grid(res, seed, count=40)
+    R = synth.radius_field(res, seed, base=2, span=span) if uniform == 0 else O.scale_grid(res, uniform=uniform)
+    return X, np.ascontiguousarray(R, dtype=np.int8)
+
+
+@pytest.mark.parametrize("name,kind,res,uniform,span,se,data_res,seed", CASES, ids=[c[0] for c in CASES])
+def test_reference_build_equals_oracle_and_gpu(gm_ctx, tmp_path, name, kind, res, uniform, span, se, data_res, seed):
+    import torch
+    X, R = _inputs(kind, res, uniform, span, seed)
+    D, S, Cg, (l_dil, l_ero) = O.close_lists(X, res, data_res, R, se)
+    Vo, To = O.mc(Cg, res, np.zeros(3, np.float32), 1.0 / res)
+    cells = _mcm_cells(Cg, res)
+    # the input keeps the reference kernels inside their buffers (module docstring)
+    assert l_ero >= 1600 and l_ero % 4 == 0, (l_dil, l_ero)
+    assert l_dil % 16 == 0, (l_dil, l_ero)
+    assert 0 < cells and 8 * cells <= 1_600_000 and len(Vo) <= 1_000_000 and len(To) <= 2_000_000
+    assert res <= 64
+    r = _run_reference(tmp_path, X, R, res, data_res, se, len(Vo) + 16, len(To) + 16)
+    rD, rS, rC, rV, rN, rT = r["D"], r["S"], r["C"], r["V"], r["N"], r["T"]
+    # grids: the reference against the oracle
+    assert np.array_equal(rD, D), int((rD != D).sum())
+    assert np.array_equal(rS, S), int((rS != S).sum())
+    assert np.array_equal(rC, Cg), int((rC != Cg).sum())
+    assert (int(r["nv"]), int(r["nt"])) == (len(Vo), len(To))
+    # mesh: the reference against the oracle
+    iters = 200 if se == 1 else 20  # GMorpho::Update's bilateral iterations (GMorpho.cu:7808-7811)
+    n91 = _cases_91(Cg, res)
+    bad = np.nonzero((rT != To).any(axis=1))[0]
+    assert len(bad) <= n91, (len(bad), n91)
+    np.testing.assert_allclose(rV, Vo, rtol=1e-6, atol=0)
+    No = O.normals(Vo, To, iters)
+    np.testing.assert_allclose(rN, No, atol=2e-3, rtol=0, equal_nan=True)
+    # and this library's CUDA path against the reference
+    desc = api.make_desc(res, data_res=data_res, cell_size=1.0 / res)
+    Xd = torch.as_tensor(X).cuda()
+    Rd = torch.as_tensor(R).cuda() if uniform == 0 else None
+    gD, gS = torch.empty_like(Xd), torch.empty_like(Xd)
+    gC = gm_ctx.close(desc, Xd, Rd, uniform, L.GM_REF, se, D=gD, S=gS)
+    gV, gN, gT = gm_ctx.mesh(desc, gC, iters)
+    torch.cuda.synchronize()
+    assert np.array_equal(gD.cpu().numpy(), rD)
+    assert np.array_equal(gS.cpu().numpy(), rS)
+    assert np.array_equal(gC.cpu().numpy(), rC)
+    bad = np.nonzero((gT.cpu().numpy() != rT).any(axis=1))[0]
+    assert len(bad) <= n91, (len(bad), n91)
+    np.testing.assert_allclose(gV.cpu().numpy(), rV, rtol=1e-6, atol=0)
+    np.testing.assert_allclose(gN.cpu().numpy(), rN, atol=2e-3, rtol=0, equal_nan=True)
