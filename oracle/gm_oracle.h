@@ -7,12 +7,16 @@
  * against it.  Only the test-suite, __graft_entry__.smoke() and the CPU
  * baseline leg of bench.py load it.  The product never calls it.
  *
- * Parity status: the reference ships no tests, golden vectors or fixtures
- * for this path and cannot be built on this machine (OpenGL/Qt/Eigen and a
- * compute_52 target), so this restatement is "parity unpinned" against the
- * reference binary.  It is pinned instead against a second, independent
- * transliteration of the reference's float traversal kernels
- * (tests/golden/gen_golden.py) on small grids.
+ * Parity status: pinned to the reference itself.  The reference ships no
+ * tests, golden vectors or fixtures for this path; its own CUDA morphology
+ * and meshing sources are compiled for the GPU (oracle/refbuild/, output in
+ * oracle/_ref/) and run through GMorpho::Update on seeded inputs, and its
+ * dilation, contour and closing grids equal this restatement's byte for
+ * byte, its meshes triangle for triangle (tests/test_oracle_ref.py).  A
+ * second, independent transliteration of the reference's float traversal
+ * kernels (tests/golden/gen_golden.py) checks it on small grids on the CPU.
+ * The frame-field solver (oracle/framefield.py) is the exception: it is not
+ * part of the reference build, so its parity stays unpinned.
  *
  * Layouts (same as the reference):
  *   grid   : uint8[res^3], byte c = cx + res*cy + res*res*cz packs the 2x2x2

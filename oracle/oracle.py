@@ -2,9 +2,10 @@
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
 CPU baseline leg of bench.py, never by the product package.  See gm_oracle.h
-for what each function restates and its parity status ("parity unpinned"
-against the reference binary, pinned against a float transliteration of the
-reference traversal kernels).
+for what each function restates and its parity status (pinned to the
+reference GMorpho built from its own sources, tests/test_oracle_ref.py, and
+to a float transliteration of the reference traversal kernels on small
+grids).
 """
 import ctypes as C
 import os
