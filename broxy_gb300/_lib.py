@@ -76,6 +76,7 @@ PROTOTYPES = {
     "gm_ctx_destroy": (C.c_int, [_P]),
     "gm_ctx_last_error": (C.c_char_p, [_P]),
     "gm_ctx_kernel_launches": (C.c_longlong, [_P]),
+    "gm_kernel_error_flags": (C.c_int, [C.POINTER(C.c_uint32), C.c_int32]),
     "gm_ctx_profile": (C.c_int, [_P, C.c_int32]),
     "gm_ctx_profile_reset": (C.c_int, [_P]),
     "gm_ctx_profile_read": (C.c_int64, [_P, C.c_char_p, C.c_int64]),

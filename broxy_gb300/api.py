@@ -28,6 +28,14 @@ class DevicePtrArray:
                                          "version": 3, "strides": None}
 
 
+def kernel_error_flags(clear=False):
+    """Error bits this library's kernels recorded on the current device
+    (bit 0: a TMA tile load not complete within its poll limit)."""
+    f = C.c_uint32(0)
+    L.check(None, L.load().gm_kernel_error_flags(C.byref(f), 1 if clear else 0))
+    return int(f.value)
+
+
 def make_desc(res, data_res=None, bbox_min=(0.0, 0.0, 0.0), cell_size=None):
     d = L.GridDesc()
     cs = cell_size if cell_size is not None else 1.0 / res

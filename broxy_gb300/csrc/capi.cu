@@ -15,6 +15,7 @@
 
 #include "../../include/gmorpho_gb300.h"
 #include "gm_common.cuh"
+#include "tma.cuh"
 #include "gm_internal.h"
 
 namespace gm {
@@ -220,6 +221,7 @@ gm_status gm_ctx_create(int device, gm_ctx** out) {
   if (cudaSetDevice(device) != cudaSuccess) { delete c; return GM_ERR_CUDA; }
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (cudaMalloc(&c->d_int, 16 * sizeof(int)) != cudaSuccess) { delete c; return GM_ERR_OUT_OF_MEMORY; }
+  gm::tma_init();
   *out = c;
   return GM_OK;
 }
@@ -252,6 +254,17 @@ gm_status gm_ctx_destroy(gm_ctx* ctx) {
 const char* gm_ctx_last_error(const gm_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "NULL context"; }
 
 long long gm_ctx_kernel_launches(const gm_ctx* ctx) { return ctx ? ctx->kc.launches : -1; }
+
+gm_status gm_kernel_error_flags(uint32_t* flags, int32_t clear) {
+  if (!flags) return GM_ERR_INVALID_ARGUMENT;
+  unsigned int f = 0;
+  if (cudaDeviceSynchronize() != cudaSuccess || gm::kernel_error_flags(&f, clear != 0) != cudaSuccess) {
+    cudaGetLastError();
+    return GM_ERR_CUDA;
+  }
+  *flags = f;
+  return GM_OK;
+}
 
 gm_status gm_ctx_profile(gm_ctx* ctx, int32_t enable) {
   if (!ctx) return GM_ERR_INVALID_ARGUMENT;

@@ -39,6 +39,10 @@ struct KernelCounter {
 // Needed only above the default 48 KB.
 cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes);
 
+// The error bits kernels of this library recorded on the current device
+// (kErrTmaTimeout: a TMA tile wait ran out of polls), cleared when `clear`.
+cudaError_t kernel_error_flags(unsigned int* flags, bool clear);
+
 // JSON {"name": {"launches": n, "ms": t}, ...} of the counter's totals;
 // returns the bytes needed (with the terminating zero), copies when cap allows
 int64_t profile_json(KernelCounter& kc, char* buf, int64_t cap);

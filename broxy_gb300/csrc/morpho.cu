@@ -22,10 +22,20 @@
 // refinement of contour cells only) is then applied exactly by the select
 // kernels, which reproduces the reference grids bit for bit (GM_REF), or
 // skipped (GM_EXACT).
+#include <cudaTypedefs.h>
+#include <string.h>
+
+#include <mutex>
+
 #include "gm_common.cuh"
 #include "gm_internal.h"
+#include "tma.cuh"
 
 namespace gm {
+
+// Error bits recorded by kernels (kErrTmaTimeout, ...); read and cleared by
+// kernel_error_flags().
+__device__ unsigned int g_kernel_errors = 0;
 
 // A radius field read in place: element (x, y, z) at p[x + y sy + z sz]
 // (a whole field, or a crop of a larger one without copying it).
@@ -780,9 +790,14 @@ __device__ __forceinline__ uint32_t load_pair(const TIn* p, uint32_t capp) {
   return __vminu2(v, capp);  // both lanes saturated at cap
 }
 
+// TMA tiles arrive in chunks of kDpxChunk rows; each third-axis slice of
+// the tile gets span + kDpxChunk rows so that the last chunk's overrun stays
+// inside its own slice.
+constexpr int kDpxChunk = 16;
+
 size_t dpx_smem_bytes(int sub, int halo) {
   const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
-  return (size_t)2 * span * 32 * sizeof(uint32_t);
+  return (size_t)2 * (span + kDpxChunk) * 32 * sizeof(uint32_t) + 128;  // + alignment slack
 }
 
 // Where a pass's outputs are needed: tiles whose cells, grown by (gx, ga,
@@ -861,13 +876,18 @@ __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, i
   return clamp_radius(rt_s);
 }
 
+// With use_tma, the u16 input tile is staged by TMA (tmap: boxes of 64
+// columns x kDpxChunk rows x 1 slice along (x, pass axis, third axis)).
 template <int G, typename TIn, int FIN>
 __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
                                                   int sub, int halo, uint32_t cap, RField R,
                                                   int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
-                                                  int rext, NeedMap need) {
-  extern __shared__ uint32_t tileu[];
+                                                  int rext, NeedMap need, const __grid_constant__ CUtensorMap tmap,
+                                                  int use_tma) {
+  extern __shared__ uint32_t tile_raw[];
+  uint32_t* tileu = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(tile_raw) + 127) & ~(uintptr_t)127);
+  __shared__ uint64_t tma_bar;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tpar = w >> 2, grp = w & 3;
   const int x = blockIdx.x * kDpxCols + 2 * lane;
@@ -897,15 +917,43 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   const bool needed = tile_needed(need, axis, sub, o0, nout);
   const int skip = needed ? halo - halo_e : span;  // tile rows never read
   const uint32_t capp = cap | (cap << 16);
-  uint32_t* tile = tileu + tpar * span * 32;
+  const int tile_rows = span + kDpxChunk;
+  uint32_t* tile = tileu + tpar * tile_rows * 32;
   const bool colok = x < nx && third < n3;
   int finite = 0;
   constexpr bool kTileMin = G == KERN_CEN2 || G == KERN_LAT2 || (G == KERN_LAT && FIN == 1);
   uint32_t vmin = 0xffffffffu;  // smallest loaded value (both lanes)
+  // TMA staging (u16 inputs): rows [skip, span - skip) of both slices, in
+  // chunks of kDpxChunk rows issued by one thread; rows past the field come
+  // back as zeros and are set to the saturation value below.
+  const int nchunks = sizeof(TIn) == 2 && use_tma && span - 2 * skip > 0
+                          ? (span - 2 * skip + kDpxChunk - 1) / kDpxChunk : 0;  // block-uniform
+  if (nchunks > 0) {
+    if (threadIdx.x == 0) {
+      tma_prefetch_map(&tmap);
+      mbar_init(&tma_bar, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_arrive_expect_tx(&tma_bar, (uint32_t)(2 * nchunks * kDpxChunk * kDpxCols * sizeof(uint16_t)));
+      const int x0 = blockIdx.x * kDpxCols, t0 = 2 * ((int)blockIdx.z + need.third0);
+      for (int tp = 0; tp < 2; tp++)
+        for (int c = 0; c < nchunks; c++) {
+          const int r0 = skip + kDpxChunk * c;
+          uint32_t* dst = tileu + (tp * tile_rows + r0) * 32;
+          if (axis == 1)
+            tma_load_3d(dst, &tmap, x0, lo + r0, t0 + tp, &tma_bar);
+          else
+            tma_load_3d(dst, &tmap, x0, t0 + tp, lo + r0, &tma_bar);
+        }
+    }
+    if (!mbar_wait_bounded(&tma_bar, 0, 1u << 22)) atomicOr(&g_kernel_errors, kErrTmaTimeout);
+  }
   for (int s = skip + grp; s < span - skip; s += 4) {
     const int a = lo + s;
     uint32_t v = capp;
-    if (colok && a >= 0 && a < na) v = load_pair<G, TIn>(in + x + sa * a + s3 * third, capp);
+    if (colok && a >= 0 && a < na)
+      v = nchunks > 0 ? __vminu2(tile[s * 32 + lane], capp) : load_pair<G, TIn>(in + x + sa * a + s3 * third, capp);
     tile[s * 32 + lane] = v;
     finite |= v != capp;
     if (kTileMin) vmin = __vminu2(vmin, v);
@@ -1107,9 +1155,60 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   const int nout = sub ? na / 2 : na;
   dim3 g((nx + kDpxCols - 1) / kDpxCols, need.out_n > 0 ? need.out_n : (nout + kDpxOut - 1) / kDpxOut,
          need.third_n > 0 ? need.third_n : (n3 + 1) / 2);
+  // u16 tiles go through TMA when the field's rows are whole 64-column boxes
+  CUtensorMap tmap;
+  memset(&tmap, 0, sizeof(tmap));
+  int use_tma = 0;
+  if (sizeof(TIn) == 2 && nx % kDpxCols == 0 && na >= kDpxChunk && (reinterpret_cast<uintptr_t>(in) & 15) == 0)
+    use_tma = encode_tensor_map_3d(&tmap, in, 2, nx, ny, nz, kDpxCols, axis == 1 ? kDpxChunk : 1,
+                                   axis == 1 ? 1 : kDpxChunk)
+                  ? 1
+                  : 0;
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
-                                                          uniform_r, rx, ry, rmap, rext, need));
+                                                          uniform_r, rx, ry, rmap, rext, need, tmap, use_tma));
+}
+
+// The driver's tensor-map encoder, looked up once per process (before any
+// stream capture: gm_ctx_create calls tma_init).
+static PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  std::call_once(once, [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    cudaGetLastError();
+  });
+  return encode;
+}
+
+void tma_init() { tma_encoder(); }
+
+bool encode_tensor_map_3d(CUtensorMap* map, const void* base, int elem_bytes, int nx, int ny, int nz, int bx, int by,
+                          int bz) {
+  const PFN_cuTensorMapEncodeTiled_v12000 encode = tma_encoder();
+  if (encode == nullptr || (elem_bytes != 1 && elem_bytes != 2)) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * elem_bytes, (cuuint64_t)nx * ny * elem_bytes};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(map, elem_bytes == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8, 3,
+                const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+cudaError_t kernel_error_flags(unsigned int* flags, bool clear) {
+  cudaError_t e = cudaMemcpyFromSymbol(flags, g_kernel_errors, sizeof(unsigned int));
+  if (e == cudaSuccess && clear && *flags != 0) {
+    const unsigned int zero = 0;
+    e = cudaMemcpyToSymbol(g_kernel_errors, &zero, sizeof(unsigned int));
+  }
+  return e;
 }
 
 // Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius

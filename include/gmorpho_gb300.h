@@ -90,6 +90,13 @@ gm_status gm_ctx_destroy(gm_ctx* ctx);
 const char* gm_ctx_last_error(const gm_ctx* ctx);
 /* number of this library's kernels launched on the context so far */
 long long gm_ctx_kernel_launches(const gm_ctx* ctx);
+/* Error bits that this library's kernels recorded on the current device
+ * instead of trapping: bit 0 = a shared-memory tile load (TMA) was not
+ * complete within its poll limit (the results of that call are not
+ * trustworthy).  Waits for the device's work; clears the bits when `clear`.
+ * No counterpart in the reference (which checks cudaGetLastError only,
+ * GMorpho/GMorpho.cu:50-56). */
+gm_status gm_kernel_error_flags(uint32_t* flags, int32_t clear);
 /* Per-kernel timing (the reference prints GET_TIME spans around each
  * kernel, GMorpho/timing.h:28): when enabled, every launch is bracketed by
  * CUDA events on its own stream.  gm_ctx_profile_read writes a JSON object

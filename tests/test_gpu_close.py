@@ -179,3 +179,20 @@ def test_kernel_launch_counter_moves(gm_ctx):
     before = gm_ctx.kernel_launches
     _run(gm_ctx, 16, synth.random_grid(16, 61), uniform=3)
     assert gm_ctx.kernel_launches > before
+
+
+def test_tma_tiles_leave_no_error_flags(gm_ctx):
+    """Grids whose rows are whole 64-column boxes stage their min-plus tiles
+    with TMA; after closings in every mode the kernels have recorded no
+    tile-load timeout, and the grids equal the oracle's."""
+    api.kernel_error_flags(clear=True)
+    res = 64
+    X = synth.random_grid(res, 71)
+    rng = np.random.default_rng(71)
+    scale = rng.integers(2, 12, size=(2 * res) ** 3).astype(np.int8)
+    for mode, se in ((L.GM_REF, L.GM_SE_SPHERE), (L.GM_EXACT, L.GM_SE_SPHERE), (L.GM_REF, L.GM_SE_CUBE)):
+        _, _, Co = O.close(X, res, [res] * 3, scale, mode, se)
+        desc = api.make_desc(res)
+        Cg = gm_ctx.close(desc, _dev(X), _dev(scale), 0, mode, se)
+        assert np.array_equal(Cg.cpu().numpy(), Co), (mode, se)
+    assert api.kernel_error_flags() == 0
