@@ -790,14 +790,9 @@ __device__ __forceinline__ uint32_t load_pair(const TIn* p, uint32_t capp) {
   return __vminu2(v, capp);  // both lanes saturated at cap
 }
 
-// TMA tiles arrive in chunks of kDpxChunk rows; each third-axis slice of
-// the tile gets span + kDpxChunk rows so that the last chunk's overrun stays
-// inside its own slice.
-constexpr int kDpxChunk = 16;
-
 size_t dpx_smem_bytes(int sub, int halo) {
   const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
-  return (size_t)2 * (span + kDpxChunk) * 32 * sizeof(uint32_t) + 128;  // + alignment slack
+  return (size_t)2 * span * 32 * sizeof(uint32_t) + 128;  // + slack to align the tile to 128 bytes (TMA)
 }
 
 // Where a pass's outputs are needed: tiles whose cells, grown by (gx, ga,
@@ -877,7 +872,8 @@ __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, i
 }
 
 // With use_tma, the u16 input tile is staged by TMA (tmap: boxes of 64
-// columns x kDpxChunk rows x 1 slice along (x, pass axis, third axis)).
+// columns x span rows x 1 slice along (x, pass axis, third axis), one per
+// slice; rows are 128 bytes, so each slice starts 128-byte aligned).
 template <int G, typename TIn, int FIN>
 __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
@@ -917,17 +913,17 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   const bool needed = tile_needed(need, axis, sub, o0, nout);
   const int skip = needed ? halo - halo_e : span;  // tile rows never read
   const uint32_t capp = cap | (cap << 16);
-  const int tile_rows = span + kDpxChunk;
+  const int tile_rows = span;
   uint32_t* tile = tileu + tpar * tile_rows * 32;
   const bool colok = x < nx && third < n3;
   int finite = 0;
   constexpr bool kTileMin = G == KERN_CEN2 || G == KERN_LAT2 || (G == KERN_LAT && FIN == 1);
   uint32_t vmin = 0xffffffffu;  // smallest loaded value (both lanes)
-  // TMA staging (u16 inputs): rows [skip, span - skip) of both slices, in
-  // chunks of kDpxChunk rows issued by one thread; rows past the field come
-  // back as zeros and are set to the saturation value below.
-  const int nchunks = sizeof(TIn) == 2 && use_tma && span - 2 * skip > 0
-                          ? (span - 2 * skip + kDpxChunk - 1) / kDpxChunk : 0;  // block-uniform
+  // TMA staging (u16 inputs): the whole span of both slices, one copy per
+  // slice issued by one thread; rows past the field come back as zeros and
+  // are set to the saturation value below, with the rows [skip, span - skip)
+  // that the taps read.
+  const int nchunks = sizeof(TIn) == 2 && use_tma && span - 2 * skip > 0 ? 1 : 0;  // block-uniform
   if (nchunks > 0) {
     if (threadIdx.x == 0) {
       tma_prefetch_map(&tmap);
@@ -935,17 +931,15 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      mbar_arrive_expect_tx(&tma_bar, (uint32_t)(2 * nchunks * kDpxChunk * kDpxCols * sizeof(uint16_t)));
+      mbar_arrive_expect_tx(&tma_bar, (uint32_t)(2 * span * kDpxCols * sizeof(uint16_t)));
       const int x0 = blockIdx.x * kDpxCols, t0 = 2 * ((int)blockIdx.z + need.third0);
-      for (int tp = 0; tp < 2; tp++)
-        for (int c = 0; c < nchunks; c++) {
-          const int r0 = skip + kDpxChunk * c;
-          uint32_t* dst = tileu + (tp * tile_rows + r0) * 32;
-          if (axis == 1)
-            tma_load_3d(dst, &tmap, x0, lo + r0, t0 + tp, &tma_bar);
-          else
-            tma_load_3d(dst, &tmap, x0, t0 + tp, lo + r0, &tma_bar);
-        }
+      for (int tp = 0; tp < 2; tp++) {
+        uint32_t* dst = tileu + tp * tile_rows * 32;
+        if (axis == 1)
+          tma_load_3d(dst, &tmap, x0, lo, t0 + tp, &tma_bar);
+        else
+          tma_load_3d(dst, &tmap, x0, t0 + tp, lo, &tma_bar);
+      }
     }
     if (!mbar_wait_bounded(&tma_bar, 0, 1u << 22)) atomicOr(&g_kernel_errors, kErrTmaTimeout);
   }
@@ -1155,13 +1149,19 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   const int nout = sub ? na / 2 : na;
   dim3 g((nx + kDpxCols - 1) / kDpxCols, need.out_n > 0 ? need.out_n : (nout + kDpxOut - 1) / kDpxOut,
          need.third_n > 0 ? need.third_n : (n3 + 1) / 2);
-  // u16 tiles go through TMA when the field's rows are whole 64-column boxes
+  // Full-resolution u16 tiles go through TMA (one box of the whole span per
+  // third-axis slice) when the field's rows are whole 64-column boxes.
+  // Measured at 1024^3: dilation z 2.71 -> 2.64 ms, centre erosion y
+  // 1.27 -> 1.24 ms; the half-resolution lattice passes (sub) were a third
+  // slower with TMA (0.63 -> 0.84, 0.31 -> 0.42 ms; 16-row boxes: slower
+  // everywhere) and keep their per-thread loads.
   CUtensorMap tmap;
   memset(&tmap, 0, sizeof(tmap));
   int use_tma = 0;
-  if (sizeof(TIn) == 2 && nx % kDpxCols == 0 && na >= kDpxChunk && (reinterpret_cast<uintptr_t>(in) & 15) == 0)
-    use_tma = encode_tensor_map_3d(&tmap, in, 2, nx, ny, nz, kDpxCols, axis == 1 ? kDpxChunk : 1,
-                                   axis == 1 ? 1 : kDpxChunk)
+  const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
+  if (sizeof(TIn) == 2 && sub == 0 && nx % kDpxCols == 0 && span <= 256 &&
+      (reinterpret_cast<uintptr_t>(in) & 15) == 0)
+    use_tma = encode_tensor_map_3d(&tmap, in, 2, nx, ny, nz, kDpxCols, axis == 1 ? span : 1, axis == 1 ? 1 : span)
                   ? 1
                   : 0;
   GM_LAUNCH(kc, name, st,
