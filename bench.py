@@ -96,11 +96,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_inputs(res, seed, device):
+def make_inputs(ctx, res):
+    """Configuration 3: the ~3.8M-triangle blob mesh voxelized into the grid
+    (grid attributes from the mesh's box, conservative voxelization, timed
+    apart), and the radius field r = 2 + floor(30 s(x))."""
     from broxy_gb300 import synth
-    X = synth.blob_grid(res, seed, count=BLOBS, device=device)
-    R = synth.radius_field(res, seed, base=2, span=30, device=device)
-    return X.contiguous(), R.contiguous()
+    return synth.config_inputs(ctx, 3, res=res, voxelize_reps=5)
 
 
 # Algorithmic bytes per fine voxel of each kernel (its compulsory input and
@@ -148,8 +149,8 @@ def run_ours(args, rank, world):
     ctx = api.Context(dev.index)
     res = args.res
     V = (2 * res) ** 3
-    X, R = make_inputs(res, SEED + rank * 0, dev)
-    desc = api.make_desc(res, cell_size=1.0 / res)
+    inp = make_inputs(ctx, res)
+    X, R, desc = inp["X"], inp["R"], inp["desc"]
     out = torch.empty_like(X)
 
     def step():
@@ -196,7 +197,13 @@ def run_ours(args, rank, world):
     else:
         e2e_ms, nv2, nt2 = run_e2e(args, ctx, desc, X, R, nv, nt, world, dev)
     assert (nv2, nt2) == (nv, nt)
-    return finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value)
+    r = finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value, desc)
+    r["voxelize"] = {"ms": round(inp["voxelize_ms"], 3), "input_triangles": int(inp["T"].shape[0]),
+                     "input_vertices": int(inp["P"].shape[0]), "grid": "%d^3 fine" % (2 * res),
+                     "data_res": [int(v) for v in desc.data_res],
+                     "note": "gm_voxelize (conservative surface + parity fill), device time, median of 5; "
+                             "reported apart, not part of value (GMorpho::Load runs it once per mesh)"}
+    return r
 
 
 def run_e2e(args, ctx, desc, X, R, nv, nt, world, dev):
@@ -233,7 +240,7 @@ def run_e2e(args, ctx, desc, X, R, nv, nt, world, dev):
     return e2e_ms, nv2, nt2
 
 
-def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value):
+def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value, desc):
     # ---- roofline of the dominant kernel and of the morphology passes
     hbm, peak_kind = peaks()
     top = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else (None, None)
@@ -273,8 +280,9 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u8/u16 (integer distance transforms), f32 mesh", "data": "synthetic",
-        "config": {"workload": "1024^3 fine grid (res 512), 200-blob solid, variable radius "
-                               "r = 2 + floor(30 s(x)), GM_REF sphere closing + contour MC + 20 bilateral",
+        "config": {"workload": "%d^3 fine grid (res %d): 200-blob solid's triangle mesh voxelized "
+                               "(data_res %s), variable radius r = 2 + floor(30 s(x)), GM_REF sphere closing + "
+                               "contour MC + 20 bilateral" % (2 * res, res, list(desc.data_res)),
                    "fine_voxels": V, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (1 GiB radius field + 2 GiB intermediate fields)",
                    "mesh_vertices": nv, "mesh_triangles": nt},
@@ -301,7 +309,7 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
             result["batch"] = {"error": repr(exc)[:300]}
     if rank == 0 and not args.no_frame_field:
         try:
-            result["frame_field"] = run_frame_field(args, ctx, X, R, res)
+            result["frame_field"] = run_frame_field(args, ctx, X, R, res, desc)
         except Exception as exc:
             result["frame_field"] = {"error": repr(exc)[:300]}
     if rank == 0 and not args.no_serve:
@@ -361,7 +369,7 @@ def run_batch(args, ctx):
             "batched_gvoxel_s": round(vox / (batch_ms * 1e-3) / 1e9, 3)}
 
 
-def run_frame_field(args, ctx, X, R, res):
+def run_frame_field(args, ctx, X, R, res, desc):
     """Frame-field workload on the same grid and radius field: a frame field
     of (res/16)^3 nodes over the grid's box with 4 seeded hard constraints
     (FrameField::Generate, biharmonic system), then the rotated-cube closing
@@ -371,14 +379,14 @@ def run_frame_field(args, ctx, X, R, res):
     from broxy_gb300 import api
     qres = max(2, res // 16)
     rng = np.random.default_rng(6000)
-    ff = api.FrameField(ctx, (0, 0, 0), (1, 1, 1), qres)
+    lo, hi = np.array(desc.bbox_min, np.float64), np.array(desc.bbox_max, np.float64)
+    ff = api.FrameField(ctx, tuple(lo), tuple(hi), qres)
     for _ in range(4):
-        ff.add_point(rng.uniform(0.1, 0.9, 3), rng.normal(size=3) * 0.6)
+        ff.add_point(lo + (hi - lo) * rng.uniform(0.1, 0.9, 3), rng.normal(size=3) * 0.6)
     t0 = time.perf_counter()
     iters = ff.generate()
     gen_ms = (time.perf_counter() - t0) * 1e3
     Q = ff.quats()
-    desc = api.make_desc(res, cell_size=1.0 / res)
     out = torch.empty_like(X)
     st = torch.cuda.current_stream()
     ctx.close_rotcube(desc, X, Q, qres, R, 0, api.L.GM_REF, out=out)
@@ -418,9 +426,15 @@ def run_serve(args):
     from broxy_gb300 import api, synth
     res = args.serve_res
     dev = torch.device("cuda")
-    X = synth.blob_grid(res, 5000, count=BLOBS, device=dev).contiguous()
+    # configuration 5's input: the ~8M-triangle blob mesh voxelized into the grid
+    mctx = api.Context(dev.index)
+    inp = synth.config_inputs(mctx, 5, res=res)
+    X, desc = inp["X"], inp["desc"]
+    mesh_triangles = int(inp["T"].shape[0])
+    del inp
+    mctx.close_ctx()
+    torch.cuda.empty_cache()
     R = torch.full(((2 * res) ** 3,), 8, dtype=torch.int8, device=dev)
-    desc = api.make_desc(res, cell_size=1.0 / res)
     t0 = time.perf_counter()
     srv = api.Server(desc, X, R, slots=args.serve_slots, max_crop_res=min(res, 512), rmax=32, mode=api.L.GM_REF,
                      bilateral_iters=0)
@@ -428,10 +442,11 @@ def run_serve(args):
     rng = np.random.default_rng(5001)
     n = args.serve_edits
     arrivals = np.cumsum(rng.exponential(1.0 / 200.0, size=n))
-    cs = 0.5 / res
+    cs = 0.5 * desc.cell_size  # fine voxel edge in world units
+    lo, hi = np.array(desc.bbox_min, np.float64), np.array(desc.bbox_max, np.float64)
     edits = []
     for i in range(n):
-        c = rng.uniform(0.2, 0.8, size=3)
+        c = lo + (hi - lo) * rng.uniform(0.2, 0.8, size=3)
         reach = float(rng.uniform(16, 256))
         r_new = int(rng.integers(1, 33))
         core = min(r_new, reach - 1)
@@ -459,7 +474,7 @@ def run_serve(args):
     lat = np.array([r["latency_ms"] for r in ok])
     dev_ms = np.array([r["device_ms"] for r in ok])
     crops = np.array([r["crop_res"] for r in ok])
-    out = {"grid": "%d^3 fine" % (2 * res), "edits": n, "completed": len(ok), "rejected": len(results) - len(ok),
+    out = {"grid": "%d^3 fine" % (2 * res), "input_mesh_triangles": mesh_triangles, "edits": n, "completed": len(ok), "rejected": len(results) - len(ok),
            "arrival_rate_per_s": 200, "edits_per_s": round(len(ok) / wall, 2),
            "latency_p50_ms": round(float(np.percentile(lat, 50)), 3) if len(lat) else None,
            "latency_p99_ms": round(float(np.percentile(lat, 99)), 3) if len(lat) else None,
@@ -500,6 +515,33 @@ def cpu_baseline(X, R, res, sub):
                       (2 * sub, BILATERAL, dt)}
 
 
+def reference_inputs(res):
+    """Configuration 3's inputs built on the host by the oracle (the
+    reference arm runs none of this library's kernels): the blob solid
+    classified (torch), its marching-cubes mesh and conservative
+    voxelization by the oracle, the radius field.  The oracle's mesher and
+    voxelizer restate this library's (tests), up to the last bit of a
+    vertex coordinate."""
+    import torch
+    from broxy_gb300 import synth
+    from oracle import oracle as O
+    c = synth.CONFIGS[3]
+    cells = synth.mesh_cells(3, res)
+    dev = "cuda" if torch.cuda.is_available() else None
+    Xb = synth.blob_grid(cells, c["seed"], count=BLOBS, device=dev)
+    Xb = Xb.cpu().numpy() if dev else Xb
+    p = 1
+    while p < cells:
+        p *= 2
+    dense = np.zeros((2 * p,) * 3, bool)
+    dense[:2 * cells, :2 * cells, :2 * cells] = synth.unpack_dense(Xb, cells)
+    P, T = O.mc(synth.pack_dense(dense), p, np.zeros(3, np.float32), 1.0 / cells)
+    bmin, _, cell, _ = O.grid_attributes(P, res, synth.MESH_MARGIN)
+    X = O.voxelize(P, T, res, bmin, cell)
+    R = synth.radius_field(res, c["seed"], base=2, span=30, device=dev)
+    return X, (R.cpu().numpy() if dev else R)
+
+
 def run_reference(args, rank, world):
     """Reference arm: the reference's algorithm on the host cores (the oracle
     port; the reference itself cannot be built here), same metric."""
@@ -507,16 +549,11 @@ def run_reference(args, rank, world):
         return None
     import torch
     from broxy_gb300 import synth
-    res, sub = args.res, args.cpu_res
-    X = synth.blob_grid(res, SEED, count=BLOBS, device=None if not torch.cuda.is_available() else "cuda")
-    R = synth.radius_field(res, SEED, base=2, span=30,
-                           device=None if not torch.cuda.is_available() else "cuda")
-    import torch as _t
-    X = _t.as_tensor(X)
-    R = _t.as_tensor(R)
-    times = []
     from oracle import oracle as O
-    Xc, Rc = cpu_crop(X, R, res, sub)
+    res, sub = args.res, args.cpu_res
+    X, R = reference_inputs(res)
+    times = []
+    Xc, Rc = cpu_crop(torch.as_tensor(X), torch.as_tensor(R), res, sub)
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         _, _, Cc = O.close(Xc, sub, [sub] * 3, Rc, 0, 0)

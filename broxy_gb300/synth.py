@@ -11,7 +11,12 @@ benchmark configurations:
     U[0.5,1.5], centres U[0.2,0.8]^3) classified at level 0.5;
   * a variable radius field r = 2 + floor(30 s(x)), s a normalised sum of
     16 Gaussian RBFs clamped to [0,1], evaluated in double on the host side
-    of the generator and stored as int8 per fine voxel.
+    of the generator and stored as int8 per fine voxel;
+  * the blob solid's triangulated isosurface (blob_mesh: marching cubes of
+    the classified solid on a box of `cells` cells, ~1M / 4M / 8M triangles
+    at 176 / 352 / 512 cells), which config_inputs voxelizes into the
+    benchmark grids the way GMorpho::Load does (grid attributes from the
+    mesh's box, conservative voxelization).
 
 Seeds follow seed = 1000 * config + instance.
 """
@@ -254,3 +259,75 @@ def _blob_box(res, E, seed, count, device):
         f = torch.einsum("kz,ky,kx->zyx", gz[:, z0:z0 + 16], gy, gx)
         occ[z0:z0 + 16] = f >= 0.5
     return pack_dense_torch(occ)
+
+
+def blob_mesh(ctx, cells, seed, count=200):
+    """Triangle mesh (device float32 (n, 3) vertices in [0, 1]^3, uint32
+    (m, 3) triangles) of the blob solid: this library's marching cubes of
+    blob_grid on a box of `cells`^3 cells (a multiple of 16), no filtering."""
+    import torch
+    from . import api
+    X = blob_grid(cells, seed, count=count, device="cuda")
+    box = api.make_box((cells, cells, cells), cell_size=1.0 / cells)
+    V, _, T = ctx.mesh_box(box, X, bilateral_iters=0)
+    Vc = torch.empty_like(V)
+    Vc.copy_(V)
+    Tc = torch.empty((T.shape[0], 3), dtype=torch.int32, device=V.device)
+    Tc.copy_(T.view(torch.int32))
+    torch.cuda.synchronize()
+    return Vc, Tc
+
+
+# Benchmark configurations with a voxelized blob mesh: (base res, mesh box
+# cells, seed, uniform radius or 0 for the radius field r = 2 + floor(30 s)).
+CONFIGS = {
+    2: dict(res=256, cells=176, seed=2000, uniform=12),
+    3: dict(res=512, cells=352, seed=3000, uniform=0),
+    5: dict(res=1024, cells=512, seed=5000, uniform=8),
+}
+MESH_MARGIN = 0.05  # world units added around the mesh's box (GMorpho::Load's margin, GMorpho.cu:7735)
+
+
+def mesh_cells(config, res=None):
+    """Mesh box cells of a configuration, scaled with the grid when `res`
+    differs from the configuration's own (a multiple of 16)."""
+    c = CONFIGS[config]
+    if res is None or res == c["res"]:
+        return c["cells"]
+    return max(16, int(round(c["cells"] * res / c["res"] / 16.0)) * 16)
+
+
+def config_inputs(ctx, config, res=None, voxelize_reps=0):
+    """The inputs of benchmark configuration 2, 3 or 5 (optionally at another
+    base resolution `res`, the mesh scaled with it): the blob mesh,
+    voxelized like GMorpho::Load (gm_grid_attributes + gm_voxelize), and the
+    fine radius field (None for a uniform radius).  Returns a dict with
+    desc, X (device packed grid), R, uniform, P, T (device mesh) and, with
+    voxelize_reps > 0, the voxelization's device time in ms (median of that
+    many timed runs after one untimed)."""
+    import torch
+    from . import api
+    c = CONFIGS[config]
+    res = c["res"] if res is None else res
+    P, T = blob_mesh(ctx, mesh_cells(config, res), c["seed"])
+    desc = api.grid_attributes(P.cpu().numpy(), res, MESH_MARGIN)
+    X = torch.zeros(res ** 3, dtype=torch.uint8, device=P.device)
+    ctx.voxelize(desc, P, T, out=X)
+    out = dict(desc=desc, X=X, P=P, T=T, res=res, uniform=c["uniform"], seed=c["seed"], config=config)
+    if voxelize_reps > 0:
+        times = []
+        st = torch.cuda.current_stream()
+        for _ in range(voxelize_reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            ctx.voxelize(desc, P, T, out=X)
+            e1.record(st)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        out["voxelize_ms"] = float(np.median(times))
+    if c["uniform"] == 0:
+        out["R"] = radius_field(res, c["seed"], base=2, span=30, device=P.device).contiguous()
+    else:
+        out["R"] = None
+    torch.cuda.synchronize()
+    return out

@@ -1,10 +1,12 @@
 """Whole-grid parity at the benchmark's own sizes and inputs (the reference
-path GMorpho::Update, GMorpho/GMorpho.cu:7775-7817, GM_REF sphere closing
-then contour marching cubes with 20 bilateral iterations):
+path GMorpho::Load + GMorpho::Update, GMorpho/GMorpho.cu:7731-7817: the
+mesh voxelized, then the GM_REF sphere closing and contour marching cubes
+with 20 bilateral iterations):
 
-* 512^3 fine grid, 200-blob solid (seed 2000), uniform radius 12;
-* 1024^3 fine grid, 200-blob solid and radius field r = 2 + floor(30 s(x))
-  (seed 3000): exactly the inputs bench.py times.
+* 512^3 fine grid, the 200-blob solid's ~1M-triangle mesh (seed 2000)
+  voxelized, uniform radius 12; the voxelization itself equals the oracle's;
+* 1024^3 fine grid, the ~3.8M-triangle mesh (seed 3000) voxelized, radius
+  field r = 2 + floor(30 s(x)): exactly the inputs bench.py times.
 
 The GPU closing must equal the oracle's on every cell, the meshes must have
 identical triangle index arrays, vertices within 1e-6 relative and normals
@@ -13,9 +15,9 @@ tests/golden/bench_manifest.json; when this run's inputs hash as recorded
 there, its outputs must hash as recorded too (the same bits as the run that
 wrote the manifest, which was itself checked against the oracle).
 
-* 2048^3 resident serving grid (seed 5000, base radius 8): after a stream of
-  brush edits, the server's resident closing equals a full closing of the
-  edited radius field (both on the GPU).
+* 2048^3 resident serving grid (the ~8M-triangle mesh, seed 5000, voxelized;
+  base radius 8): after a stream of brush edits, the server's resident
+  closing equals a full closing of the edited radius field (both on the GPU).
 """
 import hashlib
 import json
@@ -40,28 +42,30 @@ def _sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-CASES = {
-    "blob_512_uniform_12": dict(res=256, seed=2000, uniform=12, variable=False),
-    "blob_1024_radius_field": dict(res=512, seed=3000, uniform=0, variable=True),
-}
+CASES = {"blob_512_uniform_12": 2, "blob_1024_radius_field": 3}
 
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_bench_config_whole_grid_equals_oracle(gm_ctx, name):
     import torch
-    c = CASES[name]
-    res = c["res"]
-    X = synth.blob_grid(res, c["seed"], count=200, device="cuda").contiguous()
-    R = synth.radius_field(res, c["seed"], base=2, span=30, device="cuda").contiguous() if c["variable"] else None
-    desc = api.make_desc(res, cell_size=1.0 / res)
-    Cd = gm_ctx.close(desc, X, R, c["uniform"], L.GM_REF, L.GM_SE_SPHERE)
+    inp = synth.config_inputs(gm_ctx, CASES[name])
+    res, desc, X, R, uniform = inp["res"], inp["desc"], inp["X"], inp["R"], inp["uniform"]
+    dr = [int(v) for v in desc.data_res]
+    Xh = X.cpu().numpy()
+    if CASES[name] == 2:
+        # the voxelization of the ~1M-triangle mesh, against the oracle's
+        Xo = O.voxelize(inp["P"].cpu().numpy(), inp["T"].cpu().numpy().astype(np.uint32), res,
+                        np.array(desc.bbox_min, np.float32), desc.cell_size)
+        assert len(inp["T"]) > 500000
+        assert np.array_equal(Xh, Xo)
+    Cd = gm_ctx.close(desc, X, R, uniform, L.GM_REF, L.GM_SE_SPHERE)
     Vd, Nd, Td = gm_ctx.mesh(desc, Cd, 20)
     torch.cuda.synchronize()
-    Xh = X.cpu().numpy()
-    Rh = R.cpu().numpy() if R is not None else O.scale_grid(res, uniform=c["uniform"])
+    Rh = R.cpu().numpy() if R is not None else O.scale_grid(res, uniform=uniform)
     Cg, Vg, Ng, Tg = Cd.cpu().numpy(), Vd.cpu().numpy(), Nd.cpu().numpy(), Td.cpu().numpy()
     del Cd, Vd, Nd, Td
-    rec = {"res": res, "seed": c["seed"], "uniform": c["uniform"], "variable": c["variable"],
+    rec = {"res": res, "seed": inp["seed"], "uniform": uniform, "variable": R is not None, "data_res": dr,
+           "input_triangles": int(len(inp["T"])),
            "X": _sha(Xh), "R": _sha(Rh) if R is not None else None,
            "C": _sha(Cg), "T": _sha(Tg), "V": _sha(Vg), "nv": int(len(Vg)), "nt": int(len(Tg))}
     out = os.environ.get("GM_BENCH_MANIFEST_OUT")
@@ -71,7 +75,7 @@ def test_bench_config_whole_grid_equals_oracle(gm_ctx, name):
         with open(out, "w") as f:
             json.dump(prev, f, indent=1, sort_keys=True)
     # the oracle on the whole grid
-    _, _, Co = O.close(Xh, res, [res] * 3, Rh, 0, 0)
+    _, _, Co = O.close(Xh, res, dr, Rh, 0, 0)
     assert np.array_equal(Cg, Co)
     Vo, To = O.mc(Co, res, np.array(desc.bbox_min), desc.cell_size)
     assert len(To) > 100000
@@ -89,15 +93,16 @@ def test_bench_config_whole_grid_equals_oracle(gm_ctx, name):
 
 def test_server_2048_edits_equal_full_closing(gm_ctx):
     import torch
-    res = 1024
-    X = synth.blob_grid(res, 5000, count=200, device="cuda").contiguous()
+    inp = synth.config_inputs(gm_ctx, 5)
+    res, X, desc = inp["res"], inp["X"], inp["desc"]
+    del inp
     R = torch.full(((2 * res) ** 3,), 8, dtype=torch.int8, device="cuda")
-    desc = api.make_desc(res, cell_size=1.0 / res)
     srv = api.Server(desc, X, R, slots=4, max_crop_res=512, rmax=32, mode=L.GM_REF, bilateral_iters=0)
     rng = np.random.default_rng(5002)
-    cs = 0.5 / res
+    cs = 0.5 * desc.cell_size
+    lo, hi = np.array(desc.bbox_min, np.float64), np.array(desc.bbox_max, np.float64)
     for i in range(32):
-        c = rng.uniform(0.2, 0.8, size=3)
+        c = lo + (hi - lo) * rng.uniform(0.2, 0.8, size=3)
         reach = float(rng.uniform(16, 256))
         r_new = int(rng.integers(1, 33))
         core = min(r_new, reach - 1)
