@@ -97,7 +97,7 @@ class ClockSampler:
 
 
 def make_inputs(ctx, res):
-    """Configuration 3: the ~3.8M-triangle blob mesh voxelized into the grid
+    """Configuration 3: the ~4M-triangle blob isosurface voxelized into the grid
     (grid attributes from the mesh's box, conservative voxelization, timed
     apart), and the radius field r = 2 + floor(30 s(x))."""
     from broxy_gb300 import synth
@@ -516,26 +516,18 @@ def cpu_baseline(X, R, res, sub):
 
 
 def reference_inputs(res):
-    """Configuration 3's inputs built on the host by the oracle (the
-    reference arm runs none of this library's kernels): the blob solid
-    classified (torch), its marching-cubes mesh and conservative
-    voxelization by the oracle, the radius field.  The oracle's mesher and
-    voxelizer restate this library's (tests), up to the last bit of a
-    vertex coordinate."""
+    """Configuration 3's inputs built without this library's kernels (the
+    reference arm runs none of them): the blob isosurface mesh (torch), its
+    grid attributes and conservative voxelization by the oracle, which
+    restates this library's voxelizer bit for bit (tests), and the radius
+    field."""
     import torch
     from broxy_gb300 import synth
     from oracle import oracle as O
     c = synth.CONFIGS[3]
-    cells = synth.mesh_cells(3, res)
-    dev = "cuda" if torch.cuda.is_available() else None
-    Xb = synth.blob_grid(cells, c["seed"], count=BLOBS, device=dev)
-    Xb = Xb.cpu().numpy() if dev else Xb
-    p = 1
-    while p < cells:
-        p *= 2
-    dense = np.zeros((2 * p,) * 3, bool)
-    dense[:2 * cells, :2 * cells, :2 * cells] = synth.unpack_dense(Xb, cells)
-    P, T = O.mc(synth.pack_dense(dense), p, np.zeros(3, np.float32), 1.0 / cells)
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    P, T = synth.blob_mesh(synth.mesh_samples(3, res), c["seed"], count=BLOBS, device=dev)
+    P, T = P.cpu().numpy(), T.cpu().numpy().astype(np.uint32)
     bmin, _, cell, _ = O.grid_attributes(P, res, synth.MESH_MARGIN)
     X = O.voxelize(P, T, res, bmin, cell)
     R = synth.radius_field(res, c["seed"], base=2, span=30, device=dev)

@@ -99,6 +99,7 @@ PROTOTYPES = {
     "gm_batch_close_mesh": (C.c_int, [_P, C.c_int32, C.POINTER(BatchItem), C.c_int, C.c_int, C.c_int32, C.c_int32,
                                        C.POINTER(MeshView), _P]),
     "gm_batch_lanes": (C.c_int32, [_P]),
+    "gm_batch_inject_alloc_failures": (C.c_int, [_P, C.c_int32]),
     "gm_server_create": (C.c_int, [C.POINTER(GridDesc), _P, _P, C.POINTER(ServerOpts), C.POINTER(_P)]),
     "gm_server_destroy": (C.c_int, [_P]),
     "gm_server_submit": (C.c_int, [_P, C.POINTER(Edit), C.POINTER(C.c_uint64)]),
@@ -106,6 +107,9 @@ PROTOTYPES = {
     "gm_server_pending": (C.c_int32, [_P]),
     "gm_server_closing": (C.c_void_p, [_P]),
     "gm_server_kernel_launches": (C.c_longlong, [_P]),
+    "gm_server_set_admission": (C.c_int, [_P, C.c_int64, C.c_float]),
+    "gm_server_memory": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "gm_server_inject_alloc_failures": (C.c_int, [_P, C.c_int32]),
     "gm_server_profile": (C.c_int, [_P, C.c_int32]),
     "gm_server_snapshot": (C.c_int, [_P, _P, _P]),
     "gm_server_restore": (C.c_int, [_P, _P, _P]),

@@ -480,6 +480,26 @@ class Server:
     def kernel_launches(self):
         return int(self.lib.gm_server_kernel_launches(self.h))
 
+    def set_admission(self, budget_bytes=0, timeout_ms=0.0):
+        """Memory budget of the edits on the GPU (<= 0: keep) and the queue
+        timeout in ms (0: none)."""
+        st = self.lib.gm_server_set_admission(self.h, int(budget_bytes), float(timeout_ms))
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_set_admission")
+
+    def memory(self):
+        """(bytes of crop buffers of the edits on the GPU, budget)."""
+        a, b = C.c_int64(0), C.c_int64(0)
+        st = self.lib.gm_server_memory(self.h, C.byref(a), C.byref(b))
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_memory")
+        return a.value, b.value
+
+    def inject_alloc_failures(self, count):
+        st = self.lib.gm_server_inject_alloc_failures(self.h, int(count))
+        if st != L.GM_OK:
+            raise L.GMError(st, "gm_server_inject_alloc_failures")
+
     def snapshot(self):
         """Host copies (closed grid, radius field) of the resident state."""
         n = self.desc.res ** 3

@@ -43,6 +43,7 @@ struct BatchLane {
 };
 
 struct BatchState {
+  int inject_fail = 0;  // lane buffer allocations still to fail as out of memory (fault injection)
   std::vector<BatchLane> lanes;
   std::vector<MeshBuffers> meshes;
   std::vector<int64_t> nv, nt;
@@ -212,6 +213,20 @@ static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* i
   return cudaSuccess;
 }
 
+// a lane buffer, or the injected out-of-memory failure
+static cudaError_t lane_malloc(BatchState* b, void** p, size_t bytes) {
+  if (b->inject_fail > 0) {
+    b->inject_fail--;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+
+void batch_inject_alloc_failures(void** state, int count) {
+  if (!*state) *state = new BatchState();
+  static_cast<BatchState*>(*state)->inject_fail = count;
+}
+
 cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, int se, int bilateral, int lanes_req,
                       gm_mesh_view* meshes, int sms, cudaStream_t st, KernelCounter* kc) {
   if (!*state) *state = new BatchState();
@@ -296,7 +311,7 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
       cudaFree(ln.ws);
       ln.ws = nullptr;
       ln.ws_bytes = 0;
-      if ((e = cudaMalloc(&ln.ws, wsb)) != cudaSuccess) return e;
+      if ((e = lane_malloc(b, (void**)&ln.ws, wsb)) != cudaSuccess) return e;
       ln.ws_bytes = wsb;
     }
     if (ln.crop_cells < ccells) {
@@ -304,8 +319,8 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
       cudaFree(ln.Cc);
       ln.Xc = ln.Cc = nullptr;
       ln.crop_cells = 0;
-      if ((e = cudaMalloc(&ln.Xc, ccells)) != cudaSuccess) return e;
-      if ((e = cudaMalloc(&ln.Cc, ccells)) != cudaSuccess) return e;
+      if ((e = lane_malloc(b, (void**)&ln.Xc, ccells)) != cudaSuccess) return e;
+      if ((e = lane_malloc(b, (void**)&ln.Cc, ccells)) != cudaSuccess) return e;
       ln.crop_cells = ccells;
     }
   }

@@ -948,6 +948,12 @@ gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items
 
 int32_t gm_batch_lanes(gm_ctx* ctx) { return ctx ? gm::batch_lanes_tuned(ctx->batch) : 0; }
 
+gm_status gm_batch_inject_alloc_failures(gm_ctx* ctx, int32_t count) {
+  if (!ctx || count < 0) return GM_ERR_INVALID_ARGUMENT;
+  gm::batch_inject_alloc_failures(&ctx->batch, count);
+  return GM_OK;
+}
+
 // ------------------------------------------------------------------ a18
 
 struct gm_bvh {

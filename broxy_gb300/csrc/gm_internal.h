@@ -292,6 +292,8 @@ void batch_release(void* state);
 cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, int se, int bilateral, int lanes_req,
                       gm_mesh_view* meshes, int sms, cudaStream_t st, KernelCounter* kc);
 int batch_lanes_tuned(void* state);
+// fault injection: the next `count` lane buffer allocations fail as out of memory
+void batch_inject_alloc_failures(void** state, int count);
 
 // ---------------------------------------------------------------- BVH
 cudaError_t bvh_build(const uint8_t* grid, int res, void** handle, uint32_t* scratch_bricks, int* n_out,

@@ -15,13 +15,25 @@
 // the grid border are aligned to it, so the border rules of the reference
 // ([1, res-2] cells, data_res) act the same.
 //
-// Continuous batching: each slot owns a stream, crop buffers and a mesh
-// buffer.  Queued edits are dispatched in arrival order as slots free up; an
-// edit whose crop overlaps the crop of an edit still on the GPU is queued
-// behind it on the GPU (its stream waits for the earlier edit's write back),
+// Continuous batching: each slot owns a stream and a mesh buffer.  Queued
+// edits are dispatched in arrival order as slots and memory free up; an edit
+// whose crop overlaps the crop of an edit still on the GPU is queued behind
+// it on the GPU (its stream waits for the earlier edit's write back),
 // disjoint edits run concurrently.
+//
+// Admission by memory: an edit's crop buffers (input crop, closed crop,
+// closing workspace) are sized for its own crop and taken from a device
+// memory pool in stream order when it is dispatched, and returned when its
+// result is collected.  An edit is dispatched only while the bytes of the
+// edits on the GPU plus its own stay within the server's budget (the
+// device's free memory at creation less a reserve, or the caller's); an
+// edit that finds too little memory, or whose allocation fails, stays
+// queued and is retried as edits finish, unless its wait passes the
+// request timeout (GM_ERR_OUT_OF_MEMORY after an allocation failure,
+// GM_ERR_NOT_READY otherwise).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <deque>
@@ -77,7 +89,9 @@ struct Slot {
   uint32_t* h_tot = nullptr;  // pinned: the crop mesh's four totals
   int phase = 0;              // 0 idle, 1 closing + counting, 2 emitting
   MeshArgs ma;
-  uint8_t *Xc = nullptr, *Cc = nullptr, *ws = nullptr;
+  uint8_t *Xc = nullptr, *Cc = nullptr, *ws = nullptr;  // carved from `block`
+  void* block = nullptr;                                  // the edit's crop buffers (memory pool)
+  int64_t bytes = 0;                                      // their size
   MeshBuffers mesh;
   bool busy = false;
   bool held = false;  // result returned by the last poll: its patch stays valid until the next poll
@@ -93,6 +107,7 @@ struct Pending {
   uint64_t ticket;
   gm_edit edit;
   double t_submit;
+  int last_fail = 0;  // GM_ERR_OUT_OF_MEMORY once an allocation for it failed
 };
 
 struct Server {
@@ -117,6 +132,11 @@ struct Server {
   int rnb = 0;  // bricks per axis
   int bilateral = 0;
   std::vector<Slot> slots;
+  cudaMemPool_t pool = nullptr;  // per-edit crop buffers
+  int64_t budget = 0;            // bytes of crop buffers on the GPU at most
+  int64_t inflight = 0;          // bytes of crop buffers of the edits on the GPU
+  double timeout_ms = 0.0;       // longest wait in the queue (0: none)
+  int inject_fail = 0;           // allocations still to fail as out of memory (fault injection)
   std::deque<Pending> queue;
   std::vector<gm_edit_result> done;
   uint64_t next_ticket = 1;
@@ -390,11 +410,48 @@ static cudaError_t finish_mesh(Server& s, Slot& sl) {
   return cudaGetLastError();
 }
 
+// bytes of an edit's crop buffers: the input crop, the closed crop and the
+// closing workspace, each 256-byte aligned
+static int64_t edit_bytes(int cres) {
+  const int64_t cells = (int64_t)cres * cres * cres;
+  return 2 * ((cells + 255) / 256 * 256) + (int64_t)close_workspace_bytes(cres) + 256;
+}
+
+// the slot's crop buffers back to the pool, in its stream's order
+static void release_buffers(Server& s, Slot& sl) {
+  if (sl.block) cudaFreeAsync(sl.block, sl.st);
+  s.inflight -= sl.bytes;
+  sl.block = nullptr;
+  sl.Xc = sl.Cc = sl.ws = nullptr;
+  sl.bytes = 0;
+}
+
+// crop buffers for an edit of crop edge cres on the slot's stream
+static cudaError_t take_buffers(Server& s, Slot& sl, int cres) {
+  const int64_t bytes = edit_bytes(cres);
+  if (s.inject_fail > 0) {
+    s.inject_fail--;
+    return cudaErrorMemoryAllocation;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(&p, (size_t)bytes, s.pool, sl.st);
+  if (e != cudaSuccess) return e;
+  const int64_t cells = (int64_t)cres * cres * cres, cpad = (cells + 255) / 256 * 256;
+  sl.block = p;
+  sl.Xc = static_cast<uint8_t*>(p);
+  sl.Cc = sl.Xc + cpad;
+  sl.ws = sl.Cc + cpad;
+  sl.bytes = bytes;
+  s.inflight += bytes;
+  return cudaSuccess;
+}
+
 static void fail_slot(Server& s, Slot& sl, int status) {
   gm_edit_result r = {};
   r.ticket = sl.ticket;
   r.status = status;
   s.done.push_back(r);
+  release_buffers(s, sl);
   sl.busy = false;
   sl.phase = 0;
 }
@@ -434,9 +491,26 @@ static void progress(Server& s) {
     r.patch.num_vertices = sl.nv;
     r.patch.num_triangles = sl.nt;
     s.done.push_back(r);
+    release_buffers(s, sl);
     sl.busy = false;
     sl.held = true;
     sl.phase = 0;
+  }
+  // requests that waited in the queue past the timeout
+  if (s.timeout_ms > 0.0) {
+    const double t = now_ms();
+    for (auto it = s.queue.begin(); it != s.queue.end();) {
+      if (t - it->t_submit <= s.timeout_ms) {
+        ++it;
+        continue;
+      }
+      gm_edit_result r = {};
+      r.ticket = it->ticket;
+      r.status = it->last_fail ? it->last_fail : GM_ERR_NOT_READY;
+      r.latency_ms = (float)(t - it->t_submit);
+      s.done.push_back(r);
+      it = s.queue.erase(it);
+    }
   }
   // Dispatch queued edits while slots are free.  An edit whose crop meets
   // the crop of an earlier edit still queued waits (its result depends on
@@ -468,6 +542,27 @@ static void progress(Server& s) {
     for (const Box3& w : waiting)
       if (w.overlaps(pl.crop)) conflict = true;
     if (conflict) {
+      waiting.push_back(pl.crop);
+      ++it;
+      continue;
+    }
+    // admission by memory: its crop buffers must fit the budget next to
+    // those of the edits on the GPU (an edit larger than the whole budget
+    // is refused at once), and the allocation must succeed
+    const int64_t need = edit_bytes(pl.cres);
+    if (need > s.budget) {
+      gm_edit_result r = {};
+      r.ticket = it->ticket;
+      r.status = GM_ERR_OUT_OF_MEMORY;
+      s.done.push_back(r);
+      it = s.queue.erase(it);
+      continue;
+    }
+    if (s.inflight + need > s.budget || take_buffers(s, *free_slot, pl.cres) != cudaSuccess) {
+      if (s.inflight + need <= s.budget) {
+        cudaGetLastError();
+        it->last_fail = GM_ERR_OUT_OF_MEMORY;
+      }
       waiting.push_back(pl.crop);
       ++it;
       continue;
@@ -556,7 +651,6 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
     cudaFree(s.ws_full);
     s.ws_full = nullptr;
   }
-  const size_t ccells = (size_t)s.max_cres * s.max_cres * s.max_cres;
   for (int i = 0; i < opts->slots && e == cudaSuccess; i++) {
     gm::Slot sl;
     e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
@@ -565,14 +659,39 @@ gm_status gm_server_create(const gm_grid_desc* desc, const uint8_t* d_input, int
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.counted, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.written, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost(&sl.h_tot, 4 * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&sl.Xc, ccells);
-    if (e == cudaSuccess) e = cudaMalloc(&sl.Cc, ccells);
-    if (e == cudaSuccess) e = cudaMalloc(&sl.ws, gm::close_workspace_bytes(s.max_cres));
     // mesh buffers for a patch of a few surface layers across the largest
     // crop, so that the first large edits do not allocate
     const int64_t nt = 16 * (int64_t)s.max_cres * s.max_cres;
     if (e == cudaSuccess) e = gm::mesh_reserve(sl.mesh, s.max_cres, nt / 2, nt);
     s.slots.push_back(sl);
+  }
+  // the crop buffers' pool: it keeps what it has grown to, and is grown at
+  // once to what the slots need for the largest crops (within the budget),
+  // so that edits do not wait for the driver
+  if (e == cudaSuccess) {
+    cudaMemPoolProps pp = {};
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = s.device;
+    e = cudaMemPoolCreate(&s.pool, &pp);
+    if (e == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      e = cudaMemPoolSetAttribute(s.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
+  if (e == cudaSuccess) {
+    size_t free_b = 0, total_b = 0;
+    e = cudaMemGetInfo(&free_b, &total_b);
+    const int64_t reserve = std::max<int64_t>((int64_t)1 << 30, (int64_t)(total_b / 20));
+    s.budget = std::max<int64_t>(0, (int64_t)free_b - reserve);
+    const int64_t full = (int64_t)opts->slots * gm::edit_bytes(s.max_cres);
+    s.budget = std::min(s.budget, full);
+    void* warm = nullptr;
+    if (e == cudaSuccess && s.budget > 0 && cudaMallocFromPoolAsync(&warm, (size_t)s.budget, s.pool, 0) == cudaSuccess) {
+      cudaFreeAsync(warm, 0);
+      e = cudaStreamSynchronize(0);
+    }
+    cudaGetLastError();
   }
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -595,10 +714,12 @@ gm_status gm_server_destroy(gm_server* srv) {
     if (sl.counted) cudaEventDestroy(sl.counted);
     if (sl.written) cudaEventDestroy(sl.written);
     if (sl.h_tot) cudaFreeHost(sl.h_tot);
-    cudaFree(sl.Xc);
-    cudaFree(sl.Cc);
-    cudaFree(sl.ws);
+    if (sl.block) cudaFree(sl.block);
     sl.mesh.release();
+  }
+  if (s.pool) {
+    cudaDeviceSynchronize();
+    cudaMemPoolDestroy(s.pool);
   }
   cudaFree(s.C);
   cudaFree(s.E);
@@ -680,6 +801,26 @@ gm_status gm_server_restore(gm_server* srv, const uint8_t* h_closing, const int8
   e = cudaMemcpy(s.C, h_closing, cells, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = gm::build_radius_map(s);
   return e == cudaSuccess ? GM_OK : GM_ERR_CUDA;
+}
+
+gm_status gm_server_set_admission(gm_server* srv, int64_t budget_bytes, float timeout_ms) {
+  if (!srv || timeout_ms < 0.f) return GM_ERR_INVALID_ARGUMENT;
+  if (budget_bytes > 0) srv->s.budget = budget_bytes;
+  srv->s.timeout_ms = timeout_ms;
+  return GM_OK;
+}
+
+gm_status gm_server_memory(gm_server* srv, int64_t* inflight_bytes, int64_t* budget_bytes) {
+  if (!srv) return GM_ERR_INVALID_ARGUMENT;
+  if (inflight_bytes) *inflight_bytes = srv->s.inflight;
+  if (budget_bytes) *budget_bytes = srv->s.budget;
+  return GM_OK;
+}
+
+gm_status gm_server_inject_alloc_failures(gm_server* srv, int32_t count) {
+  if (!srv || count < 0) return GM_ERR_INVALID_ARGUMENT;
+  srv->s.inject_fail = count;
+  return GM_OK;
 }
 
 gm_status gm_server_profile(gm_server* srv, int32_t enable) {

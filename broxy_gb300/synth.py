@@ -12,11 +12,11 @@ benchmark configurations:
   * a variable radius field r = 2 + floor(30 s(x)), s a normalised sum of
     16 Gaussian RBFs clamped to [0,1], evaluated in double on the host side
     of the generator and stored as int8 per fine voxel;
-  * the blob solid's triangulated isosurface (blob_mesh: marching cubes of
-    the classified solid on a box of `cells` cells, ~1M / 4M / 8M triangles
-    at 176 / 352 / 512 cells), which config_inputs voxelizes into the
-    benchmark grids the way GMorpho::Load does (grid attributes from the
-    mesh's box, conservative voxelization).
+  * the blob field's triangulated isosurface at level 0.5 (blob_mesh:
+    marching cubes with linear interpolation on the sampled field, ~1M /
+    4M / 8M triangles), which config_inputs voxelizes into the benchmark
+    grids the way GMorpho::Load does (grid attributes from the mesh's box,
+    conservative voxelization).
 
 Seeds follow seed = 1000 * config + instance.
 """
@@ -261,40 +261,119 @@ def _blob_box(res, E, seed, count, device):
     return pack_dense_torch(occ)
 
 
-def blob_mesh(ctx, cells, seed, count=200):
-    """Triangle mesh (device float32 (n, 3) vertices in [0, 1]^3, uint32
-    (m, 3) triangles) of the blob solid: this library's marching cubes of
-    blob_grid on a box of `cells`^3 cells (a multiple of 16), no filtering."""
+_MC_TABLES = None
+
+
+def _mc_tables():
+    """The marching-cubes triangle table (edge ids per case, x-fastest corner
+    order v0=000 v1=100 v2=110 v3=010 v4=001 v5=101 v6=111 v7=011) from the
+    library's generated table file."""
+    global _MC_TABLES
+    if _MC_TABLES is None:
+        import os
+        import re
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc", "mc_tables.inc")
+        text = open(path).read()
+
+        def block(name):
+            body = text[text.index(name):]
+            body = body[body.index("{") + 1:body.index("}")]
+            return [int(v.rstrip("ULL"), 0) for v in re.findall(r"0x[0-9a-fA-F]+ULL|\b\d+\b", body)]
+
+        packed, length = block("GM_MC_TRI_PACKED_INIT"), block("GM_MC_TRI_LEN_INIT")
+        edges = np.zeros((256, 15), np.int64)
+        for c in range(256):
+            for k in range(15):
+                edges[c, k] = (packed[c] >> (4 * k)) & 0xf
+        _MC_TABLES = (edges, np.array(length, np.int64))
+    return _MC_TABLES
+
+
+_CORNERS = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+_EDGES = np.array([[0, 1], [1, 2], [2, 3], [3, 0], [4, 5], [5, 6], [6, 7], [7, 4], [0, 4], [1, 5], [2, 6], [3, 7]])
+
+
+def blob_mesh(n, seed, count=200, level=0.5, device="cuda"):
+    """The blob field's isosurface {f = level} as a triangle mesh: marching
+    cubes with linear interpolation on the field sampled at the n^3 points
+    (i + 1/2)/n of the unit cube (device float32 (3m, 3) vertices, int32
+    (m, 3) triangles, three vertices per triangle).  A vertex is computed
+    from its edge's two samples in a fixed order, so the cubes sharing an
+    edge produce the same bits and the surface is closed."""
     import torch
-    from . import api
-    X = blob_grid(cells, seed, count=count, device="cuda")
-    box = api.make_box((cells, cells, cells), cell_size=1.0 / cells)
-    V, _, T = ctx.mesh_box(box, X, bilateral_iters=0)
-    Vc = torch.empty_like(V)
-    Vc.copy_(V)
-    Tc = torch.empty((T.shape[0], 3), dtype=torch.int32, device=V.device)
-    Tc.copy_(T.view(torch.int32))
-    torch.cuda.synchronize()
-    return Vc, Tc
+    edges_tab, len_tab = (torch.as_tensor(a, device=device) for a in _mc_tables())
+    corners = torch.as_tensor(_CORNERS, device=device)
+    edge_ab = torch.as_tensor(_EDGES, device=device)
+    centres, sigmas, weights = blob_params(seed, count)
+    x = torch.as_tensor(_axis(n), device=device)
+    c = torch.as_tensor(centres, device=device)
+    s = torch.as_tensor(sigmas, device=device)
+    w = torch.as_tensor(weights, device=device)
+    gx = torch.exp(-(x[None, :] - c[:, 0:1]) ** 2 / (2 * s[:, None] ** 2)) * w[:, None]
+    gy = torch.exp(-(x[None, :] - c[:, 1:2]) ** 2 / (2 * s[:, None] ** 2))
+    gz = torch.exp(-(x[None, :] - c[:, 2:3]) ** 2 / (2 * s[:, None] ** 2))
+    f = torch.empty((n, n, n), dtype=torch.float32, device=device)  # [z, y, x]
+    for z0 in range(0, n, 8):
+        f[z0:z0 + 8] = torch.einsum("kz,ky,kx->zyx", gz[:, z0:z0 + 8], gy, gx).float()
+    h = 1.0 / n
+    tris = []
+    S = 16
+    for z0 in range(0, n - 1, S):
+        z1 = min(z0 + S, n - 1)
+        vals = [f[z0 + dz:z1 + dz, dy:n - 1 + dy, dx:n - 1 + dx] for (dx, dy, dz) in _CORNERS.tolist()]
+        case = torch.zeros(vals[0].shape, dtype=torch.int64, device=device)
+        for k, v in enumerate(vals):
+            case |= (v >= level).long() << k
+        act = torch.nonzero((case != 0) & (case != 255))
+        if act.shape[0] == 0:
+            continue
+        cz, cy, cx = act[:, 0] + z0, act[:, 1], act[:, 2]
+        cc = case[act[:, 0], act[:, 1], act[:, 2]]
+        ntri = len_tab[cc]
+        for t in range(5):
+            sel = ntri > t
+            if not bool(sel.any()):
+                break
+            bx, by, bz, bc = cx[sel], cy[sel], cz[sel], cc[sel]
+            tri = []
+            for j in range(3):
+                e = edges_tab[bc, 3 * t + j]
+                a, b = edge_ab[e, 0], edge_ab[e, 1]
+                pa = torch.stack([bx + corners[a, 0], by + corners[a, 1], bz + corners[a, 2]], 1)
+                pb = torch.stack([bx + corners[b, 0], by + corners[b, 1], bz + corners[b, 2]], 1)
+                swap = (pb < pa).any(1, keepdim=True)  # the lower sample first, whichever cube asks
+                p0, p1 = torch.where(swap, pb, pa), torch.where(swap, pa, pb)
+                f0 = f[p0[:, 2], p0[:, 1], p0[:, 0]]
+                f1 = f[p1[:, 2], p1[:, 1], p1[:, 0]]
+                tt = ((level - f0) / (f1 - f0))[:, None]
+                q0 = (p0.float() + 0.5) * h
+                q1 = (p1.float() + 0.5) * h
+                tri.append(q0 + tt * (q1 - q0))
+            tris.append(torch.stack(tri, 1))
+    P = torch.cat(tris, 0).reshape(-1, 3).contiguous()
+    T = torch.arange(P.shape[0], dtype=torch.int32, device=device).reshape(-1, 3)
+    del f
+    return P, T
 
 
-# Benchmark configurations with a voxelized blob mesh: (base res, mesh box
-# cells, seed, uniform radius or 0 for the radius field r = 2 + floor(30 s)).
+# Benchmark configurations with a voxelized blob mesh: (base res, field
+# samples per axis of the isosurface mesh (~1M / 4M / 8M triangles), seed,
+# uniform radius or 0 for the radius field r = 2 + floor(30 s)).
 CONFIGS = {
-    2: dict(res=256, cells=176, seed=2000, uniform=12),
-    3: dict(res=512, cells=352, seed=3000, uniform=0),
-    5: dict(res=1024, cells=512, seed=5000, uniform=8),
+    2: dict(res=256, samples=336, seed=2000, uniform=12),
+    3: dict(res=512, samples=672, seed=3000, uniform=0),
+    5: dict(res=1024, samples=950, seed=5000, uniform=8),
 }
 MESH_MARGIN = 0.05  # world units added around the mesh's box (GMorpho::Load's margin, GMorpho.cu:7735)
 
 
-def mesh_cells(config, res=None):
-    """Mesh box cells of a configuration, scaled with the grid when `res`
-    differs from the configuration's own (a multiple of 16)."""
+def mesh_samples(config, res=None):
+    """Field samples per axis of a configuration's mesh, scaled with the
+    grid when `res` differs from the configuration's own."""
     c = CONFIGS[config]
     if res is None or res == c["res"]:
-        return c["cells"]
-    return max(16, int(round(c["cells"] * res / c["res"] / 16.0)) * 16)
+        return c["samples"]
+    return max(16, int(round(c["samples"] * res / c["res"])))
 
 
 def config_inputs(ctx, config, res=None, voxelize_reps=0):
@@ -309,7 +388,7 @@ def config_inputs(ctx, config, res=None, voxelize_reps=0):
     from . import api
     c = CONFIGS[config]
     res = c["res"] if res is None else res
-    P, T = blob_mesh(ctx, mesh_cells(config, res), c["seed"])
+    P, T = blob_mesh(mesh_samples(config, res), c["seed"])
     desc = api.grid_attributes(P.cpu().numpy(), res, MESH_MARGIN)
     X = torch.zeros(res ** 3, dtype=torch.uint8, device=P.device)
     ctx.voxelize(desc, P, T, out=X)

@@ -270,6 +270,10 @@ gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items
                               int32_t bilateral_iters, int32_t lanes, gm_mesh_view* meshes, void* stream);
 /* Lane count the autotuner chose for the last tuned batch (0: none yet). */
 int32_t gm_batch_lanes(gm_ctx* ctx);
+/* Fault injection for tests: the next `count` lane buffer allocations of
+ * gm_batch_close_mesh on this context fail as if the device were out of
+ * memory (the call returns GM_ERR_OUT_OF_MEMORY; the context stays usable). */
+gm_status gm_batch_inject_alloc_failures(gm_ctx* ctx, int32_t count);
 
 /* ---------------------------------------------------------------- serving */
 /* Resident-grid edit server (no reference counterpart: the reference
@@ -302,7 +306,9 @@ typedef struct {
 
 typedef struct {
   uint64_t ticket;
-  int32_t status;          /* GM_OK, GM_ERR_CAPACITY (crop or radius bound), GM_ERR_CUDA */
+  int32_t status;          /* GM_OK, GM_ERR_CAPACITY (crop or radius bound), GM_ERR_OUT_OF_MEMORY
+                            * (crop buffers larger than the budget, or an allocation failed and the
+                            * request timed out), GM_ERR_NOT_READY (timed out waiting), GM_ERR_CUDA */
   float latency_ms;        /* submit -> result, host clock */
   float device_ms;         /* GPU time of the edit */
   int32_t dirty_lo[3];     /* fine-voxel box whose closing was recomputed */
@@ -335,6 +341,21 @@ long long gm_server_kernel_launches(gm_server* srv);
  * answered with GM_ERR_CAPACITY. */
 gm_status gm_server_snapshot(gm_server* srv, uint8_t* h_closing, int8_t* h_scale);
 gm_status gm_server_restore(gm_server* srv, const uint8_t* h_closing, const int8_t* h_scale);
+/* Admission (no reference counterpart).  An edit's crop buffers are taken
+ * from a device memory pool when it is dispatched and returned when its
+ * result is collected; it is dispatched only while the crop buffers of the
+ * edits on the GPU plus its own fit `budget_bytes` (default: the device's
+ * free memory at creation less a reserve of max(1 GiB, 5%), capped at the
+ * slots' needs for the largest crop; <= 0 keeps the current budget).  An
+ * edit waiting in the queue longer than `timeout_ms` (0: no limit) is
+ * answered with GM_ERR_NOT_READY, or GM_ERR_OUT_OF_MEMORY when an
+ * allocation for it failed. */
+gm_status gm_server_set_admission(gm_server* srv, int64_t budget_bytes, float timeout_ms);
+/* Bytes of crop buffers of the edits on the GPU, and the budget. */
+gm_status gm_server_memory(gm_server* srv, int64_t* inflight_bytes, int64_t* budget_bytes);
+/* Fault injection for tests: the next `count` crop-buffer allocations fail
+ * as if the device were out of memory (host side; no GPU fault). */
+gm_status gm_server_inject_alloc_failures(gm_server* srv, int32_t count);
 /* Per-kernel device time of the server's launches (CUDA events around each
  * launch on its slot stream), same JSON form as gm_ctx_profile_read. */
 gm_status gm_server_profile(gm_server* srv, int32_t enable);

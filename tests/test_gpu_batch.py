@@ -115,3 +115,31 @@ def test_batch_normals_of_large_meshes(gm_ctx):
         assert np.array_equal(Vb, V.cpu().numpy())
         assert np.array_equal(Tb, T.cpu().numpy())
         assert np.array_equal(Nb, N.cpu().numpy(), equal_nan=True)
+
+
+def test_batch_allocation_failure_injected(gm_ctx):
+    """A batch whose lane buffers cannot be allocated (failure injected on
+    the host) fails with GM_ERR_OUT_OF_MEMORY and leaves the context usable:
+    the next batch gives the same grids as separate calls."""
+    import torch
+    from broxy_gb300 import _lib as L_
+    items = []
+    for i, res in enumerate((32, 64)):
+        X = torch.as_tensor(synth.random_grid(res, 990 + i)).cuda()
+        d = api.make_desc(res)
+        items.append((d, X, None, 3 + i, torch.empty_like(X)))
+    # a fresh context, so that its lanes have no buffers yet
+    ctx = api.Context(0)
+    try:
+        assert L_.load().gm_batch_inject_alloc_failures(ctx.ctx, 1) == L_.GM_OK
+        with pytest.raises(L_.GMError) as e:
+            ctx.batch_close_mesh(items, bilateral_iters=0, lanes=2, mesh=False)
+        assert e.value.status == L_.GM_ERR_OUT_OF_MEMORY
+        ctx.batch_close_mesh(items, bilateral_iters=0, lanes=2, mesh=False)
+        torch.cuda.synchronize()
+        for d, X, R, r, out in items:
+            ref = gm_ctx.close(d, X, None, r)
+            torch.cuda.synchronize()
+            assert torch.equal(out, ref)
+    finally:
+        ctx.close_ctx()

@@ -3,9 +3,9 @@ path GMorpho::Load + GMorpho::Update, GMorpho/GMorpho.cu:7731-7817: the
 mesh voxelized, then the GM_REF sphere closing and contour marching cubes
 with 20 bilateral iterations):
 
-* 512^3 fine grid, the 200-blob solid's ~1M-triangle mesh (seed 2000)
+* 512^3 fine grid, the 200-blob field's ~1M-triangle isosurface (seed 2000)
   voxelized, uniform radius 12; the voxelization itself equals the oracle's;
-* 1024^3 fine grid, the ~3.8M-triangle mesh (seed 3000) voxelized, radius
+* 1024^3 fine grid, the ~4M-triangle isosurface (seed 3000) voxelized, radius
   field r = 2 + floor(30 s(x)): exactly the inputs bench.py times.
 
 The GPU closing must equal the oracle's on every cell, the meshes must have
@@ -15,7 +15,7 @@ tests/golden/bench_manifest.json; when this run's inputs hash as recorded
 there, its outputs must hash as recorded too (the same bits as the run that
 wrote the manifest, which was itself checked against the oracle).
 
-* 2048^3 resident serving grid (the ~8M-triangle mesh, seed 5000, voxelized;
+* 2048^3 resident serving grid (the ~8M-triangle isosurface, seed 5000, voxelized;
   base radius 8): after a stream of brush edits, the server's resident
   closing equals a full closing of the edited radius field (both on the GPU).
 """

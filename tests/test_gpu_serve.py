@@ -178,3 +178,60 @@ def test_snapshot_restore_and_patch_export(tmp_path):
     assert nf == r["patch_triangles"] and 0 < nv <= r["patch_vertices"]
     srv.destroy()
     srv2.destroy()
+
+
+def test_admission_by_memory_failures_and_timeout(gm_ctx):
+    """Admission by memory, with failures injected on the host (no GPU
+    fault): allocations that fail leave their edits queued and retried; a
+    budget that holds one edit at a time serialises the edits; an edit
+    larger than the budget is refused; a queue timeout answers the edits
+    that cannot get memory.  Every edit that ran was applied exactly: the
+    resident closing equals a full closing of the edited field."""
+    import torch
+    edits = _edits(128, n=10, seed=11)
+    desc, X, R = _setup(128)
+    srv = api.Server(desc, X, R, slots=3, max_crop_res=96, rmax=8)
+    inflight, budget = srv.memory()
+    assert inflight == 0 and budget > 0
+    # 1. the first allocations fail: the edits wait and are retried
+    srv.inject_alloc_failures(3)
+    results = []
+    for c, scale, support, mode in edits[:5]:
+        srv.submit(c, scale, support, 0.0, mode)
+        results += srv.poll()
+    results += srv.drain()
+    assert len(results) == 5 and all(r["status"] == L.GM_OK for r in results)
+    assert srv.memory()[0] == 0
+    # 2. a budget that holds one edit: edits run one after the other
+    one = max(1, budget // 3 // 2)
+    srv.set_admission(budget_bytes=one, timeout_ms=0.0)
+    results = []
+    for c, scale, support, mode in edits[5:8]:
+        srv.submit(c, scale, support, 0.0, mode)
+        assert srv.memory()[0] <= one
+        results += srv.poll()
+    results += srv.drain()
+    statuses = sorted(r["status"] for r in results)
+    # an edit needing more than the budget is refused at once, the others run
+    assert all(st in (L.GM_OK, L.GM_ERR_OUT_OF_MEMORY) for st in statuses)
+    ran = [r for r in results if r["status"] == L.GM_OK]
+    # 3. failures without end and a timeout: the edits are answered
+    srv.set_admission(budget_bytes=budget, timeout_ms=50.0)
+    srv.inject_alloc_failures(1 << 20)
+    for c, scale, support, mode in edits[8:]:
+        srv.submit(c, scale, support, 0.0, mode)
+    timed = srv.drain()
+    assert len(timed) == 2 and all(r["status"] == L.GM_ERR_OUT_OF_MEMORY for r in timed)
+    srv.inject_alloc_failures(0)
+    srv.set_admission(budget_bytes=budget, timeout_ms=0.0)
+    # still serving
+    c, scale, support, mode = edits[0]
+    srv.submit(c, scale, support, 0.0, mode)
+    assert all(r["status"] == L.GM_OK for r in srv.drain())
+    torch.cuda.synchronize()
+    full = gm_ctx.close(desc, X, R, 0, L.GM_REF, L.GM_SE_SPHERE)
+    torch.cuda.synchronize()
+    assert torch.equal(srv.closing(), full)
+    assert srv.memory()[0] == 0
+    assert len(ran) >= 1
+    srv.destroy()
