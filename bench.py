@@ -132,6 +132,11 @@ LIMITER = {
 }
 
 
+# ALU pipe utilisation of the min-plus passes from their ncu capture
+# (sm__inst_executed_pipe_alu, profiles/k_pass_dpx_512.md, 512^3 case).
+ALU_PIPE_NCU = {}
+
+
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # one ncu capture of each kernel, scaled to the 1024^3 workload by the
 # units processed (see profiles/).
@@ -258,10 +263,21 @@ def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, worl
             return {"kernel": name, "bound": "hbm", "achieved": None, "peak": hbm, "unit": "GB/s", "frac": None,
                     "peak_kind": peak_kind, "traffic": None, "per_launch_ms": round(per_launch_ms, 4)}
         ach = nbytes / (per_launch_ms * 1e-3) / 1e9
-        return {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": TRAFFIC.get(name) if res == RES else None,
-                "algorithmic_bytes_per_launch": int(nbytes), "bytes_model": model, "limiter": LIMITER.get(name),
-                "per_launch_ms": round(per_launch_ms, 4)}
+        out = {"kernel": name, "bound": "hbm", "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+               "frac": round(ach / hbm, 4), "peak_kind": peak_kind, "traffic": TRAFFIC.get(name) if res == RES else None,
+               "algorithmic_bytes_per_launch": int(nbytes), "bytes_model": model, "limiter": LIMITER.get(name),
+               "per_launch_ms": round(per_launch_ms, 4)}
+        if name in ALU_PIPE_NCU:
+            # HBM is the only memory roofline the peaks give; this kernel is
+            # bound by the integer ALU pipe, whose measured utilisation is here
+            out["alu_pipe_util_ncu"] = ALU_PIPE_NCU[name]
+        if name.startswith(("k_pass_dil", "k_dil_pass", "k_pass_ero", "k_ero_pass")):
+            # the operation-level bytes of a morphology pass (read X + read R
+            # + write the result, V/8 + V + V/8), credited to this one kernel
+            sb = 1.25 * V
+            out["operation_bytes_per_launch"] = int(sb)
+            out["frac_of_operation_bytes"] = round(sb / (per_launch_ms * 1e-3) / 1e9 / hbm, 4)
+        return out
 
     if top[0] is not None:
         roof = kernel_roof(*top)
@@ -427,7 +443,7 @@ def run_serve(args):
     res = args.serve_res
     dev = torch.device("cuda")
     # configuration 5's input: the ~8M-triangle blob mesh voxelized into the grid
-    mctx = api.Context(dev.index)
+    mctx = api.Context(torch.cuda.current_device())
     inp = synth.config_inputs(mctx, 5, res=res)
     X, desc = inp["X"], inp["desc"]
     mesh_triangles = int(inp["T"].shape[0])
@@ -498,6 +514,18 @@ def cpu_crop(X, R, res, sub):
     return Xc, Rc
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return None
+
+
 def cpu_baseline(X, R, res, sub):
     """The oracle's reference-algorithm closing + MC + normals on all host
     cores, on a centre crop of the same inputs (bounded sample)."""
@@ -510,6 +538,7 @@ def cpu_baseline(X, R, res, sub):
     dt = time.perf_counter() - t0
     vox = (2 * sub) ** 3
     return {"value": round(vox / dt / 1e9, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "cpu_model": cpu_model(),
             "sample": "centre crop of %d^3 fine voxels of the same grid and radius field; oracle GM_REF closing "
                       "(pyramid traversal, OpenMP) + contour MC + %d bilateral iterations; %.1f s" %
                       (2 * sub, BILATERAL, dt)}
@@ -561,6 +590,7 @@ def run_reference(args, rank, world):
             "data": "synthetic",
             "config": {"workload": "crop: %d^3 fine voxels of the 1024^3 grid, same radius field" % (2 * sub)},
             "cpu_baseline": {"value": round(val, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": "centre crop of %d^3 fine voxels per step" % (2 * sub)},
             "e2e": {"value": round(val, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
