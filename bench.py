@@ -156,6 +156,13 @@ def run_ours(args, rank, world):
     V = (2 * res) ** 3
     inp = make_inputs(ctx, res)
     X, R, desc = inp["X"], inp["R"], inp["desc"]
+    # the voxelizer's kernels, one more run with per-kernel events
+    ctx.profile(True)
+    ctx.profile_reset()
+    ctx.voxelize(desc, inp["P"], inp["T"], out=X)
+    torch.cuda.synchronize()
+    vox_kernels = {k: round(v["ms"], 3) for k, v in ctx.profile_read().items()}
+    ctx.profile(False)
     out = torch.empty_like(X)
 
     def step():
@@ -205,7 +212,7 @@ def run_ours(args, rank, world):
     r = finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value, desc)
     r["voxelize"] = {"ms": round(inp["voxelize_ms"], 3), "input_triangles": int(inp["T"].shape[0]),
                      "input_vertices": int(inp["P"].shape[0]), "grid": "%d^3 fine" % (2 * res),
-                     "data_res": [int(v) for v in desc.data_res],
+                     "data_res": [int(v) for v in desc.data_res], "kernels_ms": vox_kernels,
                      "note": "gm_voxelize (conservative surface + parity fill), device time, median of 5; "
                              "reported apart, not part of value (GMorpho::Load runs it once per mesh)"}
     return r

@@ -922,7 +922,7 @@ __device__ __forceinline__ uint32_t put_records(const uint64_t* kv, int m, uint2
   return w;
 }
 
-__global__ void __launch_bounds__(256, 3) k_adj_finish(const float* __restrict__ V, const uint32_t* __restrict__ T,
+__global__ void __launch_bounds__(256, 4) k_adj_finish(const float* __restrict__ V, const uint32_t* __restrict__ T,
                              const uint32_t* __restrict__ rowptr, uint32_t* __restrict__ adj, int64_t nv,
                              int zero_isolated, float4* __restrict__ N4, float* __restrict__ N3,
                              uint2* __restrict__ ent, uint32_t* __restrict__ ncnt) {

@@ -141,11 +141,14 @@ __global__ void k_voxelize_tris(const float* __restrict__ P, const uint32_t* __r
     const double cz = dsub(dmul(d0[0], d2[1]), dmul(d0[1], d2[0]));
     const double a2 = dadd(dadd(dmul(cx, cx), dmul(cy, cy)), dmul(cz, cz));
     if (!(a2 > 0) || !(__ddiv_rn(dmul(maxl2, maxl2), a2) < 2500.0)) continue;
+    // voxels x whose closed box [x, x + 1] meets [mn, mx] on every axis:
+    // ceil(mn) - 1 <= x <= floor(mx) (the box test of tri_box_overlap, so
+    // the voxels outside could not pass it)
     int lo[3], hi[3];
     for (int a = 0; a < 3; a++) {
       const double mn = fmin(g[0][a], fmin(g[1][a], g[2][a])), mx = fmax(g[0][a], fmax(g[1][a], g[2][a]));
-      lo[a] = max((int)floor(mn) - 1, 0);
-      hi[a] = min((int)floor(mx) + 1, N - 1);
+      lo[a] = max((int)ceil(mn) - 1, 0);
+      hi[a] = min((int)floor(mx), N - 1);
     }
     for (int z = lo[2]; z <= hi[2]; z++)
       for (int y = lo[1]; y <= hi[1]; y++)
