@@ -985,7 +985,11 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   const int obase = o0 + grp * kDpxPer;
   const int sp0 = (sub ? 2 * obase + 1 : obase) - lo;
   uint32_t best[kDpxPer];
-  if (finite && step == 1) {
+  // The lattice-point erosion (KERN_LAT2) is the only pass with outputs at
+  // every other position (sub, step 2) and the only one that has them:
+  // each instantiation compiles one of the two tap loops.
+  constexpr bool kSub = G == KERN_LAT2;
+  if (finite && !kSub) {
     // Register sliding windows: wp[(j + k) % 16] holds tile row sp0 + j + k
     // and wm[(j - k) mod 16] holds row sp0 + j - k, so that after tap k only
     // one new row per side is loaded (into the slot its leaving row frees).
@@ -1035,27 +1039,68 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
       }
     }
   dpx_done:;
-  } else if (finite) {
-    const uint32_t g0 = gpair<G>(0, cap);
+  } else if (finite && kSub) {
+    // Outputs at every other position (sub): output j sits on tile row
+    // sp0 + 2j and reads rows sp0 + 2j + delta.  The taps split by the
+    // parity of delta into two stride-1 sequences over the rows of one
+    // parity, R(h) = row b + 2h (b = sp0: delta = 2d; b = sp0 - 1:
+    // delta = 2d - 1; h = j + d), each run with the register sliding window
+    // of the full-resolution path: one new row per side and tap instead of
+    // one load per output and tap.
 #pragma unroll
-    for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tile[(sp0 + step * j) * 32 + lane], g0, capp);
-    for (int k = 1; k <= halo_t; k++) {
-      const uint32_t gp = gpair<G>(k, cap), gm_ = gpair<G>(-k, cap);
+    for (int j = 0; j < kDpxPer; j++) best[j] = capp;
+    const uint32_t* tcol = tile + lane;
+#pragma unroll 1
+    for (int par = 0; par < 2; par++) {
+      const int e0 = -par;                   // delta of the group's centre tap (d = 0)
+      const uint32_t* tb = tcol + (sp0 - par) * 32;  // R(h) = tb[64 h]
+      const int kp = (halo_t - e0) >> 1;     // plus taps d = k: delta = 2k + e0 <= halo_t
+      const int km = (halo_t + e0) >> 1;     // minus taps d = -k: delta = -2k + e0 >= -halo_t
+      const int kmax = kp > km ? kp : km;
+      uint32_t wp[kDpxPer], wm[kDpxPer];
 #pragma unroll
       for (int j = 0; j < kDpxPer; j++) {
-        const int sp = sp0 + step * j;
-        best[j] = step_min<G>(tile[(sp + k) * 32 + lane], gp, best[j]);
-        best[j] = step_min<G>(tile[(sp - k) * 32 + lane], gm_, best[j]);
+        wp[j] = tb[(j < 1 ? kDpxPer : j) * 64];
+        wm[j] = tb[(j < kDpxPer - 1 ? j : -1) * 64];
       }
-      if ((k & 1) == 0) {
-        uint32_t m = best[0];
+      const uint32_t gc = pack_cap(kern_g<G>(e0), cap);
 #pragma unroll
-        for (int j = 1; j < kDpxPer; j++) m = __vmaxu2(m, best[j]);
-        const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
-        const uint32_t np = kern_g<G>(k + 1), nm = kern_g<G>(-(k + 1));
-        const uint32_t nxt = np < nm ? np : nm;
-        if (__all_sync(0xffffffffu, nxt + tmin >= mx)) break;
+      for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tb[j * 64], gc, best[j]);
+      for (int kb = 0; kb <= kmax; kb += kDpxPer) {
+#pragma unroll
+        for (int u = 0; u < kDpxPer; u++) {
+          const int k = kb + u;
+          if (k == 0) continue;
+          if (k > kmax) goto sub_done;
+          if (k <= kp) {
+            const uint32_t gp = pack_cap(kern_g<G>(2 * k + e0), cap);
+#pragma unroll
+            for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(wp[(j + u) % kDpxPer], gp, best[j]);
+          }
+          if (k <= km) {
+            const uint32_t gm_ = pack_cap(kern_g<G>(-2 * k + e0), cap);
+#pragma unroll
+            for (int j = 0; j < kDpxPer; j++)
+              best[j] = step_min<G>(wm[(j - u + kDpxPer) % kDpxPer], gm_, best[j]);
+          }
+          if (k == kmax) goto sub_done;
+          // R(k + 16) and R(-k - 1) enter for the next tap, in the slots
+          // that R(k) and R(15 - k) leave
+          if (k < kp) wp[u] = tb[(k + kDpxPer) * 64];
+          if (k < km) wm[(kDpxPer - 1 - u) % kDpxPer] = tb[(-k - 1) * 64];
+          if ((u & 3) == 3) {  // every fourth tap: leave once no output can improve
+            uint32_t m = best[0];
+#pragma unroll
+            for (int j = 1; j < kDpxPer; j++) m = __vmaxu2(m, best[j]);
+            const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
+            const uint32_t np = k + 1 <= kp ? kern_g<G>(2 * (k + 1) + e0) : 0xffffu;
+            const uint32_t nm = k + 1 <= km ? kern_g<G>(-2 * (k + 1) + e0) : 0xffffu;
+            const uint32_t nxt = np < nm ? np : nm;
+            if (__all_sync(0xffffffffu, nxt + tmin >= mx)) goto sub_done;
+          }
+        }
       }
+    sub_done:;
     }
   } else {
 #pragma unroll
@@ -1142,6 +1187,7 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
                        int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry, cudaStream_t st,
                        KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0,
                        NeedMap need = NeedMap{nullptr, 0, 0, 0, 0, 0, 0, 0, 0, CBox{{0, 0, 0}, {1 << 30, 1 << 30, 1 << 30}}}) {
+  if ((G == KERN_LAT2) != (sub != 0)) return;  // (every call site pairs them; see k_pass_dpx)
   const size_t smem = dpx_smem_bytes(sub, halo);
   ensure_dynamic_smem(reinterpret_cast<const void*>(k_pass_dpx<G, TIn, FIN>), smem);
   const int na = axis == 1 ? ny : nz;
