@@ -383,13 +383,37 @@ def run_batch(args, ctx):
     plain_ms, t_plain = timed(plain, 3)
     batch_ms, t_batch = timed(batched, 3)
     assert t_plain == t_batch
+
+    def kernel_time(fn):
+        """Device time of the kernels of one run, by phase (events around
+        each launch; the batch then runs without its graph)."""
+        ctx.profile(True)
+        ctx.profile_reset()
+        fn()
+        torch.cuda.synchronize()
+        prof = ctx.profile_read()
+        ctx.profile(False)
+        ph = {"closing": 0.0, "mesh": 0.0, "bilateral": 0.0}
+        for k, v in prof.items():
+            key = "bilateral" if k.startswith("k_bilateral") else (
+                "mesh" if k.startswith(("k_mc", "k_adj", "k_scan", "k_rec", "k_row0", "k_brick")) else "closing")
+            ph[key] += v["ms"]
+        return {k: round(v, 2) for k, v in ph.items()}, round(sum(v["ms"] for v in prof.values()), 2)
+
+    plain_phases, plain_kernel_ms = kernel_time(plain)
+    batch_phases, batch_kernel_ms = kernel_time(batched)
     vox = sum((2 * it["res"]) ** 3 for it in inst)
     edges = [it["edge"] for it in inst]
     return {"instances": len(inst), "plain_ms": round(plain_ms, 3), "batched_ms": round(batch_ms, 3),
             "speedup": round(plain_ms / batch_ms, 3), "lanes": ctx.batch_lanes,
             "edge_min": min(edges), "edge_max": max(edges), "fine_voxels": int(vox), "triangles": int(t_batch),
             "radius": "U{1..24}", "closing": "GM_REF sphere, 20 bilateral iterations",
-            "batched_gvoxel_s": round(vox / (batch_ms * 1e-3) / 1e9, 3)}
+            "batched_gvoxel_s": round(vox / (batch_ms * 1e-3) / 1e9, 3),
+            "breakdown": {"plain_kernel_ms": plain_kernel_ms, "plain_phases_ms": plain_phases,
+                          "batched_kernel_ms": batch_kernel_ms, "batched_phases_ms": batch_phases,
+                          "note": "kernel device time summed over launches (concurrent lanes overlap in the "
+                                  "batched wall time); the plain calls' kernel time is their wall time, so "
+                                  "batching removes work (padding, per-grid tails), not launch overhead"}}
 
 
 def run_frame_field(args, ctx, X, R, res, desc):
