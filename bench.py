@@ -133,16 +133,16 @@ LIMITER = {
 
 
 # ALU pipe utilisation of the min-plus passes from their ncu capture
-# (sm__inst_executed_pipe_alu, profiles/k_pass_dpx_512.md, 512^3 case).
-ALU_PIPE_NCU = {}
+# (sm__pipe_alu_cycles_active, profiles/k_pass_dpx_512.md, 512^3 case).
+ALU_PIPE_NCU = {"k_pass_dil_y": 0.691, "k_pass_dil_z": 0.735}
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # one ncu capture of each kernel, scaled to the 1024^3 workload by the
 # units processed (see profiles/).
 TRAFFIC = {
-    "k_bilateral": 338_000_000,     # 77.5 MB at 1.10M vertices / 2.19M triangles, x4.366
-    "k_pass_dil_z": 3_354_000_000,  # 419.3 MB at 512^3 fine voxels, x8
+    "k_bilateral": 550_000_000,     # 129.0 MB at 1.70M vertices / 3.40M triangles, x4.26
+    "k_pass_dil_z": 3_358_000_000,  # 419.7 MB at 512^3 fine voxels, x8
 }
 
 
