@@ -874,29 +874,6 @@ __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, i
 // With use_tma, the u16 input tile is staged by TMA (tmap: boxes of 64
 // columns x span rows x 1 slice along (x, pass axis, third axis), one per
 // slice; rows are 128 bytes, so each slice starts 128-byte aligned).
-// The same bound for one warp's outputs (its kDpxPer positions along the
-// axis starting at `ob`, the tile's x columns, the third axis widened by
-// rext): a tighter window where the radii vary across the tile.  Every
-// reader of these outputs has r <= the bound.
-__device__ int warp_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, int nx, int n3, int axis, int nout,
-                           int ob, int rext, int bz) {
-  const int lane = threadIdx.x & 31;
-  const int xa = (blockIdx.x * kDpxCols) >> 4, xb = (min(blockIdx.x * kDpxCols + kDpxCols, nx) - 1) >> 4;
-  const int aa = ob >> 4, ab = (min(ob + kDpxPer, nout) - 1) >> 4;
-  const int ta = max(2 * bz - rext, 0) >> 4, tb = min(2 * bz + 1 + rext, n3 - 1) >> 4;
-  const int cx = xb - xa + 1, ca = ab - aa + 1, ct = tb - ta + 1;
-  int m = 0;
-  if (ca > 0)
-    for (int i = lane; i < cx * ca * ct; i += 32) {
-      const int ix = xa + i % cx, ia = aa + (i / cx) % ca, it = ta + i / (cx * ca);
-      const int my = axis == 1 ? ia : it, mz = axis == 1 ? it : ia;
-      const int v = rmap[idx3(ix, my, mz, mbx, mby)];
-      m = v > m ? v : m;
-    }
-  m = __reduce_max_sync(0xffffffffu, m);
-  return clamp_radius(m);
-}
-
 template <int G, typename TIn, int FIN>
 __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
                                                   uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
@@ -1007,18 +984,6 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   }
   const int obase = o0 + grp * kDpxPer;
   const int sp0 = (sub ? 2 * obase + 1 : obase) - lo;
-  // Dilation passes with a radius field: the warp's own window and the
-  // saturation its outputs' readers can tell apart ((rw + 1)^2): taps past
-  // it cannot change a thresholded bit downstream.
-  int halo_w = halo_t;
-  uint32_t capw = cap;
-  if (rmap != nullptr && step == 1 && finite) {
-    const int rw = warp_radius(rmap, nx >> 4, ny >> 4, nx, n3, axis, nout, obase, rext,
-                               (int)blockIdx.z + need.third0);
-    halo_w = rw + 2 < halo_t ? rw + 2 : halo_t;
-    const uint32_t cw = G == KERN_CUBE ? (uint32_t)(rw + 1) : (uint32_t)((rw + 1) * (rw + 1));
-    capw = cw < cap ? cw : cap;
-  }
   uint32_t best[kDpxPer];
   // The lattice-point erosion (KERN_LAT2) is the only pass with outputs at
   // every other position (sub, step 2) and the only one that has them:
@@ -1042,12 +1007,12 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
 #pragma unroll
     for (int j = 0; j < kDpxPer; j++) best[j] = step_min<G>(tcol[(sp0 + j) * 32], g0, capp);
     uint32_t gprev = g0;  // +side kernel of the previous tap (the -side of this one for LAT, CUBE)
-    for (int kb = 0; kb <= halo_w; kb += kDpxPer) {
+    for (int kb = 0; kb <= halo_t; kb += kDpxPer) {
 #pragma unroll
       for (int u = 0; u < kDpxPer; u++) {
         const int k = kb + u;
         if (k == 0) continue;
-        if (k > halo_w) goto dpx_done;
+        if (k > halo_t) goto dpx_done;
         const uint32_t graw = kern_pos<G>(k);
         const uint32_t gp = pack_cap(graw, cap);
         const uint32_t gm_ = G == KERN_CEN2 ? gp : gprev;
@@ -1057,7 +1022,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
           best[j] = step_min<G>(wp[(j + u) % kDpxPer], gp, best[j]);
           best[j] = step_min<G>(wm[(j - u + kDpxPer) % kDpxPer], gm_, best[j]);
         }
-        if (k == halo_w) goto dpx_done;  // no further tap: load nothing past the window
+        if (k == halo_t) goto dpx_done;  // no further tap: load nothing past the window
         // rows sp0 + k + 16 and sp0 - k - 1 enter; the slots of rows
         // sp0 + k and sp0 + 15 - k are free now (k < halo_e keeps both in the window)
         wp[u] = tcol[(sp0 + k + kDpxPer) * 32];
@@ -1069,7 +1034,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
           const uint32_t mx = (m & 0xffffu) > (m >> 16) ? (m & 0xffffu) : (m >> 16);
           // smallest kernel value of the taps to come (k + 1 on either side)
           const uint32_t nxt = G == KERN_CEN2 ? kern_pos<G>(k + 1) : graw;
-          if (__all_sync(0xffffffffu, nxt + tmin >= (mx < capw ? mx : capw))) goto dpx_done;
+          if (__all_sync(0xffffffffu, nxt + tmin >= mx)) goto dpx_done;
         }
       }
     }
