@@ -378,11 +378,24 @@ def run_batch(args, ctx):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) * 1e3 / reps, v
 
+    def form(lanes):
+        def run():
+            ms = ctx.batch_close_mesh(items, bilateral_iters=BILATERAL, lanes=lanes)
+            return sum(m[2].shape[0] for m in ms)
+        return run
+
     timed(plain, 1)
-    timed(batched, 1)  # first call: autotunes the lane count and captures the graph
+    timed(batched, 1)  # first call: autotunes the form (lane count or grouped) and captures the graph
+    tuned = ctx.batch_lanes
     plain_ms, t_plain = timed(plain, 3)
     batch_ms, t_batch = timed(batched, 3)
     assert t_plain == t_batch
+    forms_ms = {}
+    for name, lanes in (("lanes_4", 4), ("grouped", api.L.GM_BATCH_GROUPED)):
+        timed(form(lanes), 1)
+        forms_ms[name], t_form = timed(form(lanes), 3)
+        forms_ms[name] = round(forms_ms[name], 3)
+        assert t_form == t_plain
 
     def kernel_time(fn):
         """Device time of the kernels of one run, by phase (events around
@@ -402,10 +415,22 @@ def run_batch(args, ctx):
 
     plain_phases, plain_kernel_ms = kernel_time(plain)
     batch_phases, batch_kernel_ms = kernel_time(batched)
+    # the grouped form: its min-plus passes (one launch each for all grids,
+    # nothing beside them) against the rest of its kernels
+    ctx.profile(True)
+    ctx.profile_reset()
+    form(api.L.GM_BATCH_GROUPED)()
+    torch.cuda.synchronize()
+    gprof = ctx.profile_read()
+    ctx.profile(False)
+    gpass = {k: round(v["ms"], 3) for k, v in gprof.items() if k.endswith("_group")}
     vox = sum((2 * it["res"]) ** 3 for it in inst)
     edges = [it["edge"] for it in inst]
     return {"instances": len(inst), "plain_ms": round(plain_ms, 3), "batched_ms": round(batch_ms, 3),
-            "speedup": round(plain_ms / batch_ms, 3), "lanes": ctx.batch_lanes,
+            "speedup": round(plain_ms / batch_ms, 3),
+            "form": "grouped" if tuned == api.L.GM_BATCH_GROUPED else "lanes", "lanes": tuned,
+            "forms_ms": forms_ms, "grouped_passes_ms": gpass,
+            "grouped_passes_total_ms": round(sum(gpass.values()), 3),
             "edge_min": min(edges), "edge_max": max(edges), "fine_voxels": int(vox), "triangles": int(t_batch),
             "radius": "U{1..24}", "closing": "GM_REF sphere, 20 bilateral iterations",
             "batched_gvoxel_s": round(vox / (batch_ms * 1e-3) / 1e9, 3),

@@ -19,6 +19,7 @@ GM_ERR_NOT_READY = 6
 
 GM_REF, GM_EXACT = 0, 1
 GM_SE_SPHERE, GM_SE_CUBE = 0, 1
+GM_BATCH_GROUPED = -1  # batch form: one persistent launch per min-plus pass for all grids
 GM_BRUSH_MAX, GM_BRUSH_MIN, GM_BRUSH_ZERO = 1, 2, 3
 
 

@@ -31,6 +31,9 @@
 
 namespace gm {
 
+constexpr int kBatchGrouped = GM_BATCH_GROUPED;  // one launch per min-plus pass for all grids
+constexpr int kGroupedLanes = 4;   // streams for the grouped form's per-grid kernels
+
 struct BatchLane {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
@@ -59,6 +62,13 @@ struct BatchState {
   void* d_filter = nullptr;   // table of the grouped normal filtering (mesh_filter_table_bytes)
   void* h_filter = nullptr;   // pinned
   int filter_cap = 0;
+  // grouped form: per-grid workspaces (all grids' closings are in flight
+  // together) and the min-plus pass of each phase, one set for live runs
+  // and one owned by the captured graph
+  uint8_t* arena = nullptr;
+  size_t arena_bytes = 0;
+  std::vector<size_t> arena_off;  // per grid: workspace, then crop buffers
+  std::vector<DpxGroup*> groups[2];
   cudaEvent_t fork = nullptr;
   cudaStream_t cap_st = nullptr;  // capture / replay stream (the caller's may be the legacy stream)
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
@@ -66,6 +76,7 @@ struct BatchState {
   uint64_t graph_sig = 0;
   long long graph_kernels = 0;
   std::map<uint64_t, int> tuned;
+  int last_tuned = 0;  // the form chosen by the latest tuning
 };
 
 void batch_release(void* p) {
@@ -94,6 +105,9 @@ void batch_release(void* p) {
   if (b->ev_in) cudaEventDestroy(b->ev_in);
   if (b->ev_out) cudaEventDestroy(b->ev_out);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->arena);
+  for (auto& gs : b->groups)
+    for (DpxGroup* g : gs) dpx_group_free(g);
   delete b;
 }
 
@@ -156,6 +170,33 @@ static std::vector<int> assign(int n, const std::vector<int>& ext, int L) {
   return lane;
 }
 
+// Closing arguments of grid i on the extent E (crop buffers Xc / Cc when the
+// extent is smaller than the grid).
+static CloseArgs batch_close_args(const gm_batch_item& it, int E, int rmax, int mode, int se, uint8_t* ws,
+                                  uint8_t* Xc, uint8_t* Cc, int sms) {
+  const bool crop = E < it.desc.res;
+  CloseArgs a;
+  a.res = E;
+  for (int k = 0; k < 3; k++) a.data_res[k] = it.desc.data_res[k] < E ? it.desc.data_res[k] : E;
+  a.X = crop ? Xc : it.d_input;
+  a.R = it.d_scale;
+  if (crop) {
+    // the radius field is read in place, with the instance grid's strides
+    a.r_sy = 2 * (int64_t)it.desc.res;
+    a.r_sz = 4 * (int64_t)it.desc.res * it.desc.res;
+  }
+  a.uniform_r = it.uniform_radius;
+  a.rmax = rmax;
+  a.mode = mode;
+  a.se = se;
+  a.C_out = crop ? Cc : it.d_closing;
+  a.D_out = nullptr;
+  a.S_out = nullptr;
+  a.workspace = ws;
+  a.num_sms = sms;
+  return a;
+}
+
 // The closing phase: fork from `st`, every lane runs its instances, join.
 // With `ma`, each closing is followed on its lane by the mesh counts of the
 // grid (totals to the pinned b->h_tot) and the grid's event, so that its
@@ -171,28 +212,11 @@ static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* i
     BatchLane& ln = b->lanes[lane[i]];
     const int res = it[i].desc.res, E = ext[i];
     const bool crop = E < res;
-    CloseArgs a;
-    a.res = E;
-    for (int k = 0; k < 3; k++) a.data_res[k] = it[i].desc.data_res[k] < E ? it[i].desc.data_res[k] : E;
-    a.X = it[i].d_input;
-    a.R = it[i].d_scale;
     if (crop) {
       const int zero[3] = {0, 0, 0}, e3[3] = {E, E, E};
       if ((e = launch_box_copy(it[i].d_input, res, zero, ln.Xc, E, zero, e3, ln.st, kc)) != cudaSuccess) return e;
-      a.X = ln.Xc;
-      // the radius field is read in place, with the instance grid's strides
-      a.r_sy = 2 * (int64_t)res;
-      a.r_sz = 4 * (int64_t)res * res;
     }
-    a.uniform_r = it[i].uniform_radius;
-    a.rmax = rmax[i];
-    a.mode = mode;
-    a.se = se;
-    a.C_out = crop ? ln.Cc : it[i].d_closing;
-    a.D_out = nullptr;
-    a.S_out = nullptr;
-    a.workspace = ln.ws;
-    a.num_sms = sms;
+    const CloseArgs a = batch_close_args(it[i], E, rmax[i], mode, se, ln.ws, ln.Xc, ln.Cc, sms);
     if ((e = launch_close(a, ln.st, kc)) != cudaSuccess) return e;
     if (crop && (e = launch_embed(ln.Cc, E, it[i].d_closing, res, ln.st, kc)) != cudaSuccess) return e;
     if (ma) {
@@ -210,6 +234,94 @@ static cudaError_t enqueue_closings(BatchState* b, int n, const gm_batch_item* i
     if ((e = cudaEventRecord(b->lanes[l].done, b->lanes[l].st)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(st, b->lanes[l].done, 0)) != cudaSuccess) return e;
   }
+  return cudaSuccess;
+}
+
+// Grouped form: the closings go phase by phase (close_phases); the kernels
+// of a phase run per grid on the lanes, then the phase's min-plus pass of
+// all the grids as one persistent launch on `st` (dpx_group_launch: its
+// blocks pull the tiles of every grid from one work counter).  Each grid
+// has its own workspace in the arena.  `set` selects the pass tables: 0
+// for live runs, 1 for the tables a captured graph keeps reading.
+static cudaError_t enqueue_closings_grouped(BatchState* b, int set, int n, const gm_batch_item* it, const int* rmax,
+                                            const std::vector<int>& ext, int mode, int se, int L,
+                                            const std::vector<int>& lane, int sms, cudaStream_t st, KernelCounter* kc,
+                                            const MeshArgs* ma = nullptr) {
+  cudaError_t e;
+  const int P = close_phases(mode);
+  for (int p = 0; p < P; p++) {
+    if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return e;
+    for (int l = 0; l < L; l++)
+      if ((e = cudaStreamWaitEvent(b->lanes[l].st, b->fork, 0)) != cudaSuccess) return e;
+    DpxGroup* g = b->groups[set][p];
+    dpx_group_clear(g);
+    for (int i = 0; i < n; i++) {
+      BatchLane& ln = b->lanes[lane[i]];
+      const int res = it[i].desc.res, E = ext[i];
+      const bool crop = E < res;
+      uint8_t* ws = b->arena + b->arena_off[i];
+      uint8_t* Xc = crop ? ws + ((close_workspace_bytes(E) + 255) & ~(size_t)255) : nullptr;
+      uint8_t* Cc = crop ? Xc + (((size_t)E * E * E + 255) & ~(size_t)255) : nullptr;
+      if (p == 0 && crop) {
+        const int zero[3] = {0, 0, 0}, e3[3] = {E, E, E};
+        if ((e = launch_box_copy(it[i].d_input, res, zero, Xc, E, zero, e3, ln.st, kc)) != cudaSuccess) return e;
+      }
+      CloseArgs a = batch_close_args(it[i], E, rmax[i], mode, se, ws, Xc, Cc, sms);
+      a.phase = p;
+      a.group = g;
+      if ((e = launch_close(a, ln.st, kc)) != cudaSuccess) return e;
+      if (p == P - 1) {
+        if (crop && (e = launch_embed(Cc, E, it[i].d_closing, res, ln.st, kc)) != cudaSuccess) return e;
+        if (ma) {
+          if ((e = mesh_count_launch(ma[i], b->meshes[i], ln.st, kc, b->h_tot + 4 * i)) != cudaSuccess) return e;
+          cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+          if ((e = cudaStreamIsCapturing(ln.st, &cs)) != cudaSuccess) return e;
+          if ((e = cudaEventRecordWithFlags(b->ev_count[i], ln.st,
+                                            cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal
+                                                                                : cudaEventRecordDefault)) !=
+              cudaSuccess)
+            return e;
+        }
+      }
+    }
+    for (int l = 0; l < L; l++) {
+      if ((e = cudaEventRecord(b->lanes[l].done, b->lanes[l].st)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(st, b->lanes[l].done, 0)) != cudaSuccess) return e;
+    }
+    if (p < P - 1 && (e = dpx_group_launch(g, sms, st, kc)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Per-grid workspaces of the grouped form (grown when a batch needs more)
+// and the pass tables of its phases.
+static cudaError_t ensure_arena(BatchState* b, int n, const gm_batch_item* it, const std::vector<int>& ext, int mode) {
+  b->arena_off.assign(n, 0);
+  size_t total = 0;
+  for (int i = 0; i < n; i++) {
+    b->arena_off[i] = total;
+    size_t sz = (close_workspace_bytes(ext[i]) + 255) & ~(size_t)255;
+    if (ext[i] < it[i].desc.res) sz += 2 * ((((size_t)ext[i] * ext[i] * ext[i]) + 255) & ~(size_t)255);
+    total += sz;
+  }
+  cudaError_t e;
+  if (b->arena_bytes < total) {
+    cudaFree(b->arena);
+    b->arena = nullptr;
+    b->arena_bytes = 0;
+    if (b->inject_fail > 0) {
+      b->inject_fail--;
+      return cudaErrorMemoryAllocation;
+    }
+    if ((e = cudaMalloc(&b->arena, total)) != cudaSuccess) return e;
+    b->arena_bytes = total;
+  }
+  const int P = close_phases(mode);
+  for (auto& gs : b->groups)
+    while ((int)gs.size() < P) gs.push_back(dpx_group_new());
+  for (auto& gs : b->groups)
+    for (int p = 0; p < P; p++)
+      if ((e = dpx_group_reserve(gs[p], n)) != cudaSuccess) return e;
   return cudaSuccess;
 }
 
@@ -284,17 +396,29 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     if (se == GM_SE_CUBE) E = (std::max(reach + 1, 32) + 31) / 32 * 32;
     ext[i] = E >= it[i].desc.res ? it[i].desc.res : E;
   }
-  // lane count: requested, tuned for this signature, or tuned now
+  // form: the lane count requested (> 0), the grouped form (kBatchGrouped),
+  // or the one tuned for this signature (tuned now on its first call)
   int L = lanes_req;
   const uint64_t tune_sig = signature(n, it, ext, mode, se, 0);
-  if (L <= 0) {
+  if (L == 0) {
     auto f = b->tuned.find(tune_sig);
     if (f != b->tuned.end()) L = f->second;
   }
-  const bool tune = L <= 0;
+  const bool tune = L == 0;
+  bool phase_ok = true;
+  for (int i = 0; i < n; i++) phase_ok = phase_ok && close_phase_ok(rmax[i], se);
+  if (L == kBatchGrouped && !phase_ok) return cudaErrorNotSupported;  // a radius bound > 91
   const int cands[5] = {1, 2, 4, 8, 16};
-  const int maxL = tune ? 16 : std::max(1, std::min(L, 64));
+  const int maxL = tune ? 16 : L == kBatchGrouped ? std::min(kGroupedLanes, n) : std::max(1, std::min(L, 64));
   if ((e = ensure_lanes(b, maxL)) != cudaSuccess) return e;
+  // the grouped form's per-grid workspaces (a candidate of the tuner only
+  // when they fit)
+  bool grouped_ok = phase_ok && (tune || L == kBatchGrouped);
+  if (grouped_ok && (e = ensure_arena(b, n, it, ext, mode)) != cudaSuccess) {
+    if (L == kBatchGrouped) return e;
+    cudaGetLastError();
+    grouped_ok = false;
+  }
   // per-lane workspaces and crop buffers sized for the largest closing
   int maxres = 16, maxcrop = 0;
   for (int i = 0; i < n; i++) {
@@ -305,7 +429,7 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
   }
   const size_t wsb = close_workspace_bytes(maxres);
   const size_t ccells = (size_t)maxcrop * maxcrop * maxcrop;
-  for (int l = 0; l < maxL; l++) {
+  for (int l = 0; l < (L == kBatchGrouped ? 0 : maxL); l++) {
     BatchLane& ln = b->lanes[l];
     if (ln.ws_bytes < wsb) {
       cudaFree(ln.ws);
@@ -330,12 +454,18 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     cudaEventCreate(&t1);
     float best_ms = 1e30f;
     int best = 1;
-    for (int c : cands) {
-      const std::vector<int> lane = assign(n, ext, c);
+    std::vector<int> forms(cands, cands + 5);
+    if (grouped_ok) forms.push_back(kBatchGrouped);
+    for (int c : forms) {
+      const int cl = c == kBatchGrouped ? std::min(kGroupedLanes, n) : c;
+      const std::vector<int> lane = assign(n, ext, cl);
       // one untimed pass (first-touch, function attributes), one timed
       for (int rep = 0; rep < 2; rep++) {
         cudaEventRecord(t0, st);
-        if ((e = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, c, lane, sms, st, nullptr)) != cudaSuccess) {
+        e = c == kBatchGrouped
+                ? enqueue_closings_grouped(b, 0, n, it, rmax.data(), ext, mode, se, cl, lane, sms, st, nullptr)
+                : enqueue_closings(b, n, it, rmax.data(), ext, mode, se, c, lane, sms, st, nullptr);
+        if (e != cudaSuccess) {
           cudaEventDestroy(t0);
           cudaEventDestroy(t1);
           return e;
@@ -351,8 +481,11 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     cudaEventDestroy(t1);
     L = best;
     b->tuned[tune_sig] = L;
+    b->last_tuned = L;
   }
-  const std::vector<int> lane = assign(n, ext, L);
+  const bool grouped = L == kBatchGrouped;
+  const int LL = grouped ? std::min(kGroupedLanes, n) : L;  // lanes in use
+  const std::vector<int> lane = assign(n, ext, LL);
   // mesh arguments, count buffers, pinned totals and per-grid events, all
   // allocated before the closing phase (which may be captured)
   std::vector<MeshArgs> ma;
@@ -408,9 +541,15 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
       }
       cudaGraph_t g = nullptr;
       KernelCounter cap;  // counts the kernels the graph holds
+      // no replay of the earlier graph may still read the pass tables that
+      // this capture rewrites
+      if ((e = cudaEventSynchronize(b->ev_out)) != cudaSuccess) return e;
       if ((e = cudaStreamBeginCapture(b->cap_st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
-      const cudaError_t ec = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, b->cap_st, &cap,
-                                              meshes ? ma.data() : nullptr);
+      const cudaError_t ec =
+          grouped ? enqueue_closings_grouped(b, 1, n, it, rmax.data(), ext, mode, se, LL, lane, sms, b->cap_st, &cap,
+                                             meshes ? ma.data() : nullptr)
+                  : enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, b->cap_st, &cap,
+                                     meshes ? ma.data() : nullptr);
       e = cudaStreamEndCapture(b->cap_st, &g);
       if (ec != cudaSuccess) return ec;
       if (e != cudaSuccess) return e;
@@ -427,9 +566,11 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     if ((e = cudaStreamWaitEvent(st, b->ev_out, 0)) != cudaSuccess) return e;
     if (kc) kc->launches += b->graph_kernels;
   } else {
-    if ((e = enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, st, kc,
-                              meshes ? ma.data() : nullptr)) != cudaSuccess)
-      return e;
+    e = grouped ? enqueue_closings_grouped(b, 0, n, it, rmax.data(), ext, mode, se, LL, lane, sms, st, kc,
+                                           meshes ? ma.data() : nullptr)
+                : enqueue_closings(b, n, it, rmax.data(), ext, mode, se, L, lane, sms, st, kc,
+                                   meshes ? ma.data() : nullptr);
+    if (e != cudaSuccess) return e;
   }
   if (!meshes) return cudaGetLastError();
   // meshing: each grid's emission, on its lane's emission stream, once its
@@ -447,7 +588,7 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
     meshes[i].num_vertices = b->nv[i];
     meshes[i].num_triangles = b->nt[i];
   }
-  for (int l = 0; l < L; l++) {
+  for (int l = 0; l < LL; l++) {
     cudaEventRecord(b->lanes[l].em_done, b->lanes[l].em);
     cudaStreamWaitEvent(st, b->lanes[l].em_done, 0);
   }
@@ -478,8 +619,7 @@ cudaError_t batch_run(void** state, int n, const gm_batch_item* it, int mode, in
 
 int batch_lanes_tuned(void* state) {
   BatchState* b = static_cast<BatchState*>(state);
-  if (!b || b->tuned.empty()) return 0;
-  return b->tuned.rbegin()->second;
+  return b ? b->last_tuned : 0;
 }
 
 }  // namespace gm

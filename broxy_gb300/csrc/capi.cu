@@ -924,7 +924,7 @@ gm_status gm_mesh_download(gm_ctx* ctx, float* h_V, float* h_N, uint32_t* h_T, v
 gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items, gm_mode mode, gm_se se,
                               int32_t bilateral_iters, int32_t lanes, gm_mesh_view* meshes, void* stream) {
   if (!ctx) return GM_ERR_INVALID_ARGUMENT;
-  if (n < 0 || (n > 0 && !items) || bilateral_iters < 0 || lanes < 0 || lanes > 64)
+  if (n < 0 || (n > 0 && !items) || bilateral_iters < 0 || lanes < GM_BATCH_GROUPED || lanes > 64)
     return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: bad argument");
   if (mode != GM_REF && mode != GM_EXACT) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: mode");
   if (se != GM_SE_SPHERE && se != GM_SE_CUBE) return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: se");
@@ -939,10 +939,11 @@ gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items
   gm_status s = set_device(ctx);
   if (s != GM_OK) return s;
   ctx->has_mesh = false;
-  GM_CHECK_CUDA(ctx,
-                gm::batch_run(&ctx->batch, n, items, (int)mode, (int)se, bilateral_iters, lanes, meshes, ctx->num_sms,
-                              (cudaStream_t)stream, &ctx->kc),
-                "gm_batch_close_mesh");
+  const cudaError_t e = gm::batch_run(&ctx->batch, n, items, (int)mode, (int)se, bilateral_iters, lanes, meshes,
+                                      ctx->num_sms, (cudaStream_t)stream, &ctx->kc);
+  if (e == cudaErrorNotSupported)
+    return fail(ctx, GM_ERR_INVALID_ARGUMENT, "gm_batch_close_mesh: the grouped form needs radius bounds <= 91");
+  GM_CHECK_CUDA(ctx, e, "gm_batch_close_mesh");
   return GM_OK;
 }
 

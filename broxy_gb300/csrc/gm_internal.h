@@ -55,6 +55,19 @@ int64_t profile_json(KernelCounter& kc, char* buf, int64_t cap);
     if ((kc) != nullptr) (kc)->stop(name, st, gm_ev0_);            \
   } while (0)
 
+// The min-plus passes of many closings, gathered for one persistent
+// launch per pass (launch_close in phase mode records into it).
+struct DpxGroup;
+DpxGroup* dpx_group_new();
+void dpx_group_free(DpxGroup* g);
+void dpx_group_clear(DpxGroup* g);
+int dpx_group_size(const DpxGroup* g);
+// Room for `njobs` grids (allocates; not while a stream is being captured).
+cudaError_t dpx_group_reserve(DpxGroup* g, int njobs);
+// Uploads the recorded grids' pass arguments and launches one kernel whose
+// resident blocks pull the tiles of all of them from one work counter.
+cudaError_t dpx_group_launch(DpxGroup* g, int sms, cudaStream_t st, KernelCounter* kc);
+
 struct CloseArgs {
   int res = 0;        // base resolution of a cubic grid (a multiple of 16)
   int dims[3] = {0, 0, 0};  // box grid rx, ry, rz (multiples of 16) when dims[0] > 0; res is then unused
@@ -88,7 +101,19 @@ struct CloseArgs {
   uint8_t* S_out = nullptr;     // optional dilation contour, res^3
   uint8_t* workspace = nullptr; // close_workspace_bytes(res)
   int num_sms = 0;
+  // Phase mode (grouped launches over many grids): phase p >= 0 runs only
+  // the kernels between the closing's p-th and (p+1)-th min-plus passes
+  // (the ones before the first for p = 0) and records its p-th pass into
+  // `group` instead of launching it; close_phases() gives the number of
+  // phases.  Not for the radius-clamp fallbacks (rmax > 91) or `edt`.
+  int phase = -1;
+  DpxGroup* group = nullptr;
 };
+
+// Phases of launch_close in phase mode: the min-plus passes + 1.
+int close_phases(int mode);
+// Whether a closing with this radius bound can run in phase mode.
+bool close_phase_ok(int rmax, int se);
 
 size_t close_workspace_bytes(int res);
 size_t close_workspace_bytes_box(int rx, int ry, int rz);

@@ -25,7 +25,9 @@
 #include <cudaTypedefs.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "gm_common.cuh"
 #include "gm_internal.h"
@@ -813,12 +815,11 @@ struct NeedMap {
   int third0 = 0, third_n = 0, out0 = 0, out_n = 0;
 };
 
-__device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int nout) {
-  const int x0 = (int)blockIdx.x * kDpxCols;
+__device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int nout, int bx, int bz) {
+  const int x0 = bx * kDpxCols;
   const int cx0 = x0 >> nm.x_shift, cx1 = (x0 + kDpxCols - 1) >> nm.x_shift;
   const int oa = o0, ob = min(o0 + kDpxOut, nout) - 1;
   const int ca0 = sub ? oa : oa >> 1, ca1 = sub ? ob : ob >> 1;
-  const int bz = (int)blockIdx.z + nm.third0;
   const int ct0 = (2 * bz) >> nm.t_shift, ct1 = (2 * bz + 1) >> nm.t_shift;
   // (a, t) are (y, z) for the y pass and (z, y) for the z pass
   {
@@ -850,11 +851,11 @@ __device__ bool tile_needed(const NeedMap& nm, int axis, int sub, int o0, int no
 // and its two third-axis coordinates widened by `rext` (the y pass feeds z
 // outputs up to a halo away).  Block-uniform.
 __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, int nx, int n3, int axis, int nout,
-                           int o0, int rext, int bz) {
+                           int o0, int rext, int bx, int bz) {
   __shared__ int rt_s;
   if (threadIdx.x == 0) rt_s = 0;
   __syncthreads();
-  const int xa = (blockIdx.x * kDpxCols) >> 4, xb = (min(blockIdx.x * kDpxCols + kDpxCols, nx) - 1) >> 4;
+  const int xa = (bx * kDpxCols) >> 4, xb = (min(bx * kDpxCols + kDpxCols, nx) - 1) >> 4;
   const int aa = o0 >> 4, ab = (min(o0 + kDpxOut, nout) - 1) >> 4;
   const int ta = max(2 * bz - rext, 0) >> 4, tb = min(2 * bz + 1 + rext, n3 - 1) >> 4;
   const int cx = xb - xa + 1, ca = ab - aa + 1, ct = tb - ta + 1;
@@ -871,29 +872,31 @@ __device__ int tile_radius(const uint8_t* __restrict__ rmap, int mbx, int mby, i
   return clamp_radius(rt_s);
 }
 
-// With use_tma, the u16 input tile is staged by TMA (tmap: boxes of 64
+// One tile of a min-plus pass: 64 columns x 64 outputs x 2 third-axis
+// slices, at tile coordinates (bx, by, bz) along (x, outputs, slice pairs),
+// the need map's out0 / third0 offsets included.  The whole block works on
+// it.  With use_tma, the u16 input tile is staged by TMA (tmap: boxes of 64
 // columns x span rows x 1 slice along (x, pass axis, third axis), one per
 // slice; rows are 128 bytes, so each slice starts 128-byte aligned).
 template <int G, typename TIn, int FIN>
-__global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
-                                                  uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
-                                                  int sub, int halo, uint32_t cap, RField R,
-                                                  int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
-                                                  int rext, NeedMap need, const __grid_constant__ CUtensorMap tmap,
-                                                  int use_tma) {
+__device__ __forceinline__ void dpx_tile(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
+                                         uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis, int sub,
+                                         int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry,
+                                         const uint8_t* __restrict__ rmap, int rext, const NeedMap& need,
+                                         const CUtensorMap* tmap, int use_tma, int bx, int by, int bz) {
   extern __shared__ uint32_t tile_raw[];
   uint32_t* tileu = reinterpret_cast<uint32_t*>((reinterpret_cast<uintptr_t>(tile_raw) + 127) & ~(uintptr_t)127);
   __shared__ uint64_t tma_bar;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int tpar = w >> 2, grp = w & 3;
-  const int x = blockIdx.x * kDpxCols + 2 * lane;
+  const int x = bx * kDpxCols + 2 * lane;
   const int na = axis == 1 ? ny : nz;
   const int n3 = axis == 1 ? nz : ny;
   const int nout = sub ? na / 2 : na;
-  const int third = 2 * ((int)blockIdx.z + need.third0) + tpar;
+  const int third = 2 * bz + tpar;
   const int64_t sa = axis == 1 ? (int64_t)nx : (int64_t)nx * ny;
   const int64_t s3 = axis == 1 ? (int64_t)nx * ny : (int64_t)nx;
-  const int o0 = ((int)blockIdx.y + need.out0) * kDpxOut;
+  const int o0 = by * kDpxOut;
   const int step = sub ? 2 : 1;
   const int lo = (sub ? 2 * o0 + 1 : o0) - halo;
   const int span = (sub ? 2 * kDpxOut - 1 : kDpxOut) + 2 * halo;
@@ -902,7 +905,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   // that reads this tile has r(p) <= rt, so terms >= (rt+1)^2 never decide.
   int halo_e = halo;
   if (rmap != nullptr && step == 1) {
-    const int rt = tile_radius(rmap, nx >> 4, ny >> 4, nx, n3, axis, nout, o0, rext, (int)blockIdx.z + need.third0);
+    const int rt = tile_radius(rmap, nx >> 4, ny >> 4, nx, n3, axis, nout, o0, rext, bx, bz);
     const uint32_t ct = G == KERN_CUBE ? (uint32_t)(rt + 1) : (uint32_t)((rt + 1) * (rt + 1));
     cap = ct < cap ? ct : cap;
     halo_e = rt + 2 < halo ? rt + 2 : halo;
@@ -910,7 +913,7 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   // Erosion outputs matter only where the dilation has voxels (and the
   // passes feeding them within their window): a tile outside writes its
   // saturation value ("not eroded") without work.
-  const bool needed = tile_needed(need, axis, sub, o0, nout);
+  const bool needed = tile_needed(need, axis, sub, o0, nout, bx, bz);
   const int skip = needed ? halo - halo_e : span;  // tile rows never read
   const uint32_t capp = cap | (cap << 16);
   const int tile_rows = span;
@@ -926,19 +929,19 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
   const int nchunks = sizeof(TIn) == 2 && use_tma && span - 2 * skip > 0 ? 1 : 0;  // block-uniform
   if (nchunks > 0) {
     if (threadIdx.x == 0) {
-      tma_prefetch_map(&tmap);
+      tma_prefetch_map(tmap);
       mbar_init(&tma_bar, 1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
       mbar_arrive_expect_tx(&tma_bar, (uint32_t)(2 * span * kDpxCols * sizeof(uint16_t)));
-      const int x0 = blockIdx.x * kDpxCols, t0 = 2 * ((int)blockIdx.z + need.third0);
+      const int x0 = bx * kDpxCols, t0 = 2 * bz;
       for (int tp = 0; tp < 2; tp++) {
         uint32_t* dst = tileu + tp * tile_rows * 32;
         if (axis == 1)
-          tma_load_3d(dst, &tmap, x0, lo, t0 + tp, &tma_bar);
+          tma_load_3d(dst, tmap, x0, lo, t0 + tp, &tma_bar);
         else
-          tma_load_3d(dst, &tmap, x0, t0 + tp, lo, &tma_bar);
+          tma_load_3d(dst, tmap, x0, t0 + tp, lo, &tma_bar);
       }
     }
     if (!mbar_wait_bounded(&tma_bar, 0, 1u << 22)) atomicOr(&g_kernel_errors, kErrTmaTimeout);
@@ -1183,6 +1186,17 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in,
 }
 
 template <int G, typename TIn, int FIN>
+__global__ void __launch_bounds__(256, 4) k_pass_dpx(const TIn* __restrict__ in, uint16_t* __restrict__ out16,
+                                                  uint8_t* __restrict__ out8, int nx, int ny, int nz, int axis,
+                                                  int sub, int halo, uint32_t cap, RField R,
+                                                  int uniform_r, int rx, int ry, const uint8_t* __restrict__ rmap,
+                                                  int rext, NeedMap need, const __grid_constant__ CUtensorMap tmap,
+                                                  int use_tma) {
+  dpx_tile<G, TIn, FIN>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R, uniform_r, rx, ry, rmap, rext, need,
+                        &tmap, use_tma, (int)blockIdx.x, (int)blockIdx.y + need.out0, (int)blockIdx.z + need.third0);
+}
+
+template <int G, typename TIn, int FIN>
 static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis, int sub,
                        int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry, cudaStream_t st,
                        KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr, int rext = 0,
@@ -1213,6 +1227,266 @@ static void launch_dpx(const TIn* in, uint16_t* out16, uint8_t* out8, int nx, in
   GM_LAUNCH(kc, name, st,
             k_pass_dpx<G, TIn, FIN><<<g, 256, smem, st>>>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
                                                           uniform_r, rx, ry, rmap, rext, need, tmap, use_tma));
+}
+
+// ---- grouped min-plus passes (many grids, one persistent launch) ----
+//
+// One pass of the closing of many grids (the same pass of each: same
+// kernel shape, own sizes, radius bounds, buffers and need maps), recorded
+// by launch_close in phase mode and run as one launch: a grid of resident
+// blocks pulls tiles of all the grids from one work counter, so that small
+// grids fill the GPU together and the cost differences between tiles
+// (window lengths vary with the local radius and the early exits) balance
+// across blocks.  The tiles and their results are those of the per-grid
+// launches (the same tile function on the same tile coordinates).
+struct DpxJob {
+  const void* in;
+  uint16_t* out16;
+  uint8_t* out8;
+  int nx, ny, nz, axis, sub, halo;
+  uint32_t cap;
+  RField R;
+  int uniform_r, rx, ry;
+  const uint8_t* rmap;
+  int rext;
+  NeedMap need;
+  int gx, gy, gz;  // tiles of this grid's pass
+  int first;       // its first work item (tiles of the jobs before it)
+};
+
+// Instantiations a grouped launch may hold: the passes of launch_close.
+enum DpxKind {
+  DPXK_LAT_U8_0 = 0,   // sphere dilation y
+  DPXK_LAT_U16_1,      // sphere dilation z (threshold + packing)
+  DPXK_CUBE_U8_0,      // cube dilation y
+  DPXK_CUBE_U16_1,     // cube dilation z
+  DPXK_CEN2_U16_0,     // centre erosion y
+  DPXK_CEN2_U16_2,     // centre erosion z
+  DPXK_LAT2_U16_0,     // lattice-point erosion y
+  DPXK_LAT2_U16_3,     // lattice-point erosion z
+  DPXK_COUNT
+};
+template <int G, typename TIn, int FIN>
+constexpr int dpx_kind() {
+  return G == KERN_LAT && sizeof(TIn) == 1 && FIN == 0    ? DPXK_LAT_U8_0
+         : G == KERN_LAT && sizeof(TIn) == 2 && FIN == 1  ? DPXK_LAT_U16_1
+         : G == KERN_CUBE && sizeof(TIn) == 1 && FIN == 0 ? DPXK_CUBE_U8_0
+         : G == KERN_CUBE && sizeof(TIn) == 2 && FIN == 1 ? DPXK_CUBE_U16_1
+         : G == KERN_CEN2 && sizeof(TIn) == 2 && FIN == 0 ? DPXK_CEN2_U16_0
+         : G == KERN_CEN2 && sizeof(TIn) == 2 && FIN == 2 ? DPXK_CEN2_U16_2
+         : G == KERN_LAT2 && sizeof(TIn) == 2 && FIN == 0 ? DPXK_LAT2_U16_0
+         : G == KERN_LAT2 && sizeof(TIn) == 2 && FIN == 3 ? DPXK_LAT2_U16_3
+                                                          : -1;
+}
+
+template <int G, typename TIn, int FIN>
+__global__ void __launch_bounds__(256, 4) k_pass_dpx_group(const DpxJob* __restrict__ jobs, int njobs, int total,
+                                                        unsigned int* __restrict__ counter) {
+  __shared__ int item_s;     // the block's current work item
+  __shared__ int job_end_s;  // first item past the job held in job_s
+  // the job of the current item (kept while the block's items stay in it)
+  __shared__ __align__(16) unsigned char job_raw[sizeof(DpxJob)];
+  DpxJob& job_s = *reinterpret_cast<DpxJob*>(job_raw);
+  if (threadIdx.x == 0) {
+    item_s = (int)atomicAdd(counter, 1u);
+    job_end_s = -1;
+  }
+  __syncthreads();
+  for (;;) {
+    const int item = item_s;
+    if (item >= total) return;  // block-uniform
+    if (item >= job_end_s || item < job_s.first) {  // block-uniform (job_end_s = -1 at first)
+      if (threadIdx.x < 32) {
+        // the job holding the item: the last one whose first item is <= it
+        int lo = 0, hi = njobs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (jobs[mid].first <= item) lo = mid; else hi = mid - 1;
+        }
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + lo);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&job_s);
+        for (int k = threadIdx.x; k < (int)(sizeof(DpxJob) / 4); k += 32) dst[k] = src[k];
+        if (threadIdx.x == 0) job_end_s = jobs[lo].first + jobs[lo].gx * jobs[lo].gy * jobs[lo].gz;
+      }
+      __syncthreads();
+    }
+    // the next item, fetched while this tile runs (consumed after it)
+    int next = 0;
+    if (threadIdx.x == 0) next = (int)atomicAdd(counter, 1u);
+    const DpxJob& b = job_s;
+    const int t = item - b.first;
+    const int bx = t % b.gx, by = (t / b.gx) % b.gy, bz = t / (b.gx * b.gy);
+    dpx_tile<G, TIn, FIN>(static_cast<const TIn*>(b.in), b.out16, b.out8, b.nx, b.ny, b.nz, b.axis, b.sub, b.halo,
+                          b.cap, b.R, b.uniform_r, b.rx, b.ry, b.rmap, b.rext, b.need, nullptr, 0,
+                          bx, by + b.need.out0, bz + b.need.third0);
+    __syncthreads();  // every thread is done with this tile (its shared memory, job_s, item_s)
+    if (threadIdx.x == 0) item_s = next;
+    __syncthreads();
+  }
+}
+
+struct DpxGroup {
+  int kind = -1;
+  size_t smem = 0;
+  std::vector<DpxJob> jobs;
+  int total = 0;
+  DpxJob* h_jobs = nullptr;  // pinned copy read by the upload (also at graph replays)
+  DpxJob* d_jobs = nullptr;
+  unsigned int* d_counter = nullptr;
+  int cap = 0;
+  cudaEvent_t uploaded = nullptr;  // after the last upload outside a capture (h_jobs free again)
+};
+
+DpxGroup* dpx_group_new() { return new DpxGroup(); }
+
+void dpx_group_free(DpxGroup* g) {
+  if (!g) return;
+  if (g->uploaded) {
+    cudaEventSynchronize(g->uploaded);
+    cudaEventDestroy(g->uploaded);
+  }
+  if (g->h_jobs) cudaFreeHost(g->h_jobs);
+  cudaFree(g->d_jobs);
+  cudaFree(g->d_counter);
+  delete g;
+}
+
+void dpx_group_clear(DpxGroup* g) {
+  g->kind = -1;
+  g->smem = 0;
+  g->jobs.clear();
+  g->total = 0;
+}
+
+int dpx_group_size(const DpxGroup* g) { return (int)g->jobs.size(); }
+
+cudaError_t dpx_group_reserve(DpxGroup* g, int njobs) {
+  if (njobs <= g->cap) return cudaSuccess;
+  cudaError_t e;
+  if (g->uploaded && (e = cudaEventSynchronize(g->uploaded)) != cudaSuccess) return e;
+  if (!g->uploaded && (e = cudaEventCreateWithFlags(&g->uploaded, cudaEventDisableTiming)) != cudaSuccess) return e;
+  if (g->h_jobs) cudaFreeHost(g->h_jobs);
+  cudaFree(g->d_jobs);
+  g->h_jobs = nullptr;
+  g->d_jobs = nullptr;
+  g->cap = 0;
+  if ((e = cudaMallocHost(&g->h_jobs, sizeof(DpxJob) * njobs)) != cudaSuccess) return e;
+  if ((e = cudaMalloc(&g->d_jobs, sizeof(DpxJob) * njobs)) != cudaSuccess) return e;
+  if (!g->d_counter && (e = cudaMalloc(&g->d_counter, sizeof(unsigned int))) != cudaSuccess) return e;
+  g->cap = njobs;
+  return cudaSuccess;
+}
+
+// Records one grid's pass (the arguments of launch_dpx) into the group.
+template <int G, typename TIn, int FIN>
+static bool dpx_record(DpxGroup* grp, const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny, int nz, int axis,
+                       int sub, int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry,
+                       const uint8_t* rmap, int rext, NeedMap need) {
+  constexpr int kind = dpx_kind<G, TIn, FIN>();
+  if (kind < 0 || (grp->kind >= 0 && grp->kind != kind) || (G == KERN_LAT2) != (sub != 0)) return false;
+  grp->kind = kind;
+  grp->smem = std::max(grp->smem, dpx_smem_bytes(sub, halo));
+  const int na = axis == 1 ? ny : nz;
+  const int n3 = axis == 1 ? nz : ny;
+  const int nout = sub ? na / 2 : na;
+  DpxJob j;
+  j.in = in;
+  j.out16 = out16;
+  j.out8 = out8;
+  j.nx = nx;
+  j.ny = ny;
+  j.nz = nz;
+  j.axis = axis;
+  j.sub = sub;
+  j.halo = halo;
+  j.cap = cap;
+  j.R = R;
+  j.uniform_r = uniform_r;
+  j.rx = rx;
+  j.ry = ry;
+  j.rmap = rmap;
+  j.rext = rext;
+  j.need = need;
+  j.gx = (nx + kDpxCols - 1) / kDpxCols;
+  j.gy = need.out_n > 0 ? need.out_n : (nout + kDpxOut - 1) / kDpxOut;
+  j.gz = need.third_n > 0 ? need.third_n : (n3 + 1) / 2;
+  j.first = grp->total;
+  const long long tiles = (long long)j.gx * j.gy * j.gz;
+  if (tiles <= 0) return true;
+  if (grp->total + tiles > 0x7fffffffLL) return false;
+  grp->total += (int)tiles;
+  grp->jobs.push_back(j);
+  return true;
+}
+
+static const char* const kDpxGroupNames[DPXK_COUNT] = {
+    "k_pass_dil_y_group", "k_pass_dil_z_group",  "k_pass_dil_y_group",  "k_pass_dil_z_group",
+    "k_pass_ero_y_group", "k_pass_ero_z_group", "k_pass_erob_y_group", "k_pass_erob_z_group"};
+
+template <int G, typename TIn, int FIN>
+static cudaError_t dpx_group_go(DpxGroup* g, int sms, cudaStream_t st, KernelCounter* kc) {
+  const void* k = reinterpret_cast<const void*>(k_pass_dpx_group<G, TIn, FIN>);
+  cudaError_t e = ensure_dynamic_smem(k, g->smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pass_dpx_group<G, TIn, FIN>, 256, g->smem)) !=
+      cudaSuccess)
+    return e;
+  const int blocks = std::max(1, std::min(g->total, std::max(1, sms) * std::max(1, per_sm)));
+  GM_LAUNCH(kc, kDpxGroupNames[g->kind], st,
+            k_pass_dpx_group<G, TIn, FIN><<<blocks, 256, g->smem, st>>>(g->d_jobs, (int)g->jobs.size(), g->total,
+                                                                        g->d_counter));
+  return cudaGetLastError();
+}
+
+cudaError_t dpx_group_launch(DpxGroup* g, int sms, cudaStream_t st, KernelCounter* kc) {
+  if (g->jobs.empty()) return cudaSuccess;
+  const int n = (int)g->jobs.size();
+  if (n > g->cap) return cudaErrorInvalidValue;  // dpx_group_reserve first (not while capturing)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cs);
+  if (e != cudaSuccess) return e;
+  const bool capturing = cs == cudaStreamCaptureStatusActive;
+  // the previous upload has read the pinned table (in a capture the caller
+  // guarantees that no replay of an earlier graph over it is in flight)
+  if (!capturing && (e = cudaEventSynchronize(g->uploaded)) != cudaSuccess) return e;
+  memcpy(g->h_jobs, g->jobs.data(), sizeof(DpxJob) * n);
+  if ((e = cudaMemcpyAsync(g->d_jobs, g->h_jobs, sizeof(DpxJob) * n, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return e;
+  if (!capturing && (e = cudaEventRecord(g->uploaded, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(g->d_counter, 0, sizeof(unsigned int), st)) != cudaSuccess) return e;
+  switch (g->kind) {
+    case DPXK_LAT_U8_0: return dpx_group_go<KERN_LAT, uint8_t, 0>(g, sms, st, kc);
+    case DPXK_LAT_U16_1: return dpx_group_go<KERN_LAT, uint16_t, 1>(g, sms, st, kc);
+    case DPXK_CUBE_U8_0: return dpx_group_go<KERN_CUBE, uint8_t, 0>(g, sms, st, kc);
+    case DPXK_CUBE_U16_1: return dpx_group_go<KERN_CUBE, uint16_t, 1>(g, sms, st, kc);
+    case DPXK_CEN2_U16_0: return dpx_group_go<KERN_CEN2, uint16_t, 0>(g, sms, st, kc);
+    case DPXK_CEN2_U16_2: return dpx_group_go<KERN_CEN2, uint16_t, 2>(g, sms, st, kc);
+    case DPXK_LAT2_U16_0: return dpx_group_go<KERN_LAT2, uint16_t, 0>(g, sms, st, kc);
+    case DPXK_LAT2_U16_3: return dpx_group_go<KERN_LAT2, uint16_t, 3>(g, sms, st, kc);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// A pass of launch_close: launched (a.phase < 0), recorded into a.group
+// when it is the pass of the phase asked for, or skipped.  `at` counts the
+// passes met so far.
+template <int G, typename TIn, int FIN>
+static bool dpx_step(const CloseArgs& a, int& at, const TIn* in, uint16_t* out16, uint8_t* out8, int nx, int ny,
+                     int nz, int axis, int sub, int halo, uint32_t cap, RField R, int uniform_r, int rx, int ry,
+                     cudaStream_t st, KernelCounter* kc, const char* name, const uint8_t* rmap = nullptr,
+                     int rext = 0,
+                     NeedMap need = NeedMap{nullptr, 0, 0, 0, 0, 0, 0, 0, 0,
+                                            CBox{{0, 0, 0}, {1 << 30, 1 << 30, 1 << 30}}}) {
+  bool ok = true;
+  if (a.phase < 0)
+    launch_dpx<G, TIn, FIN>(in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R, uniform_r, rx, ry, st, kc, name,
+                            rmap, rext, need);
+  else if (a.phase == at)
+    ok = a.group != nullptr && dpx_record<G, TIn, FIN>(a.group, in, out16, out8, nx, ny, nz, axis, sub, halo, cap, R,
+                                                        uniform_r, rx, ry, rmap, rext, need);
+  at++;
+  return ok;
 }
 
 // The driver's tensor-map encoder, looked up once per process (before any
@@ -1841,6 +2115,11 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   const CBox B_dil_y = cbox_grow(R_Df, win, 4, dims), B_dil_x = cbox_grow(R_Df, win, 6, dims);
   const CBox B_ero_y = cbox_grow(R_Ef, win, 4, dims), B_erob_y = cbox_grow(R_Eb, win, 4, dims);
   const CBox B_ero_x = cbox_grow(R_Eb, win, 6, dims);
+  // phase mode: the steps of phase a.phase only (see CloseArgs::phase)
+  if (a.phase >= 0 && (a.edt != nullptr || !close_phase_ok(rmax, a.se) || a.group == nullptr))
+    return cudaErrorInvalidValue;
+  int at = 0;  // min-plus passes met so far
+  auto here = [&]() { return a.phase < 0 || a.phase == at; };
 
   // ---- dilation ---- (skipped when the caller has put it in D already)
   if (!a.dilation_done) {
@@ -1855,7 +2134,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     } else if (a.R != nullptr && a.rmap_in != nullptr) {
       tile_map = a.rmap_in;  // built by the caller together with the radius bound
     } else if (a.R != nullptr) {
-      if (launch_radius_map(RF, Nx, Ny, Nz, rmap, nullptr, st, kc) != cudaSuccess) return cudaGetLastError();
+      if (here() && launch_radius_map(RF, Nx, Ny, Nz, rmap, nullptr, st, kc) != cudaSuccess)
+        return cudaGetLastError();
       tile_map = rmap;
     }
     if (a.edt != nullptr) {
@@ -1863,25 +2143,34 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                 k_dil_threshold<<<quad_grid(g), dim3(64, 4), 0, st>>>(a.edt, a.e_sy, a.e_sz, RF, a.uniform_r, g,
                                                                       exact ? D : Df, R_Df));
     } else {
-      if (!a.xpass_done && launch_dil_pass_x(a.X, buf8, rx, ry, rz, dcap, B_dil_x, st, kc) != cudaSuccess)
+      if (!a.xpass_done && here() && launch_dil_pass_x(a.X, buf8, rx, ry, rz, dcap, B_dil_x, st, kc) != cudaSuccess)
         return cudaGetLastError();
       uint8_t* dst = exact ? D : Df;
       if ((a.ypass_done || a.zpass_done) && a.se != 0) return cudaErrorInvalidValue;
       if (dil_cap <= 32767) {
+        bool ok = true;
         if (a.se == 1) {
-          launch_dpx<KERN_CUBE, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
-                                            ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
-          launch_dpx<KERN_CUBE, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF, a.uniform_r,
-                                             rx, ry, st, kc, "k_pass_dil_z", tile_map, 0, roi_only(R_Df, 1, 1));
+          ok &= dpx_step<KERN_CUBE, uint8_t, 0>(a, at, buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE,
+                                                0, rx, ry, st, kc, "k_pass_dil_y", tile_map, dil_halo,
+                                                roi_only(B_dil_y, 1, 1));
+          ok &= dpx_step<KERN_CUBE, uint16_t, 1>(a, at, buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF,
+                                                 a.uniform_r, rx, ry, st, kc, "k_pass_dil_z", tile_map, 0,
+                                                 roi_only(R_Df, 1, 1));
         } else {
           if (!a.ypass_done)
-            launch_dpx<KERN_LAT, uint8_t, 0>(buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap, RNONE, 0, rx,
-                                             ry, st, kc, "k_pass_dil_y", tile_map, dil_halo, roi_only(B_dil_y, 1, 1));
+            ok &= dpx_step<KERN_LAT, uint8_t, 0>(a, at, buf8, buf16a, nullptr, Nx, Ny, Nz, 1, 0, dil_halo, dil_cap,
+                                                 RNONE, 0, rx, ry, st, kc, "k_pass_dil_y", tile_map, dil_halo,
+                                                 roi_only(B_dil_y, 1, 1));
+          else
+            at++;
           if (!a.zpass_done)
-            launch_dpx<KERN_LAT, uint16_t, 1>(buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF,
-                                              a.uniform_r, rx, ry, st, kc, "k_pass_dil_z", tile_map, 0,
-                                              roi_only(R_Df, 1, 1));
+            ok &= dpx_step<KERN_LAT, uint16_t, 1>(a, at, buf16a, nullptr, dst, Nx, Ny, Nz, 2, 0, dil_halo, dil_cap, RF,
+                                                  a.uniform_r, rx, ry, st, kc, "k_pass_dil_z", tile_map, 0,
+                                                  roi_only(R_Df, 1, 1));
+          else
+            at++;
         }
+        if (!ok) return cudaErrorInvalidValue;
       } else {
         const int span = kTileOut + 2 * dil_halo;
         dim3 gy(cdiv(Nx, 32), cdiv(Ny, kTileOut), Nz);
@@ -1900,19 +2189,23 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                              buf16a, dst, RF, a.uniform_r, rx, ry, rz, dil_halo, dil_cap));
       }
     }
-    if (!exact) {
+    if (!exact && here()) {
       GM_LAUNCH(kc, "k_dil_select", st, k_dil_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, Df, D, g, dr, R_D));
     }
+  } else {
+    at += 2;  // the dilation's two passes
   }
   // ---- occupancy map of D (erosion outputs are needed on D only) ----
-  {
+  if (here()) {
     const int nb = mdx * mdy * mdz;
     GM_LAUNCH(kc, "k_occ_map8", st, k_occ_map8<<<(nb + 7) / 8, 256, 0, st>>>(D, rx, ry, mdx, mdy, nb, dmap));
   }
   // ---- contour ----
-  GM_LAUNCH(kc, "k_contour", st, k_contour16<<<grid16(g), dim3(32, 8), 0, st>>>(D, S, g, exact ? 1 : 0, R_S));
-  // (S holds the refinement tags after the erosion's x pass in GM_REF)
-  if (a.S_out) cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
+  if (here()) {
+    GM_LAUNCH(kc, "k_contour", st, k_contour16<<<grid16(g), dim3(32, 8), 0, st>>>(D, S, g, exact ? 1 : 0, R_S));
+    // (S holds the refinement tags after the erosion's x pass in GM_REF)
+    if (a.S_out) cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
+  }
   // ---- erosion ----
   {
     const uint32_t K = 4u * (uint32_t)((rmax - 1) * (rmax - 1));
@@ -1920,7 +2213,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     const int W = Nx >> 5;
     // bits, centre and lattice accumulators, compacted sites
     const size_t smem = sizeof(uint32_t) * (4 * (size_t)W + 4 * (size_t)Nx + 4 * (size_t)rx + 8 * (size_t)Nx);
-    if (W <= 64) {
+    if (!here()) {
+    } else if (W <= 64) {
       const size_t smem_w = kEroXWarps * ero_x_w_warp_bytes(rx);
       ensure_dynamic_smem(reinterpret_cast<const void*>(k_ero_pass_x_w), smem_w);
       const unsigned blocks = (unsigned)(((int64_t)ry * rz + kEroXWarps - 1) / kEroXWarps);
@@ -1935,37 +2229,42 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
     }
     if (K <= 32767) {
       const int gz = (ehalo + 1) / 2 + 1;  // cells covering the z window (ehalo fine voxels) of a z pass
+      bool ok = true;
       if (exact) {
         // ero z needs its outputs on D grown by one cell, ero y its outputs
         // there and within the z window of it
-        launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
-                                           kc, "k_pass_ero_y", nullptr, 0,
-                                           NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1 + gz, B_ero_y});
-        launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_ero_z", nullptr, 0,
-                                           NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1, R_Ef});
+        ok &= dpx_step<KERN_CEN2, uint16_t, 0>(a, at, buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx,
+                                               ry, st, kc, "k_pass_ero_y", nullptr, 0,
+                                               NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1 + gz, B_ero_y});
+        ok &= dpx_step<KERN_CEN2, uint16_t, 2>(a, at, buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry,
+                                               st, kc, "k_pass_ero_z", nullptr, 0,
+                                               NeedMap{dmap, mdx, mdy, mdz, 1, 1, 1, 1, 1, R_Ef});
       } else {
         // erob z needs its flags on D only, erob y within its z window
-        launch_dpx<KERN_LAT2, uint16_t, 0>(HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_y", nullptr, 0,
-                                           NeedMap{dmap, mdx, mdy, mdz, 0, 1, 0, 0, gz, B_erob_y});
-        launch_dpx<KERN_LAT2, uint16_t, 3>(HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_erob_z", nullptr, 0,
-                                           NeedMap{dmap, mdx, mdy, mdz, 0, 0, 0, 0, 0, R_Eb});
+        ok &= dpx_step<KERN_LAT2, uint16_t, 0>(a, at, HL1, HL2, nullptr, rx, Ny, Nz, 1, 1, ehalo, K, RNONE, 0, rx, ry,
+                                               st, kc, "k_pass_erob_y", nullptr, 0,
+                                               NeedMap{dmap, mdx, mdy, mdz, 0, 1, 0, 0, gz, B_erob_y});
+        ok &= dpx_step<KERN_LAT2, uint16_t, 3>(a, at, HL2, nullptr, Eb, rx, ry, Nz, 2, 1, ehalo, K, RNONE, 0, rx, ry,
+                                               st, kc, "k_pass_erob_z", nullptr, 0,
+                                               NeedMap{dmap, mdx, mdy, mdz, 0, 0, 0, 0, 0, R_Eb});
         // base erosion and refinement tags (the contour S is read by nobody
         // any more: it holds the tags), then the centre erosion only on the
         // blocks of tagged cells (ero y within the z window of them)
-        cudaMemsetAsync(tmap, 0, (size_t)mdx * mdy * mdz, st);
-        GM_LAUNCH(kc, "k_ero_tag", st,
-                  k_ero_tag16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, a.C_out, S, tmap, mdx, mdy, g, dr, F));
-        launch_dpx<KERN_CEN2, uint16_t, 0>(buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx, ry, st,
-                                           kc, "k_pass_ero_y", nullptr, 0,
-                                           NeedMap{tmap, mdx, mdy, mdz, 1, 1, 0, 0, gz, B_ero_y});
-        launch_dpx<KERN_CEN2, uint16_t, 2>(buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry, st, kc,
-                                           "k_pass_ero_z", nullptr, 0,
-                                           NeedMap{tmap, mdx, mdy, mdz, 1, 1, 0, 0, 0, R_Ef});
-        GM_LAUNCH(kc, "k_ero_fix", st, k_ero_fix16<<<grid16(g), dim3(32, 8), 0, st>>>(S, Ef, a.C_out, g, F));
+        if (here()) {
+          cudaMemsetAsync(tmap, 0, (size_t)mdx * mdy * mdz, st);
+          GM_LAUNCH(kc, "k_ero_tag", st,
+                    k_ero_tag16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, a.C_out, S, tmap, mdx, mdy, g, dr, F));
+        }
+        ok &= dpx_step<KERN_CEN2, uint16_t, 0>(a, at, buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx,
+                                               ry, st, kc, "k_pass_ero_y", nullptr, 0,
+                                               NeedMap{tmap, mdx, mdy, mdz, 1, 1, 0, 0, gz, B_ero_y});
+        ok &= dpx_step<KERN_CEN2, uint16_t, 2>(a, at, buf16b, nullptr, Ef, Nx, Ny, Nz, 2, 0, ehalo, K, RNONE, 0, rx, ry,
+                                               st, kc, "k_pass_ero_z", nullptr, 0,
+                                               NeedMap{tmap, mdx, mdy, mdz, 1, 1, 0, 0, 0, R_Ef});
+        if (here())
+          GM_LAUNCH(kc, "k_ero_fix", st, k_ero_fix16<<<grid16(g), dim3(32, 8), 0, st>>>(S, Ef, a.C_out, g, F));
       }
+      if (!ok) return cudaErrorInvalidValue;
     } else {
       const int span = kTileOut + 2 * ehalo;
       dim3 gy(cdiv(Nx, 32), cdiv(Ny, kTileOut), Nz);
@@ -1984,11 +2283,20 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
                                                 HL2, Eb, rx, ry, rz, ehalo, K));
       }
     }
-    if (exact || K > 32767)
+    if ((exact || K > 32767) && here())
       GM_LAUNCH(kc, "k_ero_select", st,
                 k_ero_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, Ef, a.C_out, g, dr, exact ? 1 : 0, F));
   }
   return cudaGetLastError();
+}
+
+int close_phases(int mode) { return mode == 1 ? 5 : 7; }
+
+bool close_phase_ok(int rmax, int se) {
+  // the min-plus passes' saturation values fit 15 bits: the dilation's
+  // (rmax + 1)^2 (sphere) or rmax + 1 (cube), the erosion's 4 (rmax - 1)^2
+  const int r = clamp_radius(rmax);
+  return (se == 1 || (r + 1) * (r + 1) <= 32767) && 4 * (r - 1) * (r - 1) <= 32767;
 }
 
 cudaError_t launch_edt(const uint8_t* X, int res, int rmax, uint8_t* workspace, uint16_t* E, cudaStream_t st,

@@ -260,15 +260,24 @@ typedef struct {
 
 /* Batched form of GMorpho::Update for n independent grids of uneven sizes
  * (no reference counterpart: the reference closes one grid per call).
- * Instances run concurrently on `lanes` internal streams (0 = autotuned on
- * the first call of a batch and cached); a uniform-radius batch replays its
- * closing phase as one CUDA graph while the batch is unchanged.  When
- * meshes != NULL every closing is meshed (bilateral_iters iterations) and
- * meshes[i] views device buffers owned by the context until the next batch.
- * Results equal n separate gm_close + gm_mesh calls bit for bit. */
+ * lanes > 0: the instances' closings run concurrently on that many internal
+ * streams.  lanes = GM_BATCH_GROUPED: the closings go pass by pass, each
+ * min-plus pass of all the instances as one persistent launch whose blocks
+ * pull the tiles of every instance from one work counter (the kernels
+ * between passes per instance on four streams; every instance keeps its
+ * own workspace meanwhile; radius bounds <= 91 only, else
+ * GM_ERR_INVALID_ARGUMENT).  lanes = 0: the form is autotuned (1, 2, 4, 8,
+ * 16 lanes and the grouped form, timed on the first call of a batch
+ * signature) and cached.  A uniform-radius batch replays its closing phase
+ * as one CUDA graph while the batch is unchanged.  When meshes != NULL
+ * every closing is meshed (bilateral_iters iterations) and meshes[i] views
+ * device buffers owned by the context until the next batch.  Results equal
+ * n separate gm_close + gm_mesh calls bit for bit, in every form. */
+#define GM_BATCH_GROUPED (-1)
 gm_status gm_batch_close_mesh(gm_ctx* ctx, int32_t n, const gm_batch_item* items, gm_mode mode, gm_se se,
                               int32_t bilateral_iters, int32_t lanes, gm_mesh_view* meshes, void* stream);
-/* Lane count the autotuner chose for the last tuned batch (0: none yet). */
+/* Form the autotuner chose for the last tuned batch: a lane count, or
+ * GM_BATCH_GROUPED (0: none yet). */
 int32_t gm_batch_lanes(gm_ctx* ctx);
 /* Fault injection for tests: the next `count` lane buffer allocations of
  * gm_batch_close_mesh on this context fail as if the device were out of

@@ -20,7 +20,7 @@ def _instances():
     return inst
 
 
-@pytest.mark.parametrize("lanes", [1, 3, 0])
+@pytest.mark.parametrize("lanes", [1, 3, 0, L.GM_BATCH_GROUPED])
 def test_batch_equals_separate_calls(gm_ctx, lanes):
     import torch
     inst = _instances()
@@ -43,10 +43,11 @@ def test_batch_equals_separate_calls(gm_ctx, lanes):
             assert np.array_equal(got[i][1], V.cpu().numpy())
             assert np.array_equal(got[i][3], N.cpu().numpy(), equal_nan=True)
     if lanes == 0:
-        assert gm_ctx.batch_lanes in (1, 2, 4, 8, 16)
+        assert gm_ctx.batch_lanes in (1, 2, 4, 8, 16, L.GM_BATCH_GROUPED)
 
 
-def test_batch_variable_radius(gm_ctx):
+@pytest.mark.parametrize("lanes", [2, L.GM_BATCH_GROUPED])
+def test_batch_variable_radius(gm_ctx, lanes):
     import torch
     inst = _instances()[:3]
     rng = np.random.default_rng(5)
@@ -56,15 +57,16 @@ def test_batch_variable_radius(gm_ctx):
         R = torch.as_tensor(rng.integers(0, 9, size=(2 * it["res"]) ** 3).astype(np.int8)).cuda()
         items.append((d, it["X"], R, 0, torch.empty_like(it["X"])))
         refs.append(gm_ctx.close(d, it["X"], R, 0))
-    gm_ctx.batch_close_mesh(items, mesh=False, lanes=2)
+    gm_ctx.batch_close_mesh(items, mesh=False, lanes=lanes)
     torch.cuda.synchronize()
     for (d, X, R, r, out), ref in zip(items, refs):
         assert torch.equal(out, ref)
 
 
+@pytest.mark.parametrize("lanes", [2, L.GM_BATCH_GROUPED])
 @pytest.mark.parametrize("mode,se", [(L.GM_REF, L.GM_SE_SPHERE), (L.GM_EXACT, L.GM_SE_SPHERE),
                                      (L.GM_REF, L.GM_SE_CUBE)])
-def test_batch_occupied_extent(gm_ctx, mode, se):
+def test_batch_occupied_extent(gm_ctx, mode, se, lanes):
     """Grids closed on their occupied extent (solid in a corner of a larger
     cube, an empty grid, a grid full to its border, a radius field) equal
     the whole-grid closings and meshes."""
@@ -81,7 +83,7 @@ def test_batch_occupied_extent(gm_ctx, mode, se):
         Rd = torch.as_tensor(R).cuda() if R is not None else None
         descs.append(d)
         items.append((d, Xd, Rd, r, torch.empty_like(Xd)))
-    meshes = gm_ctx.batch_close_mesh(items, mode=mode, se=se, bilateral_iters=3, lanes=2)
+    meshes = gm_ctx.batch_close_mesh(items, mode=mode, se=se, bilateral_iters=3, lanes=lanes)
     torch.cuda.synchronize()
     got = [(items[i][4].cpu().numpy(), meshes[i][0].cpu().numpy(), meshes[i][2].cpu().numpy(),
             meshes[i][1].cpu().numpy()) for i in range(len(items))]
@@ -95,7 +97,8 @@ def test_batch_occupied_extent(gm_ctx, mode, se):
         assert np.array_equal(got[i][3], N.cpu().numpy(), equal_nan=True)
 
 
-def test_batch_normals_of_large_meshes(gm_ctx):
+@pytest.mark.parametrize("lanes", [3, L.GM_BATCH_GROUPED])
+def test_batch_normals_of_large_meshes(gm_ctx, lanes):
     """Ten larger grids (over half a million vertices in all) filtered
     together, one launch per iteration: every mesh's normals equal its own
     gm_mesh filtering, bit for bit."""
@@ -105,7 +108,7 @@ def test_batch_normals_of_large_meshes(gm_ctx):
     for it in inst:
         d = api.make_desc(it["res"], it["data_res"], cell_size=1.0 / it["res"])
         items.append((d, it["X"].contiguous(), None, it["radius"], torch.empty_like(it["X"])))
-    meshes = gm_ctx.batch_close_mesh(items, bilateral_iters=5, lanes=3)
+    meshes = gm_ctx.batch_close_mesh(items, bilateral_iters=5, lanes=lanes)
     torch.cuda.synchronize()
     got = [(m[0].cpu().numpy(), m[1].cpu().numpy(), m[2].cpu().numpy()) for m in meshes]
     assert sum(len(g[0]) for g in got) > 3 * 192 * 1024
@@ -141,5 +144,46 @@ def test_batch_allocation_failure_injected(gm_ctx):
             ref = gm_ctx.close(d, X, None, r)
             torch.cuda.synchronize()
             assert torch.equal(out, ref)
+    finally:
+        ctx.close_ctx()
+
+
+def test_batch_grouped_radius_limit(gm_ctx):
+    """The grouped form takes radius bounds up to 91 (15-bit saturation
+    values of its passes): above, it is refused with
+    GM_ERR_INVALID_ARGUMENT, and the autotuned form closes such a batch
+    with lanes, equal to separate calls."""
+    import torch
+    X = torch.as_tensor(synth.random_grid(64, 991)).cuda()
+    d = api.make_desc(64)
+    items = [(d, X, None, 100, torch.empty_like(X)), (d, X, None, 4, torch.empty_like(X))]
+    with pytest.raises(L.GMError) as e:
+        gm_ctx.batch_close_mesh(items, bilateral_iters=0, lanes=L.GM_BATCH_GROUPED, mesh=False)
+    assert e.value.status == L.GM_ERR_INVALID_ARGUMENT
+    gm_ctx.batch_close_mesh(items, bilateral_iters=0, lanes=0, mesh=False)
+    torch.cuda.synchronize()
+    assert gm_ctx.batch_lanes in (1, 2, 4, 8, 16)
+    for dd, XX, R, r, out in items:
+        assert torch.equal(out, gm_ctx.close(dd, XX, None, r))
+
+
+def test_batch_grouped_allocation_failure_injected(gm_ctx):
+    """The grouped form's per-grid workspaces failing to allocate (injected
+    on the host) give GM_ERR_OUT_OF_MEMORY; the context stays usable."""
+    import torch
+    items = []
+    for i, res in enumerate((32, 64)):
+        X = torch.as_tensor(synth.random_grid(res, 995 + i)).cuda()
+        items.append((api.make_desc(res), X, None, 2 + i, torch.empty_like(X)))
+    ctx = api.Context(0)
+    try:
+        assert L.load().gm_batch_inject_alloc_failures(ctx.ctx, 1) == L.GM_OK
+        with pytest.raises(L.GMError) as e:
+            ctx.batch_close_mesh(items, bilateral_iters=0, lanes=L.GM_BATCH_GROUPED, mesh=False)
+        assert e.value.status == L.GM_ERR_OUT_OF_MEMORY
+        ctx.batch_close_mesh(items, bilateral_iters=0, lanes=L.GM_BATCH_GROUPED, mesh=False)
+        torch.cuda.synchronize()
+        for d, X, R, r, out in items:
+            assert torch.equal(out, gm_ctx.close(d, X, None, r))
     finally:
         ctx.close_ctx()
