@@ -123,6 +123,20 @@ __device__ __forceinline__ void cube_values(const uint8_t* tile, int lx, int ly,
   }
 }
 
+// The MC value of sub-cube s of cell (lx, ly, lz) alone (cube_values()[s]).
+__device__ __forceinline__ int cube_value(const uint8_t* tile, int lx, int ly, int lz, int s) {
+  const int fx = 2 * lx + (s & 1), fy = 2 * ly + ((s >> 1) & 1), fz = 2 * lz + (s >> 2);
+  int v = 0;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    // corners 000, 100, 110, 010, 001, 101, 111, 011
+    const int x = fx + (((c + 1) >> 1) & 1), y = fy + ((c >> 1) & 1), z = fz + (c >> 2);
+    const uint32_t cell = tile[tix(x >> 1, y >> 1, z >> 1)];
+    v |= (int)((cell >> ((x & 1) + 2 * (y & 1) + 4 * (z & 1))) & 1u) << c;
+  }
+  return v;
+}
+
 // True when the 2x2x2 block of cells c .. c+1 is all empty or all full: then
 // none of the eight sub-cubes of c is mixed (cheap test before cube_values).
 __device__ __forceinline__ bool cell_uniform(const uint8_t* tile, int lx, int ly, int lz) {
@@ -496,7 +510,7 @@ __device__ __forceinline__ uint32_t info_of(const int vals[8], int m) {
 
 // dynamic shared memory of k_mc_triangles
 constexpr size_t kTriSmem = sizeof(uint32_t) * kInfoE * kInfoE * kInfoE + sizeof(uint16_t) * kCellsPerBrick +
-                            kTileCells;
+                            sizeof(uint16_t) * 8 * kMcThreads + kTileCells;
 
 // Vertex offset of cube k of the cell whose summary is `info` (absent: -1),
 // with its edge-0 / edge-3 ownership.
@@ -510,7 +524,7 @@ __device__ __forceinline__ long long cube_voff(uint32_t info, uint32_t cell_off,
   return (long long)off;
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __restrict__ C, GDims gd, McWin w,
+__global__ void __launch_bounds__(kMcThreads, 5) k_mc_triangles(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                               const uint32_t* __restrict__ brick_off,
                                                               const uint32_t* __restrict__ cell_voff,
                                                               uint32_t* __restrict__ T, uint32_t nt_total,
@@ -539,38 +553,52 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
     info[i] = cell_info(tile, lx, ly, lz, win_tag(w, ox + lx, oy + ly, oz + lz));
   }
   __syncthreads();
-  // the candidates in rounds of one per thread: a block scan of the round's
-  // triangle counts gives each its first triangle, in list (Morton) order
+  // The candidates in rounds of one per thread; each round's mixed cubes
+  // (cell in list order, then sub-cube order) go to a cube list and are
+  // worked one per thread, a block scan of their triangle counts giving
+  // each its first triangle: the order of the cell-by-cell walk, without
+  // the lanes of a warp waiting on each other's sub-cube loops.
+  uint16_t* cubes = list + kCellsPerBrick;  // [8 * kMcThreads]: (cell slot << 3) | sub-cube
   const uint32_t tbase = brick_off[4 * blockIdx.x + 2];
   uint32_t run = 0;
   for (int j0 = 0; j0 < nc; j0 += kMcThreads) {
     const int j = j0 + (int)threadIdx.x;
-    int lx = 0, ly = 0, lz = 0, m = 0;
-    int vals[8];
-    bool emit = false;
-    uint32_t ntri = 0;
+    uint32_t m = 0;
     if (j < nc) {
+      int lx, ly, lz;
       local_coords(list[j], lx, ly, lz);
-      m = (int)(info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu);
-      emit = m != 0 && win_emit(w, ox + lx, oy + ly, oz + lz);
-      if (emit) {
-        cube_values(tile, lx, ly, lz, vals);
-        ntri = cell_counts(vals, m).tris;
-      }
+      m = info[lx + kInfoE * (ly + kInfoE * lz)] & 0xffu;
+      if (m != 0 && !win_emit(w, ox + lx, oy + ly, oz + lz)) m = 0;
     }
-    uint32_t round_total;
-    const uint32_t pre = block_scan1(ntri, round_total);
-    const uint32_t first = tbase + run + pre;
-    run += round_total;
-    if (!emit) continue;
-    uint32_t to = first;
-    const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
-    uint32_t vo = cell_voff[gidx(gx, gy, gz, gd)];
-    for (int s = 0; s < 8; s++) {
-      if (!((m >> s) & 1)) continue;
-      const int v = vals[s];
+    uint32_t nround;
+    uint32_t k = block_scan1((uint32_t)__popc(m), nround);
+    while (m) {
+      const int sc = __ffs(m) - 1;
+      m &= m - 1;
+      cubes[k++] = (uint16_t)((threadIdx.x << 3) | sc);
+    }
+    __syncthreads();
+    for (int c0 = 0; c0 < (int)nround; c0 += kMcThreads) {
+      const int c = c0 + (int)threadIdx.x;
+      int lx = 0, ly = 0, lz = 0, s = 0, v = 0, cnt = 0;
+      if (c < (int)nround) {
+        const int e = cubes[c];
+        s = e & 7;
+        local_coords(list[j0 + (e >> 3)], lx, ly, lz);
+        v = cube_value(tile, lx, ly, lz, s);
+        cnt = c_tri_count[v];
+      }
+      uint32_t ttot;
+      const uint32_t pre = block_scan1((uint32_t)cnt, ttot);
+      const uint32_t to = tbase + run + pre;
+      run += ttot;
+      if (c >= (int)nround) continue;
+      const int gx = ox + lx, gy = oy + ly, gz = oz + lz;
       const int em = edge_mask(v);
       const int fx = 2 * gx + (s & 1), fy = 2 * gy + ((s >> 1) & 1), fz = 2 * gz + (s >> 2);  // local
+      int o0 = 0, o3 = 0;
+      const uint32_t vo = (uint32_t)cube_voff(info[lx + kInfoE * (ly + kInfoE * lz)],
+                                              cell_voff[gidx(gx, gy, gz, gd)], s, o0, o3);
       uint32_t vert[12];
 #pragma unroll
       for (int e = 0; e < 12; e++) vert[e] = 0;
@@ -579,7 +607,6 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
         if (em & 1) vert[0] = vo + ind++;
         if (em & 8) vert[3] = vo + ind++;
         if (em & 256) vert[8] = vo + ind++;
-        vo += ind;
       }
       // neighbour cubes +x, +x+y, +y, +z, +x+z, +y+z (BuildNeighbors order,
       // GMorpho.cu:6480-6487) and the edges they own
@@ -588,9 +615,9 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
         const int nfx = fx + dx, nfy = fy + dy, nfz = fz + dz;
         const int cx = (nfx >> 1) - ox, cy = (nfy >> 1) - oy, cz = (nfz >> 1) - oz;
         const uint32_t ninfo = info[cx + kInfoE * (cy + kInfoE * cz)];
-        const int k = (nfx & 1) | ((nfy & 1) << 1) | ((nfz & 1) << 2);
-        if (!((ninfo >> k) & 1)) { e0 = e3 = 0; return -1; }
-        return cube_voff(ninfo, cell_voff[gidx(nfx >> 1, nfy >> 1, nfz >> 1, gd)], k, e0, e3);
+        const int kk = (nfx & 1) | ((nfy & 1) << 1) | ((nfz & 1) << 2);
+        if (!((ninfo >> kk) & 1)) { e0 = e3 = 0; return -1; }
+        return cube_voff(ninfo, cell_voff[gidx(nfx >> 1, nfy >> 1, nfz >> 1, gd)], kk, e0, e3);
       };
       int a0 = 0, a3 = 0;
       if (em & (2 | 512)) {
@@ -622,7 +649,6 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
       }
       // reversed winding (MarchingCubesMesher.cu:1487-1497)
       const uint64_t tl = c_tri_packed[v];
-      const int cnt = c_tri_count[v];
       for (int t = 0; t < cnt; t++) {
         uint32_t* o = T + 3 * (size_t)(to + t);
         o[0] = vert[(tl >> (4 * (3 * t + 2))) & 0xf];
@@ -645,8 +671,8 @@ __global__ void __launch_bounds__(kMcThreads) k_mc_triangles(const uint8_t* __re
           }
         }
       }
-      to += cnt;
     }
+    __syncthreads();  // the cube list is rewritten by the next round
   }
 }
 
