@@ -1532,50 +1532,65 @@ cudaError_t kernel_error_flags(unsigned int* flags, bool clear) {
 }
 
 // Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
-// field of edge n (a multiple of 16): one block per map cell, one 16-byte
-// row segment per thread.
-// Largest raw radius (>= 0) of each 16^3 block of fine voxels of a radius
-// field (nx, ny, nz multiples of 16).  One block per (map y, map z) row of
-// map cells; a lane owns a map cell along x and a warp 32 of the 256 fine
-// rows, so each warp load is 32 consecutive 16-byte segments.  With
-// d_rmax, the largest clamped radius is folded into *d_rmax as well.
+// field (nx, ny, nz multiples of 16, nx <= 16 * 32 * kRmapCells).  One block
+// per (map y, map z) row of map cells; a warp reads whole fine rows (lane l
+// owns the 16-byte segments of map cells l, l + 32, ...), the 8 warps take
+// every 8th of the 256 rows, so the block streams its 16 x 16 rows of the
+// field front to back.  With d_rmax, the largest clamped radius is folded
+// into *d_rmax as well.
+constexpr int kRmapCells = 4;  // map cells per lane along x
 __global__ void __launch_bounds__(256) k_radius_map(RField R, int mbx, int mby, int aligned,
                                                      uint8_t* __restrict__ out, int* __restrict__ d_rmax) {
   const int my = blockIdx.x, mz = blockIdx.y;
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __shared__ int part[8][32];
-  int gmax = 0;
-  for (int cb = 0; cb < mbx; cb += 32) {
-    const int cx = cb + lane;
-    int m = 0;
-    if (cx < mbx) {
-      for (int r = wid; r < 256; r += 8) {
-        const int8_t* row = R.p + (int64_t)16 * cx + (int64_t)(16 * my + (r & 15)) * R.sy +
-                            (int64_t)(16 * mz + (r >> 4)) * R.sz;
-        if (aligned) {
-          const uint4 v = *reinterpret_cast<const uint4*>(row);
-          const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+  __shared__ int part[8][32 * kRmapCells];
+  int m[kRmapCells];
 #pragma unroll
-          for (int k = 0; k < 4; k++)
+  for (int c = 0; c < kRmapCells; c++) m[c] = 0;
+  if (aligned) {
+    uint32_t m4[kRmapCells];
 #pragma unroll
-            for (int j = 0; j < 4; j++) m = max(m, (int)(int8_t)((w[k] >> (8 * j)) & 0xffu));
-        } else {
+    for (int c = 0; c < kRmapCells; c++) m4[c] = 0u;
+#pragma unroll 2
+    for (int r = wid; r < 256; r += 8) {
+      const int8_t* row = R.p + (int64_t)(16 * my + (r & 15)) * R.sy + (int64_t)(16 * mz + (r >> 4)) * R.sz;
 #pragma unroll
-          for (int j = 0; j < 16; j++) m = max(m, (int)row[j]);
+      for (int c = 0; c < kRmapCells; c++) {
+        const int cx = lane + 32 * c;
+        if (cx < mbx) {
+          const uint4 v = __ldcs(reinterpret_cast<const uint4*>(row + 16 * cx));
+          m4[c] = __vmaxs4(m4[c], __vmaxs4(__vmaxs4(v.x, v.y), __vmaxs4(v.z, v.w)));  // per-byte signed maxima
         }
       }
     }
-    part[wid][lane] = m;
-    __syncthreads();
-    if (wid == 0) {
-      int t = 0;
-      for (int k = 0; k < 8; k++) t = max(t, part[k][lane]);
-      if (cx < mbx) out[cx + (int64_t)mbx * (my + (int64_t)mby * mz)] = (uint8_t)t;
-      gmax = max(gmax, t);
+#pragma unroll
+    for (int c = 0; c < kRmapCells; c++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) m[c] = max(m[c], (int)((m4[c] >> (8 * j)) & 0xffu));  // bytes >= 0 here
+  } else {
+    for (int r = wid; r < 256; r += 8) {
+      const int8_t* row = R.p + (int64_t)(16 * my + (r & 15)) * R.sy + (int64_t)(16 * mz + (r >> 4)) * R.sz;
+#pragma unroll
+      for (int c = 0; c < kRmapCells; c++) {
+        const int cx = lane + 32 * c;
+        if (cx < mbx)
+#pragma unroll
+          for (int j = 0; j < 16; j++) m[c] = max(m[c], (int)row[16 * cx + j]);
+      }
     }
-    __syncthreads();
   }
-  if (d_rmax != nullptr && wid == 0) {
+#pragma unroll
+  for (int c = 0; c < kRmapCells; c++) part[wid][lane + 32 * c] = m[c];
+  __syncthreads();
+  int gmax = 0;
+  for (int cx = threadIdx.x; cx < mbx; cx += blockDim.x) {
+    int t = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) t = max(t, part[k][cx]);
+    out[cx + (int64_t)mbx * (my + (int64_t)mby * mz)] = (uint8_t)t;
+    gmax = max(gmax, t);
+  }
+  if (d_rmax != nullptr && wid * 32 < mbx) {
     for (int o = 16; o > 0; o >>= 1) gmax = max(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
     if (lane == 0) atomicMax(d_rmax, clamp_radius(gmax));
   }
@@ -1584,6 +1599,7 @@ __global__ void __launch_bounds__(256) k_radius_map(RField R, int mbx, int mby, 
 cudaError_t launch_radius_map(RField R, int nx, int ny, int nz, uint8_t* out, int* d_rmax, cudaStream_t st,
                               KernelCounter* kc) {
   const int mbx = nx / 16, mby = ny / 16, mbz = nz / 16;
+  if (mbx > 32 * kRmapCells) return cudaErrorInvalidValue;
   const int aligned = ((uintptr_t)R.p % 16 == 0 && R.sy % 16 == 0 && R.sz % 16 == 0) ? 1 : 0;
   if (d_rmax) cudaMemsetAsync(d_rmax, 0, sizeof(int), st);
   GM_LAUNCH(kc, "k_radius_map", st, k_radius_map<<<dim3(mby, mbz), 256, 0, st>>>(R, mbx, mby, aligned, out, d_rmax));
