@@ -1039,22 +1039,35 @@ __global__ void k_rec_pack(const uint2* __restrict__ ent, const uint32_t* __rest
 // the same weight; its record (8 bytes: vertex, position term) carries the
 // doubling in the sign bit, so that each neighbour is read once.  The sum
 // runs over the neighbours in vertex order (deterministic).
+// one neighbour's term, added to acc
+__device__ __forceinline__ void bilateral_add(float3& acc, uint2 e, float4 nb, float4 na, float sn2) {
+  // the reference library is built with -use_fast_math (GMorpho/cuda.prf:47),
+  // so its exp and division here are the fast forms
+  float w = __expf(-__fadd_rn(__uint_as_float(e.y & 0x7fffffffu), __fdividef(dist2n(na, nb), sn2)));
+  if (e.y >> 31) w = __fadd_rn(w, w);
+  acc.x = __fadd_rn(acc.x, __fmul_rn(w, nb.x));
+  acc.y = __fadd_rn(acc.y, __fmul_rn(w, nb.y));
+  acc.z = __fadd_rn(acc.z, __fmul_rn(w, nb.z));
+}
+
+// The records two at a time, the next two loaded one step ahead, so that
+// two neighbour-normal gathers are in flight per thread; the terms are
+// added in record order (the same sum, bit for bit, as one at a time).
 __device__ __forceinline__ float3 bilateral_sum(const float4* __restrict__ Nin, const uint2* __restrict__ rec,
                                                 uint32_t n, float4 na, float sn2) {
   float3 acc = make_float3(0.f, 0.f, 0.f);
-  uint2 en = n ? rec[0] : make_uint2(0u, 0u);  // the next record, loaded one ahead
-  for (uint32_t i = 0; i < n; i++) {
-    const uint2 e = en;
-    if (i + 1 < n) en = rec[i + 1];
-    const float4 nb = Nin[e.x];
-    // the reference library is built with -use_fast_math (GMorpho/cuda.prf:47),
-    // so its exp and division here are the fast forms
-    float w = __expf(-__fadd_rn(__uint_as_float(e.y & 0x7fffffffu), __fdividef(dist2n(na, nb), sn2)));
-    if (e.y >> 31) w = __fadd_rn(w, w);
-    acc.x = __fadd_rn(acc.x, __fmul_rn(w, nb.x));
-    acc.y = __fadd_rn(acc.y, __fmul_rn(w, nb.y));
-    acc.z = __fadd_rn(acc.z, __fmul_rn(w, nb.z));
+  const uint2 z2 = make_uint2(0u, 0u);
+  uint2 f0 = n > 0 ? rec[0] : z2, f1 = n > 1 ? rec[1] : z2;  // the next pair
+  uint32_t i = 0;
+  for (; i + 1 < n; i += 2) {
+    const uint2 e0 = f0, e1 = f1;
+    if (i + 2 < n) f0 = rec[i + 2];
+    if (i + 3 < n) f1 = rec[i + 3];
+    const float4 nb0 = Nin[e0.x], nb1 = Nin[e1.x];
+    bilateral_add(acc, e0, nb0, na, sn2);
+    bilateral_add(acc, e1, nb1, na, sn2);
   }
+  if (i < n) bilateral_add(acc, f0, Nin[f0.x], na, sn2);
   return acc;
 }
 
