@@ -1785,34 +1785,61 @@ __device__ __forceinline__ void base_dil_row(const uint8_t* X, const uint8_t* Df
   for (int j = 0; j < 4; j++) fr[j] = next_cells(f[j], j < 3 ? f[j + 1] & 0xffu : fa);
 }
 
-__global__ void __launch_bounds__(256) k_dil_select16(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
+// The select kernel computes each base-pass row once: a block of 32 x 9
+// threads walks kSelZ cells along z, each thread keeping its row's flags at
+// z and z + 1 in registers; the row y + 1 comes from the next warp through
+// shared memory (warp 8 computes that halo row only).
+constexpr int kSelZ = 16;
+__global__ void __launch_bounds__(288) k_dil_select_z(const uint8_t* __restrict__ X, const uint8_t* __restrict__ Df,
                                                       uint8_t* __restrict__ D, Dims g, DataRes dr, CBox roi) {
-  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
-  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
-  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
-  uint32_t any[4] = {0u, 0u, 0u, 0u}, all[4] = {~0u, ~0u, ~0u, ~0u}, d0c[4], dfc[4];
+  __shared__ uint4 flags_s[9][32][4];  // per thread: f, fr at z; f, fr at z + 1
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x16 = 16 * (blockIdx.x * 32 + tx);
+  const int y = (int)blockIdx.y * 8 + ty;
+  const int z0 = (int)blockIdx.z * kSelZ, z1 = min(z0 + kSelZ, g.z);
+  const bool xok = x16 < g.x;
+  auto row = [&](int zz, uint32_t d0[4], uint32_t f[4], uint32_t fr[4], uint32_t dfw[4]) {
+    if (xok) {
+      base_dil_row(X, Df, x16, y, zz, g, dr, d0, f, fr, dfw);  // zeros outside the grid
+    } else {
 #pragma unroll
-  for (int dz = 0; dz < 2; dz++)
-#pragma unroll
-    for (int dy = 0; dy < 2; dy++) {
-      uint32_t d0[4], f[4], fr[4], dfw[4];
-      base_dil_row(X, Df, x16, y + dy, z + dz, g, dr, d0, f, fr, dfw);
+      for (int j = 0; j < 4; j++) d0[j] = f[j] = fr[j] = dfw[j] = 0u;
+    }
+  };
+  uint32_t d0c[4], fc[4], frc[4], dfc[4];
+  row(z0, d0c, fc, frc, dfc);
+  for (int z = z0; z < z1; z++) {
+    uint32_t d0n[4], fn[4], frn[4], dfn[4];
+    row(z + 1, d0n, fn, frn, dfn);
+    flags_s[ty][tx][0] = make_uint4(fc[0], fc[1], fc[2], fc[3]);
+    flags_s[ty][tx][1] = make_uint4(frc[0], frc[1], frc[2], frc[3]);
+    flags_s[ty][tx][2] = make_uint4(fn[0], fn[1], fn[2], fn[3]);
+    flags_s[ty][tx][3] = make_uint4(frn[0], frn[1], frn[2], frn[3]);
+    __syncthreads();
+    if (ty < 8 && xok && y < g.y && cbox_meets(roi, x16, x16 + 15, y, y, z, z)) {
+      const uint4 f1 = flags_s[ty + 1][tx][0], fr1 = flags_s[ty + 1][tx][1];
+      const uint4 f2 = flags_s[ty + 1][tx][2], fr2 = flags_s[ty + 1][tx][3];
+      // the forward 2x2x2 block mixes full and non-full bytes (cells <= dims - 2)
+      const bool yz_ok = y <= g.y - 2 && z <= g.z - 2;
+      uint32_t o[4];
 #pragma unroll
       for (int j = 0; j < 4; j++) {
-        any[j] |= f[j] | fr[j];
-        all[j] &= f[j] & fr[j];
-        if (dz == 0 && dy == 0) { d0c[j] = d0[j]; dfc[j] = dfw[j]; }
+        const uint32_t any = fc[j] | frc[j] | fn[j] | frn[j] | w_of(f1, j) | w_of(fr1, j) | w_of(f2, j) | w_of(fr2, j);
+        const uint32_t all = fc[j] & frc[j] & fn[j] & frn[j] & w_of(f1, j) & w_of(fr1, j) & w_of(f2, j) & w_of(fr2, j);
+        const uint32_t tag = yz_ok ? (any & ~all & xrange_mask(x16 + 4 * j, 0, g.x - 1)) : 0u;
+        o[j] = (tag & dfc[j]) | (~tag & d0c[j]);
       }
+      *reinterpret_cast<uint4*>(D + cidx(x16, y, z, g)) = make_uint4(o[0], o[1], o[2], o[3]);
     }
-  // the forward 2x2x2 block mixes full and non-full bytes (cells <= dims - 2)
-  const bool yz_ok = y <= g.y - 2 && z <= g.z - 2;
-  uint32_t o[4];
+    __syncthreads();  // flags_s is rewritten for the next z
 #pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const uint32_t tag = yz_ok ? (any[j] & ~all[j] & xrange_mask(x16 + 4 * j, 0, g.x - 1)) : 0u;
-    o[j] = (tag & dfc[j]) | (~tag & d0c[j]);
+    for (int j = 0; j < 4; j++) {
+      d0c[j] = d0n[j];
+      fc[j] = fn[j];
+      frc[j] = frn[j];
+      dfc[j] = dfn[j];
+    }
   }
-  *reinterpret_cast<uint4*>(D + cidx(x16, y, z, g)) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
 // GM_REF erosion select: base pass (cells inside data_res with D != 0 and
@@ -1891,57 +1918,88 @@ __global__ void __launch_bounds__(256) k_ero_select16(const uint8_t* __restrict_
 static dim3 grid16(Dims g) { return dim3((g.x / 16 + 31) / 32, (g.y + 7) / 8, g.z); }
 
 // GM_REF erosion select in two steps, so that the centre erosion Ef is
-// computed only where it is read.  k_ero_tag16 writes the base erosion C0
+// computed only where it is read.  k_ero_tag_z writes the base erosion C0
 // into C (final for untagged cells), the refinement tags (0xff per tagged
 // cell) into T and marks the 8^3-cell blocks holding a tagged cell in tmap
 // (zeroed by the caller); once Ef is known on those blocks, k_ero_fix16
 // writes 0xff & ~Ef on the tagged cells.  The bytes equal k_ero_select16's.
-__global__ void __launch_bounds__(256) k_ero_tag16(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
+// The tag kernel computes each base-erosion row once: a block of 32 x 10
+// threads walks kTagZ cells along z, each thread keeping its row's C0 at
+// z - 1, z, z + 1 in registers; the rows y - 1 and y + 1 at z come from
+// the neighbouring warps through shared memory (warps 0 and 9 compute the
+// halo rows only), and the bytes before and after a thread's 16 cells from
+// its neighbouring lanes.
+constexpr int kTagZ = 16;
+__global__ void __launch_bounds__(320) k_ero_tag_z(const uint8_t* __restrict__ X, const uint8_t* __restrict__ D,
                                                    const uint8_t* __restrict__ Eb, uint8_t* __restrict__ C,
                                                    uint8_t* __restrict__ T, uint8_t* __restrict__ tmap, int mdx,
                                                    int mdy, Dims g, DataRes dr, CBox roi) {
-  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
-  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
-  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
-  uint32_t c0[4];
-  base_ero_row(X, D, Eb, x16, y, z, g, dr, c0);
-  const bool iyz = y < dr.v[1] && z < dr.v[2];
-  uint32_t before = 0u, after = 0u;
-  if (x16 > 0) {
-    const int64_t c = cidx(x16 - 1, y, z, g);
-    before = c0_of(X[c], D[c], Eb[c], iyz && x16 - 1 < dr.v[0]);
-  }
-  if (x16 + 16 < g.x) {
-    const int64_t c = cidx(x16 + 16, y, z, g);
-    after = c0_of(X[c], D[c], Eb[c], iyz && x16 + 16 < dr.v[0]);
-  }
-  const bool interior_yz = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
-  uint32_t tag[4] = {0u, 0u, 0u, 0u};
-  if (interior_yz) {
-    uint32_t diff[4] = {0u, 0u, 0u, 0u};
-    const int ny[4] = {y - 1, y + 1, y, y};
-    const int nz[4] = {z, z, z - 1, z + 1};
+  __shared__ uint4 rows_s[10][32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x16 = 16 * (blockIdx.x * 32 + tx);
+  const int y = (int)blockIdx.y * 8 - 1 + ty;
+  const int z0 = (int)blockIdx.z * kTagZ, z1 = min(z0 + kTagZ, g.z);
+  const bool xok = x16 < g.x, yok = y >= 0 && y < g.y;
+  auto row = [&](int zz, uint32_t c[4]) {
+    if (xok && yok && zz >= 0 && zz < g.z) {
+      base_ero_row(X, D, Eb, x16, y, zz, g, dr, c);
+    } else {
 #pragma unroll
-    for (int n = 0; n < 4; n++) {
-      uint32_t cn[4];
-      base_ero_row(X, D, Eb, x16, ny[n], nz[n], g, dr, cn);
-#pragma unroll
-      for (int j = 0; j < 4; j++) diff[j] |= __vcmpne4(c0[j], cn[j]);
+      for (int j = 0; j < 4; j++) c[j] = 0u;
     }
+  };
+  uint32_t cp[4], cc[4], cn[4];
+  row(z0 - 1, cp);
+  row(z0, cc);
+  for (int z = z0; z < z1; z++) {
+    row(z + 1, cn);
+    rows_s[ty][tx] = make_uint4(cc[0], cc[1], cc[2], cc[3]);
+    __syncthreads();
+    // C0 of the cells x16 - 1 and x16 + 16 (the neighbouring lanes' rows;
+    // at the block's x edges, from the grid)
+    uint32_t before = __shfl_up_sync(0xffffffffu, cc[3] >> 24, 1);
+    uint32_t after = __shfl_down_sync(0xffffffffu, cc[0] & 0xffu, 1);
+    const bool out = ty >= 1 && ty <= 8 && xok && yok && cbox_meets(roi, x16, x16 + 15, y, y, z, z);
+    if (out) {
+      const bool iyz = y < dr.v[1] && z < dr.v[2];
+      if (tx == 0)
+        before = 0u;
+      if (tx == 0 && x16 > 0) {
+        const int64_t c = cidx(x16 - 1, y, z, g);
+        before = c0_of(X[c], D[c], Eb[c], iyz && x16 - 1 < dr.v[0]);
+      }
+      if (tx == 31 || x16 + 16 >= g.x) after = 0u;
+      if (tx == 31 && x16 + 16 < g.x) {
+        const int64_t c = cidx(x16 + 16, y, z, g);
+        after = c0_of(X[c], D[c], Eb[c], iyz && x16 + 16 < dr.v[0]);
+      }
+      const bool interior_yz = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
+      uint32_t tag[4] = {0u, 0u, 0u, 0u};
+      if (interior_yz) {
+        const uint4 ym = rows_s[ty - 1][tx], yp = rows_s[ty + 1][tx];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const uint32_t diff = __vcmpne4(cc[j], w_of(ym, j)) | __vcmpne4(cc[j], w_of(yp, j)) |
+                                __vcmpne4(cc[j], cp[j]) | __vcmpne4(cc[j], cn[j]);
+          const uint32_t l = prev_cells(cc[j], j > 0 ? cc[j - 1] >> 24 : before);
+          const uint32_t r = next_cells(cc[j], j < 3 ? cc[j + 1] & 0xffu : after);
+          tag[j] = (diff | __vcmpne4(cc[j], l) | __vcmpne4(cc[j], r)) & xrange_mask(x16 + 4 * j, 1, g.x - 1);
+        }
+      }
+      const int64_t o = cidx(x16, y, z, g);
+      *reinterpret_cast<uint4*>(C + o) = make_uint4(cc[0], cc[1], cc[2], cc[3]);
+      *reinterpret_cast<uint4*>(T + o) = make_uint4(tag[0], tag[1], tag[2], tag[3]);
+      const int64_t mb = idx3(x16 >> 3, y >> 3, z >> 3, mdx, mdy);
+      if (tag[0] | tag[1]) tmap[mb] = 1;
+      if (tag[2] | tag[3]) tmap[mb + 1] = 1;
+    }
+    __syncthreads();  // rows_s is rewritten for the next z
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      const uint32_t l = prev_cells(c0[j], j > 0 ? c0[j - 1] >> 24 : before);
-      const uint32_t r = next_cells(c0[j], j < 3 ? c0[j + 1] & 0xffu : after);
-      tag[j] = (diff[j] | __vcmpne4(c0[j], l) | __vcmpne4(c0[j], r)) & xrange_mask(x16 + 4 * j, 1, g.x - 1);
+      cp[j] = cc[j];
+      cc[j] = cn[j];
     }
   }
-  const int64_t o = cidx(x16, y, z, g);
-  *reinterpret_cast<uint4*>(C + o) = make_uint4(c0[0], c0[1], c0[2], c0[3]);
-  *reinterpret_cast<uint4*>(T + o) = make_uint4(tag[0], tag[1], tag[2], tag[3]);
-  // cells x16 .. x16 + 7 and x16 + 8 .. x16 + 15 lie in two 8^3 blocks
-  const int64_t mb = idx3(x16 >> 3, y >> 3, z >> 3, mdx, mdy);
-  if (tag[0] | tag[1]) tmap[mb] = 1;
-  if (tag[2] | tag[3]) tmap[mb + 1] = 1;
 }
 
 __global__ void __launch_bounds__(256) k_ero_fix16(const uint8_t* __restrict__ T, const uint8_t* __restrict__ Ef,
@@ -2206,7 +2264,9 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
       }
     }
     if (!exact && here()) {
-      GM_LAUNCH(kc, "k_dil_select", st, k_dil_select16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, Df, D, g, dr, R_D));
+      GM_LAUNCH(kc, "k_dil_select", st,
+                k_dil_select_z<<<dim3((g.x / 16 + 31) / 32, (g.y + 7) / 8, (g.z + kSelZ - 1) / kSelZ), dim3(32, 9), 0,
+                                 st>>>(a.X, Df, D, g, dr, R_D));
     }
   } else {
     at += 2;  // the dilation's two passes
@@ -2269,7 +2329,8 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
         if (here()) {
           cudaMemsetAsync(tmap, 0, (size_t)mdx * mdy * mdz, st);
           GM_LAUNCH(kc, "k_ero_tag", st,
-                    k_ero_tag16<<<grid16(g), dim3(32, 8), 0, st>>>(a.X, D, Eb, a.C_out, S, tmap, mdx, mdy, g, dr, F));
+                    k_ero_tag_z<<<dim3((g.x / 16 + 31) / 32, (g.y + 7) / 8, (g.z + kTagZ - 1) / kTagZ), dim3(32, 10), 0,
+                                  st>>>(a.X, D, Eb, a.C_out, S, tmap, mdx, mdy, g, dr, F));
         }
         ok &= dpx_step<KERN_CEN2, uint16_t, 0>(a, at, buf16a, buf16b, nullptr, Nx, Ny, Nz, 1, 0, ehalo, K, RNONE, 0, rx,
                                                ry, st, kc, "k_pass_ero_y", nullptr, 0,
