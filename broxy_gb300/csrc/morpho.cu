@@ -1714,36 +1714,57 @@ __device__ __forceinline__ uint32_t prev_cells(uint32_t w, uint32_t before) { re
 // Contour of the dilation: fine voxels outside D that are 6-adjacent to D.
 // GM_REF: only for cells in [1, res-2]^3 whose byte is not 0xff
 // (TagVoxelsContourByErosion, Grid.cu:1230-1327); GM_EXACT: whole grid.
-__global__ void __launch_bounds__(256) k_contour16(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, Dims g,
+// A block of 32 x 10 threads walks kConZ cells along z, each thread
+// keeping its row of D at z - 1, z, z + 1 in registers; the rows y - 1 and
+// y + 1 come from the neighbouring warps through shared memory (warps 0 and
+// 9 load the halo rows only) and the bytes before and after a thread's 16
+// cells from its neighbouring lanes, so each row of D is read once.
+constexpr int kConZ = 16;
+__global__ void __launch_bounds__(320) k_contour_z(const uint8_t* __restrict__ D, uint8_t* __restrict__ S, Dims g,
                                                    int exact, CBox roi) {
-  const int x16 = 16 * (blockIdx.x * 32 + threadIdx.x);
-  const int y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
-  if (x16 >= g.x || y >= g.y || !cbox_meets(roi, x16, x16 + 15, y, y, z, z)) return;
+  __shared__ uint4 rows_s[10][32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x16 = 16 * (blockIdx.x * 32 + tx);
+  const int y = (int)blockIdx.y * 8 - 1 + ty;
+  const int z0 = (int)blockIdx.z * kConZ, z1 = min(z0 + kConZ, g.z);
+  const bool xok = x16 < g.x, yok = y >= 0 && y < g.y;
   const uint4 z4 = make_uint4(0u, 0u, 0u, 0u);
-  const uint4 v = ld16(D, x16, y, z, g);
-  const uint32_t before = x16 > 0 ? D[cidx(x16 - 1, y, z, g)] : 0u;
-  const uint32_t after = x16 + 16 < g.x ? D[cidx(x16 + 16, y, z, g)] : 0u;
-  const uint4 ym = y > 0 ? ld16(D, x16, y - 1, z, g) : z4, yp = y < g.y - 1 ? ld16(D, x16, y + 1, z, g) : z4;
-  const uint4 zm = z > 0 ? ld16(D, x16, y, z - 1, g) : z4, zp = z < g.z - 1 ? ld16(D, x16, y, z + 1, g) : z4;
-  const bool yz_in = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
-  uint32_t o[4];
+  auto row = [&](int zz) { return xok && yok && zz >= 0 && zz < g.z ? ld16(D, x16, y, zz, g) : z4; };
+  uint4 zm = row(z0 - 1), v = row(z0);
+  for (int z = z0; z < z1; z++) {
+    const uint4 zp = row(z + 1);
+    rows_s[ty][tx] = v;
+    __syncthreads();
+    uint32_t before = __shfl_up_sync(0xffffffffu, v.w >> 24, 1);
+    uint32_t after = __shfl_down_sync(0xffffffffu, v.x & 0xffu, 1);
+    if (ty >= 1 && ty <= 8 && xok && yok && cbox_meets(roi, x16, x16 + 15, y, y, z, z)) {
+      if (tx == 0) before = x16 > 0 ? D[cidx(x16 - 1, y, z, g)] : 0u;
+      if (tx == 31 || x16 + 16 >= g.x) after = x16 + 16 < g.x ? D[cidx(x16 + 16, y, z, g)] : 0u;
+      const uint4 ym = rows_s[ty - 1][tx], yp = rows_s[ty + 1][tx];
+      const bool yz_in = y >= 1 && z >= 1 && y <= g.y - 2 && z <= g.z - 2;
+      uint32_t o[4];
 #pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const uint32_t vw = w_of(v, j);
-    const uint32_t l = prev_cells(vw, j > 0 ? w_of(v, j - 1) >> 24 : before);
-    const uint32_t r = next_cells(vw, j < 3 ? w_of(v, j + 1) & 0xffu : after);
-    // 6-neighbours of each fine voxel (bit x + 2y + 4z of a byte)
-    uint32_t t = ((vw & 0xAAAAAAAAu) >> 1) | ((r & 0x55555555u) << 1);
-    t |= ((vw & 0x55555555u) << 1) | ((l & 0xAAAAAAAAu) >> 1);
-    t |= ((vw & 0xCCCCCCCCu) >> 2) | ((w_of(yp, j) & 0x33333333u) << 2);
-    t |= ((vw & 0x33333333u) << 2) | ((w_of(ym, j) & 0xCCCCCCCCu) >> 2);
-    t |= ((vw & 0xF0F0F0F0u) >> 4) | ((w_of(zp, j) & 0x0F0F0F0Fu) << 4);
-    t |= ((vw & 0x0F0F0F0Fu) << 4) | ((w_of(zm, j) & 0xF0F0F0F0u) >> 4);
-    uint32_t m = 0xffffffffu;
-    if (!exact) m = yz_in ? (__vcmpne4(vw, 0xffffffffu) & xrange_mask(x16 + 4 * j, 1, g.x - 1)) : 0u;
-    o[j] = t & ~vw & m;
+      for (int j = 0; j < 4; j++) {
+        const uint32_t vw = w_of(v, j);
+        const uint32_t l = prev_cells(vw, j > 0 ? w_of(v, j - 1) >> 24 : before);
+        const uint32_t r = next_cells(vw, j < 3 ? w_of(v, j + 1) & 0xffu : after);
+        // 6-neighbours of each fine voxel (bit x + 2y + 4z of a byte)
+        uint32_t t = ((vw & 0xAAAAAAAAu) >> 1) | ((r & 0x55555555u) << 1);
+        t |= ((vw & 0x55555555u) << 1) | ((l & 0xAAAAAAAAu) >> 1);
+        t |= ((vw & 0xCCCCCCCCu) >> 2) | ((w_of(yp, j) & 0x33333333u) << 2);
+        t |= ((vw & 0x33333333u) << 2) | ((w_of(ym, j) & 0xCCCCCCCCu) >> 2);
+        t |= ((vw & 0xF0F0F0F0u) >> 4) | ((w_of(zp, j) & 0x0F0F0F0Fu) << 4);
+        t |= ((vw & 0x0F0F0F0Fu) << 4) | ((w_of(zm, j) & 0xF0F0F0F0u) >> 4);
+        uint32_t m = 0xffffffffu;
+        if (!exact) m = yz_in ? (__vcmpne4(vw, 0xffffffffu) & xrange_mask(x16 + 4 * j, 1, g.x - 1)) : 0u;
+        o[j] = t & ~vw & m;
+      }
+      *reinterpret_cast<uint4*>(S + cidx(x16, y, z, g)) = make_uint4(o[0], o[1], o[2], o[3]);
+    }
+    __syncthreads();  // rows_s is rewritten for the next z
+    zm = v;
+    v = zp;
   }
-  *reinterpret_cast<uint4*>(S + cidx(x16, y, z, g)) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
 // GM_REF dilation select: base pass (cells inside data_res that are not
@@ -2278,7 +2299,9 @@ cudaError_t launch_close(const CloseArgs& a, cudaStream_t st, KernelCounter* kc)
   }
   // ---- contour ----
   if (here()) {
-    GM_LAUNCH(kc, "k_contour", st, k_contour16<<<grid16(g), dim3(32, 8), 0, st>>>(D, S, g, exact ? 1 : 0, R_S));
+    GM_LAUNCH(kc, "k_contour", st,
+            k_contour_z<<<dim3((g.x / 16 + 31) / 32, (g.y + 7) / 8, (g.z + kConZ - 1) / kConZ), dim3(32, 10), 0, st>>>(
+                D, S, g, exact ? 1 : 0, R_S));
     // (S holds the refinement tags after the erosion's x pass in GM_REF)
     if (a.S_out) cudaMemcpyAsync(a.S_out, S, cells, cudaMemcpyDeviceToDevice, st);
   }
@@ -2457,7 +2480,9 @@ cudaError_t launch_close_zpass(const CloseArgs& a, int z0, int z1, int r_bound, 
 
 cudaError_t launch_contour(const uint8_t* D, uint8_t* S, int res, int exact, cudaStream_t st, KernelCounter* kc) {
   const Dims g{res, res, res};
-  GM_LAUNCH(kc, "k_contour", st, k_contour16<<<grid16(g), dim3(32, 8), 0, st>>>(D, S, g, exact, CBox{{0, 0, 0}, {res, res, res}}));
+  GM_LAUNCH(kc, "k_contour", st,
+            k_contour_z<<<dim3((g.x / 16 + 31) / 32, (g.y + 7) / 8, (g.z + kConZ - 1) / kConZ), dim3(32, 10), 0, st>>>(
+                D, S, g, exact, CBox{{0, 0, 0}, {res, res, res}}));
   return cudaGetLastError();
 }
 
