@@ -435,7 +435,7 @@ __host__ __device__ inline size_t ero_x_w_warp_bytes(int rx) {
   return N * 2 + (size_t)rx * 2 + N * 4;  // outputs at centres, at lattice points, sites
 }
 
-__global__ void __launch_bounds__(256) k_ero_pass_x_w(const uint8_t* __restrict__ S, RField R, int uniform_r, int rx,
+__global__ void __launch_bounds__(256, 4) k_ero_pass_x_w(const uint8_t* __restrict__ S, RField R, int uniform_r, int rx,
                                                       int ry, int rz, int halo, uint32_t K,
                                                       uint16_t* __restrict__ HC, uint16_t* __restrict__ HL,
                                                       CBox rows) {
@@ -502,13 +502,35 @@ __global__ void __launch_bounds__(256) k_ero_pass_x_w(const uint8_t* __restrict_
       }
     }
     __syncwarp();
-    for (int s = 0; s < ns; s++) {
-      const uint32_t sw = sites[s];
-      const int q = (int)(sw & 0xfffu), rm1 = (int)((sw >> 12) & 0xffu), reach = (int)(sw >> 20);
+    // Runs of adjacent sites with the same radius splat as one: every
+    // output inside the run has a site at distance 0 (value u), and one
+    // outside it is nearest to the run's end on its side (both kernels grow
+    // with the distance), so the run's taps are [q0 - reach, qe + reach]
+    // with the nearest site of each, instead of 2 reach + 1 per site.
+    for (int i = 0; i < ns;) {
+      const uint32_t sw = sites[i];
+      const int q0 = (int)(sw & 0xfffu), rm1 = (int)((sw >> 12) & 0xffu), reach = (int)(sw >> 20);
+      int j = i + 1;  // first site past the run
+      for (;;) {
+        const int t = j + lane;
+        bool cont = false;
+        if (t < ns) {
+          const uint32_t st = sites[t];
+          cont = (int)(st & 0xfffu) == q0 + (t - i) && (int)((st >> 12) & 0xffu) == rm1;
+        }
+        const uint32_t brk = __ballot_sync(0xffffffffu, !cont);
+        if (brk) {
+          j += __ffs(brk) - 1;
+          break;
+        }
+        j += 32;
+      }
+      const int len = j - i, qe = q0 + len - 1;
       const uint32_t u = K - 4u * (uint32_t)(rm1 * rm1);
-      for (int dq = lane - reach; dq <= reach; dq += 32) {
-        const int p = q - dq;  // output position, delta = q - p = dq
+      for (int o = lane - reach; o <= len - 1 + reach; o += 32) {
+        const int p = q0 + o;  // output position
         if (p < 0 || p >= N) continue;
+        const int dq = (o < 0 ? q0 : (o >= len ? qe : p)) - p;  // delta to the nearest site of the run
         const int ec = center_dist2(dq);
         const uint32_t vc = u + (uint32_t)(ec * ec);
         if (vc < K && vc < hc[p]) hc[p] = (uint16_t)vc;
@@ -519,6 +541,7 @@ __global__ void __launch_bounds__(256) k_ero_pass_x_w(const uint8_t* __restrict_
         }
       }
       __syncwarp();
+      i = j;
     }
     for (int i = lane; i < N >> 3; i += 32) hcrow[i] = reinterpret_cast<const uint4*>(hc)[i];
     for (int i = lane; i < rx >> 3; i += 32) hlrow[i] = reinterpret_cast<const uint4*>(hl)[i];
