@@ -204,12 +204,15 @@ def run_ours(args, rank, world):
     value = world * V / (ms_max * 1e-3) / 1e9
 
     # ---- e2e through the host-buffer C ABI (gm_update_to_host)
+    e2e_extra = {}
     if args.no_e2e:
         e2e_ms, nv2, nt2 = float("nan"), nv, nt
     else:
-        e2e_ms, nv2, nt2 = run_e2e(args, ctx, desc, X, R, nv, nt, world, dev)
+        e2e_ms, nv2, nt2, e2e_extra = run_e2e(args, ctx, desc, X, R, nv, nt, world, dev)
     assert (nv2, nt2) == (nv, nt)
     r = finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value, desc)
+    if r is not None and "e2e" in r:
+        r["e2e"].update(e2e_extra)
     r["voxelize"] = {"ms": round(inp["voxelize_ms"], 3), "input_triangles": int(inp["T"].shape[0]),
                      "input_vertices": int(inp["P"].shape[0]), "grid": "%d^3 fine" % (2 * res),
                      "data_res": [int(v) for v in desc.data_res], "kernels_ms": vox_kernels,
@@ -241,15 +244,28 @@ def run_e2e(args, ctx, desc, X, R, nv, nt, world, dev):
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
+    marks = []
     for _ in range(args.steps):
-        nv2, nt2 = e2e_step()
+        nv2, nt2 = e2e_step()  # returns after its own stream synchronisation
+        marks.append(time.perf_counter())
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     if world > 1:
         t = torch.tensor([e2e_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    return e2e_ms, nv2, nt2
+    steps_ms = [(b - a) * 1e3 for a, b in zip([t0] + marks[:-1], marks)]
+    # the host link's bandwidth on this machine (the upload bounds the step's start)
+    dR = torch.empty_like(R)
+    dR.copy_(hR, non_blocking=True)
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    dR.copy_(hR, non_blocking=True)
+    torch.cuda.synchronize()
+    h2d_gbs = hR.numel() / (time.perf_counter() - h0) / 1e9
+    extra = {"step_ms_min": round(min(steps_ms), 3), "step_ms_median": round(statistics.median(steps_ms), 3),
+             "step_ms_max": round(max(steps_ms), 3), "h2d_gbs_pinned": round(h2d_gbs, 1)}
+    return e2e_ms, nv2, nt2, extra
 
 
 def finish(args, ctx, prof, ms_max, launches, V, X, R, nv, nt, e2e_ms, clk, world, rank, res, value, desc):
