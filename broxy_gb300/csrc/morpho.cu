@@ -169,10 +169,11 @@ constexpr int kBig = 1 << 24;
 
 template <int WPL>
 __global__ void __launch_bounds__(256) k_dil_pass_x_w(const uint8_t* __restrict__ X, uint8_t* __restrict__ A,
-                                                      int rx, int ry, int rz, int dcap, CBox rows) {
+                                                      int rx, int ry, int rz, int dcap, CBox rows, int64_t row0,
+                                                      int64_t row_end) {
   const int lane = threadIdx.x & 31;
-  const int64_t row_id = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (row_id >= (int64_t)ry * rz) return;
+  const int64_t row_id = row0 + (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (row_id >= row_end) return;
   const int cy = (int)(row_id % ry), cz = (int)(row_id / ry);
   if (cy < rows.lo[1] || cy >= rows.hi[1] || cz < rows.lo[2] || cz >= rows.hi[2]) return;  // rows nobody reads
   const int N = 2 * rx, Ny = 2 * ry, W = N >> 5;
@@ -295,12 +296,17 @@ __global__ void __launch_bounds__(256) k_dil_pass_x_w(const uint8_t* __restrict_
 static cudaError_t launch_dil_pass_x(const uint8_t* X, uint8_t* A, int rx, int ry, int rz, int dcap, CBox rows,
                                      cudaStream_t st, KernelCounter* kc) {
   const int W = (2 * rx) >> 5;
-  const int64_t nrows = (int64_t)ry * rz;
-  const unsigned blocks = (unsigned)((nrows + 7) / 8);
+  // the rows of the box's z range only (row id = y + ry z)
+  const int64_t row0 = (int64_t)ry * (rows.lo[2] > 0 ? rows.lo[2] : 0);
+  const int64_t row_end = (int64_t)ry * (rows.hi[2] < rz ? rows.hi[2] : rz);
+  if (row_end <= row0) return cudaSuccess;
+  const unsigned blocks = (unsigned)((row_end - row0 + 7) / 8);
   if (W <= 32) {
-    GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x_w<1><<<blocks, 256, 0, st>>>(X, A, rx, ry, rz, dcap, rows));
+    GM_LAUNCH(kc, "k_dil_pass_x", st,
+              k_dil_pass_x_w<1><<<blocks, 256, 0, st>>>(X, A, rx, ry, rz, dcap, rows, row0, row_end));
   } else if (W <= 64) {
-    GM_LAUNCH(kc, "k_dil_pass_x", st, k_dil_pass_x_w<2><<<blocks, 256, 0, st>>>(X, A, rx, ry, rz, dcap, rows));
+    GM_LAUNCH(kc, "k_dil_pass_x", st,
+              k_dil_pass_x_w<2><<<blocks, 256, 0, st>>>(X, A, rx, ry, rz, dcap, rows, row0, row_end));
   } else {
     GM_LAUNCH(kc, "k_dil_pass_x", st,
               k_dil_pass_x<<<dim3(ry, rz), 256, 8 * W * sizeof(uint32_t), st>>>(X, A, rx, ry, dcap, rows));
