@@ -131,7 +131,12 @@ def test_reference_build_equals_oracle_and_gpu(gm_ctx, tmp_path, name, kind, res
     assert len(bad) <= n91, (len(bad), n91)
     np.testing.assert_allclose(rV, Vo, rtol=1e-6, atol=0)
     No = O.normals(Vo, To, iters)
-    np.testing.assert_allclose(rN, No, atol=2e-3, rtol=0, equal_nan=True)
+    # The reference sums the face normals with float atomics in no fixed
+    # order, and the oracle and this library in fixed but different orders;
+    # after 200 filter iterations the orders alone move a few vertices by up
+    # to ~4e-3 (seen between runs of the reference on the same input).
+    ntol = 2e-3 if iters <= 20 else 1e-2
+    np.testing.assert_allclose(rN, No, atol=ntol, rtol=0, equal_nan=True)
     # and this library's CUDA path against the reference
     desc = api.make_desc(res, data_res=data_res, cell_size=1.0 / res)
     Xd = torch.as_tensor(X).cuda()
@@ -146,4 +151,5 @@ def test_reference_build_equals_oracle_and_gpu(gm_ctx, tmp_path, name, kind, res
     bad = np.nonzero((gT.cpu().numpy() != rT).any(axis=1))[0]
     assert len(bad) <= n91, (len(bad), n91)
     np.testing.assert_allclose(gV.cpu().numpy(), rV, rtol=1e-6, atol=0)
-    np.testing.assert_allclose(gN.cpu().numpy(), rN, atol=2e-3, rtol=0, equal_nan=True)
+    np.testing.assert_allclose(gN.cpu().numpy(), rN, atol=ntol, rtol=0, equal_nan=True)
+    np.testing.assert_allclose(gN.cpu().numpy(), No, atol=ntol, rtol=0, equal_nan=True)
