@@ -291,7 +291,7 @@ __device__ int brick_candidates(const uint8_t* tile, const McWin& w, int ox, int
   return (int)total;
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_count(const uint8_t* __restrict__ C, GDims gd, McWin w,
+__global__ void __launch_bounds__(kMcThreads, 5) k_mc_count(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                           uint32_t* __restrict__ brick_tot) {
   __shared__ __align__(16) uint8_t tile[kTileCells];
   __shared__ uint16_t list[kCellsPerBrick];
@@ -401,7 +401,7 @@ __device__ __forceinline__ float lerp_coord(float p1, float p2, float v1, float 
   return __fadd_rn(p1, __fsub_rn(v2, v1) > 0.f ? num : -num);
 }
 
-__global__ void __launch_bounds__(kMcThreads) k_mc_vertices(const uint8_t* __restrict__ C, GDims gd, McWin w,
+__global__ void __launch_bounds__(kMcThreads, 6) k_mc_vertices(const uint8_t* __restrict__ C, GDims gd, McWin w,
                                                           const uint32_t* __restrict__ brick_off,
                                                           uint32_t* __restrict__ cell_voff,
                                                           float* __restrict__ V, float bx, float by, float bz,
