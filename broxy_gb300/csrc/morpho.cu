@@ -1324,7 +1324,11 @@ __global__ void __launch_bounds__(256, 4) k_pass_dpx_group(const DpxJob* __restr
   for (;;) {
     const int item = item_s;
     if (item >= total) return;  // block-uniform
-    if (item >= job_end_s || item < job_s.first) {  // block-uniform (job_end_s = -1 at first)
+    const bool other_job = item >= job_end_s || item < job_s.first;  // (job_end_s = -1 at first)
+    // every thread has read job_s / job_end_s before warp 0 may rewrite
+    // them, so that the branch below (and its barrier) is block-uniform
+    __syncthreads();
+    if (other_job) {
       if (threadIdx.x < 32) {
         // the job holding the item: the last one whose first item is <= it
         int lo = 0, hi = njobs - 1;
