@@ -577,7 +577,9 @@ def run_serve(args):
 
 
 def cpu_crop(X, R, res, sub):
-    """Centre crop of `sub` base cells per axis of the device inputs."""
+    """Centre crop of `sub` base cells per axis of the device inputs (the
+    whole grid when sub >= res)."""
+    sub = min(sub, res)
     Xh = X.cpu().numpy().reshape(res, res, res)
     Rh = R.cpu().numpy().reshape(2 * res, 2 * res, 2 * res)
     o = (res - sub) // 2
@@ -602,6 +604,7 @@ def cpu_baseline(X, R, res, sub):
     """The oracle's reference-algorithm closing + MC + normals on all host
     cores, on a centre crop of the same inputs (bounded sample)."""
     from oracle import oracle as O
+    sub = min(sub, res)
     Xc, Rc = cpu_crop(X, R, res, sub)
     t0 = time.perf_counter()
     _, _, Cc = O.close(Xc, sub, [sub] * 3, Rc, 0, 0)
@@ -643,7 +646,7 @@ def run_reference(args, rank, world):
     import torch
     from broxy_gb300 import synth
     from oracle import oracle as O
-    res, sub = args.res, args.cpu_res
+    res, sub = args.res, min(args.cpu_res, args.res)
     X, R = reference_inputs(res)
     times = []
     Xc, Rc = cpu_crop(torch.as_tensor(X), torch.as_tensor(R), res, sub)
@@ -660,7 +663,7 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * statistics.mean(times), 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int (CPU)",
             "data": "synthetic",
-            "config": {"workload": "crop: %d^3 fine voxels of the 1024^3 grid, same radius field" % (2 * sub)},
+            "config": {"workload": "crop: %d^3 fine voxels of the %d^3 grid, same radius field" % (2 * sub, 2 * res)},
             "cpu_baseline": {"value": round(val, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                              "cpu_model": cpu_model(),
                              "sample": "centre crop of %d^3 fine voxels per step" % (2 * sub)},
