@@ -675,7 +675,6 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
     tile[s * 32 + tx] = v;
   }
   __syncthreads();
-  __shared__ uint8_t ybits[8][32][2];  // [z pair][lane][y parity] hmm: per group
   // each thread: 16 consecutive z = z0 + 16 zg + j
   uint32_t bits = 0;
   const int ru = clamp_radius(uniform_r);
@@ -714,7 +713,6 @@ __global__ void __launch_bounds__(256) k_final_z(const uint16_t* __restrict__ in
   ex[yp][zg][tx][0] = packed;
   ex[yp][zg][tx][1] = packed_hi;
   __syncthreads();
-  (void)ybits;
   if (yp == 0 && (tx & 1) == 0 && x < Nx) {
     const uint32_t w0 = packed | ex[1][zg][tx][0];
     const uint32_t w1 = packed_hi | ex[1][zg][tx][1];
